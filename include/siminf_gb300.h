@@ -1,0 +1,223 @@
+/*
+ * siminf_gb300.h -- C ABI of the GB300 ssm/mssm solver.
+ *
+ * The library replaces the reference's solver entry points behind the
+ * dispatch in SimInf_run (src/SimInf.c:382-399).  All pointers in the
+ * argument struct are host pointers owned by the caller, exactly as in the
+ * reference; the library copies what it needs to the GPU, runs there, and
+ * writes U/V back into the caller's buffers before returning.  No torch
+ * types and no CUDA types appear in any signature.
+ *
+ * Threading and errors follow the reference's convention: every call
+ * returns 0 or a negative SimInf error code, never longjmps, and frees and
+ * synchronises everything it allocated before returning.  Diagnostics of
+ * the last failing call on the calling thread are kept for
+ * siminf_gpu_last_status().
+ */
+#ifndef SIMINF_GB300_H
+#define SIMINF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Transition-rate and post-time-step callback types, unchanged from
+ * inst/include/SimInf.h:92-107.  The GPU solver never calls host
+ * callbacks; the fields are kept so that the struct below stays
+ * layout-identical to SimInf_solver_args. */
+typedef double (*siminf_gpu_trfun)(const int *u, const double *v,
+                                   const double *ldata, const double *gdata,
+                                   double t);
+typedef int (*siminf_gpu_ptsfun)(double *v_new, const int *u, const double *v,
+                                 const double *ldata, const double *gdata,
+                                 int node, double t);
+
+/* Event kinds, inst/include/SimInf.h:56-59. */
+enum {
+    SIMINF_GPU_EXIT_EVENT = 0,
+    SIMINF_GPU_ENTER_EVENT = 1,
+    SIMINF_GPU_INTERNAL_TRANSFER_EVENT = 2,
+    SIMINF_GPU_EXTERNAL_TRANSFER_EVENT = 3
+};
+
+/* Error codes: the reference's SimInf_error_code values
+ * (inst/include/SimInf.h:66-89) keep their numbers; codes from -30 down are
+ * new and only the GPU path returns them. */
+enum {
+    SIMINF_GPU_ERR_NEGATIVE_STATE = -1,
+    SIMINF_GPU_ERR_ALLOC_MEMORY_BUFFER = -2,
+    SIMINF_GPU_UNDEFINED_EVENT = -3,
+    SIMINF_GPU_ERR_SAMPLE_SELECT = -8,
+    SIMINF_GPU_ERR_INVALID_MODEL = -9,
+    SIMINF_GPU_ERR_INVALID_RATE = -11,
+    SIMINF_GPU_ERR_UNKNOWN_SOLVER = -12,
+    SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS = -13,
+    SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS = -14,
+    SIMINF_GPU_ERR_EVENTS_N = -15,
+    SIMINF_GPU_ERR_EVENT_SHIFT = -16,
+    SIMINF_GPU_ERR_SHIFT_OUT_OF_BOUNDS = -17,
+    SIMINF_GPU_ERR_INVALID_PROPORTION = -18,
+    SIMINF_GPU_ERR_CUDA = -30,              /* a CUDA runtime call failed */
+    SIMINF_GPU_ERR_EVENTS_UNSORTED = -31,   /* events not sorted by time, E1 before E2 */
+    SIMINF_GPU_ERR_UNKNOWN_MODEL = -32,     /* no device model of that name */
+    SIMINF_GPU_ERR_TIMEOUT = -33,           /* a bounded device wait gave up */
+    SIMINF_GPU_ERR_NO_DEVICE = -34          /* no CUDA device is visible */
+};
+
+/*
+ * Solver arguments.  Field for field the same struct as
+ * SimInf_solver_args (src/SimInf_internal.h:44-200): the same types in the
+ * same order, so SimInf_run can pass its own struct by pointer cast.
+ * Node, dest, select and shift in the event arrays are one-based as in the
+ * reference; events must be sorted by time with, within a time, the E1
+ * events (exit, enter, internal transfer) before the external transfers --
+ * the order R/SimInf_events.R:398 produces.
+ */
+typedef struct siminf_gpu_solver_args {
+    const int *u0;              /* Nc x (Nn * Nrep) */
+    const double *v0;           /* Nd x (Nn * Nrep) */
+    const int *irG;             /* dependency graph G (Nt x Nt), CSC */
+    const int *jcG;
+    const int *irS;             /* state-change matrix S (Nc x Nt), CSC */
+    const int *jcS;
+    const int *prS;
+    const double *tspan;
+    int tlen;
+    int *U;                     /* dense (Nn*Nc) x (Nrep*tlen), or NULL */
+    const int *irU;             /* sparse U pattern when U is NULL */
+    const int *jcU;
+    double *prU;
+    double *V;                  /* dense (Nn*Nd) x (Nrep*tlen), or NULL */
+    const int *irV;
+    const int *jcV;
+    double *prV;
+    const double *ldata;        /* Nld x Nn */
+    const double *gdata;
+    int Nn;
+    int Nc;
+    int Nt;
+    int Nd;
+    int Nld;
+    int Nrep;
+    const int *irE;             /* select matrix E, CSC */
+    const int *jcE;
+    double *prE;
+    const int *N;               /* shift matrix, Nc x Nshift, or NULL */
+    int len;                    /* number of scheduled events */
+    const int *event;
+    const int *time;
+    const int *node;
+    const int *dest;
+    const int *n;
+    const double *proportion;
+    const int *select;
+    const int *shift;
+    int Nthread;                /* ignored on the GPU */
+    int solver;                 /* 0 = ssm; 1 = aem is rejected */
+    int crn;                    /* common random numbers (mssm) */
+    int rng_type;               /* ignored: the GPU stream is Philox4x32-10 */
+    unsigned long int seed;     /* Philox key */
+    siminf_gpu_trfun *tr_fun;   /* ignored on the GPU */
+    siminf_gpu_ptsfun pts_fun;  /* ignored on the GPU */
+} siminf_gpu_solver_args;
+
+/* A compiled device model: the __device__ transition-rate functions and
+ * post-time-step function of one model.  Opaque. */
+typedef struct siminf_gpu_model siminf_gpu_model;
+
+/*
+ * Look up a device model compiled into the library by name.  Replaces the
+ * construction of `TRFun tr_fun[]` and the PTSFun pointer in each
+ * <Model>_run (e.g. src/models/SEIR.c:157-165, src/models/SIR.c,
+ * src/models/SISe.c) and the mparse-generated SIMINF_MODEL_RUN
+ * (R/C-generator.R:304-332) for the models the library ships.
+ * Names: "SIR" (SIR.c), "SEIR" (SEIR.c), "SIS" (SIS.c), "SISe" (SISe.c),
+ * "SIR_mparse" (mparse "S -> beta*S*I/N -> I", "I -> gamma*I -> R",
+ * N <- S+I+R, beta/gamma in gdata), "SISe_pf" (mparse
+ * "S -> upsilon*phi*S -> I", "I -> gamma*I -> S" with the pts_fun
+ * phi <- phi*(1-0.03) + 0.05*I/(S+I); upsilon/gamma in gdata).
+ * Returns 0 or SIMINF_GPU_ERR_UNKNOWN_MODEL.
+ */
+int siminf_gpu_model_builtin(const char *name, siminf_gpu_model **out);
+
+/* Number of transitions (Nt), compartments (Nc) and continuous state
+ * variables (Nd) the model expects; any pointer may be NULL. */
+int siminf_gpu_model_dims(const siminf_gpu_model *model, int *Nc, int *Nt, int *Nd);
+
+void siminf_gpu_model_free(siminf_gpu_model *model);
+
+/*
+ * Run one replicate (Nrep == 1) with the split-step method.  Replaces
+ * int SimInf_run_solver_ssm(SimInf_solver_args *args)
+ * (src/SimInf_internal.h:418-420, src/solvers/SimInf_solver_ssm.c:381-414).
+ * Writes U (dense) or prU (sparse) and V or prV.  Returns 0 or an error.
+ */
+int siminf_gpu_run_solver_ssm(siminf_gpu_solver_args *args,
+                              const siminf_gpu_model *model);
+
+/*
+ * Run Nrep >= 1 replicates in one batched launch.  Replaces
+ * int SimInf_run_solver_mssm(SimInf_solver_args *args)
+ * (src/SimInf_internal.h:410-412, src/solvers/SimInf_solver_mssm.c:410-443).
+ * Replicate r owns columns [r*tlen, (r+1)*tlen) of U/V and draws from the
+ * streams r*Nn + node.
+ */
+int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args,
+                               const siminf_gpu_model *model);
+
+/* Diagnostics of the last failing call on the calling thread: the fields
+ * SimInf_print_status (src/solvers/SimInf_solver.c:1191-1249) and
+ * SimInf_print_event (src/solvers/SimInf_solver.c:550-645) print. */
+typedef struct siminf_gpu_status {
+    int error;                  /* the returned code */
+    int node;                   /* zero-based node of the failure, or -1 */
+    int transition;             /* zero-based transition, or -1 */
+    int event_index;            /* zero-based index into the event arrays, or -1 */
+    double time;                /* simulation time of the failure */
+    double rate;                /* the offending rate for INVALID_RATE */
+    char message[512];          /* one human-readable line */
+} siminf_gpu_status;
+
+int siminf_gpu_last_status(siminf_gpu_status *out);
+
+/* Counters and timings of the last successful run on the calling thread. */
+typedef struct siminf_gpu_stats {
+    uint64_t transitions;       /* SSA transitions fired */
+    uint64_t node_days;         /* node x unit-time steps simulated */
+    uint64_t e1_events;         /* exit/enter/internal events applied */
+    uint64_t e2_events;         /* external transfers applied */
+    int e2_waves;               /* conflict-free wavefronts executed */
+    int days;                   /* unit-time steps simulated */
+    double ms_upload;           /* host -> device copies and planning */
+    double ms_solve;            /* device time of the day loop */
+    double ms_download;         /* device -> host copies of U/V */
+} siminf_gpu_stats;
+
+int siminf_gpu_last_stats(siminf_gpu_stats *out);
+
+/*
+ * Device-resident plans, for callers that keep a model on the GPU across
+ * runs (particle filters, ABC, serving).  plan_create copies the model,
+ * the event schedule and its per-day wave plan to the device; plan_run
+ * runs the whole horizon from u0/v0 on the given CUDA stream (a
+ * cudaStream_t passed as void*, NULL for the default stream) without any
+ * host copy; plan_download writes U/V into the args' buffers.
+ */
+typedef struct siminf_gpu_plan siminf_gpu_plan;
+
+int siminf_gpu_plan_create(const siminf_gpu_solver_args *args,
+                           const siminf_gpu_model *model,
+                           siminf_gpu_plan **out);
+int siminf_gpu_plan_run(siminf_gpu_plan *plan, void *cuda_stream);
+int siminf_gpu_plan_download(siminf_gpu_plan *plan, siminf_gpu_solver_args *args);
+int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
+void siminf_gpu_plan_free(siminf_gpu_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIMINF_GB300_H */

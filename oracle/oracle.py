@@ -1,0 +1,123 @@
+"""ctypes access to the oracle libraries (test infrastructure only).
+
+- ``liboracle.so``: the C restatement (siminf_oracle.c) of the reference's
+  ssm/mssm day loop and event engine.
+- ``_ref/libsiminf_ref.so``: the reference's own solver sources compiled
+  unmodified against stub R/GSL headers (Makefile target ``ref``); present
+  only where the reference tree was available at build time.
+
+Only the test suite, the smoke check and the CPU-baseline leg of bench.py
+may import this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libsiminf_ref.so")
+
+
+class OracleResult(C.Structure):
+    _fields_ = [
+        ("error", C.c_int),
+        ("err_node", C.c_int),
+        ("err_transition", C.c_int),
+        ("err_event", C.c_int),
+        ("err_time", C.c_double),
+        ("err_rate", C.c_double),
+        ("transitions", C.c_uint64),
+        ("node_days", C.c_uint64),
+        ("e1_events", C.c_uint64),
+        ("e2_events", C.c_uint64),
+        ("seconds_e2", C.c_double),
+    ]
+
+
+def build(ref=None):
+    """Compile liboracle.so (and _ref when the reference tree exists)."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+    ref_dir = ref or os.environ.get("SIMINF_REFERENCE", "/root/reference")
+    if os.path.isdir(os.path.join(ref_dir, "src", "solvers")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + ref_dir])
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = C.CDLL(LIB)
+        _lib.oracle_run.restype = C.c_int
+        _lib.oracle_run.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(OracleResult)]
+        _lib.oracle_si_log.restype = C.c_double
+        _lib.oracle_si_log.argtypes = [C.c_double]
+        _lib.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32]
+        _lib.oracle_uniform_pos.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_int,
+                                            C.POINTER(C.c_double)]
+        _lib.oracle_hypergeometric.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_int,
+                                               C.c_int, C.c_int, C.POINTER(C.c_int)]
+        _lib.oracle_binomial.argtypes = [C.c_uint64, C.c_uint64, C.c_double, C.c_int, C.c_int,
+                                         C.POINTER(C.c_int)]
+        assert _lib.oracle_result_size() == C.sizeof(OracleResult)
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_LIB)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        _ref = C.CDLL(REF_LIB)
+        _ref.ref_run.restype = C.c_int
+        _ref.ref_run.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+    return _ref
+
+
+def run(holder, model_name, threads=1):
+    """Run the oracle on a filled abi.ArgsHolder; returns (code, OracleResult)."""
+    res = OracleResult()
+    code = lib().oracle_run(C.cast(holder.ref(), C.c_void_p), model_name.encode(),
+                            int(threads), C.byref(res))
+    return code, res
+
+
+def run_ref(holder, model_name, threads=1):
+    """Run the reference's unmodified solver sources; returns the code."""
+    return ref_lib().ref_run(C.cast(holder.ref(), C.c_void_p), model_name.encode(), int(threads))
+
+
+def si_log(x):
+    return lib().oracle_si_log(float(x))
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    lib().oracle_philox(c, key[0], key[1])
+    return list(c)
+
+
+def uniform_pos(seed, sid, ctr, n):
+    out = np.zeros(n, dtype=np.float64)
+    lib().oracle_uniform_pos(seed, sid, ctr, n, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def hypergeometric(seed, sid, n1, n2, t, count):
+    out = np.zeros(count, dtype=np.int32)
+    lib().oracle_hypergeometric(seed, sid, n1, n2, t, count, out.ctypes.data_as(C.POINTER(C.c_int)))
+    return out
+
+
+def binomial(seed, sid, p, n, count):
+    out = np.zeros(count, dtype=np.int32)
+    lib().oracle_binomial(seed, sid, p, n, count, out.ctypes.data_as(C.POINTER(C.c_int)))
+    return out

@@ -1,0 +1,869 @@
+/*
+ * siminf_oracle.c -- CPU restatement of SimInf's ssm/mssm day loop and
+ * scheduled-event engine.  TEST INFRASTRUCTURE: only the test suite, the
+ * smoke check and the CPU-baseline leg of the benchmark load this file's
+ * library; the product (siminf_gb300/) never links it.
+ *
+ * What it restates, in the reference's order of operations:
+ *   - rate initialisation          src/solvers/SimInf_solver_ssm.c:96-117
+ *   - direct-method SSA per node    src/solvers/SimInf_solver_ssm.c:144-235
+ *   - events (E1 then E2, array order, time <= tt)
+ *                                   src/solvers/SimInf_solver.c:658-919
+ *   - sample_select                 src/solvers/SimInf_solver.c:62-214
+ *   - sample_select_enter           src/solvers/SimInf_solver.c:243-324
+ *   - post time step + rate refresh src/solvers/SimInf_solver_ssm.c:262-302
+ *   - time advance and dense store  src/solvers/SimInf_solver_ssm.c:305-334
+ *   - sparse store                  src/solvers/SimInf_solver.c:929-950,
+ *                                   src/solvers/SimInf_solver_mssm.c:332-371
+ *   - replicate loop (mssm)         src/solvers/SimInf_solver_mssm.c:105-384
+ *
+ * Random draws come from siminf_stream.h, keyed by (seed, replicate * Nn +
+ * node, draw index) instead of one GSL generator per thread, so results do
+ * not depend on the thread count.  With sorted events (R/SimInf_events.R:
+ * 398) the reference's ssm with any thread count and its mssm process a
+ * day's events in array order after the day's SSA, which is what
+ * process_events() below does.
+ *
+ * The SSA, E1 and post-time-step phases run OpenMP-parallel over nodes
+ * (one replicate) or over replicates (Nrep > 1), and the external
+ * transfers run serially, as in the reference, so that this file doubles
+ * as the CPU baseline.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#  include <omp.h>
+#endif
+
+#include "../include/siminf_gb300.h"
+#include "../siminf_gb300/csrc/siminf_stream.h"
+#include "oracle_models.h"
+
+typedef struct oracle_result {
+    int error;
+    int err_node;
+    int err_transition;
+    int err_event;
+    double err_time;
+    double err_rate;
+    uint64_t transitions;
+    uint64_t node_days;
+    uint64_t e1_events;
+    uint64_t e2_events;
+    double seconds_e2;          /* wall time of the serial E2 phase */
+} oracle_result;
+
+typedef struct ev {
+    int event, time, node, dest, n;
+    double proportion;
+    int select, shift;
+} ev;
+
+typedef struct ctx {
+    const siminf_gpu_solver_args *a;
+    const oracle_model *m;
+    ev *events;
+    int Nn, Nc, Nt, Nd, Nld;
+    uint64_t seed;
+} ctx;
+
+typedef struct rep {
+    int *u;
+    double *v, *v_new;
+    double *t_rate, *sum_t_rate, *t_time;
+    int *update_node;
+    uint64_t *ctr;              /* next draw index of each node's stream */
+    int *node_err;              /* per-node error of the current phase */
+    double *node_err_time, *node_err_rate;
+    int *node_err_tr;
+    int error, err_node, err_transition, err_event;
+    double err_time, err_rate;
+    size_t events_index;
+    int *individuals;
+} rep;
+
+static double now_seconds(void)
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
+static void set_err(rep *s, int code, int node, int tr, int evi, double t, double rate)
+{
+    s->error = code;
+    s->err_node = node;
+    s->err_transition = tr;
+    s->err_event = evi;
+    s->err_time = t;
+    s->err_rate = rate;
+}
+
+/* ------------------------------------------------------------------ */
+/* Direct-method SSA of one node up to next_unit_of_time              */
+/* (src/solvers/SimInf_solver_ssm.c:144-235).                          */
+/* Returns the number of transitions fired.                            */
+/* ------------------------------------------------------------------ */
+static uint64_t ssa_node(const ctx *c, rep *s, int r, int node, double next)
+{
+    const int Nc = c->Nc, Nt = c->Nt, Nd = c->Nd, Nld = c->Nld;
+    const siminf_gpu_solver_args *a = c->a;
+    int *u = &s->u[(size_t) node * Nc];
+    const double *v = &s->v[(size_t) node * Nd];
+    const double *ld = &a->ldata[(size_t) node * Nld];
+    double *t_rate = &s->t_rate[(size_t) node * Nt];
+    uint64_t fired = 0;
+    si_rng rng;
+
+    si_rng_init(&rng, c->seed, (uint64_t) r * c->Nn + node, s->ctr[node]);
+    for (;;) {
+        double cum, rand, tau, delta = 0.0;
+        int tr;
+
+        if (s->sum_t_rate[node] <= 0.0) {
+            s->t_time[node] = next;
+            break;
+        }
+        tau = -si_log(si_uniform_pos(&rng)) / s->sum_t_rate[node];
+        if ((tau + s->t_time[node]) >= next) {
+            s->t_time[node] = next;
+            break;
+        }
+        s->t_time[node] += tau;
+
+        rand = si_uniform_pos(&rng) * s->sum_t_rate[node];
+        tr = 0;
+        cum = t_rate[0];
+        while (tr < Nt && rand > cum) {
+            tr++;
+            if (tr < Nt)
+                cum += t_rate[tr];
+        }
+        if (tr >= Nt)
+            tr = Nt - 1;
+        if (t_rate[tr] == 0.0) {
+            for (; tr > 0 && t_rate[tr] == 0.0; tr--);
+            if (t_rate[tr] == 0.0) {
+                s->sum_t_rate[node] = 0.0;
+                break;
+            }
+        }
+
+        fired++;
+        for (int j = a->jcS[tr]; j < a->jcS[tr + 1]; j++) {
+            u[a->irS[j]] += a->prS[j];
+            if (u[a->irS[j]] < 0) {
+                s->node_err[node] = SIMINF_GPU_ERR_NEGATIVE_STATE;
+                s->node_err_time[node] = s->t_time[node];
+                s->node_err_rate[node] = 0;
+                s->node_err_tr[node] = tr;
+            }
+        }
+
+        for (int j = a->jcG[tr]; j < a->jcG[tr + 1]; j++) {
+            const int k = a->irG[j];
+            const double old = t_rate[k];
+            const double rate = c->m->tr[k](u, v, ld, a->gdata, s->t_time[node]);
+            t_rate[k] = rate;
+            delta += rate - old;
+            if (!isfinite(rate) || rate < 0.0) {
+                s->node_err[node] = SIMINF_GPU_ERR_INVALID_RATE;
+                s->node_err_time[node] = s->t_time[node];
+                s->node_err_rate[node] = rate;
+                s->node_err_tr[node] = k;
+            }
+        }
+        s->sum_t_rate[node] += delta;
+    }
+    s->ctr[node] = rng.ctr;
+    return fired;
+}
+
+/* ------------------------------------------------------------------ */
+/* Event sampling (src/solvers/SimInf_solver.c:62-324).                 */
+/* ------------------------------------------------------------------ */
+static int sample_select(const siminf_gpu_solver_args *a, int Nc, const int *u,
+                         int node, int select, int n, double proportion,
+                         int *individuals, si_rng *rng)
+{
+    const int *irE = a->irE, *jcE = a->jcE;
+    const double *prE = a->prE;
+    int i, Nstates, Nindividuals = 0, Nkinds = 0;
+
+    memset(individuals, 0, Nc * sizeof(int));
+    for (i = jcE[select]; i < jcE[select + 1]; i++) {
+        const int nk = u[node * Nc + irE[i]];
+        if (nk > 0)
+            Nkinds++;
+        Nindividuals += nk;
+    }
+    Nstates = jcE[select + 1] - jcE[select];
+
+    if (n == 0) {
+        if (proportion < 0 || proportion > 1)
+            return SIMINF_GPU_ERR_INVALID_PROPORTION;
+        n = si_binomial(rng, proportion, Nindividuals);
+    }
+    if (Nstates <= 0 || n > Nindividuals || n < 0)
+        return SIMINF_GPU_ERR_SAMPLE_SELECT;
+
+    if (n == 0)
+        return 0;
+    if (Nindividuals == n) {
+        for (i = jcE[select]; i < jcE[select + 1]; i++)
+            individuals[irE[i]] = u[node * Nc + irE[i]];
+        return 0;
+    }
+    if (Nstates == 1) {
+        individuals[irE[jcE[select]]] = n;
+        return 0;
+    }
+    if (Nkinds == 1) {
+        for (i = jcE[select]; i < jcE[select + 1]; i++) {
+            if (u[node * Nc + irE[i]] > 0) {
+                individuals[irE[i]] = n;
+                break;
+            }
+        }
+        return 0;
+    }
+
+    for (i = jcE[select] + 1; i < jcE[select + 1]; i++) {
+        if (prE[i] != prE[i - 1])
+            goto biased_urn;
+    }
+
+    /* Equal weights: sequential multivariate hypergeometric. */
+    for (i = jcE[select]; i < jcE[select + 1] - 1; i++) {
+        if (n == 0)
+            break;
+        const int nk = u[node * Nc + irE[i]];
+        individuals[irE[i]] = si_hypergeometric(rng, nk, Nindividuals - nk, n);
+        Nindividuals -= nk;
+        n -= individuals[irE[i]];
+    }
+    individuals[irE[i]] = n;
+    return 0;
+
+biased_urn:
+    /* Wallenius' noncentral hypergeometric by an urn with bias. */
+    while (n > 0) {
+        double rand, cum = 0;
+        for (i = jcE[select]; i < jcE[select + 1]; i++)
+            cum += prE[i] * (u[node * Nc + irE[i]] - individuals[irE[i]]);
+        rand = si_uniform_pos(rng) * cum;
+        i = jcE[select];
+        cum = prE[i] * (u[node * Nc + irE[i]] - individuals[irE[i]]);
+        while (i < jcE[select + 1] && rand > cum) {
+            i++;
+            if (i < jcE[select + 1])
+                cum += prE[i] * (u[node * Nc + irE[i]] - individuals[irE[i]]);
+        }
+        if (i >= jcE[select + 1])
+            i = jcE[select + 1] - 1;
+        if ((prE[i] * (u[node * Nc + irE[i]] - individuals[irE[i]])) == 0.0) {
+            for (; i > jcE[select] &&
+                     (prE[i] * (u[node * Nc + irE[i]] - individuals[irE[i]])) == 0.0;
+                 i--);
+            if ((prE[i] * (u[node * Nc + irE[i]] - individuals[irE[i]])) == 0.0)
+                return SIMINF_GPU_ERR_SAMPLE_SELECT;
+        }
+        individuals[irE[i]] += 1;
+        n--;
+    }
+    return 0;
+}
+
+static int sample_select_enter(const siminf_gpu_solver_args *a, int Nc,
+                               const int *u, int node, int select, int n,
+                               double proportion, int *individuals, si_rng *rng)
+{
+    const int *irE = a->irE, *jcE = a->jcE;
+    const double *prE = a->prE;
+    int i, Nstates = jcE[select + 1] - jcE[select];
+    double w_cum = 0;
+
+    memset(individuals, 0, Nc * sizeof(int));
+    if (n == 0) {
+        if (proportion < 0 || proportion > 1)
+            return SIMINF_GPU_ERR_INVALID_PROPORTION;
+        for (i = jcE[select]; i < jcE[select + 1]; i++)
+            n += u[node * Nc + irE[i]];
+        n = si_binomial(rng, proportion, n);
+    }
+    if (Nstates <= 0 || n < 0)
+        return SIMINF_GPU_ERR_SAMPLE_SELECT;
+    if (n == 0)
+        return 0;
+    if (Nstates == 1) {
+        individuals[irE[jcE[select]]] = n;
+        return 0;
+    }
+    for (i = jcE[select]; i < jcE[select + 1]; i++)
+        w_cum += prE[i];
+    while (n > 0) {
+        double cum, rand = si_uniform_pos(rng) * w_cum;
+        i = jcE[select];
+        cum = prE[i];
+        while (i < jcE[select + 1] && rand > cum) {
+            i++;
+            if (i < jcE[select + 1])
+                cum += prE[i];
+        }
+        if (i >= jcE[select + 1])
+            i = jcE[select + 1] - 1;
+        if (prE[i] == 0.0) {
+            for (; i > jcE[select] && prE[i] == 0.0; i--);
+            if (prE[i] == 0.0)
+                return SIMINF_GPU_ERR_SAMPLE_SELECT;
+        }
+        individuals[irE[i]] += 1;
+        n--;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Scheduled events with time <= tt, in array order                     */
+/* (src/solvers/SimInf_solver.c:658-919 with process_E2 = 1).           */
+/* ------------------------------------------------------------------ */
+static void process_events(const ctx *c, rep *s, int r, double tt,
+                           oracle_result *res, double *e2_seconds)
+{
+    const siminf_gpu_solver_args *a = c->a;
+    const int Nc = c->Nc, Ntot = c->Nn;
+    double t0 = 0.0;
+    int in_e2 = 0;
+
+    while (s->events_index < (size_t) a->len && !s->error) {
+        const ev *ee = &c->events[s->events_index];
+        const int evi = (int) s->events_index;
+        int *ind = s->individuals;
+        int err;
+        si_rng rng;
+
+        if (ee->time > tt)
+            break;
+        if (ee->node < 0 || ee->node >= Ntot) {
+            set_err(s, SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, ee->node, -1, evi, tt, 0);
+            break;
+        }
+        if (ee->event == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT && !in_e2) {
+            in_e2 = 1;
+            t0 = now_seconds();
+        }
+        si_rng_init(&rng, c->seed, (uint64_t) r * c->Nn + ee->node, s->ctr[ee->node]);
+
+        switch (ee->event) {
+        case SIMINF_GPU_EXIT_EVENT:
+            err = sample_select(a, Nc, s->u, ee->node, ee->select, ee->n,
+                                ee->proportion, ind, &rng);
+            if (err) {
+                set_err(s, err, ee->node, -1, evi, tt, 0);
+                goto done;
+            }
+            for (int i = a->jcE[ee->select]; i < a->jcE[ee->select + 1]; i++) {
+                const int jj = a->irE[i];
+                const int kn = ee->node * Nc + jj;
+                s->u[kn] -= ind[jj];
+                if (s->u[kn] < 0) {
+                    set_err(s, SIMINF_GPU_ERR_NEGATIVE_STATE, ee->node, -1, evi, tt, 0);
+                    goto done;
+                }
+            }
+            break;
+
+        case SIMINF_GPU_ENTER_EVENT:
+            err = sample_select_enter(a, Nc, s->u, ee->node, ee->select, ee->n,
+                                      ee->proportion, ind, &rng);
+            if (err) {
+                set_err(s, err, ee->node, -1, evi, tt, 0);
+                goto done;
+            }
+            for (int i = a->jcE[ee->select]; i < a->jcE[ee->select + 1]; i++) {
+                const int jj = a->irE[i];
+                const int kn = ee->node * Nc + jj;
+                if (ee->shift < 0) {
+                    s->u[kn] += ind[jj];
+                    if (s->u[kn] < 0) {
+                        set_err(s, SIMINF_GPU_ERR_NEGATIVE_STATE, ee->node, -1, evi, tt, 0);
+                        goto done;
+                    }
+                } else if (!a->N) {
+                    set_err(s, SIMINF_GPU_ERR_EVENTS_N, ee->node, -1, evi, tt, 0);
+                    goto done;
+                } else {
+                    const int ll = a->N[ee->shift * Nc + jj];
+                    if (jj + ll < 0 || jj + ll >= Nc) {
+                        set_err(s, SIMINF_GPU_ERR_SHIFT_OUT_OF_BOUNDS, ee->node, -1, evi, tt, 0);
+                        goto done;
+                    }
+                    s->u[kn + ll] += ind[jj];
+                    if (s->u[kn + ll] < 0) {
+                        set_err(s, SIMINF_GPU_ERR_NEGATIVE_STATE, ee->node, -1, evi, tt, 0);
+                        goto done;
+                    }
+                }
+            }
+            break;
+
+        case SIMINF_GPU_INTERNAL_TRANSFER_EVENT:
+            if (!a->N) {
+                set_err(s, SIMINF_GPU_ERR_EVENTS_N, ee->node, -1, evi, tt, 0);
+                goto done;
+            }
+            if (ee->shift < 0) {
+                set_err(s, SIMINF_GPU_ERR_EVENT_SHIFT, ee->node, -1, evi, tt, 0);
+                goto done;
+            }
+            err = sample_select(a, Nc, s->u, ee->node, ee->select, ee->n,
+                                ee->proportion, ind, &rng);
+            if (err) {
+                set_err(s, err, ee->node, -1, evi, tt, 0);
+                goto done;
+            }
+            for (int i = a->jcE[ee->select]; i < a->jcE[ee->select + 1]; i++) {
+                const int jj = a->irE[i];
+                const int kn = ee->node * Nc + jj;
+                const int ll = a->N[ee->shift * Nc + jj];
+                if (jj + ll < 0 || jj + ll >= Nc) {
+                    set_err(s, SIMINF_GPU_ERR_SHIFT_OUT_OF_BOUNDS, ee->node, -1, evi, tt, 0);
+                    goto done;
+                }
+                s->u[kn + ll] += ind[jj];
+                if (s->u[kn + ll] < 0) {
+                    set_err(s, SIMINF_GPU_ERR_NEGATIVE_STATE, ee->node, -1, evi, tt, 0);
+                    goto done;
+                }
+                s->u[kn] -= ind[jj];
+                if (s->u[kn] < 0) {
+                    set_err(s, SIMINF_GPU_ERR_NEGATIVE_STATE, ee->node, -1, evi, tt, 0);
+                    goto done;
+                }
+            }
+            break;
+
+        case SIMINF_GPU_EXTERNAL_TRANSFER_EVENT:
+            if (ee->dest < 0 || ee->dest >= Ntot) {
+                set_err(s, SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS, ee->node, -1, evi, tt, 0);
+                goto done;
+            }
+            err = sample_select(a, Nc, s->u, ee->node, ee->select, ee->n,
+                                ee->proportion, ind, &rng);
+            if (err) {
+                set_err(s, err, ee->node, -1, evi, tt, 0);
+                goto done;
+            }
+            for (int i = a->jcE[ee->select]; i < a->jcE[ee->select + 1]; i++) {
+                const int jj = a->irE[i];
+                const int kd = ee->dest * Nc + jj;
+                const int kn = ee->node * Nc + jj;
+                if (ee->shift < 0) {
+                    s->u[kd] += ind[jj];
+                    if (s->u[kd] < 0) {
+                        set_err(s, SIMINF_GPU_ERR_NEGATIVE_STATE, ee->node, -1, evi, tt, 0);
+                        goto done;
+                    }
+                } else if (!a->N) {
+                    set_err(s, SIMINF_GPU_ERR_EVENTS_N, ee->node, -1, evi, tt, 0);
+                    goto done;
+                } else {
+                    const int ll = a->N[ee->shift * Nc + jj];
+                    if (jj + ll < 0 || jj + ll >= Nc) {
+                        set_err(s, SIMINF_GPU_ERR_SHIFT_OUT_OF_BOUNDS, ee->node, -1, evi, tt, 0);
+                        goto done;
+                    }
+                    s->u[kd + ll] += ind[jj];
+                    if (s->u[kd + ll] < 0) {
+                        set_err(s, SIMINF_GPU_ERR_NEGATIVE_STATE, ee->node, -1, evi, tt, 0);
+                        goto done;
+                    }
+                }
+                s->u[kn] -= ind[jj];
+                if (s->u[kn] < 0) {
+                    set_err(s, SIMINF_GPU_ERR_NEGATIVE_STATE, ee->node, -1, evi, tt, 0);
+                    goto done;
+                }
+            }
+            s->update_node[ee->dest] = 1;
+            break;
+
+        default:
+            set_err(s, SIMINF_GPU_UNDEFINED_EVENT, ee->node, -1, evi, tt, 0);
+            break;
+        }
+
+        s->ctr[ee->node] = rng.ctr;
+        s->update_node[ee->node] = 1;
+        if (ee->event == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
+            res->e2_events++;
+        else
+            res->e1_events++;
+        s->events_index++;
+        continue;
+done:
+        s->ctr[ee->node] = rng.ctr;
+        break;
+    }
+    if (in_e2 && e2_seconds)
+        *e2_seconds += now_seconds() - t0;
+}
+
+/* Rate refresh of one node after the post-time-step function
+ * (src/solvers/SimInf_solver_ssm.c:262-301).  Returns the pts rc. */
+static int pts_node(const ctx *c, rep *s, int node, double tt)
+{
+    const int Nc = c->Nc, Nt = c->Nt, Nd = c->Nd, Nld = c->Nld;
+    const siminf_gpu_solver_args *a = c->a;
+    const int rc = c->m->pts(&s->v_new[(size_t) node * Nd], &s->u[(size_t) node * Nc],
+                             &s->v[(size_t) node * Nd], &a->ldata[(size_t) node * Nld],
+                             a->gdata, node, tt);
+    if (rc < 0) {
+        s->node_err[node] = rc;
+        s->node_err_time[node] = tt;
+        s->node_err_tr[node] = -1;
+        s->node_err_rate[node] = 0;
+        return rc;
+    }
+    if (rc > 0 || s->update_node[node]) {
+        double delta = 0.0;
+        double *t_rate = &s->t_rate[(size_t) node * Nt];
+        for (int j = 0; j < Nt; j++) {
+            const double old = t_rate[j];
+            const double rate = c->m->tr[j](&s->u[(size_t) node * Nc],
+                                            &s->v_new[(size_t) node * Nd],
+                                            &a->ldata[(size_t) node * Nld],
+                                            a->gdata, tt);
+            t_rate[j] = rate;
+            delta += rate - old;
+            if (!isfinite(rate) || rate < 0.0) {
+                s->node_err[node] = SIMINF_GPU_ERR_INVALID_RATE;
+                s->node_err_time[node] = tt;
+                s->node_err_rate[node] = rate;
+                s->node_err_tr[node] = j;
+            }
+        }
+        s->sum_t_rate[node] += delta;
+        s->update_node[node] = 0;
+    }
+    return rc;
+}
+
+static void store(const ctx *c, rep *s, int r, int *U_it, int *V_it, double tt)
+{
+    const siminf_gpu_solver_args *a = c->a;
+    const size_t Nn = (size_t) c->Nn, Nc = (size_t) c->Nc, Nd = (size_t) c->Nd;
+    const size_t col0 = (size_t) r * a->tlen;
+
+    while (*U_it < a->tlen && tt > a->tspan[*U_it]) {
+        if (a->U) {
+            memcpy(&a->U[(col0 + *U_it) * Nn * Nc], s->u, Nn * Nc * sizeof(int));
+        } else if (a->jcU) {
+            for (int j = a->jcU[col0 + *U_it]; j < a->jcU[col0 + *U_it + 1]; j++)
+                a->prU[j] = s->u[a->irU[j]];
+        }
+        (*U_it)++;
+    }
+    while (*V_it < a->tlen && tt > a->tspan[*V_it]) {
+        if (a->V) {
+            if (Nd > 0)
+                memcpy(&a->V[(col0 + *V_it) * Nn * Nd], s->v_new, Nn * Nd * sizeof(double));
+        } else if (a->jcV) {
+            for (int j = a->jcV[col0 + *V_it]; j < a->jcV[col0 + *V_it + 1]; j++)
+                a->prV[j] = s->v_new[a->irV[j]];
+        }
+        (*V_it)++;
+    }
+}
+
+/* Lowest node with an error in the SSA phase decides the code, as with
+ * one reference thread: later nodes of that day are not simulated. */
+static void resolve_ssa_errors(const ctx *c, rep *s)
+{
+    for (int node = 0; node < c->Nn; node++) {
+        if (s->node_err[node]) {
+            set_err(s, s->node_err[node], node, s->node_err_tr[node], -1,
+                    s->node_err_time[node], s->node_err_rate[node]);
+            return;
+        }
+    }
+}
+
+/* One reference thread walks the post-time-step loop in node order: a
+ * negative rc stops it, an invalid rate is recorded and the walk goes on. */
+static void resolve_pts_errors(const ctx *c, rep *s)
+{
+    for (int node = 0; node < c->Nn; node++) {
+        const int e = s->node_err[node];
+        if (!e)
+            continue;
+        set_err(s, e, node, s->node_err_tr[node], -1, s->node_err_time[node],
+                s->node_err_rate[node]);
+        if (e != SIMINF_GPU_ERR_INVALID_RATE)
+            return;
+    }
+}
+
+static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
+                         oracle_result *res)
+{
+    const siminf_gpu_solver_args *a = c->a;
+    const int Nn = c->Nn, Nc = c->Nc, Nt = c->Nt, Nd = c->Nd, Nld = c->Nld;
+    double tt = a->tspan[0];
+    double next = floor(tt) + 1.0;
+    int U_it = 0, V_it = 0;
+    uint64_t fired = 0;
+    int any_err = 0;
+
+    memcpy(s->u, &a->u0[(size_t) r * Nn * Nc], (size_t) Nn * Nc * sizeof(int));
+    if (Nd > 0) {
+        memcpy(s->v, &a->v0[(size_t) r * Nn * Nd], (size_t) Nn * Nd * sizeof(double));
+        memcpy(s->v_new, &a->v0[(size_t) r * Nn * Nd], (size_t) Nn * Nd * sizeof(double));
+    }
+    memset(s->update_node, 0, Nn * sizeof(int));
+    memset(s->ctr, 0, Nn * sizeof(uint64_t));
+    memset(s->node_err, 0, Nn * sizeof(int));
+    s->error = 0;
+    s->events_index = 0;
+
+    /* Rates at the start (src/solvers/SimInf_solver_ssm.c:96-117). */
+#pragma omp parallel for schedule(static) if (parallel_nodes) reduction(|:any_err)
+    for (int node = 0; node < Nn; node++) {
+        s->sum_t_rate[node] = 0.0;
+        for (int j = 0; j < Nt; j++) {
+            const double rate = c->m->tr[j](&s->u[(size_t) node * Nc], &s->v[(size_t) node * Nd],
+                                            &a->ldata[(size_t) node * Nld], a->gdata, tt);
+            s->t_rate[(size_t) node * Nt + j] = rate;
+            s->sum_t_rate[node] += rate;
+            if (!isfinite(rate) || rate < 0.0) {
+                s->node_err[node] = SIMINF_GPU_ERR_INVALID_RATE;
+                s->node_err_time[node] = tt;
+                s->node_err_rate[node] = rate;
+                s->node_err_tr[node] = j;
+                any_err = 1;
+            }
+        }
+        s->t_time[node] = tt;
+    }
+    if (any_err) {
+        /* Every node is initialised; the last failing node's message is
+         * printed last, the code is the same for all. */
+        resolve_ssa_errors(c, s);
+        return s->error;
+    }
+
+    for (;;) {
+        /* (1) SSA per node. */
+        any_err = 0;
+#pragma omp parallel for schedule(static) if (parallel_nodes) reduction(+:fired) reduction(|:any_err)
+        for (int node = 0; node < Nn; node++) {
+            fired += ssa_node(c, s, r, node, next);
+            any_err |= (s->node_err[node] != 0);
+        }
+        res->node_days += (uint64_t) Nn;
+        if (any_err)
+            resolve_ssa_errors(c, s);
+
+        /* (2, 3) Scheduled events. */
+        process_events(c, s, r, tt, res, &res->seconds_e2);
+
+        /* (4) Post time step and rate refresh for every node. */
+        memset(s->node_err, 0, Nn * sizeof(int));
+        any_err = 0;
+#pragma omp parallel for schedule(static) if (parallel_nodes) reduction(|:any_err)
+        for (int node = 0; node < Nn; node++) {
+            pts_node(c, s, node, tt);
+            any_err |= (s->node_err[node] != 0);
+        }
+        if (any_err)
+            resolve_pts_errors(c, s);
+
+        /* (5) Advance time, (6) store. */
+        tt = next;
+        next += 1.0;
+        store(c, s, r, &U_it, &V_it, tt);
+
+        double *tmp = s->v;
+        s->v = s->v_new;
+        s->v_new = tmp;
+
+        if (s->error)
+            break;
+        if (U_it >= a->tlen)
+            break;
+    }
+    res->transitions += fired;
+    return s->error;
+}
+
+static int rep_alloc(rep *s, int Nn, int Nc, int Nt, int Nd)
+{
+    memset(s, 0, sizeof(*s));
+    s->u = malloc((size_t) Nn * Nc * sizeof(int) + 1);
+    s->v = malloc((size_t) Nn * Nd * sizeof(double) + 8);
+    s->v_new = malloc((size_t) Nn * Nd * sizeof(double) + 8);
+    s->t_rate = malloc((size_t) Nn * Nt * sizeof(double) + 8);
+    s->sum_t_rate = malloc((size_t) Nn * sizeof(double) + 8);
+    s->t_time = malloc((size_t) Nn * sizeof(double) + 8);
+    s->update_node = malloc((size_t) Nn * sizeof(int) + 4);
+    s->ctr = malloc((size_t) Nn * sizeof(uint64_t) + 8);
+    s->node_err = malloc((size_t) Nn * sizeof(int) + 4);
+    s->node_err_time = malloc((size_t) Nn * sizeof(double) + 8);
+    s->node_err_rate = malloc((size_t) Nn * sizeof(double) + 8);
+    s->node_err_tr = malloc((size_t) Nn * sizeof(int) + 4);
+    s->individuals = malloc((size_t) Nc * sizeof(int) + 4);
+    return (s->u && s->v && s->v_new && s->t_rate && s->sum_t_rate && s->t_time &&
+            s->update_node && s->ctr && s->node_err && s->node_err_time &&
+            s->node_err_rate && s->node_err_tr && s->individuals) ? 0 : -1;
+}
+
+static void rep_free(rep *s)
+{
+    free(s->u); free(s->v); free(s->v_new); free(s->t_rate); free(s->sum_t_rate);
+    free(s->t_time); free(s->update_node); free(s->ctr); free(s->node_err);
+    free(s->node_err_time); free(s->node_err_rate); free(s->node_err_tr);
+    free(s->individuals);
+}
+
+/*
+ * Run every replicate of args with the named host model.  nthreads <= 0
+ * uses the OpenMP default.  Returns 0 or the first failing replicate's
+ * error code; res receives counters and the failure's diagnostics.
+ */
+int oracle_run(const siminf_gpu_solver_args *args, const char *model_name,
+               int nthreads, oracle_result *res)
+{
+    ctx c;
+    int err = 0;
+
+    memset(res, 0, sizeof(*res));
+    c.m = oracle_model_lookup(model_name);
+    if (!c.m)
+        return SIMINF_GPU_ERR_UNKNOWN_MODEL;
+    if (args->Nc != c.m->Nc || args->Nt != c.m->Nt || args->Nd != c.m->Nd)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    c.a = args;
+    c.Nn = args->Nn;
+    c.Nc = args->Nc;
+    c.Nt = args->Nt;
+    c.Nd = args->Nd;
+    c.Nld = args->Nld;
+    c.seed = (uint64_t) args->seed;
+#ifdef _OPENMP
+    if (nthreads > 0)
+        omp_set_num_threads(nthreads);
+#else
+    (void) nthreads;
+#endif
+
+    /* Zero-based events (src/solvers/SimInf_solver.c:371-374). */
+    c.events = malloc(((size_t) args->len + 1) * sizeof(ev));
+    if (!c.events)
+        return SIMINF_GPU_ERR_ALLOC_MEMORY_BUFFER;
+    for (int i = 0; i < args->len; i++) {
+        ev e = {args->event[i], args->time[i], args->node[i] - 1, args->dest[i] - 1,
+                args->n[i], args->proportion[i], args->select[i] - 1, args->shift[i] - 1};
+        c.events[i] = e;
+    }
+
+    const int Nrep = args->Nrep > 0 ? args->Nrep : 1;
+    if (Nrep == 1) {
+        rep s;
+        if (rep_alloc(&s, c.Nn, c.Nc, c.Nt, c.Nd)) {
+            rep_free(&s);
+            free(c.events);
+            return SIMINF_GPU_ERR_ALLOC_MEMORY_BUFFER;
+        }
+        err = run_replicate(&c, &s, 0, 1, res);
+        if (err) {
+            res->err_node = s.err_node;
+            res->err_transition = s.err_transition;
+            res->err_event = s.err_event;
+            res->err_time = s.err_time;
+            res->err_rate = s.err_rate;
+        }
+        rep_free(&s);
+    } else {
+        int *errs = calloc((size_t) Nrep, sizeof(int));
+        oracle_result *rr = calloc((size_t) Nrep, sizeof(oracle_result));
+        rep *ss = calloc((size_t) Nrep, sizeof(rep));
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int r = 0; r < Nrep; r++) {
+            if (rep_alloc(&ss[r], c.Nn, c.Nc, c.Nt, c.Nd)) {
+                errs[r] = SIMINF_GPU_ERR_ALLOC_MEMORY_BUFFER;
+            } else {
+                errs[r] = run_replicate(&c, &ss[r], r, 0, &rr[r]);
+                rr[r].err_node = ss[r].err_node;
+                rr[r].err_transition = ss[r].err_transition;
+                rr[r].err_event = ss[r].err_event;
+                rr[r].err_time = ss[r].err_time;
+                rr[r].err_rate = ss[r].err_rate;
+            }
+            rep_free(&ss[r]);
+        }
+        for (int r = 0; r < Nrep; r++) {
+            res->transitions += rr[r].transitions;
+            res->node_days += rr[r].node_days;
+            res->e1_events += rr[r].e1_events;
+            res->e2_events += rr[r].e2_events;
+            res->seconds_e2 += rr[r].seconds_e2;
+            if (!err && errs[r]) {
+                err = errs[r];
+                res->err_node = rr[r].err_node;
+                res->err_transition = rr[r].err_transition;
+                res->err_event = rr[r].err_event;
+                res->err_time = rr[r].err_time;
+                res->err_rate = rr[r].err_rate;
+            }
+        }
+        free(errs);
+        free(rr);
+        free(ss);
+    }
+    free(c.events);
+    res->error = err;
+    return err;
+}
+
+/* ------------------------------------------------------------------ */
+/* Wrappers of the shared random source, for the test suite.            */
+/* ------------------------------------------------------------------ */
+double oracle_si_log(double x) { return si_log(x); }
+
+void oracle_philox(uint32_t *ctr4, uint32_t k0, uint32_t k1)
+{
+    si_philox4x32_10(&ctr4[0], &ctr4[1], &ctr4[2], &ctr4[3], k0, k1);
+}
+
+void oracle_uniform_pos(uint64_t seed, uint64_t sid, uint64_t ctr, int n, double *out)
+{
+    si_rng r;
+    si_rng_init(&r, seed, sid, ctr);
+    for (int i = 0; i < n; i++)
+        out[i] = si_uniform_pos(&r);
+}
+
+void oracle_hypergeometric(uint64_t seed, uint64_t sid, int n1, int n2, int t,
+                           int count, int *out)
+{
+    si_rng r;
+    si_rng_init(&r, seed, sid, 0);
+    for (int i = 0; i < count; i++)
+        out[i] = si_hypergeometric(&r, n1, n2, t);
+}
+
+void oracle_binomial(uint64_t seed, uint64_t sid, double p, int n, int count, int *out)
+{
+    si_rng r;
+    si_rng_init(&r, seed, sid, 0);
+    for (int i = 0; i < count; i++)
+        out[i] = si_binomial(&r, p, n);
+}
+
+int oracle_result_size(void) { return (int) sizeof(oracle_result); }
+int oracle_args_size(void) { return (int) sizeof(siminf_gpu_solver_args); }

@@ -1,0 +1,66 @@
+"""Generate the constant tables of the integer fixed-point logarithm in
+siminf_stream.h (``si_log``).
+
+The logarithm is evaluated as ln(x) = K*ln(2) + L_j + ln(1 + z), where
+x = 2^e * f, f in [1, 2), j = the top 7 fraction bits of f, and
+z = f * R_j / 2^10 - 1 is exact in 64-bit integer arithmetic because
+R_j has at most 11 bits.  This script prints R_j, L_j = ln(2^10 / R_j)
+in Q64, ln(2) to 128 bits and the Q62 Taylor coefficients of
+ln(1+z)/z = sum_i (-1)^i z^i / (i+1), using mpmath at 200 bits so the
+constants are correctly rounded.
+
+Run:  python siminf_gb300/csrc/gen_log_table.py > siminf_gb300/csrc/siminf_log_table.h
+"""
+import mpmath as mp
+
+mp.mp.prec = 200
+
+
+def q(x, bits):
+    return int(mp.nint(x * mp.mpf(2) ** bits))
+
+
+def main():
+    R, L, D = [], [], []
+    for j in range(128):
+        if j == 0:
+            r, d = 1024, 0           # f in [1, 1+1/128): z = f - 1 exactly
+        elif j == 127:
+            r, d = 512, 1            # f in [2-1/128, 2): ln f = ln 2 + ln(f/2)
+        else:
+            c = 1 + (mp.mpf(j) + mp.mpf("0.5")) / 128
+            r, d = int(mp.nint(1024 / c)), 0
+        R.append(r)
+        D.append(d)
+        lj = mp.log(mp.mpf(1024) / r) - d * mp.log(2)
+        L.append(q(lj, 64))
+    ln2 = q(mp.log(2), 128)
+    coef = [q(mp.mpf((-1) ** i) / (i + 1), 62) for i in range(9)]
+    out = []
+    out.append("/* Generated by gen_log_table.py: constants of si_log (do not edit). */")
+    out.append("#ifndef SIMINF_LOG_TABLE_H")
+    out.append("#define SIMINF_LOG_TABLE_H")
+    out.append("#define SI_LN2_Q128_HI 0x%016xULL" % (ln2 >> 64))
+    out.append("#define SI_LN2_Q128_LO 0x%016xULL" % (ln2 & (2 ** 64 - 1)))
+    out.append("/* R_j | (delta_j << 16): reciprocal of the bucket centre in Q10. */")
+    out.append("#define SI_LOG_R_INIT { \\")
+    for i in range(0, 128, 8):
+        out.append("    " + ", ".join("0x%05xu" % (R[k] | (D[k] << 16)) for k in range(i, i + 8)) + ", \\")
+    out.append("}")
+    out.append("/* L_j = ln(2^10 / R_j) - delta_j ln 2 in Q64 (unsigned, 0 <= L_j < 1). */")
+    out.append("#define SI_LOG_L_INIT { \\")
+    for i in range(0, 128, 4):
+        out.append("    " + ", ".join("0x%016xULL" % L[k] for k in range(i, i + 4)) + ", \\")
+    out.append("}")
+    out.append("/* (-1)^i / (i+1) in Q62, i = 0..8. */")
+    for i, c in enumerate(coef):
+        if c < 0:
+            out.append("#define SI_LOG_C%d (-(int64_t)0x%016xLL)" % (i, -c))
+        else:
+            out.append("#define SI_LOG_C%d ((int64_t)0x%016xLL)" % (i, c))
+    out.append("#endif")
+    print("\n".join(out))
+
+
+if __name__ == "__main__":
+    main()

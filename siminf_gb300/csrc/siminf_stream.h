@@ -1,0 +1,442 @@
+/*
+ * siminf_stream.h -- the random source of the solver, shared by the CUDA
+ * kernels and by host C code.
+ *
+ * The reference solver draws from one GSL generator per OpenMP thread
+ * (src/solvers/SimInf_solver.c:474-477) through three calls:
+ * gsl_rng_uniform_pos (src/solvers/SimInf_solver_ssm.c:155,165,
+ * src/solvers/SimInf_solver.c:184,298), gsl_ran_binomial
+ * (src/solvers/SimInf_solver.c:98,274) and gsl_ran_hypergeometric
+ * (src/solvers/SimInf_solver.c:149).  Here every draw comes instead from a
+ * counter-based stream keyed by (seed, stream id, draw index), where the
+ * stream id is replicate * Nn + node.  A node's draws therefore do not
+ * depend on how nodes are split over threads, warps or kernels, which is
+ * what lets a GPU run reproduce a CPU run bit for bit.
+ *
+ *  - Philox4x32-10: J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw,
+ *    "Parallel random numbers: as easy as 1, 2, 3", SC 2011.
+ *  - uniform_pos: (2w + 1) * 2^-33 for a 32-bit word w, so 0 < u < 1 with
+ *    the 32-bit resolution of a 32-bit Mersenne twister draw.
+ *  - si_log: natural logarithm by table reduction (Tang's method: x =
+ *    2^e f, f ~ c_j, ln f = -ln r_j + ln(1 + (f r_j - 1))) followed by the
+ *    Taylor series of ln(1+z)/z, all in 64/128-bit integer fixed point.
+ *    Pure integer arithmetic makes it bit-identical on every CPU and GPU,
+ *    and on GB300 integer ALUs are ~40x faster than the FP64 pipe.
+ *  - si_hypergeometric: sequential urn draws without replacement (one
+ *    word per draw, compared exactly in integers), sampling the smaller of
+ *    the draw and its complement.
+ *  - si_binomial: sequential-search inversion (L. Devroye, Non-Uniform
+ *    Random Variate Generation, 1986, ch. X.4) on chunks of at most 512
+ *    trials, summed; Binomial(a + b, p) = Binomial(a, p) + Binomial(b, p).
+ *
+ * The header compiles as C99 (gcc) and as CUDA C++ (nvcc).  Host code that
+ * includes it must be compiled with -ffp-contract=off and device code with
+ * -fmad=false so that the few floating-point operations round identically.
+ */
+#ifndef SIMINF_STREAM_H
+#define SIMINF_STREAM_H
+
+#include <stdint.h>
+#ifndef __CUDACC__
+#  include <string.h>
+#endif
+
+#include "siminf_log_table.h"
+
+#ifdef __CUDACC__
+#  define SI_HD __host__ __device__ __forceinline__
+#else
+#  define SI_HD static inline
+#endif
+
+/* ---------------------------------------------------------------- */
+/* Integer helpers that give the same bits on host and device.       */
+/* ---------------------------------------------------------------- */
+
+SI_HD uint64_t si_double_bits(double x)
+{
+#ifdef __CUDA_ARCH__
+    return (uint64_t) __double_as_longlong(x);
+#else
+    uint64_t b;
+    memcpy(&b, &x, sizeof(b));
+    return b;
+#endif
+}
+
+SI_HD double si_bits_double(uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long) b);
+#else
+    double x;
+    memcpy(&x, &b, sizeof(x));
+    return x;
+#endif
+}
+
+SI_HD uint32_t si_umulhi32(uint32_t a, uint32_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t) (((uint64_t) a * b) >> 32);
+#endif
+}
+
+/* High 64 bits of the unsigned 128-bit product. */
+SI_HD uint64_t si_umulhi64(uint64_t a, uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __umul64hi(a, b);
+#else
+    return (uint64_t) (((unsigned __int128) a * b) >> 64);
+#endif
+}
+
+/* High 64 bits of the signed 128-bit product (floor of a*b / 2^64). */
+SI_HD int64_t si_mulhi64(int64_t a, int64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return (int64_t) __mul64hi((long long) a, (long long) b);
+#else
+    return (int64_t) (((__int128) a * b) >> 64);
+#endif
+}
+
+SI_HD int si_clz64(uint64_t x)
+{
+#ifdef __CUDA_ARCH__
+    return __clzll((long long) x);
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+/* floor(a * b / 2^62) for signed Q62 operands whose product fits. */
+SI_HD int64_t si_mul_q62(int64_t a, int64_t b)
+{
+    const uint64_t hi = (uint64_t) si_mulhi64(a, b);
+    const uint64_t lo = (uint64_t) a * (uint64_t) b;
+    return (int64_t) ((hi << 2) | (lo >> 62));
+}
+
+/* ---------------------------------------------------------------- */
+/* Philox4x32-10.                                                    */
+/* ---------------------------------------------------------------- */
+
+#define SI_PHILOX_M0 0xD2511F53u
+#define SI_PHILOX_M1 0xCD9E8D57u
+#define SI_PHILOX_W0 0x9E3779B9u
+#define SI_PHILOX_W1 0xBB67AE85u
+
+SI_HD void si_philox4x32_10(uint32_t *c0, uint32_t *c1, uint32_t *c2,
+                            uint32_t *c3, uint32_t k0, uint32_t k1)
+{
+    uint32_t x0 = *c0, x1 = *c1, x2 = *c2, x3 = *c3;
+#ifdef __CUDA_ARCH__
+#  pragma unroll
+#endif
+    for (int round = 0; round < 10; round++) {
+        const uint32_t hi0 = si_umulhi32(SI_PHILOX_M0, x0);
+        const uint32_t lo0 = SI_PHILOX_M0 * x0;
+        const uint32_t hi1 = si_umulhi32(SI_PHILOX_M1, x2);
+        const uint32_t lo1 = SI_PHILOX_M1 * x2;
+        const uint32_t y0 = hi1 ^ x1 ^ k0;
+        const uint32_t y2 = hi0 ^ x3 ^ k1;
+        x0 = y0;
+        x1 = lo1;
+        x2 = y2;
+        x3 = lo0;
+        k0 += SI_PHILOX_W0;
+        k1 += SI_PHILOX_W1;
+    }
+    *c0 = x0;
+    *c1 = x1;
+    *c2 = x2;
+    *c3 = x3;
+}
+
+/* ---------------------------------------------------------------- */
+/* The per-node stream.                                              */
+/* ---------------------------------------------------------------- */
+
+/* Draw i of stream sid under seed is word (i & 3) of
+ * Philox4x32-10(counter = {i >> 2 (64 bits), sid (64 bits)},
+ *               key = seed (64 bits)). */
+typedef struct si_rng {
+    uint32_t k0, k1;            /* seed */
+    uint32_t s0, s1;            /* stream id */
+    uint64_t ctr;               /* index of the next draw */
+    uint32_t b0, b1, b2, b3;    /* block holding draw ctr when ctr & 3 != 0 */
+} si_rng;
+
+SI_HD void si_rng_fill(si_rng *r)
+{
+    const uint64_t blk = r->ctr >> 2;
+    uint32_t c0 = (uint32_t) blk, c1 = (uint32_t) (blk >> 32);
+    uint32_t c2 = r->s0, c3 = r->s1;
+    si_philox4x32_10(&c0, &c1, &c2, &c3, r->k0, r->k1);
+    r->b0 = c0;
+    r->b1 = c1;
+    r->b2 = c2;
+    r->b3 = c3;
+}
+
+SI_HD void si_rng_init(si_rng *r, uint64_t seed, uint64_t sid, uint64_t ctr)
+{
+    r->k0 = (uint32_t) seed;
+    r->k1 = (uint32_t) (seed >> 32);
+    r->s0 = (uint32_t) sid;
+    r->s1 = (uint32_t) (sid >> 32);
+    r->ctr = ctr;
+    r->b0 = r->b1 = r->b2 = r->b3 = 0;
+    if (ctr & 3)
+        si_rng_fill(r);
+}
+
+SI_HD uint32_t si_next_u32(si_rng *r)
+{
+    const uint32_t i = (uint32_t) r->ctr & 3u;
+    if (i == 0)
+        si_rng_fill(r);
+    const uint32_t w = (i == 0) ? r->b0 : (i == 1) ? r->b1 : (i == 2) ? r->b2 : r->b3;
+    r->ctr++;
+    return w;
+}
+
+/* Word w -> (2w + 1) * 2^-33, built from integer bits (exact). */
+SI_HD double si_u32_to_uniform_pos(uint32_t w)
+{
+    const uint64_t v = 2 * (uint64_t) w + 1;          /* 1 .. 2^33 - 1 */
+    const int p = 63 - si_clz64(v);                    /* 0 .. 32 */
+    const uint64_t mant = v << (52 - p);
+    const uint64_t expo = (uint64_t) (p - 33 + 1023);
+    return si_bits_double((expo << 52) | (mant & 0x000FFFFFFFFFFFFFULL));
+}
+
+SI_HD double si_uniform_pos(si_rng *r)
+{
+    return si_u32_to_uniform_pos(si_next_u32(r));
+}
+
+/* ---------------------------------------------------------------- */
+/* Natural logarithm in integer fixed point.                         */
+/* ---------------------------------------------------------------- */
+
+/* |M| * 2^-scale, M = (hi, lo) unsigned 128-bit, to the nearest double
+ * (ties to even).  The caller guarantees a result in the normal range. */
+SI_HD double si_u128_to_double(uint64_t hi, uint64_t lo, int scale, int negative)
+{
+    const uint64_t sign = negative ? 0x8000000000000000ULL : 0;
+    if (hi == 0 && lo == 0)
+        return si_bits_double(sign);
+    const int p = hi ? 127 - si_clz64(hi) : 63 - si_clz64(lo);
+    uint64_t m;
+    int e = p;
+    if (p <= 52) {
+        m = lo << (52 - p);
+    } else {
+        const int sh = p - 52;                 /* 1 .. 75 */
+        uint64_t rnd, sticky;
+        if (sh < 64) {
+            m = (lo >> sh) | (sh ? (hi << (64 - sh)) : 0);
+            rnd = (lo >> (sh - 1)) & 1;
+            sticky = (sh > 1) ? (lo & ((1ULL << (sh - 1)) - 1)) : 0;
+        } else if (sh == 64) {
+            m = hi;
+            rnd = lo >> 63;
+            sticky = lo & 0x7FFFFFFFFFFFFFFFULL;
+        } else {
+            m = hi >> (sh - 64);
+            rnd = (hi >> (sh - 65)) & 1;
+            sticky = (hi & ((1ULL << (sh - 65)) - 1)) | lo;
+        }
+        m += rnd & ((sticky != 0) | (m & 1));
+        if (m >> 53) {
+            m >>= 1;
+            e++;
+        }
+    }
+    const uint64_t expo = (uint64_t) (e - scale + 1023);
+    return si_bits_double(sign | (expo << 52) | (m & 0x000FFFFFFFFFFFFFULL));
+}
+
+#ifdef __CUDA_ARCH__
+static __device__ const uint32_t si_log_r_dev[128] = SI_LOG_R_INIT;
+static __device__ const uint64_t si_log_l_dev[128] = SI_LOG_L_INIT;
+#  define SI_LOG_R(j) si_log_r_dev[j]
+#  define SI_LOG_L(j) si_log_l_dev[j]
+#else
+static const uint32_t si_log_r_host[128] = SI_LOG_R_INIT;
+static const uint64_t si_log_l_host[128] = SI_LOG_L_INIT;
+#  define SI_LOG_R(j) si_log_r_host[j]
+#  define SI_LOG_L(j) si_log_l_host[j]
+#endif
+
+/* ln(x) for a double x: -inf at 0, NaN below 0 or for NaN, +inf at +inf.
+ * Error below one unit in the last place over the positive doubles
+ * (checked against a 200-bit reference in the test suite). */
+SI_HD double si_log(double x)
+{
+    const uint64_t bits = si_double_bits(x);
+    const uint32_t bexp = (uint32_t) (bits >> 52) & 0x7FFu;
+    uint64_t F = bits & 0x000FFFFFFFFFFFFFULL;
+    int e;
+
+    if (bits >> 63) {
+        if ((bits << 1) == 0)
+            return si_bits_double(0xFFF0000000000000ULL);   /* -0 -> -inf */
+        return si_bits_double(0x7FF8000000000000ULL);       /* x < 0 -> NaN */
+    }
+    if (bexp == 0x7FF)
+        return x + x;                                        /* inf or NaN */
+    if (bexp == 0) {
+        if (F == 0)
+            return si_bits_double(0xFFF0000000000000ULL);   /* +0 -> -inf */
+        const int s = si_clz64(F) - 11;                     /* subnormal */
+        F <<= s;
+        e = 1 - 1023 - s;
+    } else {
+        F |= 0x0010000000000000ULL;
+        e = (int) bexp - 1023;
+    }
+
+    /* f = F / 2^52 in [1, 2); bucket j from the top 7 fraction bits. */
+    const int j = (int) ((F >> 45) & 127);
+    const uint32_t rd = SI_LOG_R(j);
+    const uint64_t R = rd & 0xFFFFu;
+    const int K = e + (int) (rd >> 16);
+    const uint64_t Lj = SI_LOG_L(j);
+
+    /* z = f R / 2^10 - 1 in Q62, exact. */
+    const int64_t Z = (int64_t) (F * R) - (int64_t) 0x4000000000000000LL;
+
+    /* P(z) = ln(1+z)/z = sum (-1)^i z^i / (i+1), Horner in Q62. */
+    int64_t P = SI_LOG_C8;
+    P = SI_LOG_C7 + si_mul_q62(Z, P);
+    P = SI_LOG_C6 + si_mul_q62(Z, P);
+    P = SI_LOG_C5 + si_mul_q62(Z, P);
+    P = SI_LOG_C4 + si_mul_q62(Z, P);
+    P = SI_LOG_C3 + si_mul_q62(Z, P);
+    P = SI_LOG_C2 + si_mul_q62(Z, P);
+    P = SI_LOG_C1 + si_mul_q62(Z, P);
+    P = SI_LOG_C0 + si_mul_q62(Z, P);
+
+    /* W = Z * P, signed 128-bit in Q124 (= ln(1+z)). */
+    const uint64_t Whi = (uint64_t) si_mulhi64(Z, P);
+    const uint64_t Wlo = (uint64_t) Z * (uint64_t) P;
+
+    if (K == 0 && Lj == 0) {
+        /* x in [1 - 2^-8, 1 + 2^-7): ln x = ln(1+z), full relative precision. */
+        if ((int64_t) Whi < 0) {
+            const uint64_t nlo = ~Wlo + 1;
+            const uint64_t nhi = ~Whi + (nlo == 0);
+            return si_u128_to_double(nhi, nlo, 124, 1);
+        }
+        return si_u128_to_double(Whi, Wlo, 124, 0);
+    }
+
+    /* T = |K| ln 2 in Q64 (128-bit), then the sign of K. */
+    const uint64_t aK = (uint64_t) (K < 0 ? -K : K);
+    uint64_t Thi = si_umulhi64(aK, SI_LN2_Q128_HI);
+    uint64_t Tlo = aK * SI_LN2_Q128_HI;
+    const uint64_t c = si_umulhi64(aK, SI_LN2_Q128_LO);
+    Tlo += c;
+    Thi += (Tlo < c);
+    if (K < 0) {
+        Tlo = ~Tlo + 1;
+        Thi = ~Thi + (Tlo == 0);
+    }
+    /* + L_j (Q64, non-negative). */
+    Tlo += Lj;
+    Thi += (Tlo < Lj);
+    /* + ln(1+z): W >> 60 with sign extension. */
+    const uint64_t slo = (Wlo >> 60) | (Whi << 4);
+    const uint64_t shi = (uint64_t) ((int64_t) Whi >> 60);
+    Tlo += slo;
+    Thi += shi + (Tlo < slo);
+
+    if ((int64_t) Thi < 0) {
+        const uint64_t nlo = ~Tlo + 1;
+        const uint64_t nhi = ~Thi + (nlo == 0);
+        return si_u128_to_double(nhi, nlo, 64, 1);
+    }
+    return si_u128_to_double(Thi, Tlo, 64, 0);
+}
+
+/* ---------------------------------------------------------------- */
+/* Samplers.                                                         */
+/* ---------------------------------------------------------------- */
+
+/* Number of type-1 items in t draws without replacement from an urn with
+ * n1 type-1 and n2 type-2 items; 0 <= t <= n1 + n2.  A draw takes a
+ * type-1 item iff (2w + 1) * remaining < a * 2^33, i.e. iff
+ * uniform_pos < a / remaining, evaluated exactly in 64-bit integers. */
+SI_HD int si_hypergeometric(si_rng *r, int n1, int n2, int t)
+{
+    const int64_t N = (int64_t) n1 + n2;
+    int complement = 0;
+    if (t <= 0 || n1 <= 0)
+        return 0;
+    if ((int64_t) t >= N)
+        return n1;
+    if (2 * (int64_t) t > N) {
+        t = (int) (N - t);
+        complement = 1;
+    }
+    uint64_t a = (uint64_t) n1, rem = (uint64_t) N;
+    int k = 0;
+    for (int i = 0; i < t; i++) {
+        if (a == 0)
+            break;
+        if (a == rem) {
+            k += t - i;
+            break;
+        }
+        const uint32_t w = si_next_u32(r);
+        if ((2 * (uint64_t) w + 1) * rem < (a << 33)) {
+            k++;
+            a--;
+        }
+        rem--;
+    }
+    return complement ? n1 - k : k;
+}
+
+/* Binomial(n, p) by chunked sequential-search inversion.  One draw per
+ * chunk of at most 512 trials; none when p <= 0, p >= 1 or n <= 0. */
+SI_HD int si_binomial(si_rng *r, double p, int n)
+{
+    if (n <= 0 || !(p > 0.0))
+        return 0;
+    if (p >= 1.0)
+        return n;
+    const int flip = p > 0.5;
+    const double q = flip ? 1.0 - p : p;
+    const double qc = 1.0 - q;
+    const double s = q / qc;
+    int total = 0, rem = n;
+    while (rem > 0) {
+        const int m = rem < 512 ? rem : 512;
+        rem -= m;
+        /* f0 = qc^m by binary powering. */
+        double f = 1.0, b = qc;
+        for (int e = m; e; e >>= 1) {
+            if (e & 1)
+                f = f * b;
+            b = b * b;
+        }
+        double u = si_uniform_pos(r);
+        int k = 0;
+        while (u > f && k < m) {
+            u = u - f;
+            k++;
+            f = f * ((s * (double) (m - k + 1)) / (double) k);
+        }
+        total += k;
+    }
+    return flip ? n - total : total;
+}
+
+#endif /* SIMINF_STREAM_H */

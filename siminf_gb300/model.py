@@ -1,0 +1,189 @@
+"""Model containers mirroring the reference's SimInf_model slots.
+
+``SimInfModel`` carries exactly the slots the solver reads (R/classes.R:
+112-124, 235-251): u0, v0, G, S, E, N, tspan, events, ldata, gdata and
+replicates, plus the name of the device model that holds the
+transition-rate and post-time-step code.  The constructors below build the
+same G, S, E and ldata/gdata layouts as the reference's R constructors:
+
+- ``SIR``   R/SIR.R:57-61 (E), :127-137 (G, S, ldata = beta, gamma)
+- ``SEIR``  R/SEIR.R:57-61 (E), :136-147 (G, S, ldata = beta, epsilon, gamma)
+- ``SIS``   R/SIS.R:54-59 (E), :122-130 (G, S, ldata = beta, gamma)
+- ``SISe``  R/SISe.R:140-150 (G, S, ldata = end_t1..end_t4, gdata = upsilon,
+  gamma, alpha, beta_t1..beta_t4, epsilon; v0 = phi)
+- ``SIR_mparse`` and ``SISe_pf``: the models mparse (R/mparse.R:477-491)
+  builds from the transition strings named in their docstrings.
+
+Events use the reference's one-based node, dest, select and shift
+(shift 0 = no shift) and must be sorted by (time, event, select) as
+R/SimInf_events.R:398 sorts them.
+"""
+import numpy as np
+
+from .abi import ENTER_EVENT, EXIT_EVENT, EXTERNAL_TRANSFER_EVENT, INTERNAL_TRANSFER_EVENT
+
+EVENT_FIELDS = ("event", "time", "node", "dest", "n", "proportion", "select", "shift")
+
+
+def empty_events():
+    return {k: np.zeros(0, dtype=np.float64 if k == "proportion" else np.int32)
+            for k in EVENT_FIELDS}
+
+
+def make_events(event, time, node, dest, n, proportion, select, shift, sort=True):
+    """Event arrays, stably sorted by (time, event, select) like
+    R/SimInf_events.R:398 when ``sort`` is true."""
+    ev = {
+        "event": np.asarray(event, dtype=np.int32),
+        "time": np.asarray(time, dtype=np.int32),
+        "node": np.asarray(node, dtype=np.int32),
+        "dest": np.asarray(dest, dtype=np.int32),
+        "n": np.asarray(n, dtype=np.int32),
+        "proportion": np.asarray(proportion, dtype=np.float64),
+        "select": np.asarray(select, dtype=np.int32),
+        "shift": np.asarray(shift, dtype=np.int32),
+    }
+    m = len(ev["event"])
+    for k in EVENT_FIELDS:
+        ev[k] = np.broadcast_to(ev[k], (m,)).copy() if ev[k].ndim == 0 else ev[k]
+    if sort and m:
+        order = np.lexsort((ev["select"], ev["event"], ev["time"]))
+        ev = {k: np.ascontiguousarray(v[order]) for k, v in ev.items()}
+    return ev
+
+
+class SimInfModel:
+    """The solver-facing slots of a SimInf_model."""
+
+    def __init__(self, name, G, S, u0, tspan, v0=None, ldata=None, gdata=None,
+                 E=None, N=None, events=None, replicates=1):
+        self.name = name
+        self.G = np.asarray(G, dtype=np.int32)
+        self.S = np.asarray(S, dtype=np.int32)
+        self.u0 = np.asarray(u0, dtype=np.int32)
+        if self.u0.ndim == 1:
+            self.u0 = self.u0.reshape(-1, 1)
+        self.tspan = np.asarray(tspan, dtype=np.float64)
+        self.replicates = int(replicates)
+        ncol = self.u0.shape[1]
+        if ncol % self.replicates:
+            raise ValueError("ncol(u0) must be a multiple of replicates")
+        self.Nn = ncol // self.replicates
+        self.Nc = self.S.shape[0]
+        self.Nt = self.S.shape[1]
+        self.v0 = np.zeros((0, ncol)) if v0 is None else np.asarray(v0, dtype=np.float64)
+        if self.v0.ndim == 1:
+            self.v0 = self.v0.reshape(1, -1)
+        self.Nd = self.v0.shape[0]
+        self.ldata = np.zeros((0, self.Nn)) if ldata is None else np.asarray(ldata, dtype=np.float64)
+        if self.ldata.ndim == 1:
+            self.ldata = self.ldata.reshape(-1, 1)
+        self.Nld = self.ldata.shape[0]
+        self.gdata = np.zeros(0) if gdata is None else np.asarray(gdata, dtype=np.float64).reshape(-1)
+        self.E = None if E is None else np.asarray(E, dtype=np.float64)
+        self.N = None if N is None else np.asarray(N, dtype=np.int32)
+        self.events = empty_events() if events is None else events
+        if self.G.shape != (self.Nt, self.Nt):
+            raise ValueError("G must be Nt x Nt")
+        if self.u0.shape[0] != self.Nc:
+            raise ValueError("u0 must have Nc rows")
+
+    def replicate(self, n):
+        """The same model with n replicates of u0/v0 (R's replicates slot)."""
+        u0 = np.tile(self.u0[:, :self.Nn], (1, n))
+        v0 = np.tile(self.v0[:, :self.Nn], (1, n)) if self.Nd else None
+        return SimInfModel(self.name, self.G, self.S, u0, self.tspan, v0=v0,
+                           ldata=self.ldata, gdata=self.gdata, E=self.E, N=self.N,
+                           events=self.events, replicates=n)
+
+
+def _rep_ldata(n, *params):
+    return np.vstack([np.broadcast_to(np.asarray(p, dtype=np.float64), (n,)) for p in params])
+
+
+def SIR(u0, tspan, beta, gamma, events=None):
+    """u0: array (3, Nn) or dict with S, I, R."""
+    u0 = _u0(u0, ("S", "I", "R"))
+    G = np.ones((2, 2), dtype=np.int32)
+    S = np.array([[-1, 0], [1, -1], [0, 1]], dtype=np.int32)
+    E = np.array([[1, 0, 0, 1], [0, 1, 0, 1], [0, 0, 1, 1]], dtype=np.float64)
+    return SimInfModel("SIR", G, S, u0, tspan, ldata=_rep_ldata(u0.shape[1], beta, gamma),
+                       E=E, events=events)
+
+
+def SEIR(u0, tspan, beta, epsilon, gamma, events=None):
+    """u0: array (4, Nn) or dict with S, E, I, R."""
+    u0 = _u0(u0, ("S", "E", "I", "R"))
+    G = np.ones((3, 3), dtype=np.int32)
+    S = np.array([[-1, 0, 0], [1, -1, 0], [0, 1, -1], [0, 0, 1]], dtype=np.int32)
+    E = np.array([[1, 1], [0, 1], [0, 1], [0, 1]], dtype=np.float64)
+    return SimInfModel("SEIR", G, S, u0, tspan,
+                       ldata=_rep_ldata(u0.shape[1], beta, epsilon, gamma), E=E, events=events)
+
+
+def SIS(u0, tspan, beta, gamma, events=None):
+    u0 = _u0(u0, ("S", "I"))
+    G = np.ones((2, 2), dtype=np.int32)
+    S = np.array([[-1, 1], [1, -1]], dtype=np.int32)
+    E = np.array([[1, 1], [0, 1]], dtype=np.float64)
+    return SimInfModel("SIS", G, S, u0, tspan, ldata=_rep_ldata(u0.shape[1], beta, gamma),
+                       E=E, events=events)
+
+
+def SISe(u0, tspan, phi, upsilon, gamma, alpha, beta_t1, beta_t2, beta_t3, beta_t4,
+         end_t1, end_t2, end_t3, end_t4, epsilon, events=None):
+    u0 = _u0(u0, ("S", "I"))
+    n = u0.shape[1]
+    G = np.ones((2, 2), dtype=np.int32)
+    S = np.array([[-1, 1], [1, -1]], dtype=np.int32)
+    E = np.array([[1, 1], [0, 1]], dtype=np.float64)
+    ldata = _rep_ldata(n, end_t1, end_t2, end_t3, end_t4)
+    gdata = np.array([upsilon, gamma, alpha, beta_t1, beta_t2, beta_t3, beta_t4, epsilon],
+                     dtype=np.float64)
+    v0 = np.broadcast_to(np.asarray(phi, dtype=np.float64), (n,)).reshape(1, n)
+    return SimInfModel("SISe", G, S, u0, tspan, v0=v0, ldata=ldata, gdata=gdata,
+                       E=E, events=events)
+
+
+def SIR_mparse(u0, tspan, beta, gamma, events=None):
+    """mparse(transitions = c("S -> beta*S*I/N -> I", "I -> gamma*I -> R",
+    "N <- S+I+R"), compartments = c("S","I","R"), gdata = c(beta, gamma)).
+    G = (depends %*% abs(S)) > 0 (R/mparse.R:485-491) is all ones here."""
+    u0 = _u0(u0, ("S", "I", "R"))
+    G = np.ones((2, 2), dtype=np.int32)
+    S = np.array([[-1, 0], [1, -1], [0, 1]], dtype=np.int32)
+    E = np.array([[1, 0, 0, 1], [0, 1, 0, 1], [0, 0, 1, 1]], dtype=np.float64)
+    return SimInfModel("SIR_mparse", G, S, u0, tspan, gdata=np.array([beta, gamma]),
+                       E=E, events=events)
+
+
+def SISe_pf(u0, tspan, upsilon, gamma, phi0=0.0, events=None):
+    """mparse(transitions = c("S -> upsilon*phi*S -> I", "I -> gamma*I -> S"),
+    compartments = c("S","I"), v0 = phi, gdata = c(upsilon, gamma),
+    pts_fun = phi <- phi*(1-0.03) + 0.05*I/(S+I))."""
+    u0 = _u0(u0, ("S", "I"))
+    n = u0.shape[1]
+    G = np.ones((2, 2), dtype=np.int32)
+    S = np.array([[-1, 1], [1, -1]], dtype=np.int32)
+    E = np.array([[1, 0, 1], [0, 1, 1]], dtype=np.float64)
+    v0 = np.full((1, n), phi0, dtype=np.float64)
+    return SimInfModel("SISe_pf", G, S, u0, tspan, v0=v0, gdata=np.array([upsilon, gamma]),
+                       E=E, events=events)
+
+
+def _u0(u0, names):
+    if isinstance(u0, dict):
+        cols = [np.atleast_1d(np.asarray(u0[k])) for k in names]
+        n = max(len(c) for c in cols)
+        return np.vstack([np.broadcast_to(c, (n,)) for c in cols]).astype(np.int32)
+    a = np.asarray(u0, dtype=np.int32)
+    if a.ndim == 1:
+        a = a.reshape(-1, 1)
+    if a.shape[0] != len(names):
+        raise ValueError("u0 must have rows %s" % (names,))
+    return a
+
+
+__all__ = ["SimInfModel", "SIR", "SEIR", "SIS", "SISe", "SIR_mparse", "SISe_pf",
+           "make_events", "empty_events", "EXIT_EVENT", "ENTER_EVENT",
+           "INTERNAL_TRANSFER_EVENT", "EXTERNAL_TRANSFER_EVENT"]
