@@ -135,6 +135,7 @@ typedef struct siminf_gpu_model siminf_gpu_model;
  * src/models/SISe.c) and the mparse-generated SIMINF_MODEL_RUN
  * (R/C-generator.R:304-332) for the models the library ships.
  * Names: "SIR" (SIR.c), "SEIR" (SEIR.c), "SIS" (SIS.c), "SISe" (SISe.c),
+ * "SISe3" (SISe3.c),
  * "SIR_mparse" (mparse "S -> beta*S*I/N -> I", "I -> gamma*I -> R",
  * N <- S+I+R, beta/gamma in gdata), "SISe_pf" (mparse
  * "S -> upsilon*phi*S -> I", "I -> gamma*I -> S" with the pts_fun

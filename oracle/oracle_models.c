@@ -6,6 +6,7 @@
  *   SIR   src/models/SIR.c:43-87     (ldata: beta, gamma)
  *   SEIR  src/models/SEIR.c:43-112   (ldata: beta, epsilon, gamma)
  *   SIS   src/models/SIS.c           (ldata: beta, gamma)
+ *   SISe3 src/models/SISe3.c:51-250 (N shift matrix, block-diagonal G)
  *   SISe  src/models/SISe.c:51-144   (ldata: end_t1..end_t4; gdata: upsilon,
  *         gamma, alpha, beta_t1..beta_t4, epsilon) with
  *         src/misc/SimInf_forward_euler_linear_decay.c:57-93
@@ -159,6 +160,72 @@ static int sise_pts(double *v_new, const int *u, const double *v,
     return phi != v_new[0];
 }
 
+/* SISe3, src/models/SISe3.c; u = (S_1, I_1, S_2, I_2, S_3, I_3), v = (phi),
+ * ldata = (end_t1..end_t4), gdata = (upsilon_1..3, gamma_1..3, alpha,
+ * beta_t1..beta_t4, epsilon); transition order of SISe3_run. */
+static double sise3_s1(const int *u, const double *v, const double *ldata,
+                       const double *gdata, double t)
+{
+    UNUSED(ldata); UNUSED(t);
+    return gdata[0] * v[0] * u[0];
+}
+
+static double sise3_i1(const int *u, const double *v, const double *ldata,
+                       const double *gdata, double t)
+{
+    UNUSED(v); UNUSED(ldata); UNUSED(t);
+    return gdata[3] * u[1];
+}
+
+static double sise3_s2(const int *u, const double *v, const double *ldata,
+                       const double *gdata, double t)
+{
+    UNUSED(ldata); UNUSED(t);
+    return gdata[1] * v[0] * u[2];
+}
+
+static double sise3_i2(const int *u, const double *v, const double *ldata,
+                       const double *gdata, double t)
+{
+    UNUSED(v); UNUSED(ldata); UNUSED(t);
+    return gdata[4] * u[3];
+}
+
+static double sise3_s3(const int *u, const double *v, const double *ldata,
+                       const double *gdata, double t)
+{
+    UNUSED(ldata); UNUSED(t);
+    return gdata[2] * v[0] * u[4];
+}
+
+static double sise3_i3(const int *u, const double *v, const double *ldata,
+                       const double *gdata, double t)
+{
+    UNUSED(v); UNUSED(ldata); UNUSED(t);
+    return gdata[5] * u[5];
+}
+
+static int sise3_pts(double *v_new, const int *u, const double *v,
+                     const double *ldata, const double *gdata, int node, double t)
+{
+    UNUSED(node);
+    const int day = (int) t % 365;
+    const double I_n = u[1] + u[3] + u[5];
+    const double n = I_n + u[0] + u[2] + u[4];
+    const double phi = v[0];
+    v_new[0] = decay(phi, day, (int) ldata[0], (int) ldata[1], (int) ldata[2],
+                     (int) ldata[3], gdata[7], gdata[8], gdata[9], gdata[10]);
+    if (n > 0.0)
+        v_new[0] += gdata[6] * I_n / n + gdata[11];
+    else
+        v_new[0] += gdata[11];
+    if (!isfinite(v_new[0]))
+        return -7;
+    if (v_new[0] < 0.0)
+        return -10;
+    return phi != v_new[0];
+}
+
 /* mparse SIR: N <- S+I+R; beta = gdata[0], gamma = gdata[1]. */
 static double mp_sir_1(const int *u, const double *v, const double *ldata,
                        const double *gdata, double t)
@@ -209,6 +276,7 @@ static const oracle_model models[] = {
     {"SEIR", 4, 3, 0, {seir_s_to_e, seir_e_to_i, seir_i_to_r}, pts_none},
     {"SIS", 2, 2, 0, {sis_s_to_i, sis_i_to_s}, pts_none},
     {"SISe", 2, 2, 1, {sise_s_to_i, sise_i_to_s}, sise_pts},
+    {"SISe3", 6, 6, 1, {sise3_s1, sise3_i1, sise3_s2, sise3_i2, sise3_s3, sise3_i3}, sise3_pts},
     {"SIR_mparse", 3, 2, 0, {mp_sir_1, mp_sir_2}, pts_none},
     {"SISe_pf", 2, 2, 1, {pf_s_to_i, pf_i_to_s}, pf_pts},
 };

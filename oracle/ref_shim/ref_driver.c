@@ -14,8 +14,8 @@
 int shim_configure(uint64_t seed, int Nn, int Nthread, int Nrep, int threads);
 void shim_release(void);
 
-extern TRFun ref_SIR_tr[], ref_SEIR_tr[], ref_SIS_tr[], ref_SISe_tr[];
-extern PTSFun ref_SIR_pts, ref_SEIR_pts, ref_SIS_pts, ref_SISe_pts;
+extern TRFun ref_SIR_tr[], ref_SEIR_tr[], ref_SIS_tr[], ref_SISe_tr[], ref_SISe3_tr[];
+extern PTSFun ref_SIR_pts, ref_SEIR_pts, ref_SIS_pts, ref_SISe_pts, ref_SISe3_pts;
 
 _Static_assert(sizeof(SimInf_solver_args) == sizeof(siminf_gpu_solver_args),
                "siminf_gpu_solver_args must stay layout-identical to SimInf_solver_args");
@@ -35,6 +35,8 @@ int ref_run(const siminf_gpu_solver_args *ga, const char *model, int threads)
         memcpy(tr, ref_SIS_tr, 2 * sizeof(TRFun)); pts = ref_SIS_pts;
     } else if (strcmp(model, "SISe") == 0) {
         memcpy(tr, ref_SISe_tr, 2 * sizeof(TRFun)); pts = ref_SISe_pts;
+    } else if (strcmp(model, "SISe3") == 0) {
+        memcpy(tr, ref_SISe3_tr, 6 * sizeof(TRFun)); pts = ref_SISe3_pts;
     } else {
         /* mparse models have no source in the reference tree: use the
          * oracle's host versions of the generated code. */

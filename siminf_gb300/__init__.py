@@ -1,0 +1,14 @@
+"""siminf_gb300: SimInf's ssm/mssm Gillespie solver and scheduled-event engine
+on one GB300 GPU, behind a C ABI (include/siminf_gb300.h) that replaces the
+reference's SimInf_run_solver_ssm / SimInf_run_solver_mssm."""
+from . import abi, model
+from .model import SEIR, SIR, SIS, SISe, SISe3, SIR_mparse, SISe_pf, SimInfModel, make_events
+from .abi import SimInfError
+
+__all__ = ["abi", "model", "SimInfModel", "SIR", "SEIR", "SIS", "SISe", "SIR_mparse",
+           "SISe_pf", "make_events", "SimInfError", "run"]
+
+
+def run(*args, **kwargs):
+    from .run import run as _run
+    return _run(*args, **kwargs)

@@ -15,7 +15,8 @@ c_double_p = C.POINTER(C.c_double)
 # inst/include/SimInf.h:56-59
 EXIT_EVENT, ENTER_EVENT, INTERNAL_TRANSFER_EVENT, EXTERNAL_TRANSFER_EVENT = 0, 1, 2, 3
 
-# inst/include/SimInf.h:66-89 plus the GPU-only codes of siminf_gb300.h
+# Messages of SimInf_raise_error (src/SimInf.c:28-97) for the codes of
+# inst/include/SimInf.h:66-89, plus the GPU-only codes of siminf_gb300.h
 ERRORS = {
     -1: "Negative state detected.",
     -2: "Unable to allocate memory buffer.",
@@ -28,8 +29,8 @@ ERRORS = {
     -12: "Invalid 'solver' value.",
     -13: "'dest' is out of bounds.",
     -14: "'node' is out of bounds.",
-    -15: "Unable to shift individuals: 'N' is not defined.",
-    -16: "'shift' must be > 0 for an internal transfer event.",
+    -15: "'N' is invalid.",
+    -16: "'shift' is invalid.",
     -17: "'shift' is out of bounds.",
     -18: "Invalid proportion detected (< 0.0 or > 1.0).",
     -30: "A CUDA runtime call failed.",

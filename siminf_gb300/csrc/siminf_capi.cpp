@@ -1,0 +1,815 @@
+/*
+ * siminf_capi.cpp -- host side of the C ABI in include/siminf_gb300.h.
+ *
+ * Replaces, behind SimInf_run's dispatch (src/SimInf.c:382-399), the
+ * reference's SimInf_run_solver_ssm / _mssm
+ * (src/solvers/SimInf_solver_ssm.c:381-414, _mssm.c:410-443).  What the
+ * reference does in SimInf_compartment_model_create and
+ * SimInf_scheduled_events_create (src/solvers/SimInf_solver.c:443-510,
+ * 998-1173) happens here as a plan:
+ *
+ *  - the day schedule: tt starts at tspan[0], next = floor(tt) + 1, and
+ *    column k of U/V is written after the first day whose end time is past
+ *    tspan[k] (src/solvers/SimInf_solver_ssm.c:305-334);
+ *  - E1 events (exit, enter, internal transfer) bucketed per node in array
+ *    order, each tagged with the day whose event pass applies it (events
+ *    with time <= tt, src/solvers/SimInf_solver.c:671);
+ *  - E2 events (external transfers) of each day split into conflict-free
+ *    wavefronts: an event waits for every earlier event of the day that
+ *    touched its source, and for every earlier event whose source was its
+ *    destination.  Adds into a common destination commute and share a wave.
+ *    Running the waves in order reproduces the reference's serial array
+ *    order (src/solvers/SimInf_solver_ssm.c:244-250) exactly.
+ *
+ * Errors follow the reference: a negative SimInf code, diagnostics kept per
+ * calling thread, every device buffer freed before returning.
+ */
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/siminf_gb300.h"
+#include "siminf_launch.h"
+#include "siminf_plan.h"
+
+using namespace siminf;
+
+struct siminf_gpu_model {
+    char name[64];
+    const Launchers *L;
+};
+
+namespace {
+
+thread_local siminf_gpu_status g_status;
+thread_local siminf_gpu_stats g_stats;
+
+void set_status(int code, int node, int tr, int evi, double time, double rate, const char *msg)
+{
+    g_status.error = code;
+    g_status.node = node;
+    g_status.transition = tr;
+    g_status.event_index = evi;
+    g_status.time = time;
+    g_status.rate = rate;
+    snprintf(g_status.message, sizeof(g_status.message), "%s", msg ? msg : "");
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    char buf[400];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    set_status(SIMINF_GPU_ERR_CUDA, -1, -1, -1, 0, 0, buf);
+    return SIMINF_GPU_ERR_CUDA;
+}
+
+template <class T>
+int dalloc(T **p, size_t n, std::vector<void *> &owned)
+{
+    *p = nullptr;
+    if (n == 0)
+        n = 1;
+    cudaError_t e = cudaMalloc((void **) p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    owned.push_back(*p);
+    return 0;
+}
+
+template <class T>
+int upload(T **p, const T *src, size_t n, std::vector<void *> &owned, cudaStream_t st)
+{
+    int rc = dalloc(p, n, owned);
+    if (rc)
+        return rc;
+    if (n && src) {
+        cudaError_t e = cudaMemcpyAsync(*p, src, n * sizeof(T), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpyAsync H2D");
+    }
+    return 0;
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0)
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+/* A planned failure: an event the device cannot apply (bad node, dest or
+ * kind) that the reference would reject when it reaches it. */
+struct PlannedErr {
+    int day, code, index, node, phase;
+};
+
+struct siminf_gpu_plan {
+    const Launchers *L = nullptr;
+    DevState s{};
+    cudaStream_t stream = nullptr;
+    std::vector<void *> owned;
+
+    int ndays = 0;
+    std::vector<DayInfo> days;
+    DayInfo *d_days = nullptr;
+    bool horizon = false;
+
+    /* E2 waves */
+    E2Rec *d_e2 = nullptr;
+    std::vector<long long> wave_ptr;    /* offsets into d_e2, one past the last */
+    std::vector<int> day_wave;          /* ndays + 1 */
+    uint64_t e1_count = 0, e2_count = 0;
+
+    std::vector<PlannedErr> planned;
+
+    /* host-side copies needed to write results back */
+    size_t U_len = 0, V_len = 0, prU_len = 0, prV_len = 0;
+    const int *u0_host = nullptr;
+    const double *v0_host = nullptr;
+    double tt0 = 0;
+
+    siminf_gpu_stats stats{};
+    bool ran = false;
+};
+
+static int validate(const siminf_gpu_solver_args *a, const Launchers *L)
+{
+    char msg[256];
+    if (!a || !L)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    if (a->solver != 0) {
+        set_status(SIMINF_GPU_ERR_UNKNOWN_SOLVER, -1, -1, -1, 0, 0,
+                   "the GPU path implements the ssm solver only");
+        return SIMINF_GPU_ERR_UNKNOWN_SOLVER;
+    }
+    if (a->Nc != L->Nc || a->Nt != L->Nt || a->Nd != L->Nd || a->Nn < 1 || a->tlen < 1 ||
+        (a->Nrep < 1) || !a->u0 || !a->tspan || !a->irG || !a->jcG || !a->irS || !a->jcS ||
+        !a->prS || (a->Nld > 0 && !a->ldata) || (a->Nd > 0 && !a->v0)) {
+        snprintf(msg, sizeof(msg),
+                 "invalid model: Nc=%d Nt=%d Nd=%d (device model wants %d, %d, %d), Nn=%d, tlen=%d",
+                 a->Nc, a->Nt, a->Nd, L->Nc, L->Nt, L->Nd, a->Nn, a->tlen);
+        set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0, msg);
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    }
+    if (!a->U && !a->jcU) {
+        set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0, "neither U nor a U_sparse pattern");
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    }
+    /* G and S: CSC with row indices in range and ascending per column (the
+     * dgCMatrix invariant the refresh order relies on). */
+    for (int j = 0; j < a->Nt; j++) {
+        for (int k = a->jcG[j]; k < a->jcG[j + 1]; k++) {
+            if (a->irG[k] < 0 || a->irG[k] >= a->Nt ||
+                (k > a->jcG[j] && a->irG[k] <= a->irG[k - 1])) {
+                set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, j, -1, 0, 0, "invalid G");
+                return SIMINF_GPU_ERR_INVALID_MODEL;
+            }
+        }
+        for (int k = a->jcS[j]; k < a->jcS[j + 1]; k++) {
+            if (a->irS[k] < 0 || a->irS[k] >= a->Nc) {
+                set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, j, -1, 0, 0, "invalid S");
+                return SIMINF_GPU_ERR_INVALID_MODEL;
+            }
+        }
+    }
+    if (a->len > 0 && (!a->event || !a->time || !a->node || !a->dest || !a->n ||
+                       !a->proportion || !a->select || !a->shift || !a->jcE || !a->irE ||
+                       !a->prE)) {
+        set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0, "incomplete event arrays");
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    }
+    return 0;
+}
+
+/* Day index whose event pass applies an event at `time`. */
+static inline long long event_day(int time, double tt0)
+{
+    if ((double) time <= tt0)
+        return 0;
+    return (long long) time - (long long) std::floor(tt0);
+}
+
+static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int nsel,
+                       std::vector<E1Rec> &e1, std::vector<int> &e1_ptr,
+                       std::vector<E2Rec> &e2)
+{
+    const int Nn = a->Nn, ndays = p->ndays;
+    const double tt0 = a->tspan[0];
+    std::vector<int> e1_count(Nn + 1, 0);
+    std::vector<int> day_e2_count(ndays + 1, 0);
+    int prev_time = INT_MIN, seen_e2_at = INT_MIN;
+
+    /* pass 1: validate order, count */
+    for (int i = 0; i < a->len; i++) {
+        const int t = a->time[i], kind = a->event[i];
+        if (t < prev_time || (kind != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT && seen_e2_at == t)) {
+            char msg[200];
+            snprintf(msg, sizeof(msg), "event %d (time %d) breaks the (time, E1 before E2) order", i + 1, t);
+            set_status(SIMINF_GPU_ERR_EVENTS_UNSORTED, -1, -1, i, t, 0, msg);
+            return SIMINF_GPU_ERR_EVENTS_UNSORTED;
+        }
+        prev_time = t;
+        if (kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
+            seen_e2_at = t;
+        const long long d = event_day(t, tt0);
+        if (d >= ndays)
+            continue;                       /* never reached */
+        const int node = a->node[i] - 1, dest = a->dest[i] - 1;
+        const int phase = kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT ? PHASE_E2 : PHASE_E1;
+        if (node < 0 || node >= Nn) {
+            p->planned.push_back({(int) d, SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, i, node, phase});
+            continue;
+        }
+        if (kind < 0 || kind > 3) {
+            p->planned.push_back({(int) d, SIMINF_GPU_UNDEFINED_EVENT, i, node, phase});
+            continue;
+        }
+        if (a->select[i] - 1 < 0 || a->select[i] - 1 >= nsel) {
+            p->planned.push_back({(int) d, SIMINF_GPU_ERR_SAMPLE_SELECT, i, node, phase});
+            continue;
+        }
+        if (kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT) {
+            if (dest < 0 || dest >= Nn) {
+                p->planned.push_back({(int) d, SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS, i, node, phase});
+                continue;
+            }
+            day_e2_count[d]++;
+        } else {
+            e1_count[node]++;
+        }
+    }
+
+    /* E1: stable bucket by node (array order within a node is day order) */
+    e1_ptr.assign(Nn + 1, 0);
+    for (int k = 0; k < Nn; k++)
+        e1_ptr[k + 1] = e1_ptr[k] + e1_count[k];
+    e1.resize(e1_ptr[Nn]);
+    std::vector<int> fill(e1_ptr.begin(), e1_ptr.end() - 1);
+
+    /* E2: per-day array order first, then waves */
+    std::vector<long long> day_ptr(ndays + 1, 0);
+    for (int d = 0; d < ndays; d++)
+        day_ptr[d + 1] = day_ptr[d] + day_e2_count[d];
+    std::vector<E2Rec> raw(day_ptr[ndays]);
+    std::vector<long long> rfill(day_ptr.begin(), day_ptr.end() - 1);
+
+    for (int i = 0; i < a->len; i++) {
+        const long long d = event_day(a->time[i], tt0);
+        if (d >= ndays)
+            continue;
+        const int kind = a->event[i], node = a->node[i] - 1, dest = a->dest[i] - 1;
+        if (node < 0 || node >= Nn || kind < 0 || kind > 3 || a->select[i] - 1 < 0 ||
+            a->select[i] - 1 >= nsel)
+            continue;
+        if (kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT) {
+            if (dest < 0 || dest >= Nn)
+                continue;
+            raw[rfill[d]++] = E2Rec{node, dest, a->n[i], a->select[i] - 1, a->shift[i] - 1, i,
+                                    a->proportion[i]};
+        } else {
+            e1[fill[node]++] = E1Rec{(int) d, kind, a->n[i], a->select[i] - 1, a->shift[i] - 1, i,
+                                     a->proportion[i]};
+        }
+    }
+    p->e1_count = e1.size();
+    p->e2_count = raw.size();
+
+    /* Wave levels per day: level = 1 + max(level of the last event with
+     * the same source, of any add into the source, of the last event whose
+     * source is our destination). */
+    std::vector<int> excl(Nn, 0), add(Nn, 0), stamp(Nn, -1), level(raw.size());
+    p->day_wave.assign(ndays + 1, 0);
+    p->wave_ptr.clear();
+    p->wave_ptr.push_back(0);
+    e2.resize(raw.size());
+    std::vector<long long> lvl_count;
+    for (int d = 0; d < ndays; d++) {
+        int maxl = 0;
+        for (long long k = day_ptr[d]; k < day_ptr[d + 1]; k++) {
+            const int s = raw[k].src, t = raw[k].dst;
+            if (stamp[s] != d) {
+                stamp[s] = d;
+                excl[s] = add[s] = 0;
+            }
+            if (stamp[t] != d) {
+                stamp[t] = d;
+                excl[t] = add[t] = 0;
+            }
+            const int L = 1 + std::max(std::max(excl[s], add[s]), excl[t]);
+            excl[s] = L;
+            add[t] = std::max(add[t], L);
+            level[k] = L;
+            maxl = std::max(maxl, L);
+        }
+        /* counting sort of the day's events by level (stable) */
+        lvl_count.assign(maxl + 1, 0);
+        for (long long k = day_ptr[d]; k < day_ptr[d + 1]; k++)
+            lvl_count[level[k]]++;
+        std::vector<long long> off(maxl + 2, day_ptr[d]);
+        for (int L = 1; L <= maxl; L++)
+            off[L + 1] = off[L] + lvl_count[L];
+        for (long long k = day_ptr[d]; k < day_ptr[d + 1]; k++)
+            e2[off[level[k]]++] = raw[k];
+        for (int L = 1; L <= maxl; L++)
+            p->wave_ptr.push_back(p->wave_ptr.back() + lvl_count[L]);
+        p->day_wave[d + 1] = (int) p->wave_ptr.size() - 1;
+    }
+    return 0;
+}
+
+extern "C" {
+
+int siminf_gpu_model_builtin(const char *name, siminf_gpu_model **out)
+{
+    if (!name || !out)
+        return SIMINF_GPU_ERR_UNKNOWN_MODEL;
+    const Launchers *L = launchers_for(name);
+    if (!L) {
+        set_status(SIMINF_GPU_ERR_UNKNOWN_MODEL, -1, -1, -1, 0, 0, name);
+        return SIMINF_GPU_ERR_UNKNOWN_MODEL;
+    }
+    siminf_gpu_model *m = (siminf_gpu_model *) calloc(1, sizeof(siminf_gpu_model));
+    if (!m)
+        return SIMINF_GPU_ERR_ALLOC_MEMORY_BUFFER;
+    snprintf(m->name, sizeof(m->name), "%s", name);
+    m->L = L;
+    *out = m;
+    return 0;
+}
+
+int siminf_gpu_model_dims(const siminf_gpu_model *model, int *Nc, int *Nt, int *Nd)
+{
+    if (!model)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    if (Nc)
+        *Nc = model->L->Nc;
+    if (Nt)
+        *Nt = model->L->Nt;
+    if (Nd)
+        *Nd = model->L->Nd;
+    return 0;
+}
+
+void siminf_gpu_model_free(siminf_gpu_model *model)
+{
+    free(model);
+}
+
+int siminf_gpu_last_status(siminf_gpu_status *out)
+{
+    if (out)
+        *out = g_status;
+    return g_status.error;
+}
+
+int siminf_gpu_last_stats(siminf_gpu_stats *out)
+{
+    if (out)
+        *out = g_stats;
+    return 0;
+}
+
+void siminf_gpu_plan_free(siminf_gpu_plan *p)
+{
+    if (!p)
+        return;
+    for (void *q : p->owned)
+        cudaFree(q);
+    delete p;
+}
+
+int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
+                           siminf_gpu_plan **out)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    int rc;
+    memset(&g_status, 0, sizeof(g_status));
+    if (!out || !model)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        set_status(SIMINF_GPU_ERR_NO_DEVICE, -1, -1, -1, 0, 0, "no CUDA device");
+        return SIMINF_GPU_ERR_NO_DEVICE;
+    }
+    const Launchers *L = model->L;
+    if ((rc = validate(a, L)))
+        return rc;
+
+    siminf_gpu_plan *p = new siminf_gpu_plan();
+    p->L = L;
+    DevState &s = p->s;
+    const int Nn = a->Nn, Nc = a->Nc, Nt = a->Nt, Nd = a->Nd, Nrep = a->Nrep, tlen = a->tlen;
+    const long long Ntot = (long long) Nn * Nrep;
+    s.Nn = Nn;
+    s.Nc = Nc;
+    s.Nt = Nt;
+    s.Nd = Nd;
+    s.Nld = a->Nld;
+    s.Nrep = Nrep;
+    s.tlen = tlen;
+    s.Ntot = Ntot;
+    s.seed = (uint64_t) a->seed;
+    p->tt0 = a->tspan[0];
+
+    /* Day schedule (src/solvers/SimInf_solver_ssm.c:305-334). */
+    {
+        double tt = a->tspan[0], next = std::floor(tt) + 1.0;
+        int it = 0;
+        while (it < tlen) {
+            DayInfo di;
+            di.tt = tt;
+            di.next = next;
+            tt = next;
+            next += 1.0;
+            di.c0 = it;
+            while (it < tlen && tt > a->tspan[it])
+                it++;
+            di.c1 = it;
+            p->days.push_back(di);
+            if (p->days.size() > (size_t) 100000000) {
+                delete p;
+                set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0, "tspan too long");
+                return SIMINF_GPU_ERR_INVALID_MODEL;
+            }
+        }
+        p->ndays = (int) p->days.size();
+    }
+
+    /* Dense S (Nt rows of Nc) and G column masks. */
+    std::vector<int> Sd((size_t) Nt * Nc, 0);
+    std::vector<uint32_t> Gm(Nt, 0);
+    for (int j = 0; j < Nt; j++) {
+        for (int k = a->jcS[j]; k < a->jcS[j + 1]; k++)
+            Sd[(size_t) j * Nc + a->irS[k]] += a->prS[k];
+        for (int k = a->jcG[j]; k < a->jcG[j + 1]; k++)
+            Gm[j] |= 1u << a->irG[k];
+    }
+
+    const int nsel = (a->len > 0 && a->jcE) ? INT_MAX : 0;
+    std::vector<E1Rec> e1;
+    std::vector<int> e1_ptr;
+    std::vector<E2Rec> e2;
+    if ((rc = plan_events(p, a, nsel, e1, e1_ptr, e2))) {
+        delete p;
+        return rc;
+    }
+    p->horizon = (p->e2_count == 0) && L->pts_local;
+
+    cudaStream_t st = nullptr;
+    p->stream = st;
+    auto &own = p->owned;
+    int *dS;
+    uint32_t *dG;
+    double *dld, *dgd;
+    const size_t nld = a->Nld > 0 ? (size_t) a->Nld * Nn : 1;
+    rc = upload(&dS, Sd.data(), Sd.size(), own, st);
+    if (!rc) rc = upload(&dG, Gm.data(), Gm.size(), own, st);
+    if (!rc) rc = upload(&dld, a->ldata, a->ldata ? nld : 0, own, st);
+    if (!rc) rc = upload(&dgd, a->gdata, a->gdata ? (size_t) L->Ngd : 0, own, st);
+    s.S = dS;
+    s.Gmask = dG;
+    s.ldata = dld;
+    s.gdata = dgd;
+    if (!rc && a->len > 0) {
+        /* E and N have as many columns as the largest select and shift
+         * the events use (the struct carries no column counts). */
+        int maxsel = 0, maxshift = 0;
+        for (int i = 0; i < a->len; i++) {
+            maxsel = std::max(maxsel, a->select[i]);
+            maxshift = std::max(maxshift, a->shift[i]);
+        }
+        const int ncolE = maxsel;
+        const int nnzE = a->jcE[ncolE];
+        int *dirE, *djcE;
+        double *dprE;
+        rc = upload(&djcE, a->jcE, (size_t) ncolE + 1, own, st);
+        if (!rc) rc = upload(&dirE, a->irE, (size_t) nnzE, own, st);
+        if (!rc) rc = upload(&dprE, (const double *) a->prE, (size_t) nnzE, own, st);
+        s.jcE = djcE;
+        s.irE = dirE;
+        s.prE = dprE;
+        if (!rc && a->N && maxshift > 0) {
+            int *dN;
+            rc = upload(&dN, a->N, (size_t) maxshift * Nc, own, st);
+            s.Nshift = dN;
+        } else {
+            s.Nshift = nullptr;
+        }
+    }
+    if (!rc) {
+        int *de1p;
+        E1Rec *de1;
+        rc = upload(&de1p, e1_ptr.data(), e1_ptr.size(), own, st);
+        if (!rc) rc = upload(&de1, e1.data(), e1.size(), own, st);
+        s.e1_ptr = de1p;
+        s.e1 = de1;
+    }
+    if (!rc) rc = upload(&p->d_e2, e2.data(), e2.size(), own, st);
+    if (!rc) rc = upload(&p->d_days, p->days.data(), p->days.size(), own, st);
+
+    /* state */
+    if (!rc) rc = dalloc(&s.u, (size_t) Ntot * Nc, own);
+    if (!rc) rc = dalloc(&s.vA, (size_t) Ntot * Nd, own);
+    if (!rc) rc = dalloc(&s.vB, (size_t) Ntot * Nd, own);
+    if (!rc) rc = dalloc(&s.t_rate, (size_t) Ntot * Nt, own);
+    if (!rc) rc = dalloc(&s.sum_rate, (size_t) Ntot, own);
+    if (!rc) rc = dalloc(&s.t_time, (size_t) Ntot, own);
+    if (!rc) rc = dalloc(&s.ctr, (size_t) Ntot, own);
+    if (!rc) rc = dalloc(&s.update, (size_t) Ntot, own);
+    if (!rc) rc = dalloc(&s.err, (size_t) MAX_ERR, own);
+    if (!rc) rc = dalloc(&s.err_count, 3, own);
+    if (!rc) rc = dalloc(&s.fired, 1, own);
+    if (!rc) {
+        s.err_day = s.err_count + 1;
+        s.err_day_pre_e2 = s.err_count + 2;
+    }
+
+    /* outputs */
+    if (!rc) {
+        if (a->U) {
+            p->U_len = (size_t) Nn * Nc * (size_t) Nrep * tlen;
+            rc = dalloc(&s.U, p->U_len, own);
+        } else {
+            const size_t ncol = (size_t) Nrep * tlen;
+            p->prU_len = (size_t) a->jcU[ncol];
+            int *dir, *djc;
+            rc = upload(&djc, a->jcU, ncol + 1, own, st);
+            if (!rc) rc = upload(&dir, a->irU, p->prU_len, own, st);
+            if (!rc) rc = dalloc(&s.prU, p->prU_len, own);
+            s.jcU = djc;
+            s.irU = dir;
+        }
+    }
+    if (!rc && Nd > 0) {
+        if (a->V) {
+            p->V_len = (size_t) Nn * Nd * (size_t) Nrep * tlen;
+            rc = dalloc(&s.V, p->V_len, own);
+        } else if (a->jcV) {
+            const size_t ncol = (size_t) Nrep * tlen;
+            p->prV_len = (size_t) a->jcV[ncol];
+            int *dir, *djc;
+            rc = upload(&djc, a->jcV, ncol + 1, own, st);
+            if (!rc) rc = upload(&dir, a->irV, p->prV_len, own, st);
+            if (!rc) rc = dalloc(&s.prV, p->prV_len, own);
+            s.jcV = djc;
+            s.irV = dir;
+        }
+    }
+    p->u0_host = a->u0;
+    p->v0_host = a->v0;
+    if (!rc) {
+        /* initial state stays on the device so plan_run can restart */
+        int *du0;
+        rc = upload(&du0, a->u0, (size_t) Ntot * Nc, own, st);
+        if (!rc && Nd > 0) {
+            double *dv0;
+            rc = upload(&dv0, a->v0, (size_t) Ntot * Nd, own, st);
+            p->v0_host = dv0;
+        }
+        p->u0_host = du0;
+    }
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "upload");
+    }
+    if (rc) {
+        siminf_gpu_plan_free(p);
+        return rc;
+    }
+    p->stats.e1_events = p->e1_count;
+    p->stats.e2_events = p->e2_count;
+    p->stats.e2_waves = (int) p->wave_ptr.size() - 1;
+    p->stats.days = p->ndays;
+    p->stats.ms_upload = ms_since(t0);
+    *out = p;
+    return 0;
+}
+
+/* Pick the error the reference would report from the device candidates
+ * and the planned ones. */
+static int resolve_errors(siminf_gpu_plan *p, std::vector<ErrRec> &cands)
+{
+    for (const PlannedErr &pe : p->planned) {
+        for (int r = 0; r < p->s.Nrep; r++) {
+            ErrRec e{};
+            e.code = pe.code;
+            e.phase = pe.phase;
+            e.day = pe.day;
+            e.rep = r;
+            e.node = pe.node;
+            e.transition = -1;
+            e.event_index = pe.index;
+            e.time = p->days[pe.day].tt;
+            cands.push_back(e);
+        }
+    }
+    if (cands.empty())
+        return 0;
+    /* replicate first (mssm runs replicates one after another), then day */
+    int rep = INT_MAX, day = INT_MAX;
+    for (auto &e : cands)
+        rep = std::min(rep, e.rep);
+    for (auto &e : cands)
+        if (e.rep == rep)
+            day = std::min(day, e.day);
+    std::vector<ErrRec> c;
+    for (auto &e : cands)
+        if (e.rep == rep && e.day == day)
+            c.push_back(e);
+    const ErrRec *best = nullptr;
+    /* initialisation or SSA: lowest node */
+    for (int ph : {(int) PHASE_INIT, (int) PHASE_SSA}) {
+        for (auto &e : c)
+            if (e.phase == ph && (!best || e.node < best->node))
+                best = &e;
+        if (best)
+            break;
+    }
+    if (!best) {
+        /* events: lowest position in the event arrays */
+        for (auto &e : c)
+            if ((e.phase == PHASE_E1 || e.phase == PHASE_E2) &&
+                (!best || e.event_index < best->event_index))
+                best = &e;
+    }
+    ErrRec res{};
+    bool have = false;
+    if (best) {
+        res = *best;
+        have = true;
+    }
+    if (!best || best->phase != PHASE_INIT) {
+        /* the post-time-step loop runs in node order and overwrites */
+        std::vector<ErrRec> pts;
+        for (auto &e : c)
+            if (e.phase == PHASE_PTS)
+                pts.push_back(e);
+        std::sort(pts.begin(), pts.end(), [](const ErrRec &x, const ErrRec &y) {
+            return x.node < y.node;
+        });
+        for (auto &e : pts) {
+            res = e;
+            have = true;
+            if (e.code != SIMINF_GPU_ERR_INVALID_RATE)
+                break;
+        }
+    }
+    if (!have)
+        return 0;
+    char msg[300];
+    snprintf(msg, sizeof(msg),
+             "error %d at time %g, replicate %d, node %d (one-based), transition %d, event %d, rate %g",
+             res.code, res.time, res.rep + 1, res.node + 1,
+             res.transition >= 0 ? res.transition + 1 : 0,
+             res.event_index >= 0 ? res.event_index + 1 : 0, res.rate);
+    set_status(res.code, res.node, res.transition, res.event_index, res.time, res.rate, msg);
+    return res.code;
+}
+
+int siminf_gpu_plan_run(siminf_gpu_plan *p, void *cuda_stream)
+{
+    if (!p)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    memset(&g_status, 0, sizeof(g_status));
+    cudaStream_t st = (cudaStream_t) cuda_stream;
+    DevState s = p->s;
+    const Launchers *L = p->L;
+    cudaError_t e;
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, st);
+
+    const int init_flags[3] = {0, INT_MAX, INT_MAX};
+    e = cudaMemcpyAsync(s.err_count, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(s.fired, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s.u, p->u0_host, (size_t) s.Ntot * s.Nc * sizeof(int),
+                            cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess && s.Nd > 0) {
+        e = cudaMemcpyAsync(s.vA, p->v0_host, (size_t) s.Ntot * s.Nd * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s.vB, p->v0_host, (size_t) s.Ntot * s.Nd * sizeof(double),
+                                cudaMemcpyDeviceToDevice, st);
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(e, "plan_run reset");
+
+    e = L->init(s, p->tt0, st);
+    if (e == cudaSuccess) {
+        if (p->horizon) {
+            e = L->horizon(s, p->d_days, p->ndays, st);
+        } else {
+            for (int d = 0; d < p->ndays && e == cudaSuccess; d++) {
+                const DayInfo &di = p->days[d];
+                e = L->ssa_e1(s, d, di.tt, di.next, st);
+                for (int w = p->day_wave[d]; w < p->day_wave[d + 1] && e == cudaSuccess; w++) {
+                    const long long off = p->wave_ptr[w];
+                    const int cnt = (int) (p->wave_ptr[w + 1] - off);
+                    e = L->e2_wave(s, p->d_e2 + off, cnt, d, di.tt, st);
+                }
+                if (e == cudaSuccess)
+                    e = L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
+                std::swap(s.vA, s.vB);
+            }
+        }
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(e, "kernel launch");
+    cudaEventRecord(ev1, st);
+    e = cudaEventSynchronize(ev1);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "solver kernels");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+
+    int counts[3];
+    unsigned long long fired = 0;
+    e = cudaMemcpy(counts, s.err_count, sizeof(counts), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&fired, s.fired, sizeof(fired), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "read counters");
+    p->stats.transitions = fired;
+    p->stats.node_days = (uint64_t) p->ndays * (uint64_t) s.Ntot;
+    p->stats.ms_solve = ms;
+    p->ran = true;
+
+    std::vector<ErrRec> cands;
+    if (counts[0] > 0) {
+        cands.resize(std::min(counts[0], (int) MAX_ERR));
+        e = cudaMemcpy(cands.data(), s.err, cands.size() * sizeof(ErrRec), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "read errors");
+    }
+    return resolve_errors(p, cands);
+}
+
+int siminf_gpu_plan_download(siminf_gpu_plan *p, siminf_gpu_solver_args *a)
+{
+    if (!p || !a)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    auto t0 = std::chrono::steady_clock::now();
+    cudaError_t e = cudaSuccess;
+    if (a->U && p->s.U)
+        e = cudaMemcpy(a->U, p->s.U, p->U_len * sizeof(int), cudaMemcpyDeviceToHost);
+    else if (a->prU && p->s.prU)
+        e = cudaMemcpy(a->prU, p->s.prU, p->prU_len * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && a->V && p->s.V)
+        e = cudaMemcpy(a->V, p->s.V, p->V_len * sizeof(double), cudaMemcpyDeviceToHost);
+    else if (e == cudaSuccess && a->prV && p->s.prV)
+        e = cudaMemcpy(a->prV, p->s.prV, p->prV_len * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "download");
+    p->stats.ms_download = ms_since(t0);
+    return 0;
+}
+
+int siminf_gpu_plan_stats(const siminf_gpu_plan *p, siminf_gpu_stats *out)
+{
+    if (!p || !out)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    *out = p->stats;
+    return 0;
+}
+
+static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *model)
+{
+    siminf_gpu_plan *p = nullptr;
+    int rc = siminf_gpu_plan_create(args, model, &p);
+    if (rc)
+        return rc;
+    rc = siminf_gpu_plan_run(p, nullptr);
+    if (!rc)
+        rc = siminf_gpu_plan_download(p, args);
+    g_stats = p->stats;
+    siminf_gpu_plan_free(p);
+    return rc;
+}
+
+int siminf_gpu_run_solver_ssm(siminf_gpu_solver_args *args, const siminf_gpu_model *model)
+{
+    return run_solver(args, model);
+}
+
+int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args, const siminf_gpu_model *model)
+{
+    return run_solver(args, model);
+}
+
+}  /* extern "C" */

@@ -1,0 +1,840 @@
+/*
+ * siminf_kernels.cu -- the GB300 kernels of the ssm/mssm solver.
+ *
+ * One thread owns one (replicate, node) pair g for the node phases:
+ *   k_init       rate initialisation      src/solvers/SimInf_solver_ssm.c:96-117
+ *   k_ssa_e1     direct-method SSA up to the next unit of time
+ *                                          src/solvers/SimInf_solver_ssm.c:144-235
+ *                followed by the node's E1 events of the day
+ *                                          src/solvers/SimInf_solver.c:658-822
+ *   k_e2_wave    one conflict-free wavefront of external transfers
+ *                                          src/solvers/SimInf_solver.c:824-902
+ *   k_pts_store  post time step, rate refresh, U/V store
+ *                                          src/solvers/SimInf_solver_ssm.c:262-334
+ *   k_horizon    all days of one node in one thread, for schedules without
+ *                external transfers (nodes never interact)
+ *
+ * Node state lives in registers for the whole day (u as int[NC], rates as
+ * double[NT]); S and the G column masks sit in shared memory so the
+ * transition index can stay dynamic without spilling the register arrays.
+ * Random draws come from the node's Philox stream (siminf_stream.h), and
+ * the logarithm is the integer fixed-point si_log: on GB300 the FP64 pipe
+ * retires one warp instruction per 64 cycles per SM sub-partition, while the
+ * integer pipes are ~40x faster, so the SSA chain keeps only the FP64
+ * operations the reference's arithmetic requires.
+ *
+ * Compiled with -fmad=false: every double operation rounds as in the
+ * reference's C, which is what makes trajectories bit-identical.
+ */
+#include <climits>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "siminf_stream.h"
+#include "siminf_models.cuh"
+#include "siminf_plan.h"
+#include "siminf_launch.h"
+
+namespace siminf {
+
+enum { ERR_NEGATIVE_STATE = -1, ERR_UNDEFINED_EVENT = -3, ERR_SAMPLE_SELECT = -8,
+       ERR_INVALID_RATE = -11, ERR_EVENTS_N = -15, ERR_EVENT_SHIFT = -16,
+       ERR_SHIFT_OUT_OF_BOUNDS = -17, ERR_INVALID_PROPORTION = -18 };
+
+enum { EV_EXIT = 0, EV_ENTER = 1, EV_INTERNAL = 2, EV_EXTERNAL = 3 };
+
+__device__ __forceinline__ void record_error(const DevState &s, int code, int phase, int day,
+                                             long long g, int tr, int evi, double time,
+                                             double rate)
+{
+    const int slot = atomicAdd(s.err_count, 1);
+    atomicMin(s.err_day, day);
+    if (phase <= PHASE_E1)
+        atomicMin(s.err_day_pre_e2, day);
+    if (slot < MAX_ERR) {
+        ErrRec e;
+        e.code = code;
+        e.phase = phase;
+        e.day = day;
+        e.rep = (int) (g / s.Nn);
+        e.node = (int) (g % s.Nn);
+        e.transition = tr;
+        e.event_index = evi;
+        e.pad = 0;
+        e.time = time;
+        e.rate = rate;
+        s.err[slot] = e;
+    }
+}
+
+__device__ __forceinline__ int load_flag(const int *p)
+{
+    return *(volatile const int *) p;
+}
+
+/* Sum the per-thread transition counts of a warp into the global counter. */
+__device__ __forceinline__ void add_fired(const DevState &s, unsigned long long n)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        n += __shfl_down_sync(0xFFFFFFFFu, n, o);
+    if ((threadIdx.x & 31) == 0 && n)
+        atomicAdd(s.fired, n);
+}
+
+/* ------------------------------------------------------------------ */
+/* Direct-method SSA of one node up to `next`.                          */
+/* ------------------------------------------------------------------ */
+template <class M>
+__device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::NT], double &sum,
+                                            double &t, const double *v, const double *ld,
+                                            const double *gd, si_rng &r, double next,
+                                            const int *sS, const uint32_t *sG, int &err,
+                                            int &err_tr, double &err_t, double &err_rate)
+{
+    constexpr int NC = M::NC, NT = M::NT;
+    unsigned fired = 0;
+    for (;;) {
+        if (sum <= 0.0) {
+            t = next;
+            break;
+        }
+        const double tau = -si_log(si_uniform_pos(&r)) / sum;
+        if ((tau + t) >= next) {
+            t = next;
+            break;
+        }
+        t += tau;
+
+        /* Inversion over the rates in transition order. */
+        const double rnd = si_uniform_pos(&r) * sum;
+        int tr = 0;
+        double cum = rate[0];
+#pragma unroll
+        for (int k = 1; k < NT; k++) {
+            if (tr == k - 1 && rnd > cum) {
+                tr = k;
+                cum += rate[k];
+            }
+        }
+        double rtr = rate[0];
+#pragma unroll
+        for (int k = 1; k < NT; k++)
+            if (tr == k)
+                rtr = rate[k];
+        if (rtr == 0.0) {
+            /* Back-scan to the first non-zero rate (ssm.c:171-189). */
+#pragma unroll
+            for (int k = NT - 1; k >= 1; k--)
+                if (tr == k && rate[k] == 0.0)
+                    tr = k - 1;
+            double r2 = rate[0];
+#pragma unroll
+            for (int k = 1; k < NT; k++)
+                if (tr == k)
+                    r2 = rate[k];
+            if (r2 == 0.0) {
+                sum = 0.0;
+                break;
+            }
+        }
+
+        fired++;
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int d = sS[tr * NC + c];
+            if (d != 0) {
+                u[c] += d;
+                if (u[c] < 0) {
+                    err = ERR_NEGATIVE_STATE;
+                    err_tr = tr;
+                    err_t = t;
+                    err_rate = 0.0;
+                }
+            }
+        }
+
+        /* Refresh the rates flagged in column tr of G, in row order. */
+        double delta = 0.0;
+        const uint32_t gm = sG[tr];
+#pragma unroll
+        for (int k = 0; k < NT; k++) {
+            if (gm & (1u << k)) {
+                const double old = rate[k];
+                const double nr = M::rate(k, u, v, ld, gd, t);
+                rate[k] = nr;
+                delta += nr - old;
+                if (!isfinite(nr) || nr < 0.0) {
+                    err = ERR_INVALID_RATE;
+                    err_tr = k;
+                    err_t = t;
+                    err_rate = nr;
+                }
+            }
+        }
+        sum += delta;
+    }
+    return fired;
+}
+
+/* ------------------------------------------------------------------ */
+/* Event sampling on a node's compartments uu (src/solvers/             */
+/* SimInf_solver.c:62-324), drawing from the node's stream.             */
+/* ------------------------------------------------------------------ */
+template <int NC>
+__device__ int sample_select(const DevState &s, const int *uu, int select, int n,
+                             double proportion, int *ind, si_rng *r)
+{
+    const int *irE = s.irE, *jcE = s.jcE;
+    const double *prE = s.prE;
+    int i, Nstates, Nindividuals = 0, Nkinds = 0;
+
+    for (int c = 0; c < NC; c++)
+        ind[c] = 0;
+    for (i = jcE[select]; i < jcE[select + 1]; i++) {
+        const int nk = uu[irE[i]];
+        if (nk > 0)
+            Nkinds++;
+        Nindividuals += nk;
+    }
+    Nstates = jcE[select + 1] - jcE[select];
+    if (n == 0) {
+        if (proportion < 0 || proportion > 1)
+            return ERR_INVALID_PROPORTION;
+        n = si_binomial(r, proportion, Nindividuals);
+    }
+    if (Nstates <= 0 || n > Nindividuals || n < 0)
+        return ERR_SAMPLE_SELECT;
+    if (n == 0)
+        return 0;
+    if (Nindividuals == n) {
+        for (i = jcE[select]; i < jcE[select + 1]; i++)
+            ind[irE[i]] = uu[irE[i]];
+        return 0;
+    }
+    if (Nstates == 1) {
+        ind[irE[jcE[select]]] = n;
+        return 0;
+    }
+    if (Nkinds == 1) {
+        for (i = jcE[select]; i < jcE[select + 1]; i++) {
+            if (uu[irE[i]] > 0) {
+                ind[irE[i]] = n;
+                break;
+            }
+        }
+        return 0;
+    }
+    bool equal = true;
+    for (i = jcE[select] + 1; i < jcE[select + 1]; i++)
+        if (prE[i] != prE[i - 1])
+            equal = false;
+    if (equal) {
+        /* Sequential multivariate hypergeometric. */
+        for (i = jcE[select]; i < jcE[select + 1] - 1; i++) {
+            if (n == 0)
+                break;
+            const int nk = uu[irE[i]];
+            ind[irE[i]] = si_hypergeometric(r, nk, Nindividuals - nk, n);
+            Nindividuals -= nk;
+            n -= ind[irE[i]];
+        }
+        ind[irE[i]] = n;
+        return 0;
+    }
+    /* Wallenius' noncentral hypergeometric by a biased urn. */
+    while (n > 0) {
+        double rand, cum = 0;
+        for (i = jcE[select]; i < jcE[select + 1]; i++)
+            cum += prE[i] * (uu[irE[i]] - ind[irE[i]]);
+        rand = si_uniform_pos(r) * cum;
+        i = jcE[select];
+        cum = prE[i] * (uu[irE[i]] - ind[irE[i]]);
+        while (i < jcE[select + 1] && rand > cum) {
+            i++;
+            if (i < jcE[select + 1])
+                cum += prE[i] * (uu[irE[i]] - ind[irE[i]]);
+        }
+        if (i >= jcE[select + 1])
+            i = jcE[select + 1] - 1;
+        if ((prE[i] * (uu[irE[i]] - ind[irE[i]])) == 0.0) {
+            for (; i > jcE[select] && (prE[i] * (uu[irE[i]] - ind[irE[i]])) == 0.0; i--);
+            if ((prE[i] * (uu[irE[i]] - ind[irE[i]])) == 0.0)
+                return ERR_SAMPLE_SELECT;
+        }
+        ind[irE[i]] += 1;
+        n--;
+    }
+    return 0;
+}
+
+template <int NC>
+__device__ int sample_select_enter(const DevState &s, const int *uu, int select, int n,
+                                   double proportion, int *ind, si_rng *r)
+{
+    const int *irE = s.irE, *jcE = s.jcE;
+    const double *prE = s.prE;
+    int i, Nstates = jcE[select + 1] - jcE[select];
+    double w_cum = 0;
+
+    for (int c = 0; c < NC; c++)
+        ind[c] = 0;
+    if (n == 0) {
+        if (proportion < 0 || proportion > 1)
+            return ERR_INVALID_PROPORTION;
+        for (i = jcE[select]; i < jcE[select + 1]; i++)
+            n += uu[irE[i]];
+        n = si_binomial(r, proportion, n);
+    }
+    if (Nstates <= 0 || n < 0)
+        return ERR_SAMPLE_SELECT;
+    if (n == 0)
+        return 0;
+    if (Nstates == 1) {
+        ind[irE[jcE[select]]] = n;
+        return 0;
+    }
+    for (i = jcE[select]; i < jcE[select + 1]; i++)
+        w_cum += prE[i];
+    while (n > 0) {
+        double cum, rand = si_uniform_pos(r) * w_cum;
+        i = jcE[select];
+        cum = prE[i];
+        while (i < jcE[select + 1] && rand > cum) {
+            i++;
+            if (i < jcE[select + 1])
+                cum += prE[i];
+        }
+        if (i >= jcE[select + 1])
+            i = jcE[select + 1] - 1;
+        if (prE[i] == 0.0) {
+            for (; i > jcE[select] && prE[i] == 0.0; i--);
+            if (prE[i] == 0.0)
+                return ERR_SAMPLE_SELECT;
+        }
+        ind[irE[i]] += 1;
+        n--;
+    }
+    return 0;
+}
+
+/* Apply one E1 event to the node's compartments uu
+ * (src/solvers/SimInf_solver.c:680-822).  Returns 0 or an error code. */
+template <int NC>
+__device__ int apply_e1(const DevState &s, int *uu, const E1Rec &e, si_rng *r)
+{
+    int ind[NC];
+    int err;
+    const int *irE = s.irE, *jcE = s.jcE;
+
+    switch (e.kind) {
+    case EV_EXIT:
+        err = sample_select<NC>(s, uu, e.select, e.n, e.proportion, ind, r);
+        if (err)
+            return err;
+        for (int i = jcE[e.select]; i < jcE[e.select + 1]; i++) {
+            const int jj = irE[i];
+            uu[jj] -= ind[jj];
+            if (uu[jj] < 0)
+                return ERR_NEGATIVE_STATE;
+        }
+        return 0;
+    case EV_ENTER:
+        err = sample_select_enter<NC>(s, uu, e.select, e.n, e.proportion, ind, r);
+        if (err)
+            return err;
+        for (int i = jcE[e.select]; i < jcE[e.select + 1]; i++) {
+            const int jj = irE[i];
+            if (e.shift < 0) {
+                uu[jj] += ind[jj];
+                if (uu[jj] < 0)
+                    return ERR_NEGATIVE_STATE;
+            } else if (!s.Nshift) {
+                return ERR_EVENTS_N;
+            } else {
+                const int ll = s.Nshift[e.shift * NC + jj];
+                if (jj + ll < 0 || jj + ll >= NC)
+                    return ERR_SHIFT_OUT_OF_BOUNDS;
+                uu[jj + ll] += ind[jj];
+                if (uu[jj + ll] < 0)
+                    return ERR_NEGATIVE_STATE;
+            }
+        }
+        return 0;
+    case EV_INTERNAL:
+        if (!s.Nshift)
+            return ERR_EVENTS_N;
+        if (e.shift < 0)
+            return ERR_EVENT_SHIFT;
+        err = sample_select<NC>(s, uu, e.select, e.n, e.proportion, ind, r);
+        if (err)
+            return err;
+        for (int i = jcE[e.select]; i < jcE[e.select + 1]; i++) {
+            const int jj = irE[i];
+            const int ll = s.Nshift[e.shift * NC + jj];
+            if (jj + ll < 0 || jj + ll >= NC)
+                return ERR_SHIFT_OUT_OF_BOUNDS;
+            uu[jj + ll] += ind[jj];
+            if (uu[jj + ll] < 0)
+                return ERR_NEGATIVE_STATE;
+            uu[jj] -= ind[jj];
+            if (uu[jj] < 0)
+                return ERR_NEGATIVE_STATE;
+        }
+        return 0;
+    default:
+        return ERR_UNDEFINED_EVENT;
+    }
+}
+
+/* The node's E1 events of `day`, in array order.  Returns true when an
+ * event was applied (the node is then flagged for a rate refresh). */
+template <int NC>
+__device__ bool node_e1(const DevState &s, int (&u)[NC], int node, int day, si_rng &r,
+                        long long g, double tt, int &err_code, int &err_event)
+{
+    int lo = s.e1_ptr[node], hi = s.e1_ptr[node + 1];
+    if (lo == hi)
+        return false;
+    /* first event with e.day >= day */
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s.e1[mid].day < day)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    const int end = s.e1_ptr[node + 1];
+    if (lo >= end || s.e1[lo].day != day)
+        return false;
+    int uu[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+        uu[c] = u[c];
+    bool any = false;
+    for (int k = lo; k < end; k++) {
+        const E1Rec e = s.e1[k];
+        if (e.day != day)
+            break;
+        const int err = apply_e1<NC>(s, uu, e, &r);
+        any = true;
+        if (err) {
+            err_code = err;
+            err_event = e.index;
+            break;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+        u[c] = uu[c];
+    return any;
+}
+
+/* Store the node's U/V entries for columns [c0, c1) of its replicate. */
+template <int NC, int ND>
+__device__ __forceinline__ void store_columns(const DevState &s, int rep, int node,
+                                              const int (&u)[NC], const double *vnew,
+                                              int c0, int c1)
+{
+    for (int col = c0; col < c1; col++) {
+        const size_t ccol = (size_t) rep * s.tlen + col;
+        if (s.U) {
+            int *dst = s.U + ccol * (size_t) s.Nn * NC + (size_t) node * NC;
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+                dst[c] = u[c];
+        } else if (s.jcU) {
+            /* rows of this node in the sorted CSC column */
+            int lo = s.jcU[ccol], hi = s.jcU[ccol + 1];
+            const int row0 = node * NC;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s.irU[mid] < row0)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            for (int k = lo; k < s.jcU[ccol + 1] && s.irU[k] < row0 + NC; k++) {
+                const int c = s.irU[k] - row0;
+                int val = u[0];
+#pragma unroll
+                for (int q = 1; q < NC; q++)
+                    if (c == q)
+                        val = u[q];
+                s.prU[k] = (double) val;
+            }
+        }
+        if (ND > 0) {
+            if (s.V) {
+                double *dst = s.V + ccol * (size_t) s.Nn * ND + (size_t) node * ND;
+#pragma unroll
+                for (int d = 0; d < ND; d++)
+                    dst[d] = vnew[d];
+            } else if (s.jcV) {
+                int lo = s.jcV[ccol], hi = s.jcV[ccol + 1];
+                const int row0 = node * ND;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s.irV[mid] < row0)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                for (int k = lo; k < s.jcV[ccol + 1] && s.irV[k] < row0 + ND; k++)
+                    s.prV[k] = vnew[s.irV[k] - row0];
+            }
+        }
+    }
+}
+
+template <class M>
+__device__ __forceinline__ void load_model_smem(const DevState &s, int *sS, uint32_t *sG)
+{
+    for (int i = threadIdx.x; i < M::NT * M::NC; i += blockDim.x)
+        sS[i] = s.S[i];
+    for (int i = threadIdx.x; i < M::NT; i += blockDim.x)
+        sG[i] = s.Gmask[i];
+    __syncthreads();
+}
+
+/* ------------------------------------------------------------------ */
+/* Kernels.                                                              */
+/* ------------------------------------------------------------------ */
+
+template <class M>
+__global__ void k_init(DevState s, double tt0)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (g >= s.Ntot)
+        return;
+    const int node = (int) (g % s.Nn);
+    int u[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+        u[c] = s.u[g * NC + c];
+    const double *v = s.vA + g * ND;
+    const double *ld = s.ldata + (size_t) node * s.Nld;
+    double sum = 0.0;
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        const double rate = M::rate(j, u, v, ld, s.gdata, tt0);
+        s.t_rate[(size_t) j * s.Ntot + g] = rate;
+        sum += rate;
+        if (!isfinite(rate) || rate < 0.0)
+            record_error(s, ERR_INVALID_RATE, PHASE_INIT, 0, g, j, -1, tt0, rate);
+    }
+    s.sum_rate[g] = sum;
+    s.t_time[g] = tt0;
+    s.ctr[g] = 0;
+    s.update[g] = 0;
+}
+
+template <class M>
+__global__ void __launch_bounds__(256) k_ssa_e1(DevState s, int day, double tt, double next)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    __shared__ int sS[NT * NC];
+    __shared__ uint32_t sG[NT];
+    load_model_smem<M>(s, sS, sG);
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    unsigned long long fired = 0;
+    if (g < s.Ntot && load_flag(s.err_day) >= day) {
+        const int node = (int) (g % s.Nn);
+        int u[NC];
+        double rate[NT];
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            u[c] = s.u[g * NC + c];
+#pragma unroll
+        for (int k = 0; k < NT; k++)
+            rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
+        double sum = s.sum_rate[g], t = s.t_time[g];
+        si_rng r;
+        si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
+        const double *v = s.vA + g * ND;
+        const double *ld = s.ldata + (size_t) node * s.Nld;
+        int err = 0, err_tr = -1;
+        double err_t = 0, err_rate = 0;
+        fired = ssa_day<M>(u, rate, sum, t, v, ld, s.gdata, r, next, sS, sG, err, err_tr,
+                           err_t, err_rate);
+        if (err) {
+            record_error(s, err, PHASE_SSA, day, g, err_tr, -1, err_t, err_rate);
+        } else {
+            int e_code = 0, e_idx = -1;
+            if (node_e1<NC>(s, u, node, day, r, g, tt, e_code, e_idx))
+                s.update[g] = 1;
+            if (e_code)
+                record_error(s, e_code, PHASE_E1, day, g, -1, e_idx, tt, 0);
+        }
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            s.u[g * NC + c] = u[c];
+#pragma unroll
+        for (int k = 0; k < NT; k++)
+            s.t_rate[(size_t) k * s.Ntot + g] = rate[k];
+        s.sum_rate[g] = sum;
+        s.t_time[g] = t;
+        s.ctr[g] = r.ctr;
+    }
+    add_fired(s, fired);
+}
+
+template <class M>
+__global__ void __launch_bounds__(256) k_e2_wave(DevState s, const E2Rec *ev, int count, int day,
+                                                 double tt)
+{
+    constexpr int NC = M::NC;
+    const long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (i >= (long long) count * s.Nrep)
+        return;
+    if (load_flag(s.err_day) < day || load_flag(s.err_day_pre_e2) <= day)
+        return;
+    const int rep = (int) (i / count);
+    const E2Rec e = ev[i - (long long) rep * count];
+    const long long gs = (long long) rep * s.Nn + e.src;
+    const long long gd = (long long) rep * s.Nn + e.dst;
+    int uu[NC], ind[NC];
+    for (int c = 0; c < NC; c++)
+        uu[c] = s.u[gs * NC + c];
+    si_rng r;
+    si_rng_init(&r, s.seed, (uint64_t) gs, s.ctr[gs]);
+    int err = sample_select<NC>(s, uu, e.select, e.n, e.proportion, ind, &r);
+    s.ctr[gs] = r.ctr;
+    if (err) {
+        record_error(s, err, PHASE_E2, day, gs, -1, e.index, tt, 0);
+        return;
+    }
+    for (int k = s.jcE[e.select]; k < s.jcE[e.select + 1]; k++) {
+        const int jj = s.irE[k];
+        int dj = jj;
+        if (e.shift >= 0) {
+            if (!s.Nshift) {
+                record_error(s, ERR_EVENTS_N, PHASE_E2, day, gs, -1, e.index, tt, 0);
+                return;
+            }
+            const int ll = s.Nshift[e.shift * NC + jj];
+            if (jj + ll < 0 || jj + ll >= NC) {
+                record_error(s, ERR_SHIFT_OUT_OF_BOUNDS, PHASE_E2, day, gs, -1, e.index, tt, 0);
+                return;
+            }
+            dj = jj + ll;
+        }
+        if (ind[jj]) {
+            const int old = atomicAdd(&s.u[gd * NC + dj], ind[jj]);
+            if (old + ind[jj] < 0) {
+                record_error(s, ERR_NEGATIVE_STATE, PHASE_E2, day, gs, -1, e.index, tt, 0);
+                return;
+            }
+            /* The source is exclusive to this event within the wave; a
+             * self-transfer reads back its own atomic add. */
+            const int nv = s.u[gs * NC + jj] - ind[jj];
+            s.u[gs * NC + jj] = nv;
+            if (nv < 0) {
+                record_error(s, ERR_NEGATIVE_STATE, PHASE_E2, day, gs, -1, e.index, tt, 0);
+                return;
+            }
+        }
+    }
+    s.update[gd] = 1;
+    s.update[gs] = 1;
+}
+
+template <class M>
+__global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double tt, int c0, int c1,
+                                                   const double *v_in, double *v_out)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (g >= s.Ntot || load_flag(s.err_day) < day)
+        return;
+    const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
+    int u[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+        u[c] = s.u[g * NC + c];
+    const double *vi = v_in + g * ND;
+    double *vo = v_out + g * ND;
+    const double *ld = s.ldata + (size_t) node * s.Nld;
+    const int rc = M::pts(vo, u, vi, ld, s.gdata, node, tt);
+    if (rc < 0) {
+        record_error(s, rc, PHASE_PTS, day, g, -1, -1, tt, 0);
+    } else if (rc > 0 || s.update[g]) {
+        double delta = 0.0;
+#pragma unroll
+        for (int k = 0; k < NT; k++) {
+            const double old = s.t_rate[(size_t) k * s.Ntot + g];
+            const double nr = M::rate(k, u, vo, ld, s.gdata, tt);
+            s.t_rate[(size_t) k * s.Ntot + g] = nr;
+            delta += nr - old;
+            if (!isfinite(nr) || nr < 0.0)
+                record_error(s, ERR_INVALID_RATE, PHASE_PTS, day, g, k, -1, tt, nr);
+        }
+        s.sum_rate[g] += delta;
+        s.update[g] = 0;
+    }
+    store_columns<NC, ND>(s, rep, node, u, vo, c0, c1);
+}
+
+/* Whole horizon of one (replicate, node) in one thread: valid when no
+ * external transfer couples nodes and the post-time-step function reads
+ * only its own node. */
+template <class M>
+__global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days, int ndays)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    __shared__ int sS[NT * NC];
+    __shared__ uint32_t sG[NT];
+    load_model_smem<M>(s, sS, sG);
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    unsigned long long fired = 0;
+    if (g < s.Ntot) {
+        const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
+        int u[NC];
+        double rate[NT];
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            u[c] = s.u[g * NC + c];
+#pragma unroll
+        for (int k = 0; k < NT; k++)
+            rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
+        double sum = s.sum_rate[g], t = s.t_time[g];
+        si_rng r;
+        si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
+        double *v = s.vA + g * ND, *vn = s.vB + g * ND;
+        const double *ld = s.ldata + (size_t) node * s.Nld;
+        for (int d = 0; d < ndays; d++) {
+            if (load_flag(s.err_day) < d)
+                break;
+            const DayInfo di = days[d];
+            int err = 0, err_tr = -1;
+            double err_t = 0, err_rate = 0;
+            fired += ssa_day<M>(u, rate, sum, t, v, ld, s.gdata, r, di.next, sS, sG, err,
+                                err_tr, err_t, err_rate);
+            if (err) {
+                record_error(s, err, PHASE_SSA, d, g, err_tr, -1, err_t, err_rate);
+                break;
+            }
+            int e_code = 0, e_idx = -1;
+            bool upd = node_e1<NC>(s, u, node, d, r, g, di.tt, e_code, e_idx);
+            if (e_code) {
+                record_error(s, e_code, PHASE_E1, d, g, -1, e_idx, di.tt, 0);
+                break;
+            }
+            const int rc = M::pts(vn, u, v, ld, s.gdata, node, di.tt);
+            if (rc < 0) {
+                record_error(s, rc, PHASE_PTS, d, g, -1, -1, di.tt, 0);
+                break;
+            }
+            if (rc > 0 || upd) {
+                double delta = 0.0;
+                bool bad = false;
+#pragma unroll
+                for (int k = 0; k < NT; k++) {
+                    const double old = rate[k];
+                    const double nr = M::rate(k, u, vn, ld, s.gdata, di.tt);
+                    rate[k] = nr;
+                    delta += nr - old;
+                    if (!isfinite(nr) || nr < 0.0) {
+                        record_error(s, ERR_INVALID_RATE, PHASE_PTS, d, g, k, -1, di.tt, nr);
+                        bad = true;
+                    }
+                }
+                sum += delta;
+                if (bad)
+                    break;
+            }
+            store_columns<NC, ND>(s, rep, node, u, vn, di.c0, di.c1);
+            double *tmp = v;
+            v = vn;
+            vn = tmp;
+        }
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            s.u[g * NC + c] = u[c];
+#pragma unroll
+        for (int k = 0; k < NT; k++)
+            s.t_rate[(size_t) k * s.Ntot + g] = rate[k];
+        s.sum_rate[g] = sum;
+        s.t_time[g] = t;
+        s.ctr[g] = r.ctr;
+    }
+    add_fired(s, fired);
+}
+
+/* ------------------------------------------------------------------ */
+/* Launchers, one table per model.                                      */
+/* ------------------------------------------------------------------ */
+
+static inline unsigned blocks_for(long long n, int threads)
+{
+    return (unsigned) ((n + threads - 1) / threads);
+}
+
+template <class M>
+struct Launch {
+    static cudaError_t init(const DevState &s, double tt0, cudaStream_t st)
+    {
+        k_init<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, tt0);
+        return cudaGetLastError();
+    }
+    static cudaError_t horizon(const DevState &s, const DayInfo *days, int ndays, cudaStream_t st)
+    {
+        k_horizon<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, days, ndays);
+        return cudaGetLastError();
+    }
+    static cudaError_t ssa_e1(const DevState &s, int day, double tt, double next, cudaStream_t st)
+    {
+        k_ssa_e1<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, next);
+        return cudaGetLastError();
+    }
+    static cudaError_t e2_wave(const DevState &s, const E2Rec *ev, int count, int day, double tt,
+                               cudaStream_t st)
+    {
+        const long long n = (long long) count * s.Nrep;
+        if (n == 0)
+            return cudaSuccess;
+        k_e2_wave<M><<<blocks_for(n, 256), 256, 0, st>>>(s, ev, count, day, tt);
+        return cudaGetLastError();
+    }
+    static cudaError_t pts_store(const DevState &s, int day, double tt, int c0, int c1,
+                                 const double *v_in, double *v_out, cudaStream_t st)
+    {
+        k_pts_store<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, c0, c1, v_in, v_out);
+        return cudaGetLastError();
+    }
+    static const Launchers *table()
+    {
+        static const Launchers t = {M::NC, M::NT, M::ND, M::NGD, M::PTS_LOCAL,
+                                    init, horizon, ssa_e1, e2_wave, pts_store};
+        return &t;
+    }
+};
+
+const Launchers *launchers_for(const char *name)
+{
+    struct Entry {
+        const char *name;
+        const Launchers *(*table)();
+    };
+    static const Entry entries[] = {
+        {"SIR", Launch<ModelSIR>::table},
+        {"SEIR", Launch<ModelSEIR>::table},
+        {"SIS", Launch<ModelSIS>::table},
+        {"SISe", Launch<ModelSISe>::table},
+        {"SISe3", Launch<ModelSISe3>::table},
+        {"SIR_mparse", Launch<ModelSIRmparse>::table},
+        {"SISe_pf", Launch<ModelSISePF>::table},
+    };
+    for (const Entry &e : entries) {
+        const char *a = e.name, *b = name;
+        while (*a && *a == *b) {
+            a++;
+            b++;
+        }
+        if (*a == 0 && *b == 0)
+            return e.table();
+    }
+    return nullptr;
+}
+
+}  // namespace siminf

@@ -1,0 +1,31 @@
+/*
+ * siminf_launch.h -- per-model kernel launchers (defined in
+ * siminf_kernels.cu, called by the host planner in siminf_capi.cpp).
+ */
+#ifndef SIMINF_LAUNCH_H
+#define SIMINF_LAUNCH_H
+
+#include <cuda_runtime.h>
+#include "siminf_plan.h"
+
+namespace siminf {
+
+struct Launchers {
+    int Nc, Nt, Nd;
+    int Ngd;            /* gdata entries the model reads */
+    bool pts_local;     /* post-time-step reads only its own node */
+    cudaError_t (*init)(const DevState &s, double tt0, cudaStream_t st);
+    cudaError_t (*horizon)(const DevState &s, const DayInfo *days, int ndays, cudaStream_t st);
+    cudaError_t (*ssa_e1)(const DevState &s, int day, double tt, double next, cudaStream_t st);
+    cudaError_t (*e2_wave)(const DevState &s, const E2Rec *ev, int count, int day, double tt,
+                           cudaStream_t st);
+    cudaError_t (*pts_store)(const DevState &s, int day, double tt, int c0, int c1,
+                             const double *v_in, double *v_out, cudaStream_t st);
+};
+
+/* The launcher table of a built-in device model, or nullptr. */
+const Launchers *launchers_for(const char *name);
+
+}  // namespace siminf
+
+#endif

@@ -1,0 +1,112 @@
+/*
+ * siminf_plan.h -- device-side data layout of one solver run, shared by the
+ * host planner (siminf_capi.cpp) and the kernels (siminf_kernels.cu).
+ *
+ * HBM layout, for Ntot = Nrep * Nn (replicate-major, g = rep * Nn + node):
+ *   u        int32  [Ntot][Nc]     node-major, the layout of one U column
+ *   v, v_new double [Ntot][Nd]     double-buffered, swapped every day
+ *   t_rate   double [Nt][Ntot]     transition-major (coalesced per warp)
+ *   sum_rate double [Ntot], t_time double [Ntot]
+ *   ctr      uint64 [Ntot]         next draw index of stream g
+ *   update   uint8  [Ntot]         node flagged by an event this day
+ *   U        int32  [(Nrep*tlen)][Nn*Nc]   the reference's column-major U
+ *   V        double [(Nrep*tlen)][Nn*Nd]
+ * Events are copied once per plan:
+ *   E1 (exit/enter/internal): e1[] sorted by (node, day, array order), with
+ *     e1_ptr[node] .. e1_ptr[node+1] the events of node.
+ *   E2 (external transfers): e2[] sorted by (day, wave, array order), with
+ *     the waves of day d in wave_ptr[day_wave[d]] .. wave_ptr[day_wave[d+1]].
+ */
+#ifndef SIMINF_PLAN_H
+#define SIMINF_PLAN_H
+
+#include <stdint.h>
+
+namespace siminf {
+
+enum { MAX_NC = 16, MAX_NT = 32, MAX_ERR = 1024 };
+
+enum { PHASE_INIT = 0, PHASE_SSA = 1, PHASE_E1 = 2, PHASE_E2 = 3, PHASE_PTS = 4 };
+
+struct E1Rec {          /* 32 bytes */
+    int day;
+    int kind;
+    int n;
+    int select;         /* zero-based column of E */
+    int shift;          /* zero-based column of N, or -1 */
+    int index;          /* position in the caller's event arrays */
+    double proportion;
+};
+
+struct E2Rec {          /* 32 bytes */
+    int src;            /* zero-based */
+    int dst;
+    int n;
+    int select;
+    int shift;
+    int index;
+    double proportion;
+};
+
+struct ErrRec {
+    int code;
+    int phase;
+    int day;
+    int rep;
+    int node;
+    int transition;
+    int event_index;
+    int pad;
+    double time;
+    double rate;
+};
+
+struct DayInfo {
+    double tt;          /* time at the start of the day */
+    double next;        /* next unit of time */
+    int c0, c1;         /* U/V columns stored after this day */
+};
+
+struct DevState {
+    int Nn, Nc, Nt, Nd, Nld, Nrep, tlen;
+    long long Ntot;
+    uint64_t seed;
+
+    /* model matrices */
+    const int *S;           /* dense, Nt rows of Nc */
+    const uint32_t *Gmask;  /* Nt: bit k set if rate k is refreshed after transition j */
+    const int *irE, *jcE;
+    const double *prE;
+    const int *Nshift;      /* Nc x Nshift, or NULL */
+    const double *ldata, *gdata;
+
+    /* state */
+    int *u;
+    double *vA, *vB;
+    double *t_rate, *sum_rate, *t_time;
+    uint64_t *ctr;
+    uint8_t *update;
+
+    /* events */
+    const int *e1_ptr;
+    const E1Rec *e1;
+
+    /* outputs: dense or sparse (pattern on the device) */
+    int *U;
+    double *V;
+    const int *irU, *jcU;
+    double *prU;
+    const int *irV, *jcV;
+    double *prV;
+
+    /* errors and counters */
+    ErrRec *err;
+    int *err_count;
+    int *err_day;           /* first day with an error (INT_MAX if none) */
+    int *err_day_pre_e2;    /* first day with an SSA or E1 error */
+    unsigned long long *fired;
+};
+
+}  // namespace siminf
+
+#endif

@@ -262,14 +262,18 @@ SI_HD double si_u128_to_double(uint64_t hi, uint64_t lo, int scale, int negative
     return si_bits_double(sign | (expo << 52) | (m & 0x000FFFFFFFFFFFFFULL));
 }
 
-#ifdef __CUDA_ARCH__
+/* One copy of the tables for host code and, under nvcc, one in device
+ * global memory (both compilation passes must see the declaration). */
+static const uint32_t si_log_r_host[128] = SI_LOG_R_INIT;
+static const uint64_t si_log_l_host[128] = SI_LOG_L_INIT;
+#ifdef __CUDACC__
 static __device__ const uint32_t si_log_r_dev[128] = SI_LOG_R_INIT;
 static __device__ const uint64_t si_log_l_dev[128] = SI_LOG_L_INIT;
+#endif
+#ifdef __CUDA_ARCH__
 #  define SI_LOG_R(j) si_log_r_dev[j]
 #  define SI_LOG_L(j) si_log_l_dev[j]
 #else
-static const uint32_t si_log_r_host[128] = SI_LOG_R_INIT;
-static const uint64_t si_log_l_host[128] = SI_LOG_L_INIT;
 #  define SI_LOG_R(j) si_log_r_host[j]
 #  define SI_LOG_L(j) si_log_l_host[j]
 #endif

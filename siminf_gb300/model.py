@@ -11,6 +11,7 @@ same G, S, E and ldata/gdata layouts as the reference's R constructors:
 - ``SIS``   R/SIS.R:54-59 (E), :122-130 (G, S, ldata = beta, gamma)
 - ``SISe``  R/SISe.R:140-150 (G, S, ldata = end_t1..end_t4, gdata = upsilon,
   gamma, alpha, beta_t1..beta_t4, epsilon; v0 = phi)
+- ``SISe3`` R/SISe3.R:56-61 (E), :158-197 (N, G, S, ldata, gdata, v0 = phi)
 - ``SIR_mparse`` and ``SISe_pf``: the models mparse (R/mparse.R:477-491)
   builds from the transition strings named in their docstrings.
 
@@ -43,9 +44,9 @@ def make_events(event, time, node, dest, n, proportion, select, shift, sort=True
         "select": np.asarray(select, dtype=np.int32),
         "shift": np.asarray(shift, dtype=np.int32),
     }
-    m = len(ev["event"])
+    m = max(v.size for v in ev.values())
     for k in EVENT_FIELDS:
-        ev[k] = np.broadcast_to(ev[k], (m,)).copy() if ev[k].ndim == 0 else ev[k]
+        ev[k] = np.broadcast_to(ev[k].reshape(-1), (m,)).copy() if ev[k].size == 1 else ev[k]
     if sort and m:
         order = np.lexsort((ev["select"], ev["event"], ev["time"]))
         ev = {k: np.ascontiguousarray(v[order]) for k, v in ev.items()}
@@ -145,6 +146,31 @@ def SISe(u0, tspan, phi, upsilon, gamma, alpha, beta_t1, beta_t2, beta_t3, beta_
                        E=E, events=events)
 
 
+def SISe3(u0, tspan, phi, upsilon_1, upsilon_2, upsilon_3, gamma_1, gamma_2, gamma_3,
+          alpha, beta_t1, beta_t2, beta_t3, beta_t4, end_t1, end_t2, end_t3, end_t4,
+          epsilon, events=None):
+    """R/SISe3.R:56-61 (E), :158-197 (N, G, S, v0, ldata, gdata)."""
+    u0 = _u0(u0, ("S_1", "I_1", "S_2", "I_2", "S_3", "I_3"))
+    n = u0.shape[1]
+    E = np.zeros((6, 6))
+    for col, rows in enumerate(([0], [2], [4], [0, 1], [2, 3], [4, 5])):
+        E[rows, col] = 1
+    N = np.array([[2, 0, 0], [2, 0, -1], [0, 2, 0], [0, 2, -1], [0, 0, 0], [0, 0, -1]],
+                 dtype=np.int32)
+    G = np.zeros((6, 6), dtype=np.int32)
+    S = np.zeros((6, 6), dtype=np.int32)
+    for a in range(3):
+        G[2 * a:2 * a + 2, 2 * a:2 * a + 2] = 1
+        S[2 * a, 2 * a], S[2 * a + 1, 2 * a] = -1, 1
+        S[2 * a, 2 * a + 1], S[2 * a + 1, 2 * a + 1] = 1, -1
+    ldata = _rep_ldata(n, end_t1, end_t2, end_t3, end_t4)
+    gdata = np.array([upsilon_1, upsilon_2, upsilon_3, gamma_1, gamma_2, gamma_3, alpha,
+                      beta_t1, beta_t2, beta_t3, beta_t4, epsilon], dtype=np.float64)
+    v0 = np.broadcast_to(np.asarray(phi, dtype=np.float64), (n,)).reshape(1, n)
+    return SimInfModel("SISe3", G, S, u0, tspan, v0=v0, ldata=ldata, gdata=gdata,
+                       E=E, N=N, events=events)
+
+
 def SIR_mparse(u0, tspan, beta, gamma, events=None):
     """mparse(transitions = c("S -> beta*S*I/N -> I", "I -> gamma*I -> R",
     "N <- S+I+R"), compartments = c("S","I","R"), gdata = c(beta, gamma)).
@@ -184,6 +210,6 @@ def _u0(u0, names):
     return a
 
 
-__all__ = ["SimInfModel", "SIR", "SEIR", "SIS", "SISe", "SIR_mparse", "SISe_pf",
+__all__ = ["SimInfModel", "SIR", "SEIR", "SIS", "SISe", "SISe3", "SIR_mparse", "SISe_pf",
            "make_events", "empty_events", "EXIT_EVENT", "ENTER_EVENT",
            "INTERNAL_TRANSFER_EVENT", "EXTERNAL_TRANSFER_EVENT"]

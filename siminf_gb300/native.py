@@ -1,0 +1,139 @@
+"""Loads libsiminf_gb300.so and declares the C ABI of include/siminf_gb300.h.
+
+There is no CPU fallback: if the library is missing, or no CUDA device is
+visible, every entry point fails loudly.
+"""
+import ctypes as C
+import os
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libsiminf_gb300.so")
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            "libsiminf_gb300.so is not built (expected at %s); run "
+            "`python -m siminf_gb300.build` or __graft_entry__.build()" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.siminf_gpu_model_builtin.argtypes = [C.c_char_p, C.POINTER(vp)]
+    L.siminf_gpu_model_builtin.restype = C.c_int
+    L.siminf_gpu_model_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int)]
+    L.siminf_gpu_model_free.argtypes = [vp]
+    L.siminf_gpu_model_free.restype = None
+    for name in ("siminf_gpu_run_solver_ssm", "siminf_gpu_run_solver_mssm"):
+        getattr(L, name).argtypes = [vp, vp]
+        getattr(L, name).restype = C.c_int
+    L.siminf_gpu_last_status.argtypes = [C.POINTER(abi.Status)]
+    L.siminf_gpu_last_stats.argtypes = [C.POINTER(abi.Stats)]
+    L.siminf_gpu_plan_create.argtypes = [vp, vp, C.POINTER(vp)]
+    L.siminf_gpu_plan_create.restype = C.c_int
+    L.siminf_gpu_plan_run.argtypes = [vp, vp]
+    L.siminf_gpu_plan_run.restype = C.c_int
+    L.siminf_gpu_plan_download.argtypes = [vp, vp]
+    L.siminf_gpu_plan_download.restype = C.c_int
+    L.siminf_gpu_plan_stats.argtypes = [vp, C.POINTER(abi.Stats)]
+    L.siminf_gpu_plan_free.argtypes = [vp]
+    L.siminf_gpu_plan_free.restype = None
+    _lib = L
+    return L
+
+
+EXPORTS = (
+    "siminf_gpu_model_builtin", "siminf_gpu_model_dims", "siminf_gpu_model_free",
+    "siminf_gpu_run_solver_ssm", "siminf_gpu_run_solver_mssm", "siminf_gpu_last_status",
+    "siminf_gpu_last_stats", "siminf_gpu_plan_create", "siminf_gpu_plan_run",
+    "siminf_gpu_plan_download", "siminf_gpu_plan_stats", "siminf_gpu_plan_free",
+)
+
+
+def last_status():
+    st = abi.Status()
+    lib().siminf_gpu_last_status(C.byref(st))
+    return st
+
+
+def last_stats():
+    st = abi.Stats()
+    lib().siminf_gpu_last_stats(C.byref(st))
+    return st
+
+
+def check(code):
+    if code != 0:
+        st = last_status()
+        raise abi.SimInfError(code, st.message.decode(errors="replace"))
+
+
+class DeviceModel:
+    """A device model compiled into the library (siminf_gpu_model_builtin)."""
+
+    def __init__(self, name):
+        self.name = name
+        h = C.c_void_p()
+        check(lib().siminf_gpu_model_builtin(name.encode(), C.byref(h)))
+        self.handle = h
+
+    def dims(self):
+        nc, nt, nd = C.c_int(), C.c_int(), C.c_int()
+        lib().siminf_gpu_model_dims(self.handle, C.byref(nc), C.byref(nt), C.byref(nd))
+        return nc.value, nt.value, nd.value
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.siminf_gpu_model_free(self.handle)
+            self.handle = None
+
+
+_models = {}
+
+
+def device_model(name):
+    if name not in _models:
+        _models[name] = DeviceModel(name)
+    return _models[name]
+
+
+class Plan:
+    """A device-resident run (siminf_gpu_plan_*): inputs uploaded once,
+    run() repeats the whole horizon on the GPU, download() fills the
+    holder's U/V buffers."""
+
+    def __init__(self, holder, model_name):
+        self.holder = holder
+        self.model = device_model(model_name)
+        h = C.c_void_p()
+        check(lib().siminf_gpu_plan_create(C.cast(holder.ref(), C.c_void_p), self.model.handle,
+                                           C.byref(h)))
+        self.handle = h
+
+    def run(self, stream=None):
+        check(lib().siminf_gpu_plan_run(self.handle, stream))
+
+    def download(self):
+        check(lib().siminf_gpu_plan_download(self.handle, C.cast(self.holder.ref(), C.c_void_p)))
+
+    def stats(self):
+        st = abi.Stats()
+        lib().siminf_gpu_plan_stats(self.handle, C.byref(st))
+        return st
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().siminf_gpu_plan_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,49 @@
+"""The user-facing run(): the counterpart of R's run(model, ...) (R/run.R:
+178-283) for the GPU solver.
+
+run() fills the solver argument struct from a SimInfModel, calls
+siminf_gpu_run_solver_ssm (one replicate) or siminf_gpu_run_solver_mssm
+(replicates > 1) -- the same dispatch as src/SimInf.c:382-399 -- and returns
+U and V in the reference's column-major layout: U is (Nn*Nc) x (Nrep*tlen),
+column r*tlen + k holding replicate r at tspan[k].
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi, native
+
+
+class Result:
+    def __init__(self, model, holder, stats):
+        self.model = model
+        m = model
+        tlen = len(m.tspan)
+        ncol = m.replicates * tlen
+        self.U = None if holder.U is None else holder.U.reshape((m.Nn * m.Nc, ncol), order="F")
+        self.V = None
+        if holder.V is not None and m.Nd > 0:
+            self.V = holder.V[:m.Nn * m.Nd * ncol].reshape((m.Nn * m.Nd, ncol), order="F")
+        self.prU = holder.prU
+        self.prV = holder.prV
+        self.stats = stats
+
+    def trajectory(self, compartment, replicate=0):
+        """Matrix (Nn, tlen) of one compartment (index) of one replicate."""
+        m = self.model
+        tlen = len(m.tspan)
+        cols = self.U[:, replicate * tlen:(replicate + 1) * tlen]
+        return cols[compartment::m.Nc, :]
+
+
+def run(model, seed=42, U_sparse=None, V_sparse=None):
+    """Simulate ``model`` on the GPU.  ``U_sparse``/``V_sparse`` are optional
+    (ir, jc) CSC patterns over (Nn*Nc) x (Nrep*tlen) selecting which entries
+    to record, as a punchcard does (R/punchcard.R:139-253)."""
+    holder = abi.build_args(model, seed, U_sparse=U_sparse, V_sparse=V_sparse)
+    dm = native.device_model(model.name)
+    fn = (native.lib().siminf_gpu_run_solver_mssm if model.replicates > 1
+          else native.lib().siminf_gpu_run_solver_ssm)
+    code = fn(C.cast(holder.ref(), C.c_void_p), dm.handle)
+    native.check(code)
+    return Result(model, holder, native.last_stats())

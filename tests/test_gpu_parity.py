@@ -1,0 +1,111 @@
+"""GPU trajectories against the oracle, bit for bit, through the C ABI
+(siminf_gpu_run_solver_ssm / _mssm), plus the golden vectors of the
+reference's R tests and the reference's error codes."""
+import numpy as np
+import pytest
+
+from helpers import (U_matrix, golden, model_from_fixture, parity_cases, run_gpu, run_oracle,
+                     sparse_pattern)
+from test_oracle import error_cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("label,m", parity_cases(), ids=[c[0] for c in parity_cases()])
+def test_gpu_matches_oracle(gpu, oracle_lib, label, m):
+    code_o, res, ho = run_oracle(m, threads=4)
+    code_g, hg, st = run_gpu(m)
+    assert code_o == 0 and code_g == 0
+    assert np.array_equal(hg.U, ho.U), label
+    assert np.array_equal(hg.V, ho.V), label
+    assert st.transitions == res.transitions
+    assert st.e1_events == res.e1_events and st.e2_events == res.e2_events
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 1234567, 2 ** 40 + 5])
+def test_gpu_seeds(gpu, oracle_lib, seed):
+    label, m = parity_cases()[-3]          # SEIR with all event kinds
+    _, _, ho = run_oracle(m, seed=seed, threads=4)
+    code, hg, _ = run_gpu(m, seed=seed)
+    assert code == 0 and np.array_equal(hg.U, ho.U)
+
+
+def test_gpu_golden_sise_phi(gpu):
+    fx = golden("sise_phi.json")
+    m = model_from_fixture(fx)
+    code, h, st = run_gpu(m)
+    assert code == 0 and st.transitions == 0
+    assert np.all(np.abs(h.V[:len(m.tspan)] - np.array(fx["phi_expected"])) < fx["tol"])
+
+
+def test_gpu_golden_sir_zero_rates(gpu):
+    fx = golden("sir_zero_rates.json")
+    m = model_from_fixture(fx)
+    code, h, _ = run_gpu(m)
+    assert code == 0
+    U = U_matrix(m, h)
+    for c, key in enumerate(("S_expected", "I_expected", "R_expected")):
+        assert np.array_equal(U[c::3, :], np.array(fx[key]).reshape(tuple(fx["dim"]), order="F"))
+
+
+def test_gpu_golden_sise3_transfers(gpu):
+    fx = golden("sise3_transfer_one.json")
+    m = model_from_fixture(fx)
+    code, h, _ = run_gpu(m)
+    assert code == 0
+    assert np.array_equal(U_matrix(m, h),
+                          np.array(fx["U_expected"]).reshape(tuple(fx["dim"]), order="F"))
+    fx = golden("sise3_transfer_three.json")
+    m = model_from_fixture(fx)
+    code, h, _ = run_gpu(m)
+    U = U_matrix(m, h)
+    assert code == 0
+    assert np.array_equal(U[0] + U[2] + U[4], np.array(fx["S_sum_node1_expected"]))
+
+
+def test_gpu_golden_punchcard_replicates(gpu):
+    fx = golden("sise_punchcard_rep.json")
+    m = model_from_fixture(fx)
+    ncol = m.replicates * len(m.tspan)
+    U_sp = sparse_pattern(fx["U_i"], fx["U_j"], m.Nn * m.Nc, ncol)
+    V_sp = sparse_pattern(fx["V_i"], fx["V_j"], m.Nn * m.Nd, ncol)
+    code, h, _ = run_gpu(m, U_sparse=U_sp, V_sparse=V_sp)
+    assert code == 0
+    assert np.array_equal(h.prU, np.array(fx["U_x_expected"], dtype=float))
+    assert np.all(np.abs(h.prV - np.array(fx["V_x_expected"])) < fx["tol"])
+
+
+def test_gpu_sparse_matches_dense(gpu, oracle_lib):
+    label, m = parity_cases()[4]           # SISe with V
+    rng = np.random.default_rng(3)
+    nrow_u, nrow_v, ncol = m.Nn * m.Nc, m.Nn * m.Nd, len(m.tspan)
+    mask_u = rng.random((nrow_u, ncol)) < 0.1
+    mask_v = rng.random((nrow_v, ncol)) < 0.1
+    iu, ju = np.nonzero(mask_u)
+    iv, jv = np.nonzero(mask_v)
+    U_sp = sparse_pattern(iu + 1, ju + 1, nrow_u, ncol)
+    V_sp = sparse_pattern(iv + 1, jv + 1, nrow_v, ncol)
+    code, hs, _ = run_gpu(m, U_sparse=U_sp, V_sparse=V_sp)
+    _, _, ho = run_oracle(m, U_sparse=U_sp, V_sparse=V_sp)
+    code_d, hd, _ = run_gpu(m)
+    assert code == 0 and code_d == 0
+    assert np.array_equal(hs.prU, ho.prU) and np.array_equal(hs.prV, ho.prV)
+    Ud = U_matrix(m, hd)
+    ir, jc = U_sp
+    for j in range(ncol):
+        rows = ir[jc[j]:jc[j + 1]]
+        assert np.array_equal(hs.prU[jc[j]:jc[j + 1]], Ud[rows, j].astype(float))
+
+
+@pytest.mark.parametrize("label,m,code", error_cases(), ids=[c[0] for c in error_cases()])
+def test_gpu_error_codes(gpu, label, m, code):
+    got, _, _ = run_gpu(m)
+    assert got == code
+
+
+def test_gpu_unsorted_events_rejected(gpu):
+    from siminf_gb300 import model as M
+    m = M.SIR({"S": [5, 5], "I": [0, 0], "R": [0, 0]}, [1, 2, 3], 0.0, 0.0,
+              events=M.make_events([0, 0], [2, 1], [1, 2], 0, 1, 0.0, 1, 0, sort=False))
+    got, _, _ = run_gpu(m)
+    assert got == -31
