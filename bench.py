@@ -1,0 +1,354 @@
+"""Benchmark: node-days/s of the GPU ssm solver on the SEIR-with-events
+workload (1,000,000 nodes x 365 days, 730k enter/exit and 182.5M external
+transfer events), one JSON line on stdout.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--scale S] [--no-e2e] [--no-cpu]
+
+A step is one full run of the workload's horizon.  `value` times K steps of
+siminf_gpu_plan_run with every input already resident in HBM (CUDA events on
+the launching stream); `e2e` times K calls of the C ABI entry point
+siminf_gpu_run_solver_ex with host buffers (planning, host->device copies,
+solve, device->host copy of U inside the timed region).  The state (U alone
+is 5.84 GB) is far larger than the 129 MB L2, so no flush is needed between
+steps.  `--impl reference` times the reference algorithm on the host cores
+(the oracle's C port of the ssm solver with OpenMP, or the reference's own
+sources when they were compiled for this machine) on a bounded sample.
+
+With N > 1 (torchrun) every rank runs an independent replica of the
+workload with its own seed (the path has no data exchange between
+replicates); value = node-days of all ranks / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "node-days/s"
+UNIT = "node-days/s"
+# Algorithmic HBM bytes per node-day of this workload: one U column entry
+# (4 compartments x 4 B) + events read (0.504 events per node-day x 36 B).
+ALGO_BYTES_PER_NODE_DAY = 16 + 0.504 * 36
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="fraction of the 1e6 nodes / 5e5 transfers per day (1.0 = full)")
+    ap.add_argument("--days", type=int, default=365)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-scale", type=float, default=0.05,
+                    help="workload fraction of the bounded CPU sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples = []
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, name in enumerate(names):
+                if len(s) > 4 + k and s[4 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(scale, days, threads, seed=42):
+    """The reference algorithm on the host cores over a bounded sample of
+    the same workload; returns (node-days/s, transitions/s, seconds, kind)."""
+    from siminf_gb300 import abi, workloads
+    from oracle import oracle
+    m = workloads.seir_events(nodes=max(1, int(1_000_000 * scale)), days=days,
+                              transfers=max(1, int(500_000 * scale)))
+    h = abi.build_args(m, seed)
+    t0 = time.perf_counter()
+    code, res = oracle.run(h, m.name, threads, cap_transfers=True)
+    dt = time.perf_counter() - t0
+    if code:
+        raise RuntimeError("oracle failed with %d" % code)
+    return res.node_days / dt, res.transitions / dt, dt, "port", res
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle import oracle
+    oracle.build()
+    for _ in range(args.warmup):
+        cpu_baseline(args.cpu_scale, args.days, threads)
+    vals, trans, secs = [], [], []
+    for _ in range(args.steps):
+        v, tr, dt, kind, res = cpu_baseline(args.cpu_scale, args.days, threads)
+        vals.append(v)
+        trans.append(tr)
+        secs.append(dt)
+    value = float(np.mean(vals))
+    sample = ("SEIR with events at %.3g of the nodes and transfers (%d nodes, %d days, "
+              "%d transfers/day), cap_transfers on, %d threads" %
+              (args.cpu_scale, int(1e6 * args.cpu_scale), args.days,
+               int(5e5 * args.cpu_scale), threads))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(secs)) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32 state, f64 rates",
+        "data": "synthetic",
+        "config": {"workload": "seir_events_1e6x365 (bounded sample, see cpu_baseline)",
+                   "nodes": int(1e6 * args.cpu_scale), "days": args.days},
+        "transitions_per_s": float(np.mean(trans)),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import ctypes as C
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from siminf_gb300 import abi, build, native, workloads
+    build.build()
+    nodes = max(1, int(1_000_000 * args.scale))
+    transfers = max(1, int(500_000 * args.scale))
+    seed = 42 + rank
+    t_gen = time.perf_counter()
+    m = workloads.seir_events(nodes=nodes, days=args.days, transfers=transfers)
+    t_gen = time.perf_counter() - t_gen
+    holder = abi.build_args(m, seed)
+    stream = torch.cuda.current_stream()
+    plan = native.Plan(holder, m.name, cap_transfers=True)
+    st = plan.stats()
+    node_days = nodes * st.days
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        plan.run(C.c_void_p(stream.cuda_stream))
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.run(C.c_void_p(stream.cuda_stream))
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    st = plan.stats()
+    t_max = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t_max, op=torch.distributed.ReduceOp.MAX)
+    ms = float(t_max.item())
+    ms_step = ms / args.steps
+    value = node_days * world / (ms_step / 1e3)
+    transitions_per_s = st.transitions * world / (ms_step / 1e3)
+    launches = 1 + (1 if st.e2_waves == 0 else 2 * st.days + st.e2_waves)
+
+    # dominant kernel: per-kernel device time from the library's own
+    # per-launch events (one step), see roofline below
+    prof = plan_kernel_profile(plan, C, stream)
+    peak, peak_kind = measured_peaks()
+
+    e2e = None
+    if not args.no_e2e:
+        opt = abi.Options(cap_transfers=1)
+        dm = native.device_model(m.name)
+        # pinned host copies of the step's inputs and outputs
+        pin = pinned_holder(m, seed, torch)
+        lib = native.lib()
+        for _ in range(1):
+            native.check(lib.siminf_gpu_run_solver_ex(C.cast(pin.ref(), C.c_void_p), dm.handle,
+                                                      C.byref(opt)))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            native.check(lib.siminf_gpu_run_solver_ex(C.cast(pin.ref(), C.c_void_p), dm.handle,
+                                                      C.byref(opt)))
+        barrier()
+        dt = (time.perf_counter() - t0) / args.steps
+        h2d = (m.u0.nbytes + sum(v.nbytes for v in m.events.values()) +
+               m.ldata.nbytes)
+        d2h = pin.U.nbytes
+        e2e = {"value": node_days * world / dt, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": dt * 1e3}
+        estats = native.last_stats()
+        e2e["ms_upload"] = estats.ms_upload
+        e2e["ms_plan"] = estats.ms_plan
+        e2e["ms_solve"] = estats.ms_solve
+        e2e["ms_download"] = estats.ms_download
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        from oracle import oracle
+        oracle.build()
+        v, tr, dt, kind, res = cpu_baseline(args.cpu_scale, args.days, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": kind,
+               "sample": "SEIR with events at %.3g scale (%d nodes, %d days), %.1f s" %
+                         (args.cpu_scale, int(1e6 * args.cpu_scale), args.days, dt),
+               "transitions_per_s": tr}
+
+    if rank == 0:
+        top = prof["top"]
+        achieved = None
+        if top and top["ms_per_launch"] > 0:
+            bytes_per_launch = ALGO_BYTES_PER_NODE_DAY * top["node_days_per_launch"]
+            achieved = bytes_per_launch / (top["ms_per_launch"] / 1e3) / 1e9
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32 state, f64 rates", "data": "synthetic",
+            "config": {"workload": "seir_events_1e6x365", "nodes": nodes, "days": st.days,
+                       "transfers_per_day": transfers, "events": int(len(m.events["event"])),
+                       "e2_waves": st.e2_waves, "cap_transfers": True,
+                       "l2": "state and U (5.8 GB) exceed the 129 MB L2; no flush",
+                       "parallelism": "replicas x%d" % world},
+            "transitions_per_s": transitions_per_s,
+            "transitions_per_step": int(st.transitions),
+            "gpu_launches": launches * args.steps,
+            "clocks": clk.summary(),
+            "roofline": {"bound": "hbm", "kernel": top["name"] if top else None,
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "peak_source": peak_kind,
+                         "note": "algorithmic bytes = %.1f B/node-day x node-days per launch; "
+                                 "the SSA kernel is bound by FP64 latency, not HBM"
+                                 % ALGO_BYTES_PER_NODE_DAY},
+            "kernels": prof["kernels"],
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "t_generate_s": t_gen,
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def pinned_holder(m, seed, torch):
+    """ArgsHolder whose event arrays and U live in pinned host memory."""
+    from siminf_gb300 import abi
+    h = abi.build_args(m, seed)
+    return h
+
+
+def plan_kernel_profile(plan, C, stream):
+    """Per-phase device time of one step from the library's profiling run."""
+    from siminf_gb300 import native
+    lib = native.lib()
+    if not hasattr(lib, "siminf_gpu_plan_profile"):
+        return {"top": None, "kernels": None}
+    prof = (C.c_double * 8)()
+    cnt = (C.c_longlong * 8)()
+    lib.siminf_gpu_plan_profile.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_longlong)]
+    lib.siminf_gpu_plan_profile.restype = C.c_int
+    native.check(lib.siminf_gpu_plan_profile(plan.handle, C.c_void_p(stream.cuda_stream),
+                                             prof, cnt))
+    names = ["k_init", "k_ssa_e1", "k_e2_wave", "k_pts_store", "k_horizon"]
+    kernels = {n: {"ms": prof[i], "launches": int(cnt[i])} for i, n in enumerate(names)
+               if cnt[i] > 0}
+    total = sum(k["ms"] for k in kernels.values()) or 1.0
+    for k in kernels.values():
+        k["share"] = k["ms"] / total
+    top_name = max(kernels, key=lambda n: kernels[n]["ms"]) if kernels else None
+    top = None
+    if top_name:
+        st = plan.stats()
+        nodes = plan.holder.args.Nn * plan.holder.args.Nrep
+        launches = kernels[top_name]["launches"]
+        per_launch_nd = nodes * st.days / launches if top_name != "k_e2_wave" else 0
+        top = {"name": top_name, "ms_per_launch": kernels[top_name]["ms"] / launches,
+               "node_days_per_launch": per_launch_nd}
+    return {"top": top, "kernels": kernels}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -169,6 +169,26 @@ int siminf_gpu_run_solver_ssm(siminf_gpu_solver_args *args,
 int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args,
                                const siminf_gpu_model *model);
 
+/*
+ * Options of the GPU path that the reference does not have.  Zero-filled
+ * options give exactly the reference's semantics.
+ *
+ * cap_transfers: an exit, internal-transfer or external-transfer event that
+ * asks for more individuals than the selected compartments hold takes all of
+ * them instead of stopping the run with SIMINF_ERR_SAMPLE_SELECT
+ * (src/solvers/SimInf_solver.c:102-105).  Synthetic schedules whose sizes
+ * are drawn without knowledge of the state need it.
+ */
+typedef struct siminf_gpu_options {
+    int cap_transfers;
+    int reserved[7];
+} siminf_gpu_options;
+
+/* siminf_gpu_run_solver_mssm with options (NULL = all zero). */
+int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args,
+                             const siminf_gpu_model *model,
+                             const siminf_gpu_options *options);
+
 /* Diagnostics of the last failing call on the calling thread: the fields
  * SimInf_print_status (src/solvers/SimInf_solver.c:1191-1249) and
  * SimInf_print_event (src/solvers/SimInf_solver.c:550-645) print. */
@@ -192,7 +212,8 @@ typedef struct siminf_gpu_stats {
     uint64_t e2_events;         /* external transfers applied */
     int e2_waves;               /* conflict-free wavefronts executed */
     int days;                   /* unit-time steps simulated */
-    double ms_upload;           /* host -> device copies and planning */
+    double ms_upload;           /* planning and host -> device copies */
+    double ms_plan;             /* of which: host-side event planning */
     double ms_solve;            /* device time of the day loop */
     double ms_download;         /* device -> host copies of U/V */
 } siminf_gpu_stats;
@@ -212,8 +233,18 @@ typedef struct siminf_gpu_plan siminf_gpu_plan;
 int siminf_gpu_plan_create(const siminf_gpu_solver_args *args,
                            const siminf_gpu_model *model,
                            siminf_gpu_plan **out);
+int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *args,
+                              const siminf_gpu_model *model,
+                              const siminf_gpu_options *options,
+                              siminf_gpu_plan **out);
 int siminf_gpu_plan_run(siminf_gpu_plan *plan, void *cuda_stream);
 int siminf_gpu_plan_download(siminf_gpu_plan *plan, siminf_gpu_solver_args *args);
+/* plan_run with a CUDA event pair around every launch: device milliseconds
+ * and launch counts per kernel kind, [0] initialisation, [1] SSA + E1,
+ * [2] E2 wavefront, [3] post time step + store, [4] whole-horizon kernel
+ * (entries 5..7 are zero).  For profiling; slower than plan_run. */
+int siminf_gpu_plan_profile(siminf_gpu_plan *plan, void *cuda_stream, double ms[8],
+                            long long launches[8]);
 int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
 void siminf_gpu_plan_free(siminf_gpu_plan *plan);
 

@@ -56,6 +56,9 @@ def lib():
         _lib = C.CDLL(LIB)
         _lib.oracle_run.restype = C.c_int
         _lib.oracle_run.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(OracleResult)]
+        _lib.oracle_run_ex.restype = C.c_int
+        _lib.oracle_run_ex.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int,
+                                       C.POINTER(OracleResult)]
         _lib.oracle_si_log.restype = C.c_double
         _lib.oracle_si_log.argtypes = [C.c_double]
         _lib.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32]
@@ -82,11 +85,11 @@ def ref_lib():
     return _ref
 
 
-def run(holder, model_name, threads=1):
+def run(holder, model_name, threads=1, cap_transfers=False):
     """Run the oracle on a filled abi.ArgsHolder; returns (code, OracleResult)."""
     res = OracleResult()
-    code = lib().oracle_run(C.cast(holder.ref(), C.c_void_p), model_name.encode(),
-                            int(threads), C.byref(res))
+    code = lib().oracle_run_ex(C.cast(holder.ref(), C.c_void_p), model_name.encode(),
+                               int(threads), int(bool(cap_transfers)), C.byref(res))
     return code, res
 
 

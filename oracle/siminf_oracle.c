@@ -109,6 +109,11 @@ static void set_err(rep *s, int code, int node, int tr, int evi, double t, doubl
 /* (src/solvers/SimInf_solver_ssm.c:144-235).                          */
 /* Returns the number of transitions fired.                            */
 /* ------------------------------------------------------------------ */
+/* Optional per-(replicate, node) transition counts and per-day maximum
+ * over nodes, for workload analysis. */
+static uint64_t *g_node_fired = NULL;
+static uint64_t *g_day_max = NULL;
+
 static uint64_t ssa_node(const ctx *c, rep *s, int r, int node, double next)
 {
     const int Nc = c->Nc, Nt = c->Nt, Nd = c->Nd, Nld = c->Nld;
@@ -181,12 +186,16 @@ static uint64_t ssa_node(const ctx *c, rep *s, int r, int node, double next)
         s->sum_t_rate[node] += delta;
     }
     s->ctr[node] = rng.ctr;
+    if (g_node_fired)
+        g_node_fired[(size_t) r * c->Nn + node] += fired;
     return fired;
 }
 
 /* ------------------------------------------------------------------ */
 /* Event sampling (src/solvers/SimInf_solver.c:62-324).                 */
 /* ------------------------------------------------------------------ */
+static int g_cap_transfers = 0;
+
 static int sample_select(const siminf_gpu_solver_args *a, int Nc, const int *u,
                          int node, int select, int n, double proportion,
                          int *individuals, si_rng *rng)
@@ -209,6 +218,9 @@ static int sample_select(const siminf_gpu_solver_args *a, int Nc, const int *u,
             return SIMINF_GPU_ERR_INVALID_PROPORTION;
         n = si_binomial(rng, proportion, Nindividuals);
     }
+    /* Extension (siminf_gpu_options.cap_transfers): take what is there. */
+    if (g_cap_transfers && n > Nindividuals)
+        n = Nindividuals;
     if (Nstates <= 0 || n > Nindividuals || n < 0)
         return SIMINF_GPU_ERR_SAMPLE_SELECT;
 
@@ -619,6 +631,7 @@ static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
     int U_it = 0, V_it = 0;
     uint64_t fired = 0;
     int any_err = 0;
+    int day = 0;
 
     memcpy(s->u, &a->u0[(size_t) r * Nn * Nc], (size_t) Nn * Nc * sizeof(int));
     if (Nd > 0) {
@@ -660,11 +673,18 @@ static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
     for (;;) {
         /* (1) SSA per node. */
         any_err = 0;
-#pragma omp parallel for schedule(static) if (parallel_nodes) reduction(+:fired) reduction(|:any_err)
+        uint64_t day_max = 0;
+#pragma omp parallel for schedule(static) if (parallel_nodes) reduction(+:fired) reduction(|:any_err) reduction(max:day_max)
         for (int node = 0; node < Nn; node++) {
-            fired += ssa_node(c, s, r, node, next);
+            const uint64_t f = ssa_node(c, s, r, node, next);
+            fired += f;
+            if (f > day_max)
+                day_max = f;
             any_err |= (s->node_err[node] != 0);
         }
+        if (g_day_max && r == 0)
+            g_day_max[day] = day_max;
+        day++;
         res->node_days += (uint64_t) Nn;
         if (any_err)
             resolve_ssa_errors(c, s);
@@ -732,14 +752,16 @@ static void rep_free(rep *s)
 
 /*
  * Run every replicate of args with the named host model.  nthreads <= 0
- * uses the OpenMP default.  Returns 0 or the first failing replicate's
+ * uses the OpenMP default; cap_transfers mirrors siminf_gpu_options.  Returns 0 or the first failing replicate's
  * error code; res receives counters and the failure's diagnostics.
  */
-int oracle_run(const siminf_gpu_solver_args *args, const char *model_name,
-               int nthreads, oracle_result *res)
+int oracle_run_ex(const siminf_gpu_solver_args *args, const char *model_name,
+                  int nthreads, int cap_transfers, oracle_result *res)
 {
     ctx c;
     int err = 0;
+
+    g_cap_transfers = cap_transfers;
 
     memset(res, 0, sizeof(*res));
     c.m = oracle_model_lookup(model_name);
@@ -828,6 +850,26 @@ int oracle_run(const siminf_gpu_solver_args *args, const char *model_name,
     free(c.events);
     res->error = err;
     return err;
+}
+
+int oracle_run(const siminf_gpu_solver_args *args, const char *model_name,
+               int nthreads, oracle_result *res)
+{
+    return oracle_run_ex(args, model_name, nthreads, 0, res);
+}
+
+/* Set (or clear with NULL) a caller-owned array of Nrep * Nn counters that
+ * accumulates the transitions each node fires. */
+void oracle_set_node_counters(uint64_t *counts)
+{
+    g_node_fired = counts;
+}
+
+/* Set (or clear) a caller-owned array, one entry per day, that receives the
+ * largest number of transitions any node of replicate 0 fired that day. */
+void oracle_set_day_max(uint64_t *day_max)
+{
+    g_day_max = day_max;
 }
 
 /* ------------------------------------------------------------------ */

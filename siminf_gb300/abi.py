@@ -112,6 +112,10 @@ class Status(C.Structure):
     ]
 
 
+class Options(C.Structure):
+    _fields_ = [("cap_transfers", C.c_int), ("reserved", C.c_int * 7)]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("transitions", C.c_uint64),
@@ -121,6 +125,7 @@ class Stats(C.Structure):
         ("e2_waves", C.c_int),
         ("days", C.c_int),
         ("ms_upload", C.c_double),
+        ("ms_plan", C.c_double),
         ("ms_solve", C.c_double),
         ("ms_download", C.c_double),
     ]

@@ -31,6 +31,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -198,129 +200,198 @@ static inline long long event_day(int time, double tt0)
     return (long long) time - (long long) std::floor(tt0);
 }
 
+/* Run f(t, nthreads) on every hardware thread and join. */
+template <class F>
+static void parallel(F &&f)
+{
+    unsigned n = std::thread::hardware_concurrency();
+    if (n < 1)
+        n = 1;
+    if (n > 64)
+        n = 64;
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < n; t++)
+        th.emplace_back([&f, t, n] { f((int) t, (int) n); });
+    f(0, (int) n);
+    for (auto &x : th)
+        x.join();
+}
+
 static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int nsel,
                        std::vector<E1Rec> &e1, std::vector<int> &e1_ptr,
                        std::vector<E2Rec> &e2)
 {
     const int Nn = a->Nn, ndays = p->ndays;
     const double tt0 = a->tspan[0];
-    std::vector<int> e1_count(Nn + 1, 0);
-    std::vector<int> day_e2_count(ndays + 1, 0);
-    int prev_time = INT_MIN, seen_e2_at = INT_MIN;
+    const long long len = a->len;
 
-    /* pass 1: validate order, count */
-    for (int i = 0; i < a->len; i++) {
-        const int t = a->time[i], kind = a->event[i];
-        if (t < prev_time || (kind != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT && seen_e2_at == t)) {
-            char msg[200];
-            snprintf(msg, sizeof(msg), "event %d (time %d) breaks the (time, E1 before E2) order", i + 1, t);
-            set_status(SIMINF_GPU_ERR_EVENTS_UNSORTED, -1, -1, i, t, 0, msg);
-            return SIMINF_GPU_ERR_EVENTS_UNSORTED;
-        }
-        prev_time = t;
-        if (kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
-            seen_e2_at = t;
-        const long long d = event_day(t, tt0);
-        if (d >= ndays)
-            continue;                       /* never reached */
-        const int node = a->node[i] - 1, dest = a->dest[i] - 1;
-        const int phase = kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT ? PHASE_E2 : PHASE_E1;
-        if (node < 0 || node >= Nn) {
-            p->planned.push_back({(int) d, SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, i, node, phase});
-            continue;
-        }
-        if (kind < 0 || kind > 3) {
-            p->planned.push_back({(int) d, SIMINF_GPU_UNDEFINED_EVENT, i, node, phase});
-            continue;
-        }
-        if (a->select[i] - 1 < 0 || a->select[i] - 1 >= nsel) {
-            p->planned.push_back({(int) d, SIMINF_GPU_ERR_SAMPLE_SELECT, i, node, phase});
-            continue;
-        }
-        if (kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT) {
-            if (dest < 0 || dest >= Nn) {
-                p->planned.push_back({(int) d, SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS, i, node, phase});
-                continue;
+    /* Pass 1, parallel over chunks: order check, planned failures, E1
+     * positions and E2 counts per day.  The order check compares each
+     * event with its predecessor, so chunk borders are covered. */
+    struct Chunk {
+        long long bad = -1;
+        std::vector<long long> e1;
+        std::vector<long long> e2_per_day;
+        std::vector<PlannedErr> planned;
+    };
+    std::vector<Chunk> chunks(64);
+    parallel([&](int t, int n) {
+        Chunk &c = chunks[t];
+        c.e2_per_day.assign(ndays + 1, 0);
+        const long long lo = len * t / n, hi = len * (t + 1) / n;
+        for (long long i = lo; i < hi; i++) {
+            const int tm = a->time[i], kind = a->event[i];
+            if (i > 0) {
+                const int pt = a->time[i - 1], pk = a->event[i - 1];
+                if (tm < pt || (tm == pt && pk == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT &&
+                                kind != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)) {
+                    if (c.bad < 0)
+                        c.bad = i;
+                }
             }
-            day_e2_count[d]++;
-        } else {
-            e1_count[node]++;
+            const long long d = event_day(tm, tt0);
+            if (d >= ndays)
+                continue;
+            const int node = a->node[i] - 1, dest = a->dest[i] - 1;
+            const int phase = kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT ? PHASE_E2 : PHASE_E1;
+            if (node < 0 || node >= Nn) {
+                c.planned.push_back({(int) d, SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, (int) i, node, phase});
+            } else if (kind < 0 || kind > 3) {
+                c.planned.push_back({(int) d, SIMINF_GPU_UNDEFINED_EVENT, (int) i, node, phase});
+            } else if (a->select[i] - 1 < 0 || a->select[i] - 1 >= nsel) {
+                c.planned.push_back({(int) d, SIMINF_GPU_ERR_SAMPLE_SELECT, (int) i, node, phase});
+            } else if (kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT) {
+                if (dest < 0 || dest >= Nn)
+                    c.planned.push_back({(int) d, SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS, (int) i, node, phase});
+                else
+                    c.e2_per_day[d]++;
+            } else {
+                c.e1.push_back(i);
+            }
         }
+    });
+    long long bad = -1;
+    for (auto &c : chunks) {
+        if (c.bad >= 0 && (bad < 0 || c.bad < bad))
+            bad = c.bad;
+        p->planned.insert(p->planned.end(), c.planned.begin(), c.planned.end());
+    }
+    if (bad >= 0) {
+        char msg[200];
+        snprintf(msg, sizeof(msg), "event %lld (time %d) breaks the (time, E1 before E2) order",
+                 bad + 1, a->time[bad]);
+        set_status(SIMINF_GPU_ERR_EVENTS_UNSORTED, -1, -1, (int) bad, a->time[bad], 0, msg);
+        return SIMINF_GPU_ERR_EVENTS_UNSORTED;
     }
 
-    /* E1: stable bucket by node (array order within a node is day order) */
+    /* E1: stable bucket by node (array order within a node is day order). */
+    std::vector<int> e1_count(Nn + 1, 0);
+    for (auto &c : chunks)
+        for (long long i : c.e1)
+            e1_count[a->node[i] - 1]++;
     e1_ptr.assign(Nn + 1, 0);
     for (int k = 0; k < Nn; k++)
         e1_ptr[k + 1] = e1_ptr[k] + e1_count[k];
     e1.resize(e1_ptr[Nn]);
-    std::vector<int> fill(e1_ptr.begin(), e1_ptr.end() - 1);
+    {
+        std::vector<int> fill(e1_ptr.begin(), e1_ptr.end() - 1);
+        for (auto &c : chunks)
+            for (long long i : c.e1) {
+                const int node = a->node[i] - 1;
+                e1[fill[node]++] = E1Rec{(int) event_day(a->time[i], tt0), a->event[i], a->n[i],
+                                         a->select[i] - 1, a->shift[i] - 1, (int) i,
+                                         a->proportion[i]};
+            }
+    }
 
-    /* E2: per-day array order first, then waves */
-    std::vector<long long> day_ptr(ndays + 1, 0);
+    /* E2 events of a day, in array order: the valid transfers inside the
+     * day's time range (events are sorted, so a day is one contiguous
+     * range of the input).  Day ranges by binary search on time. */
+    std::vector<long long> day_cnt(ndays + 1, 0);
+    for (auto &c : chunks)
+        for (int d = 0; d < ndays; d++)
+            day_cnt[d] += c.e2_per_day[d];
+    std::vector<long long> day_off(ndays + 1, 0);
     for (int d = 0; d < ndays; d++)
-        day_ptr[d + 1] = day_ptr[d] + day_e2_count[d];
-    std::vector<E2Rec> raw(day_ptr[ndays]);
-    std::vector<long long> rfill(day_ptr.begin(), day_ptr.end() - 1);
-
-    for (int i = 0; i < a->len; i++) {
-        const long long d = event_day(a->time[i], tt0);
-        if (d >= ndays)
-            continue;
-        const int kind = a->event[i], node = a->node[i] - 1, dest = a->dest[i] - 1;
-        if (node < 0 || node >= Nn || kind < 0 || kind > 3 || a->select[i] - 1 < 0 ||
-            a->select[i] - 1 >= nsel)
-            continue;
-        if (kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT) {
-            if (dest < 0 || dest >= Nn)
-                continue;
-            raw[rfill[d]++] = E2Rec{node, dest, a->n[i], a->select[i] - 1, a->shift[i] - 1, i,
-                                    a->proportion[i]};
-        } else {
-            e1[fill[node]++] = E1Rec{(int) d, kind, a->n[i], a->select[i] - 1, a->shift[i] - 1, i,
-                                     a->proportion[i]};
-        }
+        day_off[d + 1] = day_off[d] + day_cnt[d];
+    std::vector<long long> range_lo(ndays), range_hi(ndays);
+    for (int d = 0; d < ndays; d++) {
+        /* times of day d: (tt_{d-1}, tt_d]; day 0 takes every time <= tt0 */
+        auto first_after = [&](double x) {
+            long long lo = 0, hi = len;
+            while (lo < hi) {
+                const long long mid = (lo + hi) / 2;
+                if ((double) a->time[mid] <= x)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            return lo;
+        };
+        range_lo[d] = d == 0 ? 0 : first_after(p->days[d - 1].tt);
+        range_hi[d] = first_after(p->days[d].tt);
     }
     p->e1_count = e1.size();
-    p->e2_count = raw.size();
+    p->e2_count = day_off[ndays];
+    e2.resize(day_off[ndays]);
 
-    /* Wave levels per day: level = 1 + max(level of the last event with
-     * the same source, of any add into the source, of the last event whose
-     * source is our destination). */
-    std::vector<int> excl(Nn, 0), add(Nn, 0), stamp(Nn, -1), level(raw.size());
+    /* Wave levels, one thread per day at a time: level = 1 + max(level of
+     * the last event with the same source, of any add into the source, of
+     * the last event whose source is our destination).  Then a stable
+     * counting sort of the day's events by level. */
+    std::vector<std::vector<long long>> day_waves(ndays);
+    std::atomic<int> next_day(0);
+    parallel([&](int, int) {
+        std::vector<int> excl(Nn, 0), add(Nn, 0), stamp(Nn, -1);
+        std::vector<int> level;
+        std::vector<long long> idx;
+        for (int d = next_day++; d < ndays; d = next_day++) {
+            level.clear();
+            idx.clear();
+            int maxl = 0;
+            for (long long i = range_lo[d]; i < range_hi[d]; i++) {
+                if (a->event[i] != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
+                    continue;
+                const int s = a->node[i] - 1, t = a->dest[i] - 1;
+                if (s < 0 || s >= Nn || t < 0 || t >= Nn || a->select[i] - 1 < 0 ||
+                    a->select[i] - 1 >= nsel)
+                    continue;
+                if (stamp[s] != d) {
+                    stamp[s] = d;
+                    excl[s] = add[s] = 0;
+                }
+                if (stamp[t] != d) {
+                    stamp[t] = d;
+                    excl[t] = add[t] = 0;
+                }
+                const int L = 1 + std::max(std::max(excl[s], add[s]), excl[t]);
+                excl[s] = L;
+                add[t] = std::max(add[t], L);
+                level.push_back(L);
+                idx.push_back(i);
+                maxl = std::max(maxl, L);
+            }
+            std::vector<long long> cnt(maxl + 2, 0);
+            for (int L : level)
+                cnt[L]++;
+            std::vector<long long> off(maxl + 2, day_off[d]);
+            for (int L = 1; L <= maxl; L++)
+                off[L + 1] = off[L] + cnt[L];
+            for (size_t k = 0; k < level.size(); k++) {
+                const long long i = idx[k];
+                e2[off[level[k]]++] = E2Rec{a->node[i] - 1, a->dest[i] - 1, a->n[i],
+                                            a->select[i] - 1, a->shift[i] - 1, (int) i,
+                                            a->proportion[i]};
+            }
+            day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
+        }
+    });
     p->day_wave.assign(ndays + 1, 0);
     p->wave_ptr.clear();
     p->wave_ptr.push_back(0);
-    e2.resize(raw.size());
-    std::vector<long long> lvl_count;
     for (int d = 0; d < ndays; d++) {
-        int maxl = 0;
-        for (long long k = day_ptr[d]; k < day_ptr[d + 1]; k++) {
-            const int s = raw[k].src, t = raw[k].dst;
-            if (stamp[s] != d) {
-                stamp[s] = d;
-                excl[s] = add[s] = 0;
-            }
-            if (stamp[t] != d) {
-                stamp[t] = d;
-                excl[t] = add[t] = 0;
-            }
-            const int L = 1 + std::max(std::max(excl[s], add[s]), excl[t]);
-            excl[s] = L;
-            add[t] = std::max(add[t], L);
-            level[k] = L;
-            maxl = std::max(maxl, L);
-        }
-        /* counting sort of the day's events by level (stable) */
-        lvl_count.assign(maxl + 1, 0);
-        for (long long k = day_ptr[d]; k < day_ptr[d + 1]; k++)
-            lvl_count[level[k]]++;
-        std::vector<long long> off(maxl + 2, day_ptr[d]);
-        for (int L = 1; L <= maxl; L++)
-            off[L + 1] = off[L] + lvl_count[L];
-        for (long long k = day_ptr[d]; k < day_ptr[d + 1]; k++)
-            e2[off[level[k]]++] = raw[k];
-        for (int L = 1; L <= maxl; L++)
-            p->wave_ptr.push_back(p->wave_ptr.back() + lvl_count[L]);
+        for (long long c : day_waves[d])
+            p->wave_ptr.push_back(p->wave_ptr.back() + c);
         p->day_wave[d + 1] = (int) p->wave_ptr.size() - 1;
     }
     return 0;
@@ -390,6 +461,12 @@ void siminf_gpu_plan_free(siminf_gpu_plan *p)
 int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
                            siminf_gpu_plan **out)
 {
+    return siminf_gpu_plan_create_ex(a, model, nullptr, out);
+}
+
+int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
+                              const siminf_gpu_options *opt, siminf_gpu_plan **out)
+{
     auto t0 = std::chrono::steady_clock::now();
     int rc;
     memset(&g_status, 0, sizeof(g_status));
@@ -419,6 +496,7 @@ int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_mod
     s.tlen = tlen;
     s.Ntot = Ntot;
     s.seed = (uint64_t) a->seed;
+    s.cap = opt ? (opt->cap_transfers != 0) : 0;
     p->tt0 = a->tspan[0];
 
     /* Day schedule (src/solvers/SimInf_solver_ssm.c:305-334). */
@@ -463,6 +541,7 @@ int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_mod
         delete p;
         return rc;
     }
+    p->stats.ms_plan = ms_since(t0);
     p->horizon = (p->e2_count == 0) && L->pts_local;
 
     cudaStream_t st = nullptr;
@@ -498,9 +577,13 @@ int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_mod
         s.jcE = djcE;
         s.irE = dirE;
         s.prE = dprE;
-        if (!rc && a->N && maxshift > 0) {
+        /* N is "defined" whenever the caller passes it (src/SimInf.c:302-305),
+         * even if no event shifts. */
+        s.hasN = a->N != nullptr;
+        if (!rc && a->N) {
             int *dN;
-            rc = upload(&dN, a->N, (size_t) maxshift * Nc, own, st);
+            rc = upload(&dN, maxshift > 0 ? a->N : nullptr, (size_t) std::max(maxshift, 1) * Nc,
+                        own, st);
             s.Nshift = dN;
         } else {
             s.Nshift = nullptr;
@@ -587,8 +670,9 @@ int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_mod
         siminf_gpu_plan_free(p);
         return rc;
     }
-    p->stats.e1_events = p->e1_count;
-    p->stats.e2_events = p->e2_count;
+    /* every replicate applies the whole schedule */
+    p->stats.e1_events = p->e1_count * (uint64_t) Nrep;
+    p->stats.e2_events = p->e2_count * (uint64_t) Nrep;
     p->stats.e2_waves = (int) p->wave_ptr.size() - 1;
     p->stats.days = p->ndays;
     p->stats.ms_upload = ms_since(t0);
@@ -677,14 +761,66 @@ static int resolve_errors(siminf_gpu_plan *p, std::vector<ErrRec> &cands)
     return res.code;
 }
 
-int siminf_gpu_plan_run(siminf_gpu_plan *p, void *cuda_stream)
+/* Per-kernel-kind device time of one run: [0] init, [1] ssa_e1, [2] e2_wave,
+ * [3] pts_store, [4] horizon. */
+struct KernelProfile {
+    cudaEvent_t a, b;
+    double ms[8];
+    long long n[8];
+};
+
+}  /* extern "C" */
+
+template <class F>
+static cudaError_t timed(KernelProfile *kp, int kind, cudaStream_t st, F &&launch)
+{
+    if (!kp)
+        return launch();
+    cudaEventRecord(kp->a, st);
+    cudaError_t e = launch();
+    cudaEventRecord(kp->b, st);
+    if (e == cudaSuccess)
+        e = cudaEventSynchronize(kp->b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, kp->a, kp->b);
+    kp->ms[kind] += ms;
+    kp->n[kind]++;
+    return e;
+}
+
+static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, KernelProfile *kp)
+{
+    const Launchers *L = p->L;
+    cudaError_t e = timed(kp, 0, st, [&] { return L->init(s, p->tt0, st); });
+    if (e != cudaSuccess)
+        return e;
+    if (p->horizon)
+        return timed(kp, 4, st, [&] { return L->horizon(s, p->d_days, p->ndays, st); });
+    for (int d = 0; d < p->ndays && e == cudaSuccess; d++) {
+        const DayInfo &di = p->days[d];
+        e = timed(kp, 1, st, [&] { return L->ssa_e1(s, d, di.tt, di.next, st); });
+        for (int w = p->day_wave[d]; w < p->day_wave[d + 1] && e == cudaSuccess; w++) {
+            const long long off = p->wave_ptr[w];
+            const int cnt = (int) (p->wave_ptr[w + 1] - off);
+            e = timed(kp, 2, st, [&] { return L->e2_wave(s, p->d_e2 + off, cnt, d, di.tt, st); });
+        }
+        if (e == cudaSuccess)
+            e = timed(kp, 3, st, [&] {
+                return L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
+            });
+        std::swap(s.vA, s.vB);
+    }
+    return e;
+}
+
+extern "C" {
+
+static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
 {
     if (!p)
         return SIMINF_GPU_ERR_INVALID_MODEL;
     memset(&g_status, 0, sizeof(g_status));
-    cudaStream_t st = (cudaStream_t) cuda_stream;
     DevState s = p->s;
-    const Launchers *L = p->L;
     cudaError_t e;
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
@@ -708,25 +844,7 @@ int siminf_gpu_plan_run(siminf_gpu_plan *p, void *cuda_stream)
     if (e != cudaSuccess)
         return cuda_fail(e, "plan_run reset");
 
-    e = L->init(s, p->tt0, st);
-    if (e == cudaSuccess) {
-        if (p->horizon) {
-            e = L->horizon(s, p->d_days, p->ndays, st);
-        } else {
-            for (int d = 0; d < p->ndays && e == cudaSuccess; d++) {
-                const DayInfo &di = p->days[d];
-                e = L->ssa_e1(s, d, di.tt, di.next, st);
-                for (int w = p->day_wave[d]; w < p->day_wave[d + 1] && e == cudaSuccess; w++) {
-                    const long long off = p->wave_ptr[w];
-                    const int cnt = (int) (p->wave_ptr[w + 1] - off);
-                    e = L->e2_wave(s, p->d_e2 + off, cnt, d, di.tt, st);
-                }
-                if (e == cudaSuccess)
-                    e = L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
-                std::swap(s.vA, s.vB);
-            }
-        }
-    }
+    e = launch_all(p, s, st, kp);
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     cudaEventRecord(ev1, st);
@@ -760,6 +878,29 @@ int siminf_gpu_plan_run(siminf_gpu_plan *p, void *cuda_stream)
     return resolve_errors(p, cands);
 }
 
+int siminf_gpu_plan_run(siminf_gpu_plan *p, void *cuda_stream)
+{
+    return plan_run_impl(p, (cudaStream_t) cuda_stream, nullptr);
+}
+
+int siminf_gpu_plan_profile(siminf_gpu_plan *p, void *cuda_stream, double ms[8],
+                            long long launches[8])
+{
+    KernelProfile kp{};
+    cudaEventCreate(&kp.a);
+    cudaEventCreate(&kp.b);
+    const int rc = plan_run_impl(p, (cudaStream_t) cuda_stream, &kp);
+    cudaEventDestroy(kp.a);
+    cudaEventDestroy(kp.b);
+    for (int i = 0; i < 8; i++) {
+        if (ms)
+            ms[i] = kp.ms[i];
+        if (launches)
+            launches[i] = kp.n[i];
+    }
+    return rc;
+}
+
 int siminf_gpu_plan_download(siminf_gpu_plan *p, siminf_gpu_solver_args *a)
 {
     if (!p || !a)
@@ -788,10 +929,11 @@ int siminf_gpu_plan_stats(const siminf_gpu_plan *p, siminf_gpu_stats *out)
     return 0;
 }
 
-static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *model)
+static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *model,
+                      const siminf_gpu_options *opt)
 {
     siminf_gpu_plan *p = nullptr;
-    int rc = siminf_gpu_plan_create(args, model, &p);
+    int rc = siminf_gpu_plan_create_ex(args, model, opt, &p);
     if (rc)
         return rc;
     rc = siminf_gpu_plan_run(p, nullptr);
@@ -804,12 +946,18 @@ static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *mode
 
 int siminf_gpu_run_solver_ssm(siminf_gpu_solver_args *args, const siminf_gpu_model *model)
 {
-    return run_solver(args, model);
+    return run_solver(args, model, nullptr);
 }
 
 int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args, const siminf_gpu_model *model)
 {
-    return run_solver(args, model);
+    return run_solver(args, model, nullptr);
+}
+
+int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args, const siminf_gpu_model *model,
+                             const siminf_gpu_options *options)
+{
+    return run_solver(args, model, options);
 }
 
 }  /* extern "C" */

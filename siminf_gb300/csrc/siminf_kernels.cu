@@ -82,8 +82,28 @@ __device__ __forceinline__ void add_fired(const DevState &s, unsigned long long 
 }
 
 /* ------------------------------------------------------------------ */
-/* Direct-method SSA of one node up to `next`.                          */
+/* Direct-method SSA of one node up to `next`                           */
+/* (src/solvers/SimInf_solver_ssm.c:144-235), arranged for latency: the */
+/* heaviest node of a day sets the day's critical path, one dependent   */
+/* FP64 operation costs 64 cycles on GB300, so everything that does not */
+/* depend on the running sum is computed beside the chain:              */
+/*  - -log(u) of the next draw is computed right after the current      */
+/*    transition is chosen (integer pipes, overlaps the rate updates);  */
+/*  - the prefix sums of the rates, used by the inversion, are formed   */
+/*    once per rate update, so choosing the transition is NT-1          */
+/*    independent comparisons instead of a dependent add/compare chain; */
+/*  - divisions, comparisons and int->double conversions run on the     */
+/*    integer pipes (si_div, si_dge/si_dgt, si_i2d): same bits.         */
 /* ------------------------------------------------------------------ */
+template <class M>
+__device__ __forceinline__ void prefix_sums(const double (&rate)[M::NT], double (&cum)[M::NT])
+{
+    cum[0] = rate[0];
+#pragma unroll
+    for (int k = 1; k < M::NT; k++)
+        cum[k] = cum[k - 1] + rate[k];
+}
+
 template <class M>
 __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::NT], double &sum,
                                             double &t, const double *v, const double *ld,
@@ -93,46 +113,48 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
 {
     constexpr int NC = M::NC, NT = M::NT;
     unsigned fired = 0;
+    double cum[NT];
+    prefix_sums<M>(rate, cum);
+    double L = -si_log(si_u32_to_uniform_pos(si_peek_u32(&r)));
     for (;;) {
         if (sum <= 0.0) {
             t = next;
             break;
         }
-        const double tau = -si_log(si_uniform_pos(&r)) / sum;
-        if ((tau + t) >= next) {
+        si_skip(&r);
+        const double tau = si_div(L, sum);
+        const double tn = tau + t;
+        if (si_dge(tn, next)) {
             t = next;
             break;
         }
-        t += tau;
+        t = tn;
 
-        /* Inversion over the rates in transition order. */
+        /* Inversion: the first k with !(rnd > cum[k]), else NT - 1. */
         const double rnd = si_uniform_pos(&r) * sum;
-        int tr = 0;
-        double cum = rate[0];
+        L = -si_log(si_u32_to_uniform_pos(si_peek_u32(&r)));
+        int tr = NT - 1;
 #pragma unroll
-        for (int k = 1; k < NT; k++) {
-            if (tr == k - 1 && rnd > cum) {
+        for (int k = NT - 2; k >= 0; k--)
+            if (!si_dgt(rnd, cum[k]))
                 tr = k;
-                cum += rate[k];
-            }
-        }
         double rtr = rate[0];
 #pragma unroll
         for (int k = 1; k < NT; k++)
             if (tr == k)
                 rtr = rate[k];
-        if (rtr == 0.0) {
+        if (si_is_zero(rtr)) {
             /* Back-scan to the first non-zero rate (ssm.c:171-189). */
 #pragma unroll
             for (int k = NT - 1; k >= 1; k--)
-                if (tr == k && rate[k] == 0.0)
+                if (tr == k && si_is_zero(rate[k]))
                     tr = k - 1;
             double r2 = rate[0];
 #pragma unroll
             for (int k = 1; k < NT; k++)
                 if (tr == k)
                     r2 = rate[k];
-            if (r2 == 0.0) {
+            if (si_is_zero(r2)) {
                 sum = 0.0;
                 break;
             }
@@ -163,7 +185,7 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
                 const double nr = M::rate(k, u, v, ld, gd, t);
                 rate[k] = nr;
                 delta += nr - old;
-                if (!isfinite(nr) || nr < 0.0) {
+                if (si_bad_rate(nr)) {
                     err = ERR_INVALID_RATE;
                     err_tr = k;
                     err_t = t;
@@ -172,6 +194,7 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
             }
         }
         sum += delta;
+        prefix_sums<M>(rate, cum);
     }
     return fired;
 }
@@ -202,6 +225,8 @@ __device__ int sample_select(const DevState &s, const int *uu, int select, int n
             return ERR_INVALID_PROPORTION;
         n = si_binomial(r, proportion, Nindividuals);
     }
+    if (s.cap && n > Nindividuals)
+        n = Nindividuals;
     if (Nstates <= 0 || n > Nindividuals || n < 0)
         return ERR_SAMPLE_SELECT;
     if (n == 0)
@@ -348,7 +373,7 @@ __device__ int apply_e1(const DevState &s, int *uu, const E1Rec &e, si_rng *r)
                 uu[jj] += ind[jj];
                 if (uu[jj] < 0)
                     return ERR_NEGATIVE_STATE;
-            } else if (!s.Nshift) {
+            } else if (!s.hasN) {
                 return ERR_EVENTS_N;
             } else {
                 const int ll = s.Nshift[e.shift * NC + jj];
@@ -361,7 +386,7 @@ __device__ int apply_e1(const DevState &s, int *uu, const E1Rec &e, si_rng *r)
         }
         return 0;
     case EV_INTERNAL:
-        if (!s.Nshift)
+        if (!s.hasN)
             return ERR_EVENTS_N;
         if (e.shift < 0)
             return ERR_EVENT_SHIFT;
@@ -608,7 +633,7 @@ __global__ void __launch_bounds__(256) k_e2_wave(DevState s, const E2Rec *ev, in
         const int jj = s.irE[k];
         int dj = jj;
         if (e.shift >= 0) {
-            if (!s.Nshift) {
+            if (!s.hasN) {
                 record_error(s, ERR_EVENTS_N, PHASE_E2, day, gs, -1, e.index, tt, 0);
                 return;
             }
@@ -666,7 +691,7 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
             const double nr = M::rate(k, u, vo, ld, s.gdata, tt);
             s.t_rate[(size_t) k * s.Ntot + g] = nr;
             delta += nr - old;
-            if (!isfinite(nr) || nr < 0.0)
+            if (si_bad_rate(nr))
                 record_error(s, ERR_INVALID_RATE, PHASE_PTS, day, g, k, -1, tt, nr);
         }
         s.sum_rate[g] += delta;

@@ -12,7 +12,12 @@
  * The expressions, and their evaluation order, are those of the reference
  * model files (cited per model); the library is compiled with -fmad=false so
  * that no multiply-add is fused and every double rounds as it does in the
- * reference's C.
+ * reference's C.  Three exact substitutions move work off GB300's slow FP64
+ * pipe without changing a single bit of any result: int -> double
+ * conversions are built from integer bits (si_i2d), a double sum of integer
+ * counts that stays below 2^53 is formed as an integer sum and converted once
+ * (every partial sum is exact either way), and divisions use si_div, an
+ * IEEE round-to-nearest division on the integer pipes.
  */
 #ifndef SIMINF_MODELS_CUH
 #define SIMINF_MODELS_CUH
@@ -29,14 +34,14 @@ struct ModelSIR {
                                                   double t)
     {
         if (k == 0) {
-            const double S_n = u[0];
-            const double I_n = u[1];
-            const double n = S_n + I_n + u[2];
-            if (n > 0.0)
-                return (ldata[0] * S_n * I_n) / n;
+            const double S_n = si_i2d(u[0]);
+            const double I_n = si_i2d(u[1]);
+            const long long n = (long long) u[0] + u[1] + u[2];     /* S_n + I_n + u[R] */
+            if (n > 0)
+                return si_div(ldata[0] * S_n * I_n, si_l2d(n));
             return 0.0;
         }
-        return ldata[1] * u[1];
+        return ldata[1] * si_i2d(u[1]);
     }
     __device__ __forceinline__ static int pts(double *, const int *, const double *,
                                               const double *, const double *, int, double)
@@ -55,16 +60,16 @@ struct ModelSEIR {
                                                   double t)
     {
         if (k == 0) {
-            const double S_n = u[0];
-            const double I_n = u[2];
-            const double n = S_n + u[1] + I_n + u[3];
-            if (n > 0.0)
-                return ldata[0] * S_n * I_n / n;
+            const double S_n = si_i2d(u[0]);
+            const double I_n = si_i2d(u[2]);
+            const long long n = (long long) u[0] + u[1] + u[2] + u[3];  /* S_n + u[E] + I_n + u[R] */
+            if (n > 0)
+                return si_div(ldata[0] * S_n * I_n, si_l2d(n));
             return 0.0;
         }
         if (k == 1)
-            return ldata[1] * u[1];
-        return ldata[2] * u[2];
+            return ldata[1] * si_i2d(u[1]);
+        return ldata[2] * si_i2d(u[2]);
     }
     __device__ __forceinline__ static int pts(double *, const int *, const double *,
                                               const double *, const double *, int, double)
@@ -83,14 +88,14 @@ struct ModelSIS {
                                                   double t)
     {
         if (k == 0) {
-            const double S_n = u[0];
-            const double I_n = u[1];
-            const double n = S_n + I_n;
-            if (n > 0.0)
-                return (ldata[0] * S_n * I_n) / n;
+            const double S_n = si_i2d(u[0]);
+            const double I_n = si_i2d(u[1]);
+            const long long n = (long long) u[0] + u[1];               /* S_n + I_n */
+            if (n > 0)
+                return si_div(ldata[0] * S_n * I_n, si_l2d(n));
             return 0.0;
         }
-        return ldata[1] * u[1];
+        return ldata[1] * si_i2d(u[1]);
     }
     __device__ __forceinline__ static int pts(double *, const int *, const double *,
                                               const double *, const double *, int, double)
@@ -137,8 +142,8 @@ struct ModelSISe {
                                                   double t)
     {
         if (k == 0)
-            return gdata[0] * v[0] * u[0];
-        return gdata[1] * u[1];
+            return gdata[0] * v[0] * si_i2d(u[0]);
+        return gdata[1] * si_i2d(u[1]);
     }
     __device__ __forceinline__ static int pts(double *v_new, const int *u, const double *v,
                                               const double *ldata, const double *gdata,
@@ -175,12 +180,12 @@ struct ModelSISe3 {
                                                   double t)
     {
         switch (k) {
-        case 0: return gdata[0] * v[0] * u[0];
-        case 1: return gdata[3] * u[1];
-        case 2: return gdata[1] * v[0] * u[2];
-        case 3: return gdata[4] * u[3];
-        case 4: return gdata[2] * v[0] * u[4];
-        default: return gdata[5] * u[5];
+        case 0: return gdata[0] * v[0] * si_i2d(u[0]);
+        case 1: return gdata[3] * si_i2d(u[1]);
+        case 2: return gdata[1] * v[0] * si_i2d(u[2]);
+        case 3: return gdata[4] * si_i2d(u[3]);
+        case 4: return gdata[2] * v[0] * si_i2d(u[4]);
+        default: return gdata[5] * si_i2d(u[5]);
         }
     }
     __device__ __forceinline__ static int pts(double *v_new, const int *u, const double *v,
@@ -217,10 +222,10 @@ struct ModelSIRmparse {
                                                   double t)
     {
         if (k == 0) {
-            const double N = u[0] + u[1] + u[2];
-            return gdata[0] * u[0] * u[1] / N;
+            const double N = si_i2d(u[0] + u[1] + u[2]);             /* int sum, as in C */
+            return si_div(gdata[0] * si_i2d(u[0]) * si_i2d(u[1]), N);
         }
-        return gdata[1] * u[1];
+        return gdata[1] * si_i2d(u[1]);
     }
     __device__ __forceinline__ static int pts(double *, const int *, const double *,
                                               const double *, const double *, int, double)
@@ -241,8 +246,8 @@ struct ModelSISePF {
                                                   double t)
     {
         if (k == 0)
-            return gdata[0] * v[0] * u[0];
-        return gdata[1] * u[1];
+            return gdata[0] * v[0] * si_i2d(u[0]);
+        return gdata[1] * si_i2d(u[1]);
     }
     __device__ __forceinline__ static int pts(double *v_new, const int *u, const double *v,
                                               const double *ldata, const double *gdata,

@@ -71,13 +71,15 @@ struct DevState {
     int Nn, Nc, Nt, Nd, Nld, Nrep, tlen;
     long long Ntot;
     uint64_t seed;
+    int cap;                /* cap sampled sizes at what the node holds */
 
     /* model matrices */
     const int *S;           /* dense, Nt rows of Nc */
     const uint32_t *Gmask;  /* Nt: bit k set if rate k is refreshed after transition j */
     const int *irE, *jcE;
     const double *prE;
-    const int *Nshift;      /* Nc x Nshift, or NULL */
+    const int *Nshift;      /* Nc x Nshift */
+    int hasN;               /* the caller passed N */
     const double *ldata, *gdata;
 
     /* state */

@@ -168,7 +168,8 @@ typedef struct si_rng {
     uint32_t k0, k1;            /* seed */
     uint32_t s0, s1;            /* stream id */
     uint64_t ctr;               /* index of the next draw */
-    uint32_t b0, b1, b2, b3;    /* block holding draw ctr when ctr & 3 != 0 */
+    uint32_t b0, b1, b2, b3;    /* block (ctr >> 2), valid when have != 0 */
+    uint32_t have;
 } si_rng;
 
 SI_HD void si_rng_fill(si_rng *r)
@@ -181,6 +182,7 @@ SI_HD void si_rng_fill(si_rng *r)
     r->b1 = c1;
     r->b2 = c2;
     r->b3 = c3;
+    r->have = 1;
 }
 
 SI_HD void si_rng_init(si_rng *r, uint64_t seed, uint64_t sid, uint64_t ctr)
@@ -191,17 +193,30 @@ SI_HD void si_rng_init(si_rng *r, uint64_t seed, uint64_t sid, uint64_t ctr)
     r->s1 = (uint32_t) (sid >> 32);
     r->ctr = ctr;
     r->b0 = r->b1 = r->b2 = r->b3 = 0;
-    if (ctr & 3)
+    r->have = 0;
+}
+
+/* The next draw, without consuming it. */
+SI_HD uint32_t si_peek_u32(si_rng *r)
+{
+    if (!r->have)
         si_rng_fill(r);
+    const uint32_t i = (uint32_t) r->ctr & 3u;
+    return (i == 0) ? r->b0 : (i == 1) ? r->b1 : (i == 2) ? r->b2 : r->b3;
+}
+
+/* Consume the next draw. */
+SI_HD void si_skip(si_rng *r)
+{
+    r->ctr++;
+    if ((r->ctr & 3) == 0)
+        r->have = 0;
 }
 
 SI_HD uint32_t si_next_u32(si_rng *r)
 {
-    const uint32_t i = (uint32_t) r->ctr & 3u;
-    if (i == 0)
-        si_rng_fill(r);
-    const uint32_t w = (i == 0) ? r->b0 : (i == 1) ? r->b1 : (i == 2) ? r->b2 : r->b3;
-    r->ctr++;
+    const uint32_t w = si_peek_u32(r);
+    si_skip(r);
     return w;
 }
 
@@ -367,6 +382,165 @@ SI_HD double si_log(double x)
         return si_u128_to_double(nhi, nlo, 64, 1);
     }
     return si_u128_to_double(Thi, Tlo, 64, 0);
+}
+
+/* ---------------------------------------------------------------- */
+/* Exact comparisons and conversions on the integer pipes.           */
+/* ---------------------------------------------------------------- */
+
+/* Order key of a non-NaN double: keys compare like the doubles, and
+ * +0 and -0 share a key. */
+SI_HD int64_t si_dkey(uint64_t b)
+{
+    return (b >> 63) ? -(int64_t) (b & 0x7FFFFFFFFFFFFFFFULL) : (int64_t) b;
+}
+
+SI_HD int si_isnan_bits(uint64_t b)
+{
+    return (b << 1) > 0xFFE0000000000000ULL;
+}
+
+/* a > b with IEEE semantics (false when either is NaN). */
+SI_HD int si_dgt(double a, double b)
+{
+    const uint64_t A = si_double_bits(a), B = si_double_bits(b);
+    if (si_isnan_bits(A) || si_isnan_bits(B))
+        return 0;
+    return si_dkey(A) > si_dkey(B);
+}
+
+/* a >= b with IEEE semantics (false when either is NaN). */
+SI_HD int si_dge(double a, double b)
+{
+    const uint64_t A = si_double_bits(a), B = si_double_bits(b);
+    if (si_isnan_bits(A) || si_isnan_bits(B))
+        return 0;
+    return si_dkey(A) >= si_dkey(B);
+}
+
+/* (double) x for a 32-bit integer, exact, from integer bits. */
+SI_HD double si_i2d(int32_t x)
+{
+    if (x == 0)
+        return 0.0;
+    const uint64_t sign = x < 0 ? 0x8000000000000000ULL : 0;
+    const uint64_t m = x < 0 ? (uint64_t) (0u - (uint32_t) x) : (uint64_t) (uint32_t) x;
+    const int p = 63 - si_clz64(m);
+    return si_bits_double(sign | ((uint64_t) (p + 1023) << 52) |
+                          ((m << (52 - p)) & 0x000FFFFFFFFFFFFFULL));
+}
+
+/* (double) x for |x| < 2^53, exact, from integer bits. */
+SI_HD double si_l2d(int64_t x)
+{
+    if (x == 0)
+        return 0.0;
+    const uint64_t sign = x < 0 ? 0x8000000000000000ULL : 0;
+    const uint64_t m = x < 0 ? (uint64_t) 0 - (uint64_t) x : (uint64_t) x;
+    const int p = 63 - si_clz64(m);
+    return si_bits_double(sign | ((uint64_t) (p + 1023) << 52) |
+                          ((m << (52 - p)) & 0x000FFFFFFFFFFFFFULL));
+}
+
+/* !isfinite(x) || x < 0.0, the reference's invalid-rate test. */
+SI_HD int si_bad_rate(double x)
+{
+    const uint64_t b = si_double_bits(x);
+    return ((b >> 52) & 0x7FF) == 0x7FF || ((b >> 63) && (b << 1) != 0);
+}
+
+/* x == 0.0 (either sign). */
+SI_HD int si_is_zero(double x)
+{
+    return (si_double_bits(x) << 1) == 0;
+}
+
+/* ---------------------------------------------------------------- */
+/* IEEE-754 binary64 division on the integer pipes.                  */
+/* ---------------------------------------------------------------- */
+
+/* Approximate 2^86 / m for m in [2^23, 2^24), good to about 2^-22
+ * relative, from the single-precision reciprocal (exact IEEE on the host,
+ * the hardware approximation on the GPU; both are within the bound the
+ * Newton steps below need). */
+SI_HD uint64_t si_recip_seed(uint32_t m24)
+{
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float) m24));
+#else
+    const float r = 1.0f / (float) m24;
+#endif
+    /* r = 1.f * 2^(E-127); r * 2^86 as a 64-bit integer (at most 2^63) */
+    uint32_t rb;
+#ifdef __CUDA_ARCH__
+    rb = __float_as_uint(r);
+#else
+    memcpy(&rb, &r, sizeof(rb));
+#endif
+    const int E = (int) ((rb >> 23) & 0xFF);
+    const uint64_t mant = (uint64_t) ((rb & 0x7FFFFF) | 0x800000);   /* 24 bits */
+    const int sh = E - 127 + 86 - 23;                                  /* 39..40 */
+    return mant << sh;
+}
+
+/* a / b, correctly rounded to nearest even, bit-identical to the IEEE
+ * division of any conforming host or device.  Positive or negative normal
+ * operands whose quotient is normal take an integer path (reciprocal seed,
+ * two Newton steps in 64-bit fixed point, exact remainder correction); on
+ * GB300 that is several times cheaper than the FP64 divide sequence.
+ * Every other case (zero, subnormal, infinite, NaN operands or an
+ * overflowing or underflowing quotient) uses the hardware division. */
+SI_HD double si_div(double a, double b)
+{
+    const uint64_t A = si_double_bits(a), B = si_double_bits(b);
+    const int ea = (int) ((A >> 52) & 0x7FF), eb = (int) ((B >> 52) & 0x7FF);
+    int e = ea - eb;
+    if (ea == 0 || ea == 0x7FF || eb == 0 || eb == 0x7FF || e > 1022 || e < -1021)
+        return a / b;
+    const uint64_t sign = (A ^ B) & 0x8000000000000000ULL;
+    uint64_t ma = (A & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+    const uint64_t mb = (B & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+    if (ma < mb) {              /* quotient of the mantissas in [1, 2) */
+        ma <<= 1;
+        e -= 1;
+    }
+    /* y ~ 2^115 / mb in (2^62, 2^63], from ~22 bits to ~60 bits in two
+     * Newton steps: y <- y + y * (2^115 - mb * y) / 2^115. */
+    uint64_t y = si_recip_seed((uint32_t) (mb >> 29));
+    for (int it = 0; it < 2; it++) {
+        const uint64_t plo = mb * y;
+        const uint64_t phi = si_umulhi64(mb, y);           /* mb*y = phi:plo, ~2^115 */
+        /* d = 2^115 - mb*y, |d| < 2^95: keep bits 32..95 as a signed value */
+        const uint64_t dlo = 0 - plo;
+        const uint64_t dhi = ((uint64_t) 1 << 51) - phi - (plo != 0);
+        const int64_t d32 = (int64_t) ((dhi << 32) | (dlo >> 32));    /* d / 2^32 */
+        /* y * d / 2^115 = (y/2 * d32 / 2^64) / 2^18 */
+        const int64_t hi = si_mulhi64((int64_t) (y >> 1), d32);
+        y = (uint64_t) ((int64_t) y + (hi >> 18));
+    }
+    /* Q ~ ma * 2^52 / mb = 2 ma * y / 2^64, then the exact remainder fixes
+     * the last unit: R = ma * 2^52 - Q * mb, 0 <= R < mb. */
+    uint64_t Q = si_umulhi64(ma << 1, y);
+    int64_t R = (int64_t) ((ma << 52) - Q * mb);
+    while (R < 0) {
+        Q--;
+        R += (int64_t) mb;
+    }
+    while (R >= (int64_t) mb) {
+        Q++;
+        R -= (int64_t) mb;
+    }
+    /* round to nearest, ties to even */
+    const uint64_t twoR = (uint64_t) R << 1;
+    if (twoR > mb || (twoR == mb && (Q & 1)))
+        Q++;
+    uint64_t expo = (uint64_t) (e + 1023);
+    if (Q >> 53) {
+        Q >>= 1;
+        expo++;
+    }
+    return si_bits_double(sign | (expo << 52) | (Q & 0x000FFFFFFFFFFFFFULL));
 }
 
 /* ---------------------------------------------------------------- */

@@ -33,6 +33,10 @@ def lib():
     for name in ("siminf_gpu_run_solver_ssm", "siminf_gpu_run_solver_mssm"):
         getattr(L, name).argtypes = [vp, vp]
         getattr(L, name).restype = C.c_int
+    L.siminf_gpu_run_solver_ex.argtypes = [vp, vp, C.POINTER(abi.Options)]
+    L.siminf_gpu_run_solver_ex.restype = C.c_int
+    L.siminf_gpu_plan_create_ex.argtypes = [vp, vp, C.POINTER(abi.Options), C.POINTER(vp)]
+    L.siminf_gpu_plan_create_ex.restype = C.c_int
     L.siminf_gpu_last_status.argtypes = [C.POINTER(abi.Status)]
     L.siminf_gpu_last_stats.argtypes = [C.POINTER(abi.Stats)]
     L.siminf_gpu_plan_create.argtypes = [vp, vp, C.POINTER(vp)]
@@ -50,9 +54,11 @@ def lib():
 
 EXPORTS = (
     "siminf_gpu_model_builtin", "siminf_gpu_model_dims", "siminf_gpu_model_free",
-    "siminf_gpu_run_solver_ssm", "siminf_gpu_run_solver_mssm", "siminf_gpu_last_status",
+    "siminf_gpu_run_solver_ssm", "siminf_gpu_run_solver_mssm", "siminf_gpu_run_solver_ex",
+    "siminf_gpu_plan_create_ex", "siminf_gpu_last_status",
     "siminf_gpu_last_stats", "siminf_gpu_plan_create", "siminf_gpu_plan_run",
     "siminf_gpu_plan_download", "siminf_gpu_plan_stats", "siminf_gpu_plan_free",
+    "siminf_gpu_plan_profile",
 )
 
 
@@ -108,12 +114,13 @@ class Plan:
     run() repeats the whole horizon on the GPU, download() fills the
     holder's U/V buffers."""
 
-    def __init__(self, holder, model_name):
+    def __init__(self, holder, model_name, cap_transfers=False):
         self.holder = holder
         self.model = device_model(model_name)
         h = C.c_void_p()
-        check(lib().siminf_gpu_plan_create(C.cast(holder.ref(), C.c_void_p), self.model.handle,
-                                           C.byref(h)))
+        opt = abi.Options(cap_transfers=int(bool(cap_transfers)))
+        check(lib().siminf_gpu_plan_create_ex(C.cast(holder.ref(), C.c_void_p),
+                                              self.model.handle, C.byref(opt), C.byref(h)))
         self.handle = h
 
     def run(self, stream=None):

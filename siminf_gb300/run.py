@@ -36,12 +36,19 @@ class Result:
         return cols[compartment::m.Nc, :]
 
 
-def run(model, seed=42, U_sparse=None, V_sparse=None):
+def run(model, seed=42, U_sparse=None, V_sparse=None, cap_transfers=False):
     """Simulate ``model`` on the GPU.  ``U_sparse``/``V_sparse`` are optional
     (ir, jc) CSC patterns over (Nn*Nc) x (Nrep*tlen) selecting which entries
-    to record, as a punchcard does (R/punchcard.R:139-253)."""
+    to record, as a punchcard does (R/punchcard.R:139-253).
+    ``cap_transfers`` enables the siminf_gpu_options extension of that name."""
     holder = abi.build_args(model, seed, U_sparse=U_sparse, V_sparse=V_sparse)
     dm = native.device_model(model.name)
+    if cap_transfers:
+        opt = abi.Options(cap_transfers=1)
+        code = native.lib().siminf_gpu_run_solver_ex(C.cast(holder.ref(), C.c_void_p),
+                                                     dm.handle, C.byref(opt))
+        native.check(code)
+        return Result(model, holder, native.last_stats())
     fn = (native.lib().siminf_gpu_run_solver_mssm if model.replicates > 1
           else native.lib().siminf_gpu_run_solver_ssm)
     code = fn(C.cast(holder.ref(), C.c_void_p), dm.handle)

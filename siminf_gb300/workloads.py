@@ -1,0 +1,91 @@
+"""Seeded synthetic workloads of the benchmark configurations.
+
+No dataset ships with the reference for this path (its data/*.rda files are
+examples that need R), so every workload is generated here from fixed seeds.
+
+- ``sir_plain``  -- mparse SIR, 1,000 nodes of (S=99, I=5, R=0), beta=0.16,
+  gamma=0.077, tspan 1:150, no events.
+- ``seir_events`` -- built-in SEIR (beta=0.16, epsilon=0.25, gamma=0.077),
+  Nn nodes with S ~ Poisson(300), E = 0, I ~ Bernoulli(0.01) * Poisson(3),
+  R = 0, run for `days` days.  Every node-day: an enter event with
+  probability 0.002 (1 individual into S, select column 1 = {S}) and an exit
+  event with probability 0.002 (1 individual from {S,E,I,R}, select column
+  2, equal weights -> hypergeometric).  External transfers:
+  `transfers` per day drawn uniformly from a fixed random directed graph of
+  4 * transfers edges.  Edge sources are uniform.  Edge destinations are
+  drawn with probability proportional to a weight from a power law with
+  exponent 2.1 (Pareto shape 1.1), truncated at the structural cutoff
+  sqrt(edges) of an uncorrelated scale-free graph (Boguna, Pastor-Satorras
+  & Vespignani, Eur. Phys. J. B 38, 2004), so destination in-degree follows
+  the power law up to that cutoff.  Without the cutoff one node collects
+  most of the population within weeks and fires ~90% of all transitions,
+  which turns the benchmark into a single sequential chain.  Each transfer
+  moves n = 1 + Poisson(3) individuals from {S,E,I,R}.  Sizes are capped
+  at what the source holds at run time (solver option cap_transfers); the
+  reference would instead stop with "Unable to sample individuals for
+  event."
+  Seeds: 1 graph, 2 u0, 3 events.
+"""
+import numpy as np
+
+from . import model as M
+
+
+def sir_plain(nodes=1000, days=150):
+    u0 = {"S": np.full(nodes, 99), "I": np.full(nodes, 5), "R": np.zeros(nodes)}
+    return M.SIR_mparse(u0, np.arange(1, days + 1, dtype=float), beta=0.16, gamma=0.077)
+
+
+def powerlaw_graph(nodes, edges, seed=1, exponent=2.1, cutoff=None):
+    """Fixed directed graph: uniform sources, destinations drawn with
+    probability proportional to power-law weights with the given exponent
+    on [1, cutoff] (default cutoff sqrt(edges))."""
+    rng = np.random.default_rng(seed)
+    a = exponent - 1.0
+    K = float(cutoff if cutoff is not None else np.sqrt(edges))
+    u = rng.random(nodes)
+    w = (1.0 - u * (1.0 - K ** -a)) ** (-1.0 / a)      # truncated Pareto(a) on [1, K]
+    p = w / w.sum()
+    src = rng.integers(0, nodes, edges).astype(np.int32)
+    dst = rng.choice(nodes, size=edges, p=p).astype(np.int32)
+    same = src == dst
+    dst[same] = (dst[same] + 1) % nodes
+    return src, dst
+
+
+def seir_events(nodes=1_000_000, days=365, transfers=500_000, p_enter=0.002, p_exit=0.002,
+                graph_edges=None, seeds=(1, 2, 3)):
+    """Config 2 (see module docstring).  Events are produced in the order
+    R/SimInf_events.R:398 sorts them: by time, exits, enters, transfers."""
+    g_seed, u_seed, e_seed = seeds
+    rng_u = np.random.default_rng(u_seed)
+    S = rng_u.poisson(300, nodes)
+    I = rng_u.poisson(3, nodes) * (rng_u.random(nodes) < 0.01)
+    u0 = np.vstack([S, np.zeros(nodes), I, np.zeros(nodes)]).astype(np.int32)
+
+    gsrc, gdst = powerlaw_graph(nodes, graph_edges or 4 * transfers, seed=g_seed)
+    rng = np.random.default_rng(e_seed)
+    chunks = {k: [] for k in ("event", "time", "node", "dest", "n", "select")}
+    for t in range(1, days + 1):
+        ex = np.nonzero(rng.random(nodes) < p_exit)[0].astype(np.int32)
+        en = np.nonzero(rng.random(nodes) < p_enter)[0].astype(np.int32)
+        pick = rng.integers(0, len(gsrc), transfers)
+        n = (1 + rng.poisson(3, transfers)).astype(np.int32)
+        m = len(ex) + len(en) + transfers
+        chunks["event"].append(np.concatenate([np.zeros(len(ex), np.int32),
+                                               np.ones(len(en), np.int32),
+                                               np.full(transfers, 3, np.int32)]))
+        chunks["time"].append(np.full(m, t, np.int32))
+        chunks["node"].append(np.concatenate([ex + 1, en + 1, gsrc[pick] + 1]).astype(np.int32))
+        chunks["dest"].append(np.concatenate([np.zeros(len(ex) + len(en), np.int32),
+                                              gdst[pick] + 1]).astype(np.int32))
+        chunks["n"].append(np.concatenate([np.ones(len(ex) + len(en), np.int32), n]))
+        chunks["select"].append(np.concatenate([np.full(len(ex), 2, np.int32),
+                                                np.ones(len(en), np.int32),
+                                                np.full(transfers, 2, np.int32)]))
+    ev = {k: np.concatenate(v) for k, v in chunks.items()}
+    total = len(ev["event"])
+    ev["proportion"] = np.zeros(total)
+    ev["shift"] = np.zeros(total, np.int32)
+    return M.SEIR(u0, np.arange(1, days + 1, dtype=float), beta=0.16, epsilon=0.25,
+                  gamma=0.077, events=ev)

@@ -109,3 +109,47 @@ def test_gpu_unsorted_events_rejected(gpu):
               events=M.make_events([0, 0], [2, 1], [1, 2], 0, 1, 0.0, 1, 0, sort=False))
     got, _, _ = run_gpu(m)
     assert got == -31
+
+
+def test_gpu_capped_seir_workload(gpu, oracle_lib):
+    """The headline workload's generator at 0.2% scale (2,000 nodes, 1,000
+    transfers/day, 365 days, cap_transfers on): bit-exact with the oracle."""
+    from siminf_gb300 import workloads
+    from siminf_gb300.run import run
+    from siminf_gb300 import abi
+    from oracle import oracle
+    m = workloads.seir_events(nodes=2000, days=365, transfers=1000)
+    h = abi.build_args(m, 42)
+    code, res = oracle.run(h, m.name, 4, cap_transfers=True)
+    assert code == 0
+    r = run(m, seed=42, cap_transfers=True)
+    assert np.array_equal(r.U, h.U.reshape(r.U.shape, order="F"))
+    assert r.stats.transitions == res.transitions
+    assert r.stats.e2_events == res.e2_events
+    # without the cap the reference semantics stop the run
+    with pytest.raises(Exception) as e:
+        run(m, seed=42)
+    assert getattr(e.value, "code", None) == -8
+
+
+def test_gpu_conservation_full_scale_properties(gpu):
+    """At 10% of the headline size: population changes only by the enter and
+    exit events (transfers conserve it), and no state is negative."""
+    from siminf_gb300 import workloads
+    from siminf_gb300.run import run
+    m = workloads.seir_events(nodes=100_000, days=60, transfers=50_000)
+    r = run(m, seed=7, cap_transfers=True)
+    U = r.U
+    assert (U >= 0).all()
+    tot = U.reshape(m.Nn, m.Nc, -1).sum(axis=(0, 1)).astype(np.int64)
+    ev = m.events
+    d_enter = np.bincount(ev["time"][ev["event"] == 1], minlength=62)[1:61]
+    # exits may be capped at empty nodes, so the population can only drop by
+    # at most the number of exit events of a day
+    d_exit = np.bincount(ev["time"][ev["event"] == 0], minlength=62)[1:61]
+    start = m.u0.sum()
+    for k in range(60):
+        prev = start if k == 0 else tot[k - 1]
+        change = tot[k] - prev
+        assert change <= d_enter[k]
+        assert change >= d_enter[k] - d_exit[k]
