@@ -189,6 +189,20 @@ int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args,
                              const siminf_gpu_model *model,
                              const siminf_gpu_options *options);
 
+/*
+ * Plan an event schedule on the host only (no GPU is touched): checks the
+ * event order and splits each day's external transfers into the
+ * conflict-free wavefronts the GPU runs, exactly as siminf_gpu_plan_create
+ * does.  days, waves, e1_events, e2_events receive counts (any may be
+ * NULL); wave, if not NULL, must hold args->len ints and receives per event
+ * the zero-based wavefront of an external transfer within its day, or -1.
+ * Returns 0 or an error code.  This is the planning half of the
+ * reference's SimInf_scheduled_events_create
+ * (src/solvers/SimInf_solver.c:443-510) and SimInf_split_events (:353-385).
+ */
+int siminf_gpu_schedule(const siminf_gpu_solver_args *args, int *days, int *waves,
+                        long long *e1_events, long long *e2_events, int *wave);
+
 /* Diagnostics of the last failing call on the calling thread: the fields
  * SimInf_print_status (src/solvers/SimInf_solver.c:1191-1249) and
  * SimInf_print_event (src/solvers/SimInf_solver.c:550-645) print. */

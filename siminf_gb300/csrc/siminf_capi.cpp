@@ -200,15 +200,22 @@ static inline long long event_day(int time, double tt0)
     return (long long) time - (long long) std::floor(tt0);
 }
 
-/* Run f(t, nthreads) on every hardware thread and join. */
-template <class F>
-static void parallel(F &&f)
+/* Threads used by the host planner. */
+static int planner_threads()
 {
     unsigned n = std::thread::hardware_concurrency();
     if (n < 1)
         n = 1;
     if (n > 64)
         n = 64;
+    return (int) n;
+}
+
+/* Run f(t, n) on n = planner_threads() threads and join. */
+template <class F>
+static void parallel(F &&f)
+{
+    const unsigned n = (unsigned) planner_threads();
     std::vector<std::thread> th;
     for (unsigned t = 1; t < n; t++)
         th.emplace_back([&f, t, n] { f((int) t, (int) n); });
@@ -234,7 +241,7 @@ static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int 
         std::vector<long long> e2_per_day;
         std::vector<PlannedErr> planned;
     };
-    std::vector<Chunk> chunks(64);
+    std::vector<Chunk> chunks(planner_threads());
     parallel([&](int t, int n) {
         Chunk &c = chunks[t];
         c.e2_per_day.assign(ndays + 1, 0);
@@ -397,6 +404,34 @@ static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int 
     return 0;
 }
 
+/* The day schedule (src/solvers/SimInf_solver_ssm.c:305-334): tt starts
+ * at tspan[0], next = floor(tt) + 1, and after each day the columns k with
+ * tt > tspan[k] are stored. */
+static int make_days(siminf_gpu_plan *p, const siminf_gpu_solver_args *a)
+{
+    double tt = a->tspan[0], next = std::floor(tt) + 1.0;
+    int it = 0;
+    p->days.clear();
+    while (it < a->tlen) {
+        DayInfo di;
+        di.tt = tt;
+        di.next = next;
+        tt = next;
+        next += 1.0;
+        di.c0 = it;
+        while (it < a->tlen && tt > a->tspan[it])
+            it++;
+        di.c1 = it;
+        p->days.push_back(di);
+        if (p->days.size() > (size_t) 100000000) {
+            set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0, "tspan too long");
+            return SIMINF_GPU_ERR_INVALID_MODEL;
+        }
+    }
+    p->ndays = (int) p->days.size();
+    return 0;
+}
+
 extern "C" {
 
 int siminf_gpu_model_builtin(const char *name, siminf_gpu_model **out)
@@ -499,28 +534,9 @@ int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_
     s.cap = opt ? (opt->cap_transfers != 0) : 0;
     p->tt0 = a->tspan[0];
 
-    /* Day schedule (src/solvers/SimInf_solver_ssm.c:305-334). */
-    {
-        double tt = a->tspan[0], next = std::floor(tt) + 1.0;
-        int it = 0;
-        while (it < tlen) {
-            DayInfo di;
-            di.tt = tt;
-            di.next = next;
-            tt = next;
-            next += 1.0;
-            di.c0 = it;
-            while (it < tlen && tt > a->tspan[it])
-                it++;
-            di.c1 = it;
-            p->days.push_back(di);
-            if (p->days.size() > (size_t) 100000000) {
-                delete p;
-                set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0, "tspan too long");
-                return SIMINF_GPU_ERR_INVALID_MODEL;
-            }
-        }
-        p->ndays = (int) p->days.size();
+    if ((rc = make_days(p, a))) {
+        delete p;
+        return rc;
     }
 
     /* Dense S (Nt rows of Nc) and G column masks. */
@@ -612,6 +628,9 @@ int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_
     if (!rc) rc = dalloc(&s.err, (size_t) MAX_ERR, own);
     if (!rc) rc = dalloc(&s.err_count, 3, own);
     if (!rc) rc = dalloc(&s.fired, 1, own);
+    if (!rc) rc = dalloc(&s.heavy_list, (size_t) 2 * MAX_HEAVY, own);
+    if (!rc) rc = dalloc(&s.heavy_count, 2, own);
+    if (!rc) rc = dalloc(&s.heavy_mark, (size_t) Ntot, own);
     if (!rc) {
         s.err_day = s.err_count + 1;
         s.err_day_pre_e2 = s.err_count + 2;
@@ -832,6 +851,10 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s.fired, 0, sizeof(unsigned long long), st);
     if (e == cudaSuccess)
+        e = cudaMemsetAsync(s.heavy_count, 0, 2 * sizeof(int), st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(s.heavy_mark, 0, (size_t) s.Ntot * sizeof(int), st);
+    if (e == cudaSuccess)
         e = cudaMemcpyAsync(s.u, p->u0_host, (size_t) s.Ntot * s.Nc * sizeof(int),
                             cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess && s.Nd > 0) {
@@ -926,6 +949,44 @@ int siminf_gpu_plan_stats(const siminf_gpu_plan *p, siminf_gpu_stats *out)
     if (!p || !out)
         return SIMINF_GPU_ERR_INVALID_MODEL;
     *out = p->stats;
+    return 0;
+}
+
+int siminf_gpu_schedule(const siminf_gpu_solver_args *a, int *days, int *waves,
+                        long long *e1_events, long long *e2_events, int *wave)
+{
+    memset(&g_status, 0, sizeof(g_status));
+    if (!a || !a->tspan || a->tlen < 1 || a->Nn < 1)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    if (a->len > 0 && (!a->event || !a->time || !a->node || !a->dest || !a->n ||
+                       !a->proportion || !a->select || !a->shift))
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    siminf_gpu_plan p;
+    int rc = make_days(&p, a);
+    if (rc)
+        return rc;
+    std::vector<E1Rec> e1;
+    std::vector<int> e1_ptr;
+    std::vector<E2Rec> e2;
+    rc = plan_events(&p, a, a->len > 0 ? INT_MAX : 0, e1, e1_ptr, e2);
+    if (rc)
+        return rc;
+    if (days)
+        *days = p.ndays;
+    if (waves)
+        *waves = (int) p.wave_ptr.size() - 1;
+    if (e1_events)
+        *e1_events = (long long) p.e1_count;
+    if (e2_events)
+        *e2_events = (long long) p.e2_count;
+    if (wave) {
+        for (int i = 0; i < a->len; i++)
+            wave[i] = -1;
+        for (int d = 0; d < p.ndays; d++)
+            for (int w = p.day_wave[d]; w < p.day_wave[d + 1]; w++)
+                for (long long k = p.wave_ptr[w]; k < p.wave_ptr[w + 1]; k++)
+                    wave[e2[k].index] = w - p.day_wave[d];
+    }
     return 0;
 }
 

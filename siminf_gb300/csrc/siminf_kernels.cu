@@ -39,7 +39,10 @@ namespace siminf {
 
 enum { ERR_NEGATIVE_STATE = -1, ERR_UNDEFINED_EVENT = -3, ERR_SAMPLE_SELECT = -8,
        ERR_INVALID_RATE = -11, ERR_EVENTS_N = -15, ERR_EVENT_SHIFT = -16,
-       ERR_SHIFT_OUT_OF_BOUNDS = -17, ERR_INVALID_PROPORTION = -18 };
+       ERR_SHIFT_OUT_OF_BOUNDS = -17, ERR_INVALID_PROPORTION = -18, ERR_TIMEOUT = -33 };
+
+/* Upper bound on the transitions of one node in one unit of time. */
+#define MAX_NODE_DAY_TRANSITIONS (1u << 28)
 
 enum { EV_EXIT = 0, EV_ENTER = 1, EV_INTERNAL = 2, EV_EXTERNAL = 3 };
 
@@ -121,6 +124,18 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
             t = next;
             break;
         }
+        if (!si_finite_pos(sum)) {
+            /* A non-finite rate sum (after an invalid rate, which is
+             * recorded) would never reach the next day: stop the node. */
+            if (!err) {
+                err = ERR_INVALID_RATE;
+                err_tr = -1;
+                err_t = t;
+                err_rate = sum;
+            }
+            t = next;
+            break;
+        }
         si_skip(&r);
         const double tau = si_div(L, sum);
         const double tn = tau + t;
@@ -160,7 +175,16 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
             }
         }
 
-        fired++;
+        if (++fired > MAX_NODE_DAY_TRANSITIONS) {
+            /* Bounded work per node-day: a time step that stopped advancing
+             * t (a rate sum near the overflow threshold) ends the run
+             * with an error instead of spinning. */
+            err = ERR_TIMEOUT;
+            err_tr = tr;
+            err_t = t;
+            t = next;
+            break;
+        }
 #pragma unroll
         for (int c = 0; c < NC; c++) {
             const int d = sS[tr * NC + c];
@@ -195,6 +219,175 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
         }
         sum += delta;
         prefix_sums<M>(rate, cum);
+    }
+    return fired;
+}
+
+/* ------------------------------------------------------------------ */
+/* Warp-cooperative SSA of one heavy node (same semantics as ssa_day).  */
+/* All 32 lanes carry the node's state and run the chain on identical   */
+/* data, so it costs one warp instruction stream.  Two kinds of work    */
+/* are spread over the lanes:                                           */
+/*  - draws: lane i holds uniform and -log(uniform) of draw base + i,   */
+/*    computed for 32 draws (16 transitions) at once;                   */
+/*  - candidates: rates do not depend on t, so lane k computes the rate */
+/*    vector, delta and new sum that transition k would produce, while  */
+/*    the chain decides which transition fires; the winner is then      */
+/*    taken by shuffles.  The division inside the rate code leaves the  */
+/*    loop-carried chain that way.                                      */
+/* ------------------------------------------------------------------ */
+template <class M>
+__device__ __forceinline__ unsigned ssa_day_warp(int (&u)[M::NC], double (&rate)[M::NT], double &sum,
+                                                 double &t, const double *v, const double *ld,
+                                                 const double *gd, uint64_t seed, uint64_t sid,
+                                                 uint64_t &ctr, double next, const int *sS,
+                                                 const uint32_t *sG, int &err, int &err_tr,
+                                                 double &err_t, double &err_rate)
+{
+    constexpr int NC = M::NC, NT = M::NT;
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const int k = lane < NT ? lane : NT - 1;
+    unsigned fired = 0;
+
+    uint64_t base = ctr;
+    double Lb, Ub;
+    {
+        si_rng r;
+        si_rng_init(&r, seed, sid, base + (uint64_t) lane);
+        Ub = si_u32_to_uniform_pos(si_peek_u32(&r));
+        Lb = -si_log(Ub);
+    }
+    double cum[NT];
+    prefix_sums<M>(rate, cum);
+
+    /* candidate k from the current state */
+    double crate[NT], ccum[NT], csum, cbad_rate = 0.0;
+    int cneg = 0, cbad = 0, cbad_tr = -1;
+    auto candidates = [&]() {
+        int uk[NC];
+        cneg = 0;
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int d = sS[k * NC + c];
+            uk[c] = u[c] + d;
+            if (d != 0 && uk[c] < 0)
+                cneg = 1;
+        }
+        double delta = 0.0;
+        cbad = 0;
+        const uint32_t gm = sG[k];
+#pragma unroll
+        for (int j = 0; j < NT; j++) {
+            if (gm & (1u << j)) {
+                const double nr = M::rate(j, uk, v, ld, gd, 0.0);
+                crate[j] = nr;
+                delta += nr - rate[j];
+                if (si_bad_rate(nr)) {
+                    cbad = 1;
+                    cbad_tr = j;
+                    cbad_rate = nr;
+                }
+            } else {
+                crate[j] = rate[j];
+            }
+        }
+        csum = sum + delta;
+        prefix_sums<M>(crate, ccum);
+    };
+    candidates();
+
+    for (;;) {
+        if (sum <= 0.0) {
+            t = next;
+            break;
+        }
+        if (!si_finite_pos(sum)) {
+            if (!err) {
+                err = ERR_INVALID_RATE;
+                err_tr = -1;
+                err_t = t;
+                err_rate = sum;
+            }
+            t = next;
+            break;
+        }
+        if (ctr + 1 >= base + 32) {
+            base = ctr;
+            si_rng r;
+            si_rng_init(&r, seed, sid, base + (uint64_t) lane);
+            Ub = si_u32_to_uniform_pos(si_peek_u32(&r));
+            Lb = -si_log(Ub);
+        }
+        const int i0 = (int) (ctr - base);
+        const double L = __shfl_sync(FULL, Lb, i0);
+        const double u2 = __shfl_sync(FULL, Ub, i0 + 1);
+        const double tau = si_div(L, sum);
+        const double tn = tau + t;
+        const double rnd = u2 * sum;
+        if (si_dge(tn, next)) {
+            t = next;
+            ctr += 1;
+            break;
+        }
+        t = tn;
+        ctr += 2;
+
+        int tr = NT - 1;
+#pragma unroll
+        for (int kk = NT - 2; kk >= 0; kk--)
+            if (!si_dgt(rnd, cum[kk]))
+                tr = kk;
+        double rtr = rate[0];
+#pragma unroll
+        for (int kk = 1; kk < NT; kk++)
+            if (tr == kk)
+                rtr = rate[kk];
+        if (si_is_zero(rtr)) {
+#pragma unroll
+            for (int kk = NT - 1; kk >= 1; kk--)
+                if (tr == kk && si_is_zero(rate[kk]))
+                    tr = kk - 1;
+            double r2 = rate[0];
+#pragma unroll
+            for (int kk = 1; kk < NT; kk++)
+                if (tr == kk)
+                    r2 = rate[kk];
+            if (si_is_zero(r2)) {
+                sum = 0.0;
+                break;
+            }
+        }
+
+        if (++fired > MAX_NODE_DAY_TRANSITIONS) {
+            err = ERR_TIMEOUT;
+            err_tr = tr;
+            err_t = t;
+            t = next;
+            break;
+        }
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            u[c] += sS[tr * NC + c];
+#pragma unroll
+        for (int j = 0; j < NT; j++) {
+            rate[j] = __shfl_sync(FULL, crate[j], tr);
+            cum[j] = __shfl_sync(FULL, ccum[j], tr);
+        }
+        sum = __shfl_sync(FULL, csum, tr);
+        if (__shfl_sync(FULL, cneg, tr)) {
+            err = ERR_NEGATIVE_STATE;
+            err_tr = tr;
+            err_t = t;
+            err_rate = 0.0;
+        }
+        if (__shfl_sync(FULL, cbad, tr)) {
+            err = ERR_INVALID_RATE;
+            err_tr = __shfl_sync(FULL, cbad_tr, tr);
+            err_t = t;
+            err_rate = __shfl_sync(FULL, cbad_rate, tr);
+        }
+        candidates();
     }
     return fired;
 }
@@ -525,6 +718,22 @@ __device__ __forceinline__ void load_model_smem(const DevState &s, int *sS, uint
 /* Kernels.                                                              */
 /* ------------------------------------------------------------------ */
 
+/* List g as heavy for `day` when its rate sum promises many transitions
+ * in one unit of time (only for models whose rates ignore t). */
+template <class M>
+__device__ __forceinline__ void push_heavy(const DevState &s, long long g, double sum, int day)
+{
+    if (!M::RATES_TIME_INVARIANT || !s.heavy_list)
+        return;
+    if (si_dge(sum, SIMINF_HEAVY_RATE) && si_finite_pos(sum)) {
+        const int slot = atomicAdd(&s.heavy_count[day & 1], 1);
+        if (slot < MAX_HEAVY) {
+            s.heavy_list[(day & 1) * MAX_HEAVY + slot] = (int) g;
+            s.heavy_mark[g] = day + 1;
+        }
+    }
+}
+
 template <class M>
 __global__ void k_init(DevState s, double tt0)
 {
@@ -552,45 +761,58 @@ __global__ void k_init(DevState s, double tt0)
     s.t_time[g] = tt0;
     s.ctr[g] = 0;
     s.update[g] = 0;
+    push_heavy<M>(s, g, sum, 0);
 }
 
+/* One day of SSA and E1 events.  Blocks [0, HEAVY_BLOCKS) run the heavy
+ * nodes listed for this day, one per warp; the remaining blocks run every
+ * other (replicate, node) pair, one per thread. */
 template <class M>
-__global__ void __launch_bounds__(256) k_ssa_e1(DevState s, int day, double tt, double next)
+__device__ __forceinline__ void node_day(const DevState &s, long long g, int day, double tt,
+                                         double next, const int *sS, const uint32_t *sG,
+                                         bool warp_mode, unsigned long long &fired)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
-    __shared__ int sS[NT * NC];
-    __shared__ uint32_t sG[NT];
-    load_model_smem<M>(s, sS, sG);
-    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    unsigned long long fired = 0;
-    if (g < s.Ntot && load_flag(s.err_day) >= day) {
-        const int node = (int) (g % s.Nn);
-        int u[NC];
-        double rate[NT];
+    const int node = (int) (g % s.Nn);
+    int u[NC];
+    double rate[NT];
 #pragma unroll
-        for (int c = 0; c < NC; c++)
-            u[c] = s.u[g * NC + c];
+    for (int c = 0; c < NC; c++)
+        u[c] = s.u[g * NC + c];
 #pragma unroll
-        for (int k = 0; k < NT; k++)
-            rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
-        double sum = s.sum_rate[g], t = s.t_time[g];
-        si_rng r;
+    for (int k = 0; k < NT; k++)
+        rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
+    double sum = s.sum_rate[g], t = s.t_time[g];
+    const double *v = s.vA + g * ND;
+    const double *ld = s.ldata + (size_t) node * s.Nld;
+    int err = 0, err_tr = -1;
+    double err_t = 0, err_rate = 0;
+    si_rng r;
+    if (warp_mode) {
+        uint64_t ctr = s.ctr[g];
+        fired += ssa_day_warp<M>(u, rate, sum, t, v, ld, s.gdata, s.seed, (uint64_t) g, ctr, next,
+                                 sS, sG, err, err_tr, err_t, err_rate);
+        si_rng_init(&r, s.seed, (uint64_t) g, ctr);
+    } else {
         si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
-        const double *v = s.vA + g * ND;
-        const double *ld = s.ldata + (size_t) node * s.Nld;
-        int err = 0, err_tr = -1;
-        double err_t = 0, err_rate = 0;
-        fired = ssa_day<M>(u, rate, sum, t, v, ld, s.gdata, r, next, sS, sG, err, err_tr,
-                           err_t, err_rate);
-        if (err) {
+        fired += ssa_day<M>(u, rate, sum, t, v, ld, s.gdata, r, next, sS, sG, err, err_tr,
+                            err_t, err_rate);
+    }
+    const bool writer = !warp_mode || (threadIdx.x & 31) == 0;
+    if (err) {
+        if (writer)
             record_error(s, err, PHASE_SSA, day, g, err_tr, -1, err_t, err_rate);
-        } else {
-            int e_code = 0, e_idx = -1;
-            if (node_e1<NC>(s, u, node, day, r, g, tt, e_code, e_idx))
+    } else {
+        int e_code = 0, e_idx = -1;
+        const bool upd = node_e1<NC>(s, u, node, day, r, g, tt, e_code, e_idx);
+        if (writer) {
+            if (upd)
                 s.update[g] = 1;
             if (e_code)
                 record_error(s, e_code, PHASE_E1, day, g, -1, e_idx, tt, 0);
         }
+    }
+    if (writer) {
 #pragma unroll
         for (int c = 0; c < NC; c++)
             s.u[g * NC + c] = u[c];
@@ -600,6 +822,36 @@ __global__ void __launch_bounds__(256) k_ssa_e1(DevState s, int day, double tt, 
         s.sum_rate[g] = sum;
         s.t_time[g] = t;
         s.ctr[g] = r.ctr;
+    }
+}
+
+template <class M>
+__global__ void __launch_bounds__(256, 2) k_ssa_e1(DevState s, int day, double tt, double next)
+{
+    constexpr int NC = M::NC, NT = M::NT;
+    __shared__ int sS[NT * NC];
+    __shared__ uint32_t sG[NT];
+    load_model_smem<M>(s, sS, sG);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && s.heavy_count)
+        s.heavy_count[(day + 1) & 1] = 0;       /* filled by this day's post time step */
+    unsigned long long fired = 0;
+    const bool stop = load_flag(s.err_day) < day;
+    if (blockIdx.x < HEAVY_BLOCKS) {
+        if (M::RATES_TIME_INVARIANT && s.heavy_list && !stop) {
+            const int w = blockIdx.x * HEAVY_WARPS_PER_BLOCK + (threadIdx.x >> 5);
+            const int n = min(s.heavy_count[day & 1], (int) MAX_HEAVY);
+            if (w < n) {
+                unsigned long long f = 0;
+                node_day<M>(s, s.heavy_list[(day & 1) * MAX_HEAVY + w], day, tt, next, sS, sG,
+                            true, f);
+                if ((threadIdx.x & 31) == 0)
+                    fired += f;
+            }
+        }
+    } else {
+        const long long g = (blockIdx.x - HEAVY_BLOCKS) * (long long) blockDim.x + threadIdx.x;
+        if (g < s.Ntot && !stop && !(s.heavy_mark && s.heavy_mark[g] == day + 1))
+            node_day<M>(s, g, day, tt, next, sS, sG, false, fired);
     }
     add_fired(s, fired);
 }
@@ -697,6 +949,7 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
         s.sum_rate[g] += delta;
         s.update[g] = 0;
     }
+    push_heavy<M>(s, g, s.sum_rate[g], day + 1);
     store_columns<NC, ND>(s, rep, node, u, vo, c0, c1);
 }
 
@@ -809,7 +1062,7 @@ struct Launch {
     }
     static cudaError_t ssa_e1(const DevState &s, int day, double tt, double next, cudaStream_t st)
     {
-        k_ssa_e1<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, next);
+        k_ssa_e1<M><<<HEAVY_BLOCKS + blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, next);
         return cudaGetLastError();
     }
     static cudaError_t e2_wave(const DevState &s, const E2Rec *ev, int count, int day, double tt,

@@ -29,6 +29,7 @@ struct ModelSIR {
     static constexpr int NC = 3, NT = 2, ND = 0;
     static constexpr int NGD = 0;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
                                                   double t)
@@ -55,6 +56,7 @@ struct ModelSEIR {
     static constexpr int NC = 4, NT = 3, ND = 0;
     static constexpr int NGD = 0;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
                                                   double t)
@@ -83,6 +85,7 @@ struct ModelSIS {
     static constexpr int NC = 2, NT = 2, ND = 0;
     static constexpr int NGD = 0;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
                                                   double t)
@@ -137,6 +140,7 @@ struct ModelSISe {
     static constexpr int NC = 2, NT = 2, ND = 1;
     static constexpr int NGD = 8;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
                                                   double t)
@@ -175,6 +179,7 @@ struct ModelSISe3 {
     static constexpr int NC = 6, NT = 6, ND = 1;
     static constexpr int NGD = 12;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
                                                   double t)
@@ -217,6 +222,7 @@ struct ModelSIRmparse {
     static constexpr int NC = 3, NT = 2, ND = 0;
     static constexpr int NGD = 2;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
                                                   double t)
@@ -241,6 +247,7 @@ struct ModelSISePF {
     static constexpr int NC = 2, NT = 2, ND = 1;
     static constexpr int NGD = 2;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
                                                   double t)

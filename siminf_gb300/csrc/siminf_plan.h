@@ -26,6 +26,13 @@ namespace siminf {
 
 enum { MAX_NC = 16, MAX_NT = 32, MAX_ERR = 1024 };
 
+/* Nodes expected to fire at least HEAVY_RATE transitions in a day run one
+ * per warp (k_ssa_e1's first HEAVY_BLOCKS blocks); at most MAX_HEAVY per
+ * day, the rest take the thread-per-node path. */
+enum { HEAVY_WARPS_PER_BLOCK = 8, MAX_HEAVY = 2048,
+       HEAVY_BLOCKS = MAX_HEAVY / HEAVY_WARPS_PER_BLOCK };
+#define SIMINF_HEAVY_RATE 24.0
+
 enum { PHASE_INIT = 0, PHASE_SSA = 1, PHASE_E1 = 2, PHASE_E2 = 3, PHASE_PTS = 4 };
 
 struct E1Rec {          /* 32 bytes */
@@ -107,6 +114,11 @@ struct DevState {
     int *err_day;           /* first day with an error (INT_MAX if none) */
     int *err_day_pre_e2;    /* first day with an SSA or E1 error */
     unsigned long long *fired;
+
+    /* heavy nodes of the next two days: list[(d & 1) * MAX_HEAVY + i] */
+    int *heavy_list;
+    int *heavy_count;       /* [2] */
+    int *heavy_mark;        /* per g: day + 1 when listed for that day */
 };
 
 }  // namespace siminf

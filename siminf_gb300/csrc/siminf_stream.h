@@ -449,6 +449,13 @@ SI_HD int si_bad_rate(double x)
     return ((b >> 52) & 0x7FF) == 0x7FF || ((b >> 63) && (b << 1) != 0);
 }
 
+/* 0 < x < +inf (false for NaN). */
+SI_HD int si_finite_pos(double x)
+{
+    const uint64_t b = si_double_bits(x);
+    return !(b >> 63) && b != 0 && ((b >> 52) & 0x7FF) != 0x7FF;
+}
+
 /* x == 0.0 (either sign). */
 SI_HD int si_is_zero(double x)
 {

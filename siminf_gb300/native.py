@@ -37,6 +37,10 @@ def lib():
     L.siminf_gpu_run_solver_ex.restype = C.c_int
     L.siminf_gpu_plan_create_ex.argtypes = [vp, vp, C.POINTER(abi.Options), C.POINTER(vp)]
     L.siminf_gpu_plan_create_ex.restype = C.c_int
+    L.siminf_gpu_schedule.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                      C.POINTER(C.c_int)]
+    L.siminf_gpu_schedule.restype = C.c_int
     L.siminf_gpu_last_status.argtypes = [C.POINTER(abi.Status)]
     L.siminf_gpu_last_stats.argtypes = [C.POINTER(abi.Stats)]
     L.siminf_gpu_plan_create.argtypes = [vp, vp, C.POINTER(vp)]
@@ -58,7 +62,7 @@ EXPORTS = (
     "siminf_gpu_plan_create_ex", "siminf_gpu_last_status",
     "siminf_gpu_last_stats", "siminf_gpu_plan_create", "siminf_gpu_plan_run",
     "siminf_gpu_plan_download", "siminf_gpu_plan_stats", "siminf_gpu_plan_free",
-    "siminf_gpu_plan_profile",
+    "siminf_gpu_plan_profile", "siminf_gpu_schedule",
 )
 
 
@@ -78,6 +82,20 @@ def check(code):
     if code != 0:
         st = last_status()
         raise abi.SimInfError(code, st.message.decode(errors="replace"))
+
+
+def schedule(holder):
+    """Host-only wave planning of an args holder: (days, waves, e1, e2,
+    per-event wave array)."""
+    import numpy as np
+    n = max(1, holder.args.len)
+    wave = np.zeros(n, dtype=np.int32)
+    days, waves = C.c_int(), C.c_int()
+    e1, e2 = C.c_longlong(), C.c_longlong()
+    check(lib().siminf_gpu_schedule(C.cast(holder.ref(), C.c_void_p), C.byref(days),
+                                    C.byref(waves), C.byref(e1), C.byref(e2),
+                                    wave.ctypes.data_as(C.POINTER(C.c_int))))
+    return days.value, waves.value, e1.value, e2.value, wave[:holder.args.len]
 
 
 class DeviceModel:

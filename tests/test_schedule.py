@@ -1,0 +1,98 @@
+"""Host-side event planning (siminf_gpu_schedule), no GPU needed: the
+wavefronts must be conflict-free and equivalent to the serial array order
+of the reference's external-transfer loop (src/solvers/SimInf_solver.c:
+824-902 run by one thread, src/solvers/SimInf_solver_ssm.c:244-250)."""
+import numpy as np
+import pytest
+
+from siminf_gb300 import abi, native, workloads
+from helpers import parity_cases
+
+
+def reference_levels(m):
+    """The level rule written out serially: an external transfer goes one
+    wave after every earlier transfer of its day that touched its source,
+    and after every earlier transfer whose source is its destination."""
+    ev = m.events
+    t0 = float(m.tspan[0])
+    levels = np.full(len(ev["event"]), -1)
+    excl, add = {}, {}
+    day_prev = None
+    for i in range(len(ev["event"])):
+        if ev["event"][i] != 3:
+            continue
+        t = ev["time"][i]
+        d = 0 if t <= t0 else t - int(np.floor(t0))
+        if d != day_prev:
+            excl, add, day_prev = {}, {}, d
+        s, dst = ev["node"][i], ev["dest"][i]
+        L = 1 + max(excl.get(s, 0), add.get(s, 0), excl.get(dst, 0))
+        excl[s] = L
+        add[dst] = max(add.get(dst, 0), L)
+        levels[i] = L - 1
+    return levels
+
+
+def check_conflict_free(m, wave):
+    ev = m.events
+    t0 = float(m.tspan[0])
+    days = np.where(ev["time"] <= t0, 0, ev["time"] - int(np.floor(t0)))
+    sel = np.nonzero((ev["event"] == 3) & (wave >= 0))[0]
+    groups = {}
+    for i in sel:
+        groups.setdefault((days[i], wave[i]), []).append(i)
+    for (d, w), idx in groups.items():
+        src = [ev["node"][i] for i in idx]
+        dst = [ev["dest"][i] for i in idx]
+        assert len(set(src)) == len(src), "two transfers of one wave share a source"
+        assert not (set(src) & set(dst)) or all(s == t for s, t in zip(src, dst)
+                                                if s in dst), "a wave reads a node it writes"
+    # order: within a day, events touching a common source keep array order
+    for i in sel:
+        for j in sel:
+            if j >= i or days[j] != days[i]:
+                continue
+            si, di, sj, dj = ev["node"][i], ev["dest"][i], ev["node"][j], ev["dest"][j]
+            if si == sj or si == dj or di == sj:
+                assert wave[j] < wave[i]
+
+
+def test_schedule_levels_match_serial_rule():
+    for label, m in parity_cases():
+        if not len(m.events["event"]):
+            continue
+        h = abi.build_args(m, 1)
+        days, waves, e1, e2, wave = native.schedule(h)
+        ref = reference_levels(m)
+        e2_mask = ref >= 0
+        assert np.array_equal(wave[e2_mask], ref[e2_mask]), label
+        assert e1 == int(((m.events["event"] != 3)).sum())
+
+
+def test_schedule_conflict_free_small_workload():
+    m = workloads.seir_events(nodes=300, days=20, transfers=400)
+    h = abi.build_args(m, 1)
+    days, waves, e1, e2, wave = native.schedule(h)
+    assert days == 20 and e2 == 20 * 400
+    check_conflict_free(m, wave)
+    assert np.array_equal(wave[wave >= 0], reference_levels(m)[wave >= 0])
+
+
+def test_schedule_rejects_unsorted():
+    from siminf_gb300 import model as M
+    m = M.SIR({"S": [5, 5], "I": [0, 0], "R": [0, 0]}, [1, 2, 3], 0.0, 0.0,
+              events=M.make_events([3, 0], [1, 1], [1, 2], [2, 0], 1, 0.0, 1, 0, sort=False))
+    h = abi.build_args(m, 1)
+    with pytest.raises(abi.SimInfError) as e:
+        native.schedule(h)
+    assert e.value.code == -31
+
+
+def test_schedule_headline_scale_properties():
+    """Full day count at 2% of the headline size: planning finishes and
+    every transfer lands in a wave."""
+    m = workloads.seir_events(nodes=20_000, days=365, transfers=10_000)
+    h = abi.build_args(m, 1)
+    days, waves, e1, e2, wave = native.schedule(h)
+    assert days == 365 and e2 == 365 * 10_000
+    assert (wave[m.events["event"] == 3] >= 0).all()
