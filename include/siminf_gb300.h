@@ -178,10 +178,15 @@ int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args,
  * them instead of stopping the run with SIMINF_ERR_SAMPLE_SELECT
  * (src/solvers/SimInf_solver.c:102-105).  Synthetic schedules whose sizes
  * are drawn without knowledge of the state need it.
+ *
+ * heavy_rate: a tuning knob, not a semantic option -- nodes whose rate sum
+ * at the start of a day reaches it are simulated one per warp (results are
+ * identical either way).
  */
 typedef struct siminf_gpu_options {
     int cap_transfers;
-    int reserved[7];
+    int heavy_rate;     /* rate sum from which a node runs one per warp (0 = default) */
+    int reserved[6];
 } siminf_gpu_options;
 
 /* siminf_gpu_run_solver_mssm with options (NULL = all zero). */

@@ -113,7 +113,7 @@ class Status(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("cap_transfers", C.c_int), ("reserved", C.c_int * 7)]
+    _fields_ = [("cap_transfers", C.c_int), ("heavy_rate", C.c_int), ("reserved", C.c_int * 6)]
 
 
 class Stats(C.Structure):

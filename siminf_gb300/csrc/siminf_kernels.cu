@@ -723,14 +723,16 @@ __device__ __forceinline__ void load_model_smem(const DevState &s, int *sS, uint
 template <class M>
 __device__ __forceinline__ void push_heavy(const DevState &s, long long g, double sum, int day)
 {
-    if (!M::RATES_TIME_INVARIANT || !s.heavy_list)
+    if (!M::RATES_TIME_INVARIANT || !(s.heavy_rate > 0.0))
         return;
-    if (si_dge(sum, SIMINF_HEAVY_RATE) && si_finite_pos(sum)) {
-        const int slot = atomicAdd(&s.heavy_count[day & 1], 1);
-        if (slot < MAX_HEAVY) {
-            s.heavy_list[(day & 1) * MAX_HEAVY + slot] = (int) g;
-            s.heavy_mark[g] = day + 1;
-        }
+    if (!si_dge(sum, s.heavy_rate) || !si_finite_pos(sum))
+        return;
+    const int cls = si_dge(sum, 16.0 * s.heavy_rate) ? 0 : si_dge(sum, 4.0 * s.heavy_rate) ? 1 : 2;
+    const int q = (day & 1) * HEAVY_CLASSES + cls;
+    const int slot = atomicAdd(&s.heavy_count[q], 1);
+    if (slot < MAX_HEAVY) {
+        s.heavy_list[q * MAX_HEAVY + slot] = (int) g;
+        s.heavy_mark[g] = day + 1;
     }
 }
 
@@ -826,31 +828,48 @@ __device__ __forceinline__ void node_day(const DevState &s, long long g, int day
 }
 
 template <class M>
-__global__ void __launch_bounds__(256, 2) k_ssa_e1(DevState s, int day, double tt, double next)
+__global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, double tt,
+                                                         double next)
 {
     constexpr int NC = M::NC, NT = M::NT;
     __shared__ int sS[NT * NC];
     __shared__ uint32_t sG[NT];
     load_model_smem<M>(s, sS, sG);
-    if (blockIdx.x == 0 && threadIdx.x == 0 && s.heavy_count)
-        s.heavy_count[(day + 1) & 1] = 0;       /* filled by this day's post time step */
+    const int par = day & 1, npar = (day + 1) & 1;
+    if (blockIdx.x == 0 && threadIdx.x < HEAVY_CLASSES)
+        s.heavy_count[npar * HEAVY_CLASSES + threadIdx.x] = 0;  /* filled by this day's pts */
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        s.heavy_next[npar] = 0;
     unsigned long long fired = 0;
     const bool stop = load_flag(s.err_day) < day;
-    if (blockIdx.x < HEAVY_BLOCKS) {
-        if (M::RATES_TIME_INVARIANT && s.heavy_list && !stop) {
-            const int w = blockIdx.x * HEAVY_WARPS_PER_BLOCK + (threadIdx.x >> 5);
-            const int n = min(s.heavy_count[day & 1], (int) MAX_HEAVY);
-            if (w < n) {
+    if ((int) blockIdx.x < s.heavy_blocks) {
+        if (M::RATES_TIME_INVARIANT && !stop) {
+            int n[HEAVY_CLASSES];
+#pragma unroll
+            for (int c = 0; c < HEAVY_CLASSES; c++)
+                n[c] = min(s.heavy_count[par * HEAVY_CLASSES + c], (int) MAX_HEAVY);
+            for (;;) {
+                int idx = 0;
+                if ((threadIdx.x & 31) == 0)
+                    idx = atomicAdd(&s.heavy_next[par], 1);
+                idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
+                int c = 0;
+                while (c < HEAVY_CLASSES && idx >= n[c]) {
+                    idx -= n[c];
+                    c++;
+                }
+                if (c == HEAVY_CLASSES)
+                    break;
                 unsigned long long f = 0;
-                node_day<M>(s, s.heavy_list[(day & 1) * MAX_HEAVY + w], day, tt, next, sS, sG,
-                            true, f);
+                node_day<M>(s, s.heavy_list[(par * HEAVY_CLASSES + c) * MAX_HEAVY + idx], day, tt,
+                            next, sS, sG, true, f);
                 if ((threadIdx.x & 31) == 0)
                     fired += f;
             }
         }
     } else {
-        const long long g = (blockIdx.x - HEAVY_BLOCKS) * (long long) blockDim.x + threadIdx.x;
-        if (g < s.Ntot && !stop && !(s.heavy_mark && s.heavy_mark[g] == day + 1))
+        const long long g = (blockIdx.x - s.heavy_blocks) * (long long) blockDim.x + threadIdx.x;
+        if (g < s.Ntot && !stop && !(s.heavy_mark[g] == day + 1))
             node_day<M>(s, g, day, tt, next, sS, sG, false, fired);
     }
     add_fired(s, fired);
@@ -1062,7 +1081,8 @@ struct Launch {
     }
     static cudaError_t ssa_e1(const DevState &s, int day, double tt, double next, cudaStream_t st)
     {
-        k_ssa_e1<M><<<HEAVY_BLOCKS + blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, next);
+        k_ssa_e1<M><<<s.heavy_blocks + blocks_for(s.Ntot, SSA_BLOCK), SSA_BLOCK, 0, st>>>(
+            s, day, tt, next);
         return cudaGetLastError();
     }
     static cudaError_t e2_wave(const DevState &s, const E2Rec *ev, int count, int day, double tt,

@@ -26,12 +26,12 @@ namespace siminf {
 
 enum { MAX_NC = 16, MAX_NT = 32, MAX_ERR = 1024 };
 
-/* Nodes expected to fire at least HEAVY_RATE transitions in a day run one
- * per warp (k_ssa_e1's first HEAVY_BLOCKS blocks); at most MAX_HEAVY per
- * day, the rest take the thread-per-node path. */
-enum { HEAVY_WARPS_PER_BLOCK = 8, MAX_HEAVY = 2048,
-       HEAVY_BLOCKS = MAX_HEAVY / HEAVY_WARPS_PER_BLOCK };
-#define SIMINF_HEAVY_RATE 24.0
+/* Nodes whose rate sum at the start of a day is at least heavy_rate run one
+ * per warp: k_ssa_e1's first heavy_blocks blocks are persistent warps that
+ * take heavy nodes from a per-day queue, heaviest class first (classes:
+ * sum >= 16, 4 and 1 times heavy_rate).  At most MAX_HEAVY per class and
+ * day; the rest take the thread-per-node path. */
+enum { SSA_BLOCK = 128, HEAVY_CLASSES = 3, MAX_HEAVY = 4096 };
 
 enum { PHASE_INIT = 0, PHASE_SSA = 1, PHASE_E1 = 2, PHASE_E2 = 3, PHASE_PTS = 4 };
 
@@ -115,10 +115,14 @@ struct DevState {
     int *err_day_pre_e2;    /* first day with an SSA or E1 error */
     unsigned long long *fired;
 
-    /* heavy nodes of the next two days: list[(d & 1) * MAX_HEAVY + i] */
+    /* heavy nodes of the next two days:
+     * list[((d & 1) * HEAVY_CLASSES + class) * MAX_HEAVY + i] */
     int *heavy_list;
-    int *heavy_count;       /* [2] */
+    int *heavy_count;       /* [2][HEAVY_CLASSES] */
+    int *heavy_next;        /* [2]: queue position */
     int *heavy_mark;        /* per g: day + 1 when listed for that day */
+    double heavy_rate;      /* <= 0 disables the heavy path */
+    int heavy_blocks;
 };
 
 }  // namespace siminf
