@@ -182,11 +182,17 @@ int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args,
  * heavy_rate: a tuning knob, not a semantic option -- nodes whose rate sum
  * at the start of a day reaches it are simulated one per warp (results are
  * identical either way).
+ *
+ * gdata_per_replicate: args->gdata holds one gdata vector per replicate
+ * (Nrep rows of the model's gdata length); replicate r reads row r.  The
+ * reference shares one gdata among replicates; particle filters and ABC
+ * batches over parameter sets need one per replicate.
  */
 typedef struct siminf_gpu_options {
     int cap_transfers;
     int heavy_rate;     /* rate sum from which a node runs one per warp (0 = default) */
-    int reserved[6];
+    int gdata_per_replicate;
+    int reserved[5];
 } siminf_gpu_options;
 
 /* siminf_gpu_run_solver_mssm with options (NULL = all zero). */
@@ -207,6 +213,38 @@ int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args,
  */
 int siminf_gpu_schedule(const siminf_gpu_solver_args *args, int *days, int *waves,
                         long long *e1_events, long long *e2_events, int *wave);
+
+/*
+ * Bootstrap particle filter on the GPU: the loop of pfilter_internal
+ * (R/pfilter.R:315-499) with SimInf_systematic_resampling
+ * (src/misc/SimInf_particle_filter.c:33-67).  args describes one particle's
+ * model (Nrep is ignored; events are not supported yet); every interval
+ * (R/pfilter.R:177-193) runs all particles as replicates of one plan,
+ * resident on the device, then weights, resamples and copies the ancestors'
+ * states without leaving the GPU.  The observation process is
+ * Binomial(x, detect_p) of one compartment per node, log-density floored at
+ * -690 per node for impossible observations (the reference stops on
+ * non-finite weights, R/pfilter.R:438-442).  Interval i runs with seed
+ * seed + (i+1) * 0x9E3779B97F4A7C15 and resamples with draw 0 of stream
+ * 2^62 + i under seed.
+ */
+typedef struct siminf_gpu_pfilter_args {
+    int n_particles;
+    int gdata_per_particle;     /* args->gdata holds n_particles rows */
+    int n_obs;
+    const int *obs_time;        /* n_obs increasing times >= tspan[0] */
+    const int *obs;             /* n_obs x Nn observed counts, row-major */
+    int obs_compartment;        /* zero-based */
+    double detect_p;
+    unsigned long seed;
+    double *loglik;             /* out: log-likelihood */
+    double *ess;                /* out: n_obs effective sample sizes */
+    int *ancestors;             /* out (or NULL): n_obs x n_particles, one-based */
+    double ms_total;            /* out: wall time of the filter */
+} siminf_gpu_pfilter_args;
+
+int siminf_gpu_pfilter(const siminf_gpu_solver_args *args, const siminf_gpu_model *model,
+                       siminf_gpu_pfilter_args *pf);
 
 /* Diagnostics of the last failing call on the calling thread: the fields
  * SimInf_print_status (src/solvers/SimInf_solver.c:1191-1249) and

@@ -68,6 +68,13 @@ def lib():
                                                C.c_int, C.c_int, C.POINTER(C.c_int)]
         _lib.oracle_binomial.argtypes = [C.c_uint64, C.c_uint64, C.c_double, C.c_int, C.c_int,
                                          C.POINTER(C.c_int)]
+        _lib.oracle_pfilter.restype = C.c_int
+        _lib.oracle_pfilter.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int,
+                                        C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
+                                        C.c_double, C.c_uint64, C.c_int, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        _lib.oracle_set_node_counters.argtypes = [C.c_void_p]
+        _lib.oracle_set_day_max.argtypes = [C.c_void_p]
         assert _lib.oracle_result_size() == C.sizeof(OracleResult)
     return _lib
 
@@ -124,3 +131,31 @@ def binomial(seed, sid, p, n, count):
     out = np.zeros(count, dtype=np.int32)
     lib().oracle_binomial(seed, sid, p, n, count, out.ctypes.data_as(C.POINTER(C.c_int)))
     return out
+
+
+def pfilter(model, n_particles, obs_time, obs, obs_compartment, detect_p, seed=42,
+            gdata=None, threads=1):
+    """The particle filter restated on the CPU (same interface as
+    siminf_gb300.run.pfilter); returns (code, loglik, ess, ancestors)."""
+    from siminf_gb300 import abi
+    m = model
+    if gdata is not None:
+        m = type(model).__new__(type(model))
+        m.__dict__.update(model.__dict__)
+        m.gdata = np.ascontiguousarray(gdata, dtype=np.float64).reshape(-1)
+    h = abi.build_args(m, seed)
+    obs = np.ascontiguousarray(obs, dtype=np.int32)
+    obs_time = np.ascontiguousarray(obs_time, dtype=np.int32)
+    n_obs = len(obs_time)
+    ll = np.zeros(1)
+    ess = np.zeros(n_obs)
+    anc = np.zeros((n_obs, n_particles), dtype=np.int32)
+    stride = 0 if gdata is None else int(np.asarray(gdata).shape[1])
+    code = lib().oracle_pfilter(C.cast(h.ref(), C.c_void_p), m.name.encode(), n_particles,
+                                stride, n_obs, obs_time.ctypes.data_as(C.POINTER(C.c_int)),
+                                obs.ctypes.data_as(C.POINTER(C.c_int)), obs_compartment,
+                                detect_p, seed, threads,
+                                ll.ctypes.data_as(C.POINTER(C.c_double)),
+                                ess.ctypes.data_as(C.POINTER(C.c_double)),
+                                anc.ctypes.data_as(C.POINTER(C.c_int)))
+    return code, float(ll[0]), ess, anc

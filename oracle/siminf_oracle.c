@@ -68,7 +68,13 @@ typedef struct ctx {
     ev *events;
     int Nn, Nc, Nt, Nd, Nld;
     uint64_t seed;
+    int gdata_stride;           /* 0: one gdata; else replicate r uses gdata + r * stride */
 } ctx;
+
+static const double *gdata_of(const ctx *c, int r)
+{
+    return c->a->gdata + (size_t) r * c->gdata_stride;
+}
 
 typedef struct rep {
     int *u;
@@ -173,7 +179,7 @@ static uint64_t ssa_node(const ctx *c, rep *s, int r, int node, double next)
         for (int j = a->jcG[tr]; j < a->jcG[tr + 1]; j++) {
             const int k = a->irG[j];
             const double old = t_rate[k];
-            const double rate = c->m->tr[k](u, v, ld, a->gdata, s->t_time[node]);
+            const double rate = c->m->tr[k](u, v, ld, gdata_of(c, r), s->t_time[node]);
             t_rate[k] = rate;
             delta += rate - old;
             if (!isfinite(rate) || rate < 0.0) {
@@ -528,13 +534,14 @@ done:
 
 /* Rate refresh of one node after the post-time-step function
  * (src/solvers/SimInf_solver_ssm.c:262-301).  Returns the pts rc. */
-static int pts_node(const ctx *c, rep *s, int node, double tt)
+static int pts_node(const ctx *c, rep *s, int r, int node, double tt)
 {
     const int Nc = c->Nc, Nt = c->Nt, Nd = c->Nd, Nld = c->Nld;
     const siminf_gpu_solver_args *a = c->a;
+    const double *gd = gdata_of(c, r);
     const int rc = c->m->pts(&s->v_new[(size_t) node * Nd], &s->u[(size_t) node * Nc],
                              &s->v[(size_t) node * Nd], &a->ldata[(size_t) node * Nld],
-                             a->gdata, node, tt);
+                             gd, node, tt);
     if (rc < 0) {
         s->node_err[node] = rc;
         s->node_err_time[node] = tt;
@@ -550,7 +557,7 @@ static int pts_node(const ctx *c, rep *s, int node, double tt)
             const double rate = c->m->tr[j](&s->u[(size_t) node * Nc],
                                             &s->v_new[(size_t) node * Nd],
                                             &a->ldata[(size_t) node * Nld],
-                                            a->gdata, tt);
+                                            gd, tt);
             t_rate[j] = rate;
             delta += rate - old;
             if (!isfinite(rate) || rate < 0.0) {
@@ -650,7 +657,7 @@ static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
         s->sum_t_rate[node] = 0.0;
         for (int j = 0; j < Nt; j++) {
             const double rate = c->m->tr[j](&s->u[(size_t) node * Nc], &s->v[(size_t) node * Nd],
-                                            &a->ldata[(size_t) node * Nld], a->gdata, tt);
+                                            &a->ldata[(size_t) node * Nld], gdata_of(c, r), tt);
             s->t_rate[(size_t) node * Nt + j] = rate;
             s->sum_t_rate[node] += rate;
             if (!isfinite(rate) || rate < 0.0) {
@@ -697,7 +704,7 @@ static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
         any_err = 0;
 #pragma omp parallel for schedule(static) if (parallel_nodes) reduction(|:any_err)
         for (int node = 0; node < Nn; node++) {
-            pts_node(c, s, node, tt);
+            pts_node(c, s, r, node, tt);
             any_err |= (s->node_err[node] != 0);
         }
         if (any_err)
@@ -755,13 +762,15 @@ static void rep_free(rep *s)
  * uses the OpenMP default; cap_transfers mirrors siminf_gpu_options.  Returns 0 or the first failing replicate's
  * error code; res receives counters and the failure's diagnostics.
  */
-int oracle_run_ex(const siminf_gpu_solver_args *args, const char *model_name,
-                  int nthreads, int cap_transfers, oracle_result *res)
+static int oracle_run_impl(const siminf_gpu_solver_args *args, const char *model_name,
+                           int nthreads, int cap_transfers, int gdata_stride,
+                           oracle_result *res)
 {
     ctx c;
     int err = 0;
 
     g_cap_transfers = cap_transfers;
+    c.gdata_stride = gdata_stride;
 
     memset(res, 0, sizeof(*res));
     c.m = oracle_model_lookup(model_name);
@@ -852,10 +861,177 @@ int oracle_run_ex(const siminf_gpu_solver_args *args, const char *model_name,
     return err;
 }
 
+int oracle_run_ex(const siminf_gpu_solver_args *args, const char *model_name,
+                  int nthreads, int cap_transfers, oracle_result *res)
+{
+    return oracle_run_impl(args, model_name, nthreads, cap_transfers, 0, res);
+}
+
 int oracle_run(const siminf_gpu_solver_args *args, const char *model_name,
                int nthreads, oracle_result *res)
 {
     return oracle_run_ex(args, model_name, nthreads, 0, res);
+}
+
+/* ------------------------------------------------------------------ */
+/* Bootstrap particle filter (R/pfilter.R:315-499) over one model whose   */
+/* replicates are the particles, with a Binomial(count, p) observation of */
+/* one compartment per node.                                            */
+/* ------------------------------------------------------------------ */
+
+/* ln Binomial(k; n, p) from a log-factorial table, with a floor for
+ * impossible observations (the reference rejects non-finite weights,
+ * R/pfilter.R:438-442).  The same expression runs on the GPU. */
+#define PF_LOG_FLOOR (-690.0)
+static double pf_logdens(const double *lfact, int tablen, int k, int n, double logp, double logq)
+{
+    if (k < 0 || n < 0 || k > n || n >= tablen)
+        return PF_LOG_FLOOR;
+    return (((lfact[n] - lfact[k]) - lfact[n - k]) + (double) k * logp) +
+           (double) (n - k) * logq;
+}
+
+/* Systematic resampling, src/misc/SimInf_particle_filter.c:33-67, with the
+ * uniform from the stream (seed, sid); idx receives zero-based ancestors. */
+static int pf_resample(const double *w, int n, double unif, int *idx)
+{
+    double cumsum_w = 0;
+    for (int i = 0; i < n; i++) {
+        if (!isfinite(w[i]) || w[i] < 0.0)
+            return -1;
+        cumsum_w += w[i];
+    }
+    if (cumsum_w <= 0.0)
+        return -1;
+    const double du = cumsum_w / (double) n;
+    double u = du * unif;
+    cumsum_w = w[0];
+    for (int i = 0, j = 0; i < n; i++) {
+        while (u > cumsum_w && j < n - 1)
+            cumsum_w += w[++j];
+        idx[i] = j;
+        u += du;
+    }
+    return 0;
+}
+
+/* Seeds of interval i and of its resampling draw. */
+#define PF_SEED(seed, i) ((uint64_t) (seed) + ((uint64_t) (i) + 1) * 0x9E3779B97F4A7C15ULL)
+#define PF_RESAMPLE_SID (((uint64_t) 1) << 62)
+
+int oracle_pfilter(const siminf_gpu_solver_args *a1, const char *model_name, int Np,
+                   int gdata_stride, int n_obs, const int *obs_time, const int *obs,
+                   int obs_c, double p_detect, uint64_t seed, int nthreads,
+                   double *loglik_out, double *ess, int *ancestors)
+{
+    const int Nn = a1->Nn, Nc = a1->Nc, Nd = a1->Nd;
+    const size_t nu = (size_t) Nn * Nc, nv = (size_t) Nn * Nd;
+    int err = 0, tablen = 1;
+    for (int node = 0; node < Nn; node++) {
+        int tot = 0;
+        for (int c = 0; c < Nc; c++)
+            tot += a1->u0[(size_t) node * Nc + c];
+        if (tot + 1 > tablen)
+            tablen = tot + 1;
+    }
+    double *lfact = malloc((size_t) tablen * sizeof(double));
+    int *u0 = malloc((size_t) Np * nu * sizeof(int) + 4);
+    double *v0 = malloc((size_t) Np * nv * sizeof(double) + 8);
+    int *U = malloc((size_t) Np * 2 * nu * sizeof(int) + 4);
+    double *V = malloc((size_t) Np * 2 * nv * sizeof(double) + 8);
+    int *ulast = malloc((size_t) Np * nu * sizeof(int) + 4);
+    double *vlast = malloc((size_t) Np * nv * sizeof(double) + 8);
+    double *w = malloc((size_t) Np * sizeof(double));
+    int *anc = malloc((size_t) Np * sizeof(int));
+    si_lfact_fill(lfact, tablen);
+    for (int p = 0; p < Np; p++) {
+        memcpy(&u0[p * nu], a1->u0, nu * sizeof(int));
+        if (nv)
+            memcpy(&v0[p * nv], a1->v0, nv * sizeof(double));
+        anc[p] = p;
+    }
+    const double logp = si_log(p_detect), logq = si_log(1.0 - p_detect);
+    const double log_np = si_log((double) Np);
+    double loglik = 0.0;
+    for (int i = 0; i < n_obs && !err; i++) {
+        /* interval tspan, R/pfilter.R:177-193 */
+        double tsp[2];
+        int tlen;
+        const double prev = (i == 0) ? a1->tspan[0] : (double) obs_time[i - 1];
+        if ((i == 0 && prev < obs_time[0]) || (i > 0 && obs_time[i] - obs_time[i - 1] > 1)) {
+            tsp[0] = prev;
+            tsp[1] = obs_time[i];
+            tlen = 2;
+        } else {
+            tsp[0] = obs_time[i];
+            tlen = 1;
+        }
+        /* ancestors' states: u0[p] = last[anc[p]] (R/pfilter.R:384-398) */
+        if (i > 0) {
+            for (int p = 0; p < Np; p++) {
+                memcpy(&u0[p * nu], &ulast[(size_t) anc[p] * nu], nu * sizeof(int));
+                if (nv)
+                    memcpy(&v0[p * nv], &vlast[(size_t) anc[p] * nv], nv * sizeof(double));
+            }
+        }
+        siminf_gpu_solver_args a = *a1;
+        a.u0 = u0;
+        a.v0 = v0;
+        a.tspan = tsp;
+        a.tlen = tlen;
+        a.U = U;
+        a.V = V;
+        a.Nrep = Np;
+        a.len = 0;
+        a.seed = PF_SEED(seed, i);
+        oracle_result res;
+        err = oracle_run_impl(&a, model_name, nthreads, 0, gdata_stride, &res);
+        if (err)
+            break;
+        for (int p = 0; p < Np; p++) {
+            memcpy(&ulast[p * nu], &U[((size_t) p * tlen + tlen - 1) * nu], nu * sizeof(int));
+            if (nv)
+                memcpy(&vlast[p * nv], &V[((size_t) p * tlen + tlen - 1) * nv], nv * sizeof(double));
+        }
+        /* log-weights: sum over nodes in order */
+        for (int p = 0; p < Np; p++) {
+            double acc = 0.0;
+            for (int node = 0; node < Nn; node++)
+                acc = acc + pf_logdens(lfact, tablen, obs[(size_t) i * Nn + node],
+                                       ulast[(size_t) p * nu + (size_t) node * Nc + obs_c], logp, logq);
+            w[p] = acc;
+        }
+        /* R/pfilter.R:444-452 */
+        double max_w = w[0];
+        for (int p = 1; p < Np; p++)
+            if (w[p] > max_w)
+                max_w = w[p];
+        double sum_w = 0.0;
+        for (int p = 0; p < Np; p++) {
+            w[p] = si_exp(w[p] - max_w);
+            sum_w = sum_w + w[p];
+        }
+        loglik = ((loglik + max_w) + si_log(sum_w)) - log_np;
+        double sq = 0.0;
+        for (int p = 0; p < Np; p++) {
+            w[p] = w[p] / sum_w;
+            sq = sq + w[p] * w[p];
+        }
+        ess[i] = 1.0 / sq;
+        si_rng rr;
+        si_rng_init(&rr, seed, PF_RESAMPLE_SID + (uint64_t) i, 0);
+        if (pf_resample(w, Np, si_uniform_pos(&rr), anc)) {
+            err = SIMINF_GPU_ERR_INVALID_MODEL;
+            break;
+        }
+        if (ancestors)
+            for (int p = 0; p < Np; p++)
+                ancestors[(size_t) i * Np + p] = anc[p] + 1;
+    }
+    *loglik_out = loglik;
+    free(lfact); free(u0); free(v0); free(U); free(V); free(ulast); free(vlast);
+    free(w); free(anc);
+    return err;
 }
 
 /* Set (or clear with NULL) a caller-owned array of Nrep * Nn counters that

@@ -6,9 +6,14 @@ from .model import SEIR, SIR, SIS, SISe, SISe3, SIR_mparse, SISe_pf, SimInfModel
 from .abi import SimInfError
 
 __all__ = ["abi", "model", "SimInfModel", "SIR", "SEIR", "SIS", "SISe", "SIR_mparse",
-           "SISe_pf", "make_events", "SimInfError", "run"]
+           "SISe_pf", "make_events", "SimInfError", "run", "pfilter"]
 
 
 def run(*args, **kwargs):
     from .run import run as _run
     return _run(*args, **kwargs)
+
+
+def pfilter(*args, **kwargs):
+    from .run import pfilter as _pf
+    return _pf(*args, **kwargs)

@@ -113,7 +113,25 @@ class Status(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("cap_transfers", C.c_int), ("heavy_rate", C.c_int), ("reserved", C.c_int * 6)]
+    _fields_ = [("cap_transfers", C.c_int), ("heavy_rate", C.c_int),
+                ("gdata_per_replicate", C.c_int), ("reserved", C.c_int * 5)]
+
+
+class PfilterArgs(C.Structure):
+    _fields_ = [
+        ("n_particles", C.c_int),
+        ("gdata_per_particle", C.c_int),
+        ("n_obs", C.c_int),
+        ("obs_time", C.POINTER(C.c_int)),
+        ("obs", C.POINTER(C.c_int)),
+        ("obs_compartment", C.c_int),
+        ("detect_p", C.c_double),
+        ("seed", C.c_ulong),
+        ("loglik", C.POINTER(C.c_double)),
+        ("ess", C.POINTER(C.c_double)),
+        ("ancestors", C.POINTER(C.c_int)),
+        ("ms_total", C.c_double),
+    ]
 
 
 class Stats(C.Structure):

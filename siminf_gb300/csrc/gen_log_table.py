@@ -1,5 +1,5 @@
-"""Generate the constant tables of the integer fixed-point logarithm in
-siminf_stream.h (``si_log``).
+"""Generate the constants of the logarithm (``si_log``) and exponential
+(``si_exp``) in siminf_stream.h.
 
 The logarithm is evaluated as ln(x) = K*ln(2) + L_j + ln(1 + z), where
 x = 2^e * f, f in [1, 2), j = the top 7 fraction bits of f, and
@@ -36,6 +36,20 @@ def main():
         L.append(q(lj, 64))
     ln2 = q(mp.log(2), 128)
     coef = [q(mp.mpf((-1) ** i) / (i + 1), 62) for i in range(9)]
+    # si_exp: ln 2 split into a 32-significant-bit head (k * head is exact for
+    # |k| < 2^21) and the double nearest to the rest; 1/ln 2; 1/n! for the
+    # Taylor series of exp on |r| <= ln(2)/2.
+    ln2f = mp.log(2)
+    e = mp.floor(mp.log(ln2f, 2))
+    head = mp.floor(ln2f / mp.mpf(2) ** (e - 31)) * mp.mpf(2) ** (e - 31)
+    tail = ln2f - head
+    import struct
+
+    def dbits(x):
+        return struct.unpack("<Q", struct.pack("<d", float(x)))[0]
+    exp_consts = {"SI_EXP_LN2_HI": dbits(head), "SI_EXP_LN2_LO": dbits(tail),
+                  "SI_EXP_INV_LN2": dbits(1 / ln2f)}
+    inv_fact = [dbits(1 / mp.factorial(n)) for n in range(14)]
     out = []
     out.append("/* Generated by gen_log_table.py: constants of si_log (do not edit). */")
     out.append("#ifndef SIMINF_LOG_TABLE_H")
@@ -58,6 +72,13 @@ def main():
             out.append("#define SI_LOG_C%d (-(int64_t)0x%016xLL)" % (i, -c))
         else:
             out.append("#define SI_LOG_C%d ((int64_t)0x%016xLL)" % (i, c))
+    for k, v in exp_consts.items():
+        out.append("#define %s 0x%016xULL" % (k, v))
+    out.append("/* 1/n!, n = 0..13, as IEEE double bits. */")
+    out.append("#define SI_EXP_INV_FACT_INIT { \\")
+    for i in range(0, 14, 4):
+        out.append("    " + ", ".join("0x%016xULL" % inv_fact[k] for k in range(i, min(i + 4, 14))) + ", \\")
+    out.append("}")
     out.append("#endif")
     print("\n".join(out))
 

@@ -40,6 +40,7 @@
 #include "../../include/siminf_gb300.h"
 #include "siminf_launch.h"
 #include "siminf_plan.h"
+#include "siminf_stream.h"
 
 using namespace siminf;
 
@@ -135,12 +136,13 @@ struct siminf_gpu_plan {
 
     /* host-side copies needed to write results back */
     size_t U_len = 0, V_len = 0, prU_len = 0, prV_len = 0;
-    const int *u0_host = nullptr;
-    const double *v0_host = nullptr;
+    int *d_u0 = nullptr;            /* device copy of the initial state */
+    double *d_v0 = nullptr;
     double tt0 = 0;
 
     siminf_gpu_stats stats{};
     bool ran = false;
+    int days_cap = 0;
 };
 
 static int validate(const siminf_gpu_solver_args *a, const Launchers *L)
@@ -570,7 +572,10 @@ int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_
     rc = upload(&dS, Sd.data(), Sd.size(), own, st);
     if (!rc) rc = upload(&dG, Gm.data(), Gm.size(), own, st);
     if (!rc) rc = upload(&dld, a->ldata, a->ldata ? nld : 0, own, st);
-    if (!rc) rc = upload(&dgd, a->gdata, a->gdata ? (size_t) L->Ngd : 0, own, st);
+    const int per_rep = opt && opt->gdata_per_replicate;
+    s.gdata_stride = per_rep ? L->Ngd : 0;
+    if (!rc) rc = upload(&dgd, a->gdata, a->gdata ? (size_t) L->Ngd * (per_rep ? Nrep : 1) : 0,
+                         own, st);
     s.S = dS;
     s.Gmask = dG;
     s.ldata = dld;
@@ -681,18 +686,11 @@ int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_
             s.irV = dir;
         }
     }
-    p->u0_host = a->u0;
-    p->v0_host = a->v0;
     if (!rc) {
         /* initial state stays on the device so plan_run can restart */
-        int *du0;
-        rc = upload(&du0, a->u0, (size_t) Ntot * Nc, own, st);
-        if (!rc && Nd > 0) {
-            double *dv0;
-            rc = upload(&dv0, a->v0, (size_t) Ntot * Nd, own, st);
-            p->v0_host = dv0;
-        }
-        p->u0_host = du0;
+        rc = upload(&p->d_u0, a->u0, (size_t) Ntot * Nc, own, st);
+        if (!rc && Nd > 0)
+            rc = upload(&p->d_v0, a->v0, (size_t) Ntot * Nd, own, st);
     }
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(st);
@@ -871,13 +869,13 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s.heavy_mark, 0, (size_t) s.Ntot * sizeof(int), st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(s.u, p->u0_host, (size_t) s.Ntot * s.Nc * sizeof(int),
+        e = cudaMemcpyAsync(s.u, p->d_u0, (size_t) s.Ntot * s.Nc * sizeof(int),
                             cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess && s.Nd > 0) {
-        e = cudaMemcpyAsync(s.vA, p->v0_host, (size_t) s.Ntot * s.Nd * sizeof(double),
+        e = cudaMemcpyAsync(s.vA, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
                             cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(s.vB, p->v0_host, (size_t) s.Ntot * s.Nd * sizeof(double),
+            e = cudaMemcpyAsync(s.vB, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
                                 cudaMemcpyDeviceToDevice, st);
     }
     if (e != cudaSuccess)
@@ -1004,6 +1002,156 @@ int siminf_gpu_schedule(const siminf_gpu_solver_args *a, int *days, int *waves,
                     wave[e2[k].index] = w - p.day_wave[d];
     }
     return 0;
+}
+
+/* Re-point a plan without events at another tspan (at most 2 points here):
+ * new day schedule, uploaded; U/V columns per replicate = tlen. */
+static int plan_set_tspan(siminf_gpu_plan *p, const double *tspan, int tlen)
+{
+    siminf_gpu_solver_args a{};
+    a.tspan = tspan;
+    a.tlen = tlen;
+    int rc = make_days(p, &a);
+    if (rc)
+        return rc;
+    p->s.tlen = tlen;
+    if (p->days_cap < p->ndays) {
+        DayInfo *d = nullptr;
+        if ((rc = dalloc(&d, (size_t) p->ndays, p->owned)))
+            return rc;
+        p->d_days = d;
+        p->days_cap = p->ndays;
+    }
+    cudaError_t e = cudaMemcpy(p->d_days, p->days.data(), p->days.size() * sizeof(DayInfo),
+                               cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "days upload");
+}
+
+int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model *model,
+                       siminf_gpu_pfilter_args *pf)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    memset(&g_status, 0, sizeof(g_status));
+    if (!a1 || !model || !pf || pf->n_particles < 1 || pf->n_obs < 1 || !pf->obs ||
+        !pf->obs_time || !pf->loglik || !pf->ess || a1->len > 0 ||
+        pf->obs_compartment < 0 || pf->obs_compartment >= a1->Nc ||
+        !(pf->detect_p > 0.0 && pf->detect_p < 1.0)) {
+        set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
+                   "invalid particle filter arguments (events are not supported)");
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    }
+    for (int i = 0; i < pf->n_obs; i++) {
+        if ((i == 0 && pf->obs_time[0] < a1->tspan[0]) ||
+            (i > 0 && pf->obs_time[i] <= pf->obs_time[i - 1])) {
+            set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
+                       "observation times must increase from tspan[0]");
+            return SIMINF_GPU_ERR_INVALID_MODEL;
+        }
+    }
+    const int Np = pf->n_particles, Nn = a1->Nn, Nc = a1->Nc, Nd = a1->Nd;
+    const size_t nu = (size_t) Nn * Nc, nv = (size_t) Nn * Nd;
+    /* particles = replicates of one plan */
+    std::vector<int> u0((size_t) Np * nu);
+    std::vector<double> v0((size_t) Np * nv + 1);
+    for (int q = 0; q < Np; q++) {
+        memcpy(&u0[q * nu], a1->u0, nu * sizeof(int));
+        if (nv)
+            memcpy(&v0[q * nv], a1->v0, nv * sizeof(double));
+    }
+    int tablen = 1;
+    for (int node = 0; node < Nn; node++) {
+        long long tot = 0;
+        for (int c = 0; c < Nc; c++)
+            tot += a1->u0[(size_t) node * Nc + c];
+        tablen = (int) std::max<long long>(tablen, tot + 1);
+    }
+    std::vector<double> lfact(tablen);
+    si_lfact_fill(lfact.data(), tablen);
+    double tsp0[2] = {a1->tspan[0], a1->tspan[0] + 1.0};
+    int dummyU = 0;
+    double dummyV = 0;
+    siminf_gpu_solver_args a = *a1;
+    a.u0 = u0.data();
+    a.v0 = v0.data();
+    a.Nrep = Np;
+    a.tspan = tsp0;
+    a.tlen = 2;
+    a.U = &dummyU;
+    a.V = Nd > 0 ? &dummyV : nullptr;
+    a.len = 0;
+    siminf_gpu_options opt{};
+    opt.gdata_per_replicate = pf->gdata_per_particle;
+    siminf_gpu_plan *p = nullptr;
+    int rc = siminf_gpu_plan_create_ex(&a, model, &opt, &p);
+    if (rc)
+        return rc;
+    p->days_cap = p->ndays;
+    double *d_lfact = nullptr, *d_w = nullptr, *d_loglik = nullptr, *d_ess = nullptr;
+    int *d_anc = nullptr, *d_anc_out = nullptr, *d_obs = nullptr;
+    rc = upload(&d_lfact, lfact.data(), lfact.size(), p->owned, nullptr);
+    if (!rc) rc = dalloc(&d_w, (size_t) Np, p->owned);
+    if (!rc) rc = dalloc(&d_anc, (size_t) Np, p->owned);
+    if (!rc && pf->ancestors) rc = dalloc(&d_anc_out, (size_t) Np * pf->n_obs, p->owned);
+    if (!rc) rc = upload(&d_obs, pf->obs, (size_t) pf->n_obs * Nn, p->owned, nullptr);
+    if (!rc) rc = dalloc(&d_loglik, 1, p->owned);
+    if (!rc) rc = dalloc(&d_ess, (size_t) pf->n_obs, p->owned);
+    if (!rc && cudaMemset(d_loglik, 0, sizeof(double)) != cudaSuccess)
+        rc = cuda_fail(cudaGetLastError(), "memset");
+    const double logp = si_log(pf->detect_p), logq = si_log(1.0 - pf->detect_p);
+    const double log_np = si_log((double) Np);
+    int prev_tlen = 2;
+    for (int i = 0; i < pf->n_obs && !rc; i++) {
+        double tsp[2];
+        int tlen;
+        const double prev = (i == 0) ? a1->tspan[0] : (double) pf->obs_time[i - 1];
+        if ((i == 0 && prev < pf->obs_time[0]) ||
+            (i > 0 && pf->obs_time[i] - pf->obs_time[i - 1] > 1)) {
+            tsp[0] = prev;
+            tsp[1] = pf->obs_time[i];
+            tlen = 2;
+        } else {
+            tsp[0] = pf->obs_time[i];
+            tlen = 1;
+        }
+        if (i > 0) {
+            cudaError_t e = pf_gather(p->s.U, p->s.V, prev_tlen, (long long) nu, (long long) nv,
+                                      d_anc, Np, p->d_u0, p->d_v0, nullptr);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "pf_gather");
+                break;
+            }
+        }
+        if ((rc = plan_set_tspan(p, tsp, tlen)))
+            break;
+        p->s.seed = (uint64_t) pf->seed + ((uint64_t) i + 1) * 0x9E3779B97F4A7C15ULL;
+        if ((rc = plan_run_impl(p, nullptr, nullptr)))
+            break;
+        cudaError_t e = pf_weights(p->s.U, tlen, Nn, Nc, Np, d_obs + (size_t) i * Nn,
+                                   pf->obs_compartment, d_lfact, tablen, logp, logq, d_w, nullptr);
+        if (e == cudaSuccess)
+            e = pf_finalize(d_w, Np, log_np, d_loglik, d_ess, i, (uint64_t) pf->seed,
+                            (((uint64_t) 1) << 62) + (uint64_t) i, d_anc,
+                            d_anc_out ? d_anc_out + (size_t) i * Np : nullptr, nullptr);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "pf kernels");
+            break;
+        }
+        prev_tlen = tlen;
+    }
+    if (!rc) {
+        cudaError_t e = cudaMemcpy(pf->loglik, d_loglik, sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(pf->ess, d_ess, (size_t) pf->n_obs * sizeof(double),
+                           cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && pf->ancestors)
+            e = cudaMemcpy(pf->ancestors, d_anc_out, (size_t) pf->n_obs * Np * sizeof(int),
+                           cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "pf results");
+    }
+    pf->ms_total = ms_since(t0);
+    siminf_gpu_plan_free(p);
+    return rc;
 }
 
 static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *model,

@@ -70,6 +70,11 @@ __device__ __forceinline__ void record_error(const DevState &s, int code, int ph
     }
 }
 
+__device__ __forceinline__ const double *gdata_of(const DevState &s, long long g)
+{
+    return s.gdata + (size_t) (g / s.Nn) * s.gdata_stride;
+}
+
 __device__ __forceinline__ int load_flag(const int *p)
 {
     return *(volatile const int *) p;
@@ -753,7 +758,7 @@ __global__ void k_init(DevState s, double tt0)
     double sum = 0.0;
 #pragma unroll
     for (int j = 0; j < NT; j++) {
-        const double rate = M::rate(j, u, v, ld, s.gdata, tt0);
+        const double rate = M::rate(j, u, v, ld, gdata_of(s, g), tt0);
         s.t_rate[(size_t) j * s.Ntot + g] = rate;
         sum += rate;
         if (!isfinite(rate) || rate < 0.0)
@@ -792,12 +797,12 @@ __device__ __forceinline__ void node_day(const DevState &s, long long g, int day
     si_rng r;
     if (warp_mode) {
         uint64_t ctr = s.ctr[g];
-        fired += ssa_day_warp<M>(u, rate, sum, t, v, ld, s.gdata, s.seed, (uint64_t) g, ctr, next,
-                                 sS, sG, err, err_tr, err_t, err_rate);
+        fired += ssa_day_warp<M>(u, rate, sum, t, v, ld, gdata_of(s, g), s.seed, (uint64_t) g, ctr,
+                                 next, sS, sG, err, err_tr, err_t, err_rate);
         si_rng_init(&r, s.seed, (uint64_t) g, ctr);
     } else {
         si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
-        fired += ssa_day<M>(u, rate, sum, t, v, ld, s.gdata, r, next, sS, sG, err, err_tr,
+        fired += ssa_day<M>(u, rate, sum, t, v, ld, gdata_of(s, g), r, next, sS, sG, err, err_tr,
                             err_t, err_rate);
     }
     const bool writer = !warp_mode || (threadIdx.x & 31) == 0;
@@ -951,7 +956,8 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
     const double *vi = v_in + g * ND;
     double *vo = v_out + g * ND;
     const double *ld = s.ldata + (size_t) node * s.Nld;
-    const int rc = M::pts(vo, u, vi, ld, s.gdata, node, tt);
+    const double *gd = gdata_of(s, g);
+    const int rc = M::pts(vo, u, vi, ld, gd, node, tt);
     if (rc < 0) {
         record_error(s, rc, PHASE_PTS, day, g, -1, -1, tt, 0);
     } else if (rc > 0 || s.update[g]) {
@@ -959,7 +965,7 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
 #pragma unroll
         for (int k = 0; k < NT; k++) {
             const double old = s.t_rate[(size_t) k * s.Ntot + g];
-            const double nr = M::rate(k, u, vo, ld, s.gdata, tt);
+            const double nr = M::rate(k, u, vo, ld, gd, tt);
             s.t_rate[(size_t) k * s.Ntot + g] = nr;
             delta += nr - old;
             if (si_bad_rate(nr))
@@ -999,13 +1005,14 @@ __global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days
         si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
         double *v = s.vA + g * ND, *vn = s.vB + g * ND;
         const double *ld = s.ldata + (size_t) node * s.Nld;
+        const double *gd = gdata_of(s, g);
         for (int d = 0; d < ndays; d++) {
             if (load_flag(s.err_day) < d)
                 break;
             const DayInfo di = days[d];
             int err = 0, err_tr = -1;
             double err_t = 0, err_rate = 0;
-            fired += ssa_day<M>(u, rate, sum, t, v, ld, s.gdata, r, di.next, sS, sG, err,
+            fired += ssa_day<M>(u, rate, sum, t, v, ld, gd, r, di.next, sS, sG, err,
                                 err_tr, err_t, err_rate);
             if (err) {
                 record_error(s, err, PHASE_SSA, d, g, err_tr, -1, err_t, err_rate);
@@ -1017,7 +1024,7 @@ __global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days
                 record_error(s, e_code, PHASE_E1, d, g, -1, e_idx, di.tt, 0);
                 break;
             }
-            const int rc = M::pts(vn, u, v, ld, s.gdata, node, di.tt);
+            const int rc = M::pts(vn, u, v, ld, gd, node, di.tt);
             if (rc < 0) {
                 record_error(s, rc, PHASE_PTS, d, g, -1, -1, di.tt, 0);
                 break;
@@ -1028,7 +1035,7 @@ __global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
                     const double old = rate[k];
-                    const double nr = M::rate(k, u, vn, ld, s.gdata, di.tt);
+                    const double nr = M::rate(k, u, vn, ld, gd, di.tt);
                     rate[k] = nr;
                     delta += nr - old;
                     if (!isfinite(nr) || nr < 0.0) {
@@ -1056,6 +1063,135 @@ __global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days
         s.ctr[g] = r.ctr;
     }
     add_fired(s, fired);
+}
+
+/* ------------------------------------------------------------------ */
+/* Particle filter (R/pfilter.R:417-452, src/misc/SimInf_particle_filter.c: */
+/* 33-67): log-weights, normalisation, ESS, systematic resampling and   */
+/* the ancestors' state copy.  Sums run in particle or node order on one */
+/* thread so that every bit matches the CPU restatement.                */
+/* ------------------------------------------------------------------ */
+#define PF_LOG_FLOOR (-690.0)
+
+__device__ __forceinline__ double pf_logdens(const double *lfact, int tablen, int k, int n,
+                                             double logp, double logq)
+{
+    if (k < 0 || n < 0 || k > n || n >= tablen)
+        return PF_LOG_FLOOR;
+    return (((lfact[n] - lfact[k]) - lfact[n - k]) + (double) k * logp) +
+           (double) (n - k) * logq;
+}
+
+__global__ void k_pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, const int *obs_row,
+                             int obs_c, const double *lfact, int tablen, double logp, double logq,
+                             double *w)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= Np)
+        return;
+    const int *last = U + ((size_t) p * tlen + tlen - 1) * (size_t) Nn * Nc;
+    double acc = 0.0;
+    for (int node = 0; node < Nn; node++)
+        acc = acc + pf_logdens(lfact, tablen, obs_row[node], last[(size_t) node * Nc + obs_c],
+                               logp, logq);
+    w[p] = acc;
+}
+
+/* One block: max (exact in any order), exp in parallel, then the serial
+ * sums, log-likelihood, ESS and resampling on thread 0. */
+__global__ void k_pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess,
+                              int i, uint64_t seed, uint64_t sid, int *anc, int *anc_out)
+{
+    __shared__ double red[1024];
+    __shared__ double s_sum;
+    double m = -INFINITY;
+    for (int p = threadIdx.x; p < Np; p += blockDim.x)
+        m = fmax(m, w[p]);
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    const double max_w = red[0];
+    for (int p = threadIdx.x; p < Np; p += blockDim.x)
+        w[p] = si_exp(w[p] - max_w);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int p = 0; p < Np; p++)
+            sum = sum + w[p];
+        *loglik = ((*loglik + max_w) + si_log(sum)) - log_np;
+        s_sum = sum;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < Np; p += blockDim.x)
+        w[p] = w[p] / s_sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sq = 0.0;
+        for (int p = 0; p < Np; p++)
+            sq = sq + w[p] * w[p];
+        ess[i] = 1.0 / sq;
+        /* systematic resampling */
+        double cumsum_w = 0;
+        for (int p = 0; p < Np; p++)
+            cumsum_w += w[p];
+        si_rng r;
+        si_rng_init(&r, seed, sid, 0);
+        const double du = cumsum_w / (double) Np;
+        double u = du * si_uniform_pos(&r);
+        cumsum_w = w[0];
+        for (int p = 0, j = 0; p < Np; p++) {
+            while (u > cumsum_w && j < Np - 1)
+                cumsum_w += w[++j];
+            anc[p] = j;
+            if (anc_out)
+                anc_out[p] = j + 1;
+            u += du;
+        }
+    }
+}
+
+__global__ void k_pf_gather(const int *U, const double *V, int tlen, long long nu, long long nv,
+                            const int *anc, int Np, int *u0, double *v0)
+{
+    const long long idx = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (idx < (long long) Np * nu) {
+        const int p = (int) (idx / nu);
+        const long long r = idx - (long long) p * nu;
+        u0[idx] = U[((size_t) anc[p] * tlen + tlen - 1) * nu + r];
+    }
+    if (V && idx < (long long) Np * nv) {
+        const int p = (int) (idx / nv);
+        const long long r = idx - (long long) p * nv;
+        v0[idx] = V[((size_t) anc[p] * tlen + tlen - 1) * nv + r];
+    }
+}
+
+cudaError_t pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, const int *obs_row,
+                       int obs_c, const double *lfact, int tablen, double logp, double logq,
+                       double *w, cudaStream_t st)
+{
+    k_pf_weights<<<(Np + 127) / 128, 128, 0, st>>>(U, tlen, Nn, Nc, Np, obs_row, obs_c, lfact,
+                                                   tablen, logp, logq, w);
+    return cudaGetLastError();
+}
+
+cudaError_t pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess, int i,
+                        uint64_t seed, uint64_t sid, int *anc, int *anc_out, cudaStream_t st)
+{
+    k_pf_finalize<<<1, 1024, 0, st>>>(w, Np, log_np, loglik, ess, i, seed, sid, anc, anc_out);
+    return cudaGetLastError();
+}
+
+cudaError_t pf_gather(const int *U, const double *V, int tlen, long long nu, long long nv,
+                      const int *anc, int Np, int *u0, double *v0, cudaStream_t st)
+{
+    const long long n = (long long) Np * (nu > nv ? nu : nv);
+    k_pf_gather<<<(unsigned) ((n + 255) / 256), 256, 0, st>>>(U, V, tlen, nu, nv, anc, Np, u0, v0);
+    return cudaGetLastError();
 }
 
 /* ------------------------------------------------------------------ */

@@ -23,6 +23,15 @@ struct Launchers {
                              const double *v_in, double *v_out, cudaStream_t st);
 };
 
+/* Particle-filter kernels (model independent). */
+cudaError_t pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, const int *obs_row,
+                       int obs_c, const double *lfact, int tablen, double logp, double logq,
+                       double *w, cudaStream_t st);
+cudaError_t pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess, int i,
+                        uint64_t seed, uint64_t sid, int *anc, int *anc_out, cudaStream_t st);
+cudaError_t pf_gather(const int *U, const double *V, int tlen, long long nu, long long nv,
+                      const int *anc, int Np, int *u0, double *v0, cudaStream_t st);
+
 /* The launcher table of a built-in device model, or nullptr. */
 const Launchers *launchers_for(const char *name);
 

@@ -88,6 +88,7 @@ struct DevState {
     const int *Nshift;      /* Nc x Nshift */
     int hasN;               /* the caller passed N */
     const double *ldata, *gdata;
+    int gdata_stride;       /* 0: one gdata; else replicate r reads gdata + r * stride */
 
     /* state */
     int *u;

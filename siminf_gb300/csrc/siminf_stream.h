@@ -551,6 +551,61 @@ SI_HD double si_div(double a, double b)
 }
 
 /* ---------------------------------------------------------------- */
+/* Exponential and log-factorials for the particle filter's weights. */
+/* ---------------------------------------------------------------- */
+
+#ifdef __CUDACC__
+static __device__ const uint64_t si_exp_inv_fact_dev[14] = SI_EXP_INV_FACT_INIT;
+#endif
+static const uint64_t si_exp_inv_fact_host[14] = SI_EXP_INV_FACT_INIT;
+#ifdef __CUDA_ARCH__
+#  define SI_EXP_INV_FACT(j) si_exp_inv_fact_dev[j]
+#else
+#  define SI_EXP_INV_FACT(j) si_exp_inv_fact_host[j]
+#endif
+
+/* exp(x) by Cody-Waite reduction x = k ln2 + r, |r| <= ln(2)/2, with ln 2
+ * split into a 32-bit head (k * head exact) and a tail, the Taylor series of
+ * exp(r) to degree 13 in Horner form (separate multiply and add), and an
+ * exact scaling by 2^k.  Only IEEE add/multiply, so host and device agree
+ * bit for bit; about one ulp from the true value. */
+SI_HD double si_exp(double x)
+{
+    const uint64_t xb = si_double_bits(x);
+    if (si_isnan_bits(xb))
+        return x + x;
+    if (x > 709.782712893384)
+        return si_bits_double(0x7FF0000000000000ULL);
+    if (x < -745.1332191019412)
+        return 0.0;
+    const double magic = 6755399441055744.0;            /* 2^52 + 2^51 */
+    const double kf = (x * si_bits_double(SI_EXP_INV_LN2) + magic) - magic;
+    const int k = (int) kf;
+    const double r = (x - kf * si_bits_double(SI_EXP_LN2_HI)) - kf * si_bits_double(SI_EXP_LN2_LO);
+    double p = si_bits_double(SI_EXP_INV_FACT(13));
+    for (int n = 12; n >= 0; n--)
+        p = p * r + si_bits_double(SI_EXP_INV_FACT(n));
+    /* p * 2^k, in two exact steps when 2^k alone is not a normal double */
+    if (k >= -1021 && k <= 1023)
+        return p * si_bits_double((uint64_t) (k + 1023) << 52);
+    const int k1 = k < 0 ? -1000 : 1000;
+    return (p * si_bits_double((uint64_t) (k1 + 1023) << 52)) *
+           si_bits_double((uint64_t) (k - k1 + 1023) << 52);
+}
+
+/* tab[i] = ln(i!) for i < n, accumulated in order with si_log, the same
+ * bits wherever it is computed. */
+SI_HD void si_lfact_fill(double *tab, int n)
+{
+    double acc = 0.0;
+    for (int i = 0; i < n; i++) {
+        if (i >= 2)
+            acc = acc + si_log((double) i);
+        tab[i] = acc;
+    }
+}
+
+/* ---------------------------------------------------------------- */
 /* Samplers.                                                         */
 /* ---------------------------------------------------------------- */
 

@@ -41,6 +41,8 @@ def lib():
                                       C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                       C.POINTER(C.c_int)]
     L.siminf_gpu_schedule.restype = C.c_int
+    L.siminf_gpu_pfilter.argtypes = [vp, vp, C.POINTER(abi.PfilterArgs)]
+    L.siminf_gpu_pfilter.restype = C.c_int
     L.siminf_gpu_last_status.argtypes = [C.POINTER(abi.Status)]
     L.siminf_gpu_last_stats.argtypes = [C.POINTER(abi.Stats)]
     L.siminf_gpu_plan_create.argtypes = [vp, vp, C.POINTER(vp)]
@@ -62,7 +64,7 @@ EXPORTS = (
     "siminf_gpu_plan_create_ex", "siminf_gpu_last_status",
     "siminf_gpu_last_stats", "siminf_gpu_plan_create", "siminf_gpu_plan_run",
     "siminf_gpu_plan_download", "siminf_gpu_plan_stats", "siminf_gpu_plan_free",
-    "siminf_gpu_plan_profile", "siminf_gpu_schedule",
+    "siminf_gpu_plan_profile", "siminf_gpu_schedule", "siminf_gpu_pfilter",
 )
 
 

@@ -54,3 +54,46 @@ def run(model, seed=42, U_sparse=None, V_sparse=None, cap_transfers=False):
     code = fn(C.cast(holder.ref(), C.c_void_p), dm.handle)
     native.check(code)
     return Result(model, holder, native.last_stats())
+
+
+class PfilterResult:
+    def __init__(self, loglik, ess, ancestors, ms):
+        self.loglik = loglik
+        self.ess = ess
+        self.ancestors = ancestors
+        self.ms = ms
+
+
+def pfilter(model, n_particles, obs_time, obs, obs_compartment, detect_p, seed=42,
+            gdata=None):
+    """Bootstrap particle filter on the GPU (pfilter_internal, R/pfilter.R:
+    315-499) with a Binomial(x, detect_p) observation of one compartment in
+    every node.  ``model`` is one particle's model (no events); ``gdata``, if
+    given, is an (n_particles, ngdata) array with one parameter row per
+    particle.  Returns log-likelihood, ESS per observation and one-based
+    ancestors (n_obs, n_particles)."""
+    m = model
+    obs = np.ascontiguousarray(obs, dtype=np.int32)
+    obs_time = np.ascontiguousarray(obs_time, dtype=np.int32)
+    n_obs = len(obs_time)
+    if gdata is not None:
+        g = np.ascontiguousarray(gdata, dtype=np.float64)
+        m = type(m).__new__(type(m))
+        m.__dict__.update(model.__dict__)
+        m.gdata = g.reshape(-1)
+    holder = abi.build_args(m, seed)
+    ll = np.zeros(1)
+    ess = np.zeros(n_obs)
+    anc = np.zeros((n_obs, n_particles), dtype=np.int32)
+    pa = abi.PfilterArgs(
+        n_particles=n_particles, gdata_per_particle=int(gdata is not None), n_obs=n_obs,
+        obs_time=obs_time.ctypes.data_as(C.POINTER(C.c_int)),
+        obs=obs.ctypes.data_as(C.POINTER(C.c_int)), obs_compartment=obs_compartment,
+        detect_p=detect_p, seed=seed,
+        loglik=ll.ctypes.data_as(C.POINTER(C.c_double)),
+        ess=ess.ctypes.data_as(C.POINTER(C.c_double)),
+        ancestors=anc.ctypes.data_as(C.POINTER(C.c_int)))
+    native.check(native.lib().siminf_gpu_pfilter(C.cast(holder.ref(), C.c_void_p),
+                                                 native.device_model(m.name).handle,
+                                                 C.byref(pa)))
+    return PfilterResult(float(ll[0]), ess, anc, pa.ms_total)

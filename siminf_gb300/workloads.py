@@ -25,6 +25,13 @@ examples that need R), so every workload is generated here from fixed seeds.
   reference would instead stop with "Unable to sample individuals for
   event."
   Seeds: 1 graph, 2 u0, 3 events.
+- ``sise_pfilter`` -- the particle-filter workload: mparse SISe
+  ("S -> upsilon*phi*S -> I", "I -> gamma*I -> S", phi <- phi*(1-0.03) +
+  0.05*I/(S+I)), `nodes` nodes with S ~ Poisson(100), I ~ Bernoulli(0.05) *
+  Poisson(2), phi0 = 0.  Observations: Binomial(I, 0.8) per node every 7
+  days over 52 weeks from one ground-truth run (upsilon = 0.012, gamma =
+  0.1, seed 7).  Particles carry their own upsilon ~ U(0.005, 0.03) and
+  gamma ~ U(0.05, 0.2).
 """
 import numpy as np
 
@@ -89,3 +96,24 @@ def seir_events(nodes=1_000_000, days=365, transfers=500_000, p_enter=0.002, p_e
     ev["shift"] = np.zeros(total, np.int32)
     return M.SEIR(u0, np.arange(1, days + 1, dtype=float), beta=0.16, epsilon=0.25,
                   gamma=0.077, events=ev)
+
+
+def sise_pfilter(nodes=500, particles=4096, weeks=52, seed=7):
+    """The particle-filter workload (see module docstring).  Returns the
+    model, per-particle gdata (particles x 2), observation times and the
+    (weeks x nodes) observations."""
+    from .run import run
+    rng = np.random.default_rng(seed)
+    S = rng.poisson(100, nodes)
+    I = rng.poisson(2, nodes) * (rng.random(nodes) < 0.05)
+    u0 = np.vstack([S, I]).astype(np.int32)
+    days = 7 * weeks
+    truth = M.SISe_pf(u0, np.arange(0, days + 1, dtype=float), upsilon=0.012, gamma=0.1)
+    res = run(truth, seed=seed)
+    obs_time = np.arange(7, days + 1, 7, dtype=np.int32)
+    I_true = res.U[1::2, :][:, obs_time]
+    obs = rng.binomial(I_true.T, 0.8).astype(np.int32)
+    model = M.SISe_pf(u0, np.array([0.0]), upsilon=0.012, gamma=0.1)
+    gdata = np.column_stack([rng.uniform(0.005, 0.03, particles),
+                             rng.uniform(0.05, 0.2, particles)])
+    return model, gdata, obs_time, obs
