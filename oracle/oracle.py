@@ -61,6 +61,8 @@ def lib():
                                        C.POINTER(OracleResult)]
         _lib.oracle_si_log.restype = C.c_double
         _lib.oracle_si_log.argtypes = [C.c_double]
+        _lib.oracle_neglog_u32.restype = None
+        _lib.oracle_neglog_u32.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         _lib.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32]
         _lib.oracle_uniform_pos.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_int,
                                             C.POINTER(C.c_double)]
@@ -107,6 +109,14 @@ def run_ref(holder, model_name, threads=1):
 
 def si_log(x):
     return lib().oracle_si_log(float(x))
+
+
+def neglog_u32(words):
+    """si_neglog_u32 over an array of 32-bit words."""
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    out = np.empty(len(w))
+    lib().oracle_neglog_u32(w.ctypes.data, out.ctypes.data, len(w))
+    return out
 
 
 def philox(ctr, key):

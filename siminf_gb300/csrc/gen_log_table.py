@@ -50,6 +50,25 @@ def main():
     exp_consts = {"SI_EXP_LN2_HI": dbits(head), "SI_EXP_LN2_LO": dbits(tail),
                   "SI_EXP_INV_LN2": dbits(1 / ln2f)}
     inv_fact = [dbits(1 / mp.factorial(n)) for n in range(14)]
+    # si_neglog_u32: two-level reduction tables for x = 2w+1 < 2^33.
+    # Level 1: m in [1, 2) (Q32, M in [2^32, 2^33)), j1 = top 7 fraction bits,
+    # R1 = round(2^10 / c1), c1 the bucket centre; L1 = ln(2^10 / R1) in Q64.
+    # Level 2: z1 = M*R1/2^42 - 1 in [-2^-7, 2^-7), j2 = bucket of width
+    # 2^-14, R2 = round(2^16 / (1 + centre)); L2 = ln(2^16 / R2) in Q64 (signed).
+    R1, L1 = [], []
+    for j in range(128):
+        c = 1 + (mp.mpf(j) + mp.mpf("0.5")) / 128
+        r = int(mp.nint(1024 / c))
+        R1.append(r)
+        L1.append(q(mp.log(mp.mpf(1024) / r), 64))
+    R2, L2 = [], []
+    for j in range(256):
+        lo = -mp.mpf(2) ** -7 + mp.mpf(j) * mp.mpf(2) ** -14
+        c = 1 + lo + mp.mpf(2) ** -15
+        r = int(mp.nint(mp.mpf(2) ** 16 / c))
+        R2.append(r)
+        L2.append(q(mp.log(mp.mpf(2) ** 16 / r), 64))
+    KLN2 = [q(k * mp.log(2), 64) for k in range(34)]
     out = []
     out.append("/* Generated by gen_log_table.py: constants of si_log (do not edit). */")
     out.append("#ifndef SIMINF_LOG_TABLE_H")
@@ -78,6 +97,29 @@ def main():
     out.append("#define SI_EXP_INV_FACT_INIT { \\")
     for i in range(0, 14, 4):
         out.append("    " + ", ".join("0x%016xULL" % inv_fact[k] for k in range(i, min(i + 4, 14))) + ", \\")
+    out.append("}")
+    out.append("/* si_neglog_u32 tables. */")
+    out.append("#define SI_NL_R1_INIT { \\")
+    for i in range(0, 128, 8):
+        out.append("    " + ", ".join("%du" % R1[k] for k in range(i, i + 8)) + ", \\")
+    out.append("}")
+    out.append("#define SI_NL_L1_INIT { \\")
+    for i in range(0, 128, 4):
+        out.append("    " + ", ".join("0x%016xULL" % L1[k] for k in range(i, i + 4)) + ", \\")
+    out.append("}")
+    out.append("#define SI_NL_R2_INIT { \\")
+    for i in range(0, 256, 8):
+        out.append("    " + ", ".join("%du" % R2[k] for k in range(i, i + 8)) + ", \\")
+    out.append("}")
+    out.append("#define SI_NL_L2_INIT { \\")
+    for i in range(0, 256, 4):
+        out.append("    " + ", ".join(("-(int64_t)0x%016xLL" % -L2[k]) if L2[k] < 0 else
+                                      ("(int64_t)0x%016xLL" % L2[k]) for k in range(i, i + 4)) + ", \\")
+    out.append("}")
+    out.append("/* k ln 2 in Q64.64, k = 0..33: {integer part, fraction}. */")
+    out.append("#define SI_NL_KLN2_INIT { \\")
+    for k in range(34):
+        out.append("    {0x%xULL, 0x%016xULL}, \\" % (KLN2[k] >> 64, KLN2[k] & (2 ** 64 - 1)))
     out.append("}")
     out.append("#endif")
     print("\n".join(out))

@@ -1015,6 +1015,7 @@ static int plan_set_tspan(siminf_gpu_plan *p, const double *tspan, int tlen)
     if (rc)
         return rc;
     p->s.tlen = tlen;
+    p->tt0 = tspan[0];
     if (p->days_cap < p->ndays) {
         DayInfo *d = nullptr;
         if ((rc = dalloc(&d, (size_t) p->ndays, p->owned)))

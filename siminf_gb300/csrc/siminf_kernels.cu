@@ -18,7 +18,8 @@
  * double[NT]); S and the G column masks sit in shared memory so the
  * transition index can stay dynamic without spilling the register arrays.
  * Random draws come from the node's Philox stream (siminf_stream.h), and
- * the logarithm is the integer fixed-point si_log: on GB300 the FP64 pipe
+ * the waiting-time logarithm is the integer fixed-point si_neglog_u32 (a
+ * 32-bit-input -log(u) with two table reductions): on GB300 the FP64 pipe
  * retires one warp instruction per 64 cycles per SM sub-partition, while the
  * integer pipes are ~40x faster, so the SSA chain keeps only the FP64
  * operations the reference's arithmetic requires.
@@ -123,7 +124,7 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
     unsigned fired = 0;
     double cum[NT];
     prefix_sums<M>(rate, cum);
-    double L = -si_log(si_u32_to_uniform_pos(si_peek_u32(&r)));
+    double L = si_neglog_u32(si_peek_u32(&r));
     for (;;) {
         if (sum <= 0.0) {
             t = next;
@@ -152,7 +153,7 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
 
         /* Inversion: the first k with !(rnd > cum[k]), else NT - 1. */
         const double rnd = si_uniform_pos(&r) * sum;
-        L = -si_log(si_u32_to_uniform_pos(si_peek_u32(&r)));
+        L = si_neglog_u32(si_peek_u32(&r));
         int tr = NT - 1;
 #pragma unroll
         for (int k = NT - 2; k >= 0; k--)
@@ -260,8 +261,9 @@ __device__ __forceinline__ unsigned ssa_day_warp(int (&u)[M::NC], double (&rate)
     {
         si_rng r;
         si_rng_init(&r, seed, sid, base + (uint64_t) lane);
-        Ub = si_u32_to_uniform_pos(si_peek_u32(&r));
-        Lb = -si_log(Ub);
+        const uint32_t wb = si_peek_u32(&r);
+        Ub = si_u32_to_uniform_pos(wb);
+        Lb = si_neglog_u32(wb);
     }
     double cum[NT];
     prefix_sums<M>(rate, cum);
@@ -321,8 +323,9 @@ __device__ __forceinline__ unsigned ssa_day_warp(int (&u)[M::NC], double (&rate)
             base = ctr;
             si_rng r;
             si_rng_init(&r, seed, sid, base + (uint64_t) lane);
-            Ub = si_u32_to_uniform_pos(si_peek_u32(&r));
-            Lb = -si_log(Ub);
+            const uint32_t wb = si_peek_u32(&r);
+            Ub = si_u32_to_uniform_pos(wb);
+            Lb = si_neglog_u32(wb);
         }
         const int i0 = (int) (ctr - base);
         const double L = __shfl_sync(FULL, Lb, i0);

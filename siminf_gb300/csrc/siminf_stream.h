@@ -239,6 +239,40 @@ SI_HD double si_uniform_pos(si_rng *r)
 /* Natural logarithm in integer fixed point.                         */
 /* ---------------------------------------------------------------- */
 
+/* M * 2^-scale for M = (hi, lo) > 0 whose top set bit is bit p, to the
+ * nearest double (ties to even); the result must be normal. */
+SI_HD double si_u128_to_double_at(uint64_t hi, uint64_t lo, int p, int scale)
+{
+    uint64_t m;
+    int e = p;
+    if (p <= 52) {
+        m = lo << (52 - p);
+    } else {
+        const int sh = p - 52;                 /* 1 .. 75 */
+        uint64_t rnd, sticky;
+        if (sh < 64) {
+            m = (lo >> sh) | (hi << (64 - sh));
+            rnd = (lo >> (sh - 1)) & 1;
+            sticky = (sh > 1) ? (lo & ((1ULL << (sh - 1)) - 1)) : 0;
+        } else if (sh == 64) {
+            m = hi;
+            rnd = lo >> 63;
+            sticky = lo & 0x7FFFFFFFFFFFFFFFULL;
+        } else {
+            m = hi >> (sh - 64);
+            rnd = (hi >> (sh - 65)) & 1;
+            sticky = (hi & ((1ULL << (sh - 65)) - 1)) | lo;
+        }
+        m += rnd & ((sticky != 0) | (m & 1));
+        if (m >> 53) {
+            m >>= 1;
+            e++;
+        }
+    }
+    const uint64_t expo = (uint64_t) (e - scale + 1023);
+    return si_bits_double((expo << 52) | (m & 0x000FFFFFFFFFFFFFULL));
+}
+
 /* |M| * 2^-scale, M = (hi, lo) unsigned 128-bit, to the nearest double
  * (ties to even).  The caller guarantees a result in the normal range. */
 SI_HD double si_u128_to_double(uint64_t hi, uint64_t lo, int scale, int negative)
@@ -382,6 +416,114 @@ SI_HD double si_log(double x)
         return si_u128_to_double(nhi, nlo, 64, 1);
     }
     return si_u128_to_double(Thi, Tlo, 64, 0);
+}
+
+/* ---------------------------------------------------------------- */
+/* -log of a 32-bit uniform, for the SSA's exponential waiting time.  */
+/* ---------------------------------------------------------------- */
+
+static const uint32_t si_nl_r1_host[128] = SI_NL_R1_INIT;
+static const uint64_t si_nl_l1_host[128] = SI_NL_L1_INIT;
+static const uint32_t si_nl_r2_host[256] = SI_NL_R2_INIT;
+static const int64_t si_nl_l2_host[256] = SI_NL_L2_INIT;
+static const uint64_t si_nl_kln2_host[34][2] = SI_NL_KLN2_INIT;
+#ifdef __CUDACC__
+static __device__ const uint32_t si_nl_r1_dev[128] = SI_NL_R1_INIT;
+static __device__ const uint64_t si_nl_l1_dev[128] = SI_NL_L1_INIT;
+static __device__ const uint32_t si_nl_r2_dev[256] = SI_NL_R2_INIT;
+static __device__ const int64_t si_nl_l2_dev[256] = SI_NL_L2_INIT;
+static __device__ const uint64_t si_nl_kln2_dev[34][2] = SI_NL_KLN2_INIT;
+#endif
+#ifdef __CUDA_ARCH__
+#  define SI_NL(tab) si_nl_##tab##_dev
+#else
+#  define SI_NL(tab) si_nl_##tab##_host
+#endif
+
+SI_HD int si_clz32(uint32_t x)
+{
+#ifdef __CUDA_ARCH__
+    return __clz((int) x);
+#else
+    return x ? __builtin_clz(x) : 32;
+#endif
+}
+
+/* 32x32 -> 64-bit product (one wide multiply-add on the GPU). */
+SI_HD uint64_t si_mulw(uint32_t a, uint32_t b)
+{
+    return (uint64_t) a * (uint64_t) b;
+}
+
+/* -ln(u) for u = (2w + 1) * 2^-33, the value si_u32_to_uniform_pos(w)
+ * gives.  The logarithm of x = 2w + 1 = 2^k m is reduced twice by tables
+ * (m r1 r2 = 1 + z, |z| < 2^-14.5, all products exact in 64-bit integers),
+ * ln(1 + z) takes four series terms from 32-bit multiplies, and the sum
+ * (33 - k) ln 2 - ln(m) is formed in Q64.64 with an absolute error below
+ * 2^-61.  That is within one ulp for u <= 1 - 2^-8 (0.97 ulp at worst over
+ * all 2^32 words); si_neglog_u32 sends larger u (probability 2^-8) to
+ * si_log.  Integer-only: the same bits on every host and device. */
+SI_HD double si_neglog_u32_tab(uint32_t w)
+{
+    const uint64_t x = 2 * (uint64_t) w + 1;
+    int k;
+    uint64_t M;                                  /* m * 2^32, in [2^32, 2^33) */
+    if (x >> 32) {
+        k = 32;
+        M = x;
+    } else {
+        const uint32_t xl = (uint32_t) x;
+        k = 31 - si_clz32(xl);
+        M = (uint64_t) xl << (32 - k);
+    }
+    const int j1 = (int) ((M >> 25) & 127);
+    const uint64_t M1 = M * (uint64_t) SI_NL(r1)[j1];          /* (m r1) * 2^42 */
+    const int64_t Z1 = (int64_t) M1 - ((int64_t) 1 << 42);    /* |Z1| < 2^35 */
+    const int j2 = (int) (((uint64_t) (Z1 + ((int64_t) 1 << 35)) >> 28) & 255);
+    const uint64_t M2 = M1 * (uint64_t) SI_NL(r2)[j2];         /* (m r1 r2) * 2^58 */
+    const int64_t Z2 = (int64_t) M2 - ((int64_t) 1 << 58);    /* z * 2^58, |.| < 2^43.5 */
+
+    /* ln(1 + z) * 2^64 = z - z^2/2 + z^3/3 - z^4/4 */
+    const uint64_t a = (uint64_t) (Z2 < 0 ? -Z2 : Z2);
+    const uint32_t ah = (uint32_t) (a >> 22), al = (uint32_t) (a & 0x3FFFFF);
+    /* z^2/2 * 2^64 = a^2 / 2^53, from a = ah 2^22 + al */
+    const uint64_t t2 = (si_mulw(ah, ah) >> 9) + (si_mulw(ah, al) >> 30) +
+                        (si_mulw(al, al) >> 53);
+    const uint32_t b = (uint32_t) (a >> 12);                  /* |z| * 2^46 */
+    const uint32_t c = (uint32_t) (si_mulw(b, b) >> 32);      /* z^2 * 2^60 */
+    const uint64_t z3 = si_mulw(c, b) >> 42;                  /* |z|^3 * 2^64 */
+    const uint64_t t3v = si_umulhi64(z3, 0x5555555555555556ULL);   /* z3 / 3 */
+    const uint64_t t4 = (si_mulw(c, c) >> 56) >> 2;           /* z^4 / 4 * 2^64 */
+    const int64_t z1t = Z2 * 64;                              /* z * 2^64 */
+    const int64_t s3 = Z2 < 0 ? -(int64_t) t3v : (int64_t) t3v;
+    const int64_t ln1p = z1t - (int64_t) t2 + s3 - (int64_t) t4;
+
+    /* (33 - k) ln 2 - L1 - L2 - ln(1+z) in Q64.64 */
+    uint64_t hi = SI_NL(kln2)[33 - k][0], lo = SI_NL(kln2)[33 - k][1];
+    const uint64_t l1 = SI_NL(l1)[j1];
+    hi -= (lo < l1);
+    lo -= l1;
+    const int64_t l2 = SI_NL(l2)[j2] + ln1p;                 /* |.| < 2^58 */
+    const uint64_t l2u = (uint64_t) l2;
+    const uint64_t l2h = (uint64_t) (l2 >> 63);              /* sign extension */
+    hi -= l2h + (lo < l2u);
+    lo -= l2u;
+    /* to double: the value is >= 1/16, so its top bit is at 64 + (0..4)
+     * or at 60..63 of lo */
+    int p;
+    if (hi)
+        p = 64 + 31 - si_clz32((uint32_t) hi);
+    else
+        p = 63 - si_clz32((uint32_t) (lo >> 32));
+    return si_u128_to_double_at(hi, lo, p, 64);
+}
+
+SI_HD double si_neglog_u32(uint32_t w)
+{
+    const uint64_t x = 2 * (uint64_t) w + 1;
+    if (x >= ((uint64_t) 1 << 33) - ((uint64_t) 1 << 25))
+        return -si_log(si_u32_to_uniform_pos(w));
+    return si_neglog_u32_tab(w);
 }
 
 /* ---------------------------------------------------------------- */

@@ -44,6 +44,32 @@ def test_log_accuracy(oracle_lib):
     assert oracle_lib.si_log(math.inf) == math.inf
 
 
+def test_neglog_u32_accuracy(oracle_lib):
+    """-log(u) of a 32-bit uniform u = (2w+1) 2^-33, against 60-digit
+    arithmetic: within one ulp on random words and on the edges of the
+    table reduction (the powers of two, the hand-over to si_log at
+    u = 1 - 2^-8, the extremes)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 60
+    rng = np.random.default_rng(11)
+    words = list(rng.integers(0, 2 ** 32, 20000, dtype=np.uint64))
+    words += list(rng.integers(2 ** 32 - 2 ** 24 - 4096, 2 ** 32 - 2 ** 24 + 4096, 2000, dtype=np.uint64))
+    edges = [0, 1, 2, 2 ** 32 - 1, 2 ** 32 - 2, 2 ** 32 - 2 ** 24 - 1, 2 ** 32 - 2 ** 24]
+    for b in range(1, 33):
+        edges += [2 ** (b - 1) - 1, 2 ** (b - 1), max(0, 2 ** (b - 1) - 2)]
+    words = np.array(words + [e for e in edges if e < 2 ** 32], dtype=np.uint32)
+    got = oracle_lib.neglog_u32(words)
+    worst = 0.0
+    for w, g in zip(words, got):
+        want = -mp.log(mp.mpf(2 * int(w) + 1) / mp.mpf(2) ** 33)
+        worst = max(worst, float(abs(mp.mpf(g) - want)) / math.ulp(g))
+    assert worst < 1.0
+    # the same value the general logarithm gives, almost always bit for bit
+    u = (2 * words.astype(np.float64) + 1) * 2.0 ** -33
+    general = np.array([-oracle_lib.si_log(x) for x in u[:5000]])
+    assert np.mean(general == got[:5000]) > 0.99
+
+
 def test_uniform_pos_open_interval_and_moments(oracle_lib):
     u = oracle_lib.uniform_pos(42, 3, 0, 200000)
     assert (u > 0).all() and (u < 1).all()
