@@ -64,7 +64,8 @@ enum {
     SIMINF_GPU_ERR_EVENTS_UNSORTED = -31,   /* events not sorted by time, E1 before E2 */
     SIMINF_GPU_ERR_UNKNOWN_MODEL = -32,     /* no device model of that name */
     SIMINF_GPU_ERR_TIMEOUT = -33,           /* a bounded device wait gave up */
-    SIMINF_GPU_ERR_NO_DEVICE = -34          /* no CUDA device is visible */
+    SIMINF_GPU_ERR_NO_DEVICE = -34,         /* no CUDA device is visible */
+    SIMINF_GPU_ERR_SCRATCH_LIMIT = -35      /* too large for siminf_gpu_run_solver_ssm_noalloc */
 };
 
 /*
@@ -199,6 +200,29 @@ typedef struct siminf_gpu_options {
 int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args,
                              const siminf_gpu_model *model,
                              const siminf_gpu_options *options);
+
+/*
+ * siminf_gpu_run_solver_ssm without allocating: no counterpart in the
+ * reference, which allocates its solver state on every run.  For callers
+ * that cannot allocate when they run a trajectory: a process whose device
+ * memory is held by another allocator (cudaMalloc would fail or fragment
+ * it), or a loop that runs trajectories between its own kernels on other
+ * streams and cannot afford cudaFree, which waits for the whole device.
+ * Same arguments and results as siminf_gpu_run_solver_ssm for one
+ * replicate without scheduled events (Nrep = 1, len = 0) and a dense U;
+ * every buffer of the run lives in one static device array of
+ * SIMINF_GPU_NOALLOC_SCRATCH_BYTES, and a run that does not fit returns
+ * SIMINF_GPU_ERR_SCRATCH_LIMIT.  The call calls no allocator, runs on
+ * cuda_stream (a cudaStream_t, or NULL) and returns when U and V are
+ * written.  The first call on a device looks up the array's address on
+ * that device (the current one): make it before any stream capture.  All
+ * calls on a device share the array and each clears what must start at
+ * zero; calls that overlap on the GPU race on it.
+ */
+#define SIMINF_GPU_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+int siminf_gpu_run_solver_ssm_noalloc(siminf_gpu_solver_args *args,
+                                      const siminf_gpu_model *model,
+                                      void *cuda_stream);
 
 /*
  * Plan an event schedule on the host only (no GPU is touched): checks the

@@ -38,6 +38,7 @@ ERRORS = {
     -32: "Unknown device model.",
     -33: "A bounded device wait timed out.",
     -34: "No CUDA device is available.",
+    -35: "The run does not fit the allocation-free solver's scratch.",
 }
 
 

@@ -1,8 +1,10 @@
 """Build libsiminf_gb300.so in-tree with nvcc for sm_103a.
 
 The library is the C ABI of include/siminf_gb300.h: siminf_kernels.cu (the
-kernels, one instantiation per shipped model) and siminf_capi.cpp (planning
-and the exported entry points), compiled in parallel and linked with nvcc.
+kernels, one instantiation per shipped model), siminf_capi.cpp (planning
+and the exported entry points) and siminf_noalloc.cu (the allocation-free
+solver entry point and its static scratch), compiled in parallel and linked
+with nvcc.
 
     python -m siminf_gb300.build
 """
@@ -21,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # reference's C (bit-identical trajectories).
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off"]
-SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp"]
+SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp", "siminf_noalloc.cu"]
 
 
 def nvcc():

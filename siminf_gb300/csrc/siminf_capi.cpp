@@ -38,16 +38,12 @@
 #include <cuda_runtime.h>
 
 #include "../../include/siminf_gb300.h"
+#include "siminf_capi_internal.h"
 #include "siminf_launch.h"
 #include "siminf_plan.h"
 #include "siminf_stream.h"
 
 using namespace siminf;
-
-struct siminf_gpu_model {
-    char name[64];
-    const Launchers *L;
-};
 
 namespace {
 
@@ -193,6 +189,31 @@ static int validate(const siminf_gpu_solver_args *a, const Launchers *L)
     }
     return 0;
 }
+
+namespace siminf {
+
+int capi_validate(const siminf_gpu_solver_args *a, const Launchers *L)
+{
+    return validate(a, L);
+}
+
+void capi_set_status(int code, int node, int tr, int evi, double time, double rate,
+                     const char *msg)
+{
+    set_status(code, node, tr, evi, time, rate, msg);
+}
+
+void capi_clear_status()
+{
+    memset(&g_status, 0, sizeof(g_status));
+}
+
+int capi_cuda_fail(cudaError_t e, const char *what)
+{
+    return cuda_fail(e, what);
+}
+
+}  // namespace siminf
 
 /* Day index whose event pass applies an event at `time`. */
 static inline long long event_day(int time, double tt0)
