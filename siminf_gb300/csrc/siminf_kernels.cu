@@ -93,16 +93,24 @@ __device__ __forceinline__ void add_fired(const DevState &s, unsigned long long 
 /* ------------------------------------------------------------------ */
 /* Direct-method SSA of one node up to `next`                           */
 /* (src/solvers/SimInf_solver_ssm.c:144-235), arranged for latency: the */
-/* heaviest node of a day sets the day's critical path, one dependent   */
-/* FP64 operation costs 64 cycles on GB300, so everything that does not */
-/* depend on the running sum is computed beside the chain:              */
-/*  - -log(u) of the next draw is computed right after the current      */
-/*    transition is chosen (integer pipes, overlaps the rate updates);  */
+/* heaviest node of a day sets the day's critical path, and one node's  */
+/* transitions form a chain of dependent operations, so everything that */
+/* does not depend on the running sum leaves the chain:                 */
+/*  - the two draws of the next transition (Philox block, -log(u) by    */
+/*    si_neglog_u32, the selection uniform) are computed while the      */
+/*    current transition updates the state, from the draw index alone;  */
 /*  - the prefix sums of the rates, used by the inversion, are formed   */
 /*    once per rate update, so choosing the transition is NT-1          */
 /*    independent comparisons instead of a dependent add/compare chain; */
 /*  - divisions, comparisons and int->double conversions run on the     */
-/*    integer pipes (si_div, si_dge/si_dgt, si_i2d): same bits.         */
+/*    integer pipes (si_div, si_dge/si_dgt, si_i2d): same bits, and a   */
+/*    rate's division by a population count reuses its prepared         */
+/*    reciprocal (si_div_cached).                                       */
+/* Draw i of the node's stream is word i & 3 of Philox block i >> 2; a  */
+/* transition uses draws c (waiting time) and c + 1 (selection), so the */
+/* next transition's pair lies in block (c + 3) >> 2, except the first  */
+/* draw when (c + 2) & 3 == 3, which lies in the block this transition  */
+/* fetched.                                                             */
 /* ------------------------------------------------------------------ */
 template <class M>
 __device__ __forceinline__ void prefix_sums(const double (&rate)[M::NT], double (&cum)[M::NT])
@@ -113,47 +121,95 @@ __device__ __forceinline__ void prefix_sums(const double (&rate)[M::NT], double 
         cum[k] = cum[k - 1] + rate[k];
 }
 
+__device__ __forceinline__ uint32_t word_of(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3,
+                                            uint32_t i)
+{
+    const uint32_t lo = (i & 1) ? b1 : b0, hi = (i & 1) ? b3 : b2;
+    return (i & 2) ? hi : lo;
+}
+
+/* x <= 0.0 for the double with bits b (false for NaN), on the integer pipes. */
+__device__ __forceinline__ bool le_zero(uint64_t b)
+{
+    return (int64_t) b <= 0 && !si_isnan_bits(b);
+}
+
+/* Philox block `blk` of the stream held in r (key and stream id only). */
+__device__ __forceinline__ void philox_block(const si_rng &r, uint64_t blk, uint32_t &b0,
+                                             uint32_t &b1, uint32_t &b2, uint32_t &b3)
+{
+    b0 = (uint32_t) blk;
+    b1 = (uint32_t) (blk >> 32);
+    b2 = r.s0;
+    b3 = r.s1;
+    si_philox4x32_10(&b0, &b1, &b2, &b3, r.k0, r.k1);
+}
+
 template <class M>
 __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::NT], double &sum,
                                             double &t, const double *v, const double *ld,
                                             const double *gd, si_rng &r, double next,
-                                            const int *sS, const uint32_t *sG, int &err,
-                                            int &err_tr, double &err_t, double &err_rate)
+                                            const int *sS, const uint32_t *sG, si_recip &dc,
+                                            int &err, int &err_tr, double &err_t,
+                                            double &err_rate)
 {
     constexpr int NC = M::NC, NT = M::NT;
     unsigned fired = 0;
+    uint64_t c = r.ctr;                       /* draw index of the next waiting time */
+    const uint64_t sbits = si_double_bits(sum);
+    if (!si_finite_pos(sum)) {
+        /* sum <= 0: nothing fires (ssm.c:148-151); a non-finite sum after an
+         * invalid rate, which is recorded, would never reach `next`. */
+        if (!le_zero(sbits) && !err) {
+            err = ERR_INVALID_RATE;
+            err_tr = -1;
+            err_t = t;
+            err_rate = sum;
+        }
+        t = next;
+        return 0;
+    }
     double cum[NT];
     prefix_sums<M>(rate, cum);
-    double L = si_neglog_u32(si_peek_u32(&r));
+
+    /* the pair of the first transition */
+    uint32_t p0, p1, p2, p3, q0, q1, q2, q3;
+    philox_block(r, c >> 2, p0, p1, p2, p3);
+    philox_block(r, (c + 1) >> 2, q0, q1, q2, q3);
+    const uint32_t wl0 = word_of(p0, p1, p2, p3, (uint32_t) c & 3u);
+    const uint32_t wu0 = word_of(q0, q1, q2, q3, (uint32_t) (c + 1) & 3u);
+    double L = si_neglog_u32(wl0);
+    double U = si_u32_to_uniform_pos(wu0);
+    /* q holds block (c + 1) >> 2, the one the next pair may start in */
+    double tau = si_div(L, sum);
+
     for (;;) {
-        if (sum <= 0.0) {
-            t = next;
-            break;
-        }
-        if (!si_finite_pos(sum)) {
-            /* A non-finite rate sum (after an invalid rate, which is
-             * recorded) would never reach the next day: stop the node. */
-            if (!err) {
-                err = ERR_INVALID_RATE;
-                err_tr = -1;
-                err_t = t;
-                err_rate = sum;
-            }
-            t = next;
-            break;
-        }
-        si_skip(&r);
-        const double tau = si_div(L, sum);
         const double tn = tau + t;
         if (si_dge(tn, next)) {
             t = next;
+            c += 1;                           /* the waiting time's draw was used */
             break;
         }
         t = tn;
+        const double rnd = U * sum;
+        c += 2;
+
+        /* Draws of the next transition, off the chain. */
+        {
+            uint32_t n0, n1, n2, n3;
+            philox_block(r, (c + 1) >> 2, n0, n1, n2, n3);
+            const uint32_t ci = (uint32_t) c & 3u;
+            const uint32_t wl = (ci == 3u) ? word_of(q0, q1, q2, q3, 3u) : word_of(n0, n1, n2, n3, ci);
+            const uint32_t wu = word_of(n0, n1, n2, n3, (ci + 1u) & 3u);
+            q0 = n0;
+            q1 = n1;
+            q2 = n2;
+            q3 = n3;
+            L = si_neglog_u32(wl);
+            U = si_u32_to_uniform_pos(wu);
+        }
 
         /* Inversion: the first k with !(rnd > cum[k]), else NT - 1. */
-        const double rnd = si_uniform_pos(&r) * sum;
-        L = si_neglog_u32(si_peek_u32(&r));
         int tr = NT - 1;
 #pragma unroll
         for (int k = NT - 2; k >= 0; k--)
@@ -191,41 +247,61 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
             t = next;
             break;
         }
+        int neg = 0;
 #pragma unroll
-        for (int c = 0; c < NC; c++) {
-            const int d = sS[tr * NC + c];
-            if (d != 0) {
-                u[c] += d;
-                if (u[c] < 0) {
-                    err = ERR_NEGATIVE_STATE;
-                    err_tr = tr;
-                    err_t = t;
-                    err_rate = 0.0;
-                }
-            }
+        for (int cc = 0; cc < NC; cc++) {
+            const int d = sS[tr * NC + cc];
+            u[cc] += d;
+            neg |= (d != 0) & (u[cc] < 0);
+        }
+        if (neg) {
+            err = ERR_NEGATIVE_STATE;
+            err_tr = tr;
+            err_t = t;
+            err_rate = 0.0;
         }
 
         /* Refresh the rates flagged in column tr of G, in row order. */
         double delta = 0.0;
         const uint32_t gm = sG[tr];
+        int bad = -1;
+        double bad_rate = 0.0;
 #pragma unroll
         for (int k = 0; k < NT; k++) {
             if (gm & (1u << k)) {
                 const double old = rate[k];
-                const double nr = M::rate(k, u, v, ld, gd, t);
+                const double nr = M::rate(k, u, v, ld, gd, t, dc);
                 rate[k] = nr;
                 delta += nr - old;
                 if (si_bad_rate(nr)) {
-                    err = ERR_INVALID_RATE;
-                    err_tr = k;
-                    err_t = t;
-                    err_rate = nr;
+                    bad = k;
+                    bad_rate = nr;
                 }
             }
         }
+        if (bad >= 0) {
+            err = ERR_INVALID_RATE;
+            err_tr = bad;
+            err_t = t;
+            err_rate = bad_rate;
+        }
         sum += delta;
         prefix_sums<M>(rate, cum);
+
+        if (!si_finite_pos(sum)) {
+            if (!le_zero(si_double_bits(sum)) && !err) {
+                err = ERR_INVALID_RATE;
+                err_tr = -1;
+                err_t = t;
+                err_rate = sum;
+            }
+            t = next;
+            break;
+        }
+        tau = si_div(L, sum);
     }
+    r.ctr = c;
+    r.have = 0;
     return fired;
 }
 
@@ -254,6 +330,7 @@ __device__ __forceinline__ unsigned ssa_day_warp(int (&u)[M::NC], double (&rate)
     const unsigned FULL = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const int k = lane < NT ? lane : NT - 1;
+    si_recip dc = si_recip_none();
     unsigned fired = 0;
 
     uint64_t base = ctr;
@@ -287,7 +364,7 @@ __device__ __forceinline__ unsigned ssa_day_warp(int (&u)[M::NC], double (&rate)
 #pragma unroll
         for (int j = 0; j < NT; j++) {
             if (gm & (1u << j)) {
-                const double nr = M::rate(j, uk, v, ld, gd, 0.0);
+                const double nr = M::rate(j, uk, v, ld, gd, 0.0, dc);
                 crate[j] = nr;
                 delta += nr - rate[j];
                 if (si_bad_rate(nr)) {
@@ -758,10 +835,11 @@ __global__ void k_init(DevState s, double tt0)
         u[c] = s.u[g * NC + c];
     const double *v = s.vA + g * ND;
     const double *ld = s.ldata + (size_t) node * s.Nld;
+    si_recip dc = si_recip_none();
     double sum = 0.0;
 #pragma unroll
     for (int j = 0; j < NT; j++) {
-        const double rate = M::rate(j, u, v, ld, gdata_of(s, g), tt0);
+        const double rate = M::rate(j, u, v, ld, gdata_of(s, g), tt0, dc);
         s.t_rate[(size_t) j * s.Ntot + g] = rate;
         sum += rate;
         if (!isfinite(rate) || rate < 0.0)
@@ -805,8 +883,9 @@ __device__ __forceinline__ void node_day(const DevState &s, long long g, int day
         si_rng_init(&r, s.seed, (uint64_t) g, ctr);
     } else {
         si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
-        fired += ssa_day<M>(u, rate, sum, t, v, ld, gdata_of(s, g), r, next, sS, sG, err, err_tr,
-                            err_t, err_rate);
+        si_recip dc = si_recip_none();
+        fired += ssa_day<M>(u, rate, sum, t, v, ld, gdata_of(s, g), r, next, sS, sG, dc, err,
+                            err_tr, err_t, err_rate);
     }
     const bool writer = !warp_mode || (threadIdx.x & 31) == 0;
     if (err) {
@@ -964,11 +1043,12 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
     if (rc < 0) {
         record_error(s, rc, PHASE_PTS, day, g, -1, -1, tt, 0);
     } else if (rc > 0 || s.update[g]) {
+        si_recip dc = si_recip_none();
         double delta = 0.0;
 #pragma unroll
         for (int k = 0; k < NT; k++) {
             const double old = s.t_rate[(size_t) k * s.Ntot + g];
-            const double nr = M::rate(k, u, vo, ld, gd, tt);
+            const double nr = M::rate(k, u, vo, ld, gd, tt, dc);
             s.t_rate[(size_t) k * s.Ntot + g] = nr;
             delta += nr - old;
             if (si_bad_rate(nr))
@@ -1009,13 +1089,14 @@ __global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days
         double *v = s.vA + g * ND, *vn = s.vB + g * ND;
         const double *ld = s.ldata + (size_t) node * s.Nld;
         const double *gd = gdata_of(s, g);
+        si_recip dc = si_recip_none();
         for (int d = 0; d < ndays; d++) {
             if (load_flag(s.err_day) < d)
                 break;
             const DayInfo di = days[d];
             int err = 0, err_tr = -1;
             double err_t = 0, err_rate = 0;
-            fired += ssa_day<M>(u, rate, sum, t, v, ld, gd, r, di.next, sS, sG, err,
+            fired += ssa_day<M>(u, rate, sum, t, v, ld, gd, r, di.next, sS, sG, dc, err,
                                 err_tr, err_t, err_rate);
             if (err) {
                 record_error(s, err, PHASE_SSA, d, g, err_tr, -1, err_t, err_rate);
@@ -1038,7 +1119,7 @@ __global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
                     const double old = rate[k];
-                    const double nr = M::rate(k, u, vn, ld, gd, di.tt);
+                    const double nr = M::rate(k, u, vn, ld, gd, di.tt, dc);
                     rate[k] = nr;
                     delta += nr - old;
                     if (!isfinite(nr) || nr < 0.0) {

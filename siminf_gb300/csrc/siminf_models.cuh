@@ -17,7 +17,9 @@
  * conversions are built from integer bits (si_i2d), a double sum of integer
  * counts that stays below 2^53 is formed as an integer sum and converted once
  * (every partial sum is exact either way), and divisions use si_div, an
- * IEEE round-to-nearest division on the integer pipes.
+ * IEEE round-to-nearest division on the integer pipes.  rate() takes a
+ * one-entry cache of the prepared divisor (si_div_cached): a population
+ * count, which the transitions keep constant, is prepared once per change.
  */
 #ifndef SIMINF_MODELS_CUH
 #define SIMINF_MODELS_CUH
@@ -32,15 +34,15 @@ struct ModelSIR {
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t)
+                                                  double t, si_recip &dc)
     {
         if (k == 0) {
             const double S_n = si_i2d(u[0]);
             const double I_n = si_i2d(u[1]);
             const long long n = (long long) u[0] + u[1] + u[2];     /* S_n + I_n + u[R] */
-            if (n > 0)
-                return si_div(ldata[0] * S_n * I_n, si_l2d(n));
-            return 0.0;
+            /* the population divides every call: its reciprocal is cached */
+            const double q = si_div_cached(ldata[0] * S_n * I_n, si_l2d(n > 0 ? n : 1), &dc);
+            return n > 0 ? q : 0.0;
         }
         return ldata[1] * si_i2d(u[1]);
     }
@@ -59,15 +61,15 @@ struct ModelSEIR {
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t)
+                                                  double t, si_recip &dc)
     {
         if (k == 0) {
             const double S_n = si_i2d(u[0]);
             const double I_n = si_i2d(u[2]);
             const long long n = (long long) u[0] + u[1] + u[2] + u[3];  /* S_n + u[E] + I_n + u[R] */
-            if (n > 0)
-                return si_div(ldata[0] * S_n * I_n, si_l2d(n));
-            return 0.0;
+            /* the population divides every call: its reciprocal is cached */
+            const double q = si_div_cached(ldata[0] * S_n * I_n, si_l2d(n > 0 ? n : 1), &dc);
+            return n > 0 ? q : 0.0;
         }
         if (k == 1)
             return ldata[1] * si_i2d(u[1]);
@@ -88,15 +90,15 @@ struct ModelSIS {
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t)
+                                                  double t, si_recip &dc)
     {
         if (k == 0) {
             const double S_n = si_i2d(u[0]);
             const double I_n = si_i2d(u[1]);
             const long long n = (long long) u[0] + u[1];               /* S_n + I_n */
-            if (n > 0)
-                return si_div(ldata[0] * S_n * I_n, si_l2d(n));
-            return 0.0;
+            /* the population divides every call: its reciprocal is cached */
+            const double q = si_div_cached(ldata[0] * S_n * I_n, si_l2d(n > 0 ? n : 1), &dc);
+            return n > 0 ? q : 0.0;
         }
         return ldata[1] * si_i2d(u[1]);
     }
@@ -143,7 +145,7 @@ struct ModelSISe {
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t)
+                                                  double t, si_recip &dc)
     {
         if (k == 0)
             return gdata[0] * v[0] * si_i2d(u[0]);
@@ -182,7 +184,7 @@ struct ModelSISe3 {
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t)
+                                                  double t, si_recip &dc)
     {
         switch (k) {
         case 0: return gdata[0] * v[0] * si_i2d(u[0]);
@@ -225,11 +227,11 @@ struct ModelSIRmparse {
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t)
+                                                  double t, si_recip &dc)
     {
         if (k == 0) {
             const double N = si_i2d(u[0] + u[1] + u[2]);             /* int sum, as in C */
-            return si_div(gdata[0] * si_i2d(u[0]) * si_i2d(u[1]), N);
+            return si_div_cached(gdata[0] * si_i2d(u[0]) * si_i2d(u[1]), N, &dc);
         }
         return gdata[1] * si_i2d(u[1]);
     }
@@ -250,7 +252,7 @@ struct ModelSISePF {
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t)
+                                                  double t, si_recip &dc)
     {
         if (k == 0)
             return gdata[0] * v[0] * si_i2d(u[0]);

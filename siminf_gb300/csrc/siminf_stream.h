@@ -633,29 +633,28 @@ SI_HD uint64_t si_recip_seed(uint32_t m24)
     return mant << sh;
 }
 
-/* a / b, correctly rounded to nearest even, bit-identical to the IEEE
- * division of any conforming host or device.  Positive or negative normal
- * operands whose quotient is normal take an integer path (reciprocal seed,
- * two Newton steps in 64-bit fixed point, exact remainder correction); on
- * GB300 that is several times cheaper than the FP64 divide sequence.
- * Every other case (zero, subnormal, infinite, NaN operands or an
- * overflowing or underflowing quotient) uses the hardware division. */
-SI_HD double si_div(double a, double b)
+/* The divisor side of si_div: the divisor's bits, its 53-bit mantissa (0
+ * when the divisor is zero, subnormal, infinite or NaN) and y ~ 2^115 / mb
+ * in (2^62, 2^63], from the seed in two Newton steps
+ * y <- y + y * (2^115 - mb * y) / 2^115.  Newton's iteration for a
+ * reciprocal approaches from below and every truncation here rounds down,
+ * so y never exceeds 2^115 / mb. */
+typedef struct si_recip {
+    uint64_t B;
+    uint64_t mb;
+    uint64_t y;
+} si_recip;
+
+SI_HD si_recip si_recip_prep(double b)
 {
-    const uint64_t A = si_double_bits(a), B = si_double_bits(b);
-    const int ea = (int) ((A >> 52) & 0x7FF), eb = (int) ((B >> 52) & 0x7FF);
-    int e = ea - eb;
-    if (ea == 0 || ea == 0x7FF || eb == 0 || eb == 0x7FF || e > 1022 || e < -1021)
-        return a / b;
-    const uint64_t sign = (A ^ B) & 0x8000000000000000ULL;
-    uint64_t ma = (A & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
-    const uint64_t mb = (B & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
-    if (ma < mb) {              /* quotient of the mantissas in [1, 2) */
-        ma <<= 1;
-        e -= 1;
-    }
-    /* y ~ 2^115 / mb in (2^62, 2^63], from ~22 bits to ~60 bits in two
-     * Newton steps: y <- y + y * (2^115 - mb * y) / 2^115. */
+    si_recip r;
+    r.B = si_double_bits(b);
+    const int eb = (int) ((r.B >> 52) & 0x7FF);
+    r.mb = 0;
+    r.y = 0;
+    if (eb == 0 || eb == 0x7FF)
+        return r;
+    const uint64_t mb = (r.B & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
     uint64_t y = si_recip_seed((uint32_t) (mb >> 29));
     for (int it = 0; it < 2; it++) {
         const uint64_t plo = mb * y;
@@ -668,28 +667,79 @@ SI_HD double si_div(double a, double b)
         const int64_t hi = si_mulhi64((int64_t) (y >> 1), d32);
         y = (uint64_t) ((int64_t) y + (hi >> 18));
     }
-    /* Q ~ ma * 2^52 / mb = 2 ma * y / 2^64, then the exact remainder fixes
-     * the last unit: R = ma * 2^52 - Q * mb, 0 <= R < mb. */
-    uint64_t Q = si_umulhi64(ma << 1, y);
+    r.mb = mb;
+    r.y = y;
+    return r;
+}
+
+/* a / b for the divisor prepared in r (r = si_recip_prep(b)), correctly
+ * rounded to nearest even, bit-identical to the IEEE division of any
+ * conforming host or device.  Normal operands whose quotient is normal
+ * take the integer path: Q = 2 ma y / 2^64 is at most one unit below
+ * ma 2^52 / mb (y is a lower bound good to ~2^-60), and the exact
+ * remainder fixes it; the fix-ups are selects, so the path is straight
+ * code.  Every other case (zero, subnormal, infinite, NaN operands or an
+ * overflowing or underflowing quotient) uses the hardware division. */
+SI_HD double si_div_r(double a, const si_recip *r, double b)
+{
+    const uint64_t A = si_double_bits(a);
+    const int ea = (int) ((A >> 52) & 0x7FF), eb = (int) ((r->B >> 52) & 0x7FF);
+    const uint64_t mb = r->mb;
+    uint64_t ma = (A & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+    const int lt = ma < mb;                  /* quotient of the mantissas in [1, 2) */
+    ma <<= lt;
+    const int e = ea - eb - lt;
+    if ((mb == 0) | (ea == 0) | (ea == 0x7FF) | (e > 1022) | (e < -1022))
+        return a / b;
+    const uint64_t sign = (A ^ r->B) & 0x8000000000000000ULL;
+    uint64_t Q = si_umulhi64(ma << 1, r->y);
     int64_t R = (int64_t) ((ma << 52) - Q * mb);
-    while (R < 0) {
+    /* at most one step up is needed; one more each way is kept as margin */
+    if (R < 0) {
         Q--;
         R += (int64_t) mb;
     }
-    while (R >= (int64_t) mb) {
+    if (R >= (int64_t) mb) {
+        Q++;
+        R -= (int64_t) mb;
+    }
+    if (R >= (int64_t) mb) {
         Q++;
         R -= (int64_t) mb;
     }
     /* round to nearest, ties to even */
     const uint64_t twoR = (uint64_t) R << 1;
-    if (twoR > mb || (twoR == mb && (Q & 1)))
-        Q++;
-    uint64_t expo = (uint64_t) (e + 1023);
-    if (Q >> 53) {
-        Q >>= 1;
-        expo++;
-    }
+    Q += (twoR > mb) | ((twoR == mb) & (uint32_t) Q & 1u);
+    const int carry = (int) (Q >> 53);
+    Q >>= carry;
+    const uint64_t expo = (uint64_t) (e + carry + 1023);
     return si_bits_double(sign | (expo << 52) | (Q & 0x000FFFFFFFFFFFFFULL));
+}
+
+SI_HD double si_div(double a, double b)
+{
+    const si_recip r = si_recip_prep(b);
+    return si_div_r(a, &r, b);
+}
+
+/* a / b through a one-entry cache of prepared divisors: a rate that
+ * divides by a population count which the transitions keep constant
+ * prepares it once. */
+SI_HD double si_div_cached(double a, double b, si_recip *c)
+{
+    if (si_double_bits(b) != c->B)
+        *c = si_recip_prep(b);
+    return si_div_r(a, c, b);
+}
+
+/* An empty cache (no divisor has these bits and a zero mantissa). */
+SI_HD si_recip si_recip_none(void)
+{
+    si_recip r;
+    r.B = 0xFFFFFFFFFFFFFFFFULL;
+    r.mb = 0;
+    r.y = 0;
+    return r;
 }
 
 /* ---------------------------------------------------------------- */

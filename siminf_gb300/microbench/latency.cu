@@ -207,10 +207,13 @@ int main() {
   }
   // device-vs-host bit equality of si_div and si_log
   const long N = 1 << 24; double *ha = (double*)malloc(N*8), *hb = (double*)malloc(N*8), *hq = (double*)malloc(N*8), *hl = (double*)malloc(N*8);
-  for (long i = 0; i < N; i++) { uint64_t r = xr(), q = xr(); int m = i % 3;
+  for (long i = 0; i < N; i++) { uint64_t r = xr(), q = xr(); int m = i % 6;
     if (m == 0) { ha[i] = si_bits_double(r & 0x7FFFFFFFFFFFFFFFULL); hb[i] = si_bits_double(q); }
     else if (m == 1) { ha[i] = (double)(r % 100000) + 1; hb[i] = (double)(q % 1000) + 0.5; }
-    else { ha[i] = si_bits_double(0x3FF0000000000000ULL | (r & 0xFFFFFFFFFFFFFULL)); hb[i] = si_bits_double(0x3FF0000000000000ULL | ((r + (q & 3)) & 0xFFFFFFFFFFFFFULL)); } }
+    else if (m == 2) { ha[i] = si_bits_double(0x3FF0000000000000ULL | (r & 0xFFFFFFFFFFFFFULL)); hb[i] = si_bits_double(0x3FF0000000000000ULL | ((r + (q & 3)) & 0xFFFFFFFFFFFFFULL)); }
+    else if (m == 3) { ha[i] = si_bits_double(0x3FF0000000000000ULL | (r & 0xFFFFFFFFFFFFFULL)); hb[i] = si_bits_double(0x4010000000000000ULL | (q & 0xFF)); }
+    else if (m == 4) { ha[i] = si_bits_double(0x3FFFFFFFFFFFFFFFULL - (r & 0xFFFF)); hb[i] = si_bits_double(0x3FFFFFFFFFFFFFFFULL - (q & 0xFF)); }
+    else { ha[i] = si_bits_double(0x0010000000000000ULL | (r & 0x3FFFFFFFFFFFFFULL)); hb[i] = si_bits_double(0x7FE0000000000000ULL - (q & 0x00FFFFFFFFFFFFFFULL)); } }
   double *da, *db, *dq, *dl; CK(cudaMalloc(&da, N*8)); CK(cudaMalloc(&db, N*8)); CK(cudaMalloc(&dq, N*8)); CK(cudaMalloc(&dl, N*8));
   CK(cudaMemcpy(da, ha, N*8, cudaMemcpyHostToDevice)); CK(cudaMemcpy(db, hb, N*8, cudaMemcpyHostToDevice));
   check<<<(N+255)/256, 256>>>(da, db, dq, dl, N); CK(cudaDeviceSynchronize());
