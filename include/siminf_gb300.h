@@ -181,8 +181,9 @@ int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args,
  * are drawn without knowledge of the state need it.
  *
  * heavy_rate: a tuning knob, not a semantic option -- nodes whose rate sum
- * at the start of a day reaches it are simulated one per warp (results are
- * identical either way).
+ * at the start of a day reaches it are queued and simulated first, 32 to a
+ * warp (results are identical either way); 0 takes the default (8), a
+ * negative value turns the queue off.
  *
  * gdata_per_replicate: args->gdata holds one gdata vector per replicate
  * (Nrep rows of the model's gdata length); replicate r reads row r.  The
@@ -191,7 +192,7 @@ int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args,
  */
 typedef struct siminf_gpu_options {
     int cap_transfers;
-    int heavy_rate;     /* rate sum from which a node runs one per warp (0 = default) */
+    int heavy_rate;     /* rate sum from which a node is queued first (0 = default 8, < 0 = off) */
     int gdata_per_replicate;
     int reserved[5];
 } siminf_gpu_options;

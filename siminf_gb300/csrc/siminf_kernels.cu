@@ -306,178 +306,6 @@ __device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::N
 }
 
 /* ------------------------------------------------------------------ */
-/* Warp-cooperative SSA of one heavy node (same semantics as ssa_day).  */
-/* All 32 lanes carry the node's state and run the chain on identical   */
-/* data, so it costs one warp instruction stream.  Two kinds of work    */
-/* are spread over the lanes:                                           */
-/*  - draws: lane i holds uniform and -log(uniform) of draw base + i,   */
-/*    computed for 32 draws (16 transitions) at once;                   */
-/*  - candidates: rates do not depend on t, so lane k computes the rate */
-/*    vector, delta and new sum that transition k would produce, while  */
-/*    the chain decides which transition fires; the winner is then      */
-/*    taken by shuffles.  The division inside the rate code leaves the  */
-/*    loop-carried chain that way.                                      */
-/* ------------------------------------------------------------------ */
-template <class M>
-__device__ __forceinline__ unsigned ssa_day_warp(int (&u)[M::NC], double (&rate)[M::NT], double &sum,
-                                                 double &t, const double *v, const double *ld,
-                                                 const double *gd, uint64_t seed, uint64_t sid,
-                                                 uint64_t &ctr, double next, const int *sS,
-                                                 const uint32_t *sG, int &err, int &err_tr,
-                                                 double &err_t, double &err_rate)
-{
-    constexpr int NC = M::NC, NT = M::NT;
-    const unsigned FULL = 0xFFFFFFFFu;
-    const int lane = threadIdx.x & 31;
-    const int k = lane < NT ? lane : NT - 1;
-    si_recip dc = si_recip_none();
-    unsigned fired = 0;
-
-    uint64_t base = ctr;
-    double Lb, Ub;
-    {
-        si_rng r;
-        si_rng_init(&r, seed, sid, base + (uint64_t) lane);
-        const uint32_t wb = si_peek_u32(&r);
-        Ub = si_u32_to_uniform_pos(wb);
-        Lb = si_neglog_u32(wb);
-    }
-    double cum[NT];
-    prefix_sums<M>(rate, cum);
-
-    /* candidate k from the current state */
-    double crate[NT], ccum[NT], csum, cbad_rate = 0.0;
-    int cneg = 0, cbad = 0, cbad_tr = -1;
-    auto candidates = [&]() {
-        int uk[NC];
-        cneg = 0;
-#pragma unroll
-        for (int c = 0; c < NC; c++) {
-            const int d = sS[k * NC + c];
-            uk[c] = u[c] + d;
-            if (d != 0 && uk[c] < 0)
-                cneg = 1;
-        }
-        double delta = 0.0;
-        cbad = 0;
-        const uint32_t gm = sG[k];
-#pragma unroll
-        for (int j = 0; j < NT; j++) {
-            if (gm & (1u << j)) {
-                const double nr = M::rate(j, uk, v, ld, gd, 0.0, dc);
-                crate[j] = nr;
-                delta += nr - rate[j];
-                if (si_bad_rate(nr)) {
-                    cbad = 1;
-                    cbad_tr = j;
-                    cbad_rate = nr;
-                }
-            } else {
-                crate[j] = rate[j];
-            }
-        }
-        csum = sum + delta;
-        prefix_sums<M>(crate, ccum);
-    };
-    candidates();
-
-    for (;;) {
-        if (sum <= 0.0) {
-            t = next;
-            break;
-        }
-        if (!si_finite_pos(sum)) {
-            if (!err) {
-                err = ERR_INVALID_RATE;
-                err_tr = -1;
-                err_t = t;
-                err_rate = sum;
-            }
-            t = next;
-            break;
-        }
-        if (ctr + 1 >= base + 32) {
-            base = ctr;
-            si_rng r;
-            si_rng_init(&r, seed, sid, base + (uint64_t) lane);
-            const uint32_t wb = si_peek_u32(&r);
-            Ub = si_u32_to_uniform_pos(wb);
-            Lb = si_neglog_u32(wb);
-        }
-        const int i0 = (int) (ctr - base);
-        const double L = __shfl_sync(FULL, Lb, i0);
-        const double u2 = __shfl_sync(FULL, Ub, i0 + 1);
-        const double tau = si_div(L, sum);
-        const double tn = tau + t;
-        const double rnd = u2 * sum;
-        if (si_dge(tn, next)) {
-            t = next;
-            ctr += 1;
-            break;
-        }
-        t = tn;
-        ctr += 2;
-
-        int tr = NT - 1;
-#pragma unroll
-        for (int kk = NT - 2; kk >= 0; kk--)
-            if (!si_dgt(rnd, cum[kk]))
-                tr = kk;
-        double rtr = rate[0];
-#pragma unroll
-        for (int kk = 1; kk < NT; kk++)
-            if (tr == kk)
-                rtr = rate[kk];
-        if (si_is_zero(rtr)) {
-#pragma unroll
-            for (int kk = NT - 1; kk >= 1; kk--)
-                if (tr == kk && si_is_zero(rate[kk]))
-                    tr = kk - 1;
-            double r2 = rate[0];
-#pragma unroll
-            for (int kk = 1; kk < NT; kk++)
-                if (tr == kk)
-                    r2 = rate[kk];
-            if (si_is_zero(r2)) {
-                sum = 0.0;
-                break;
-            }
-        }
-
-        if (++fired > MAX_NODE_DAY_TRANSITIONS) {
-            err = ERR_TIMEOUT;
-            err_tr = tr;
-            err_t = t;
-            t = next;
-            break;
-        }
-#pragma unroll
-        for (int c = 0; c < NC; c++)
-            u[c] += sS[tr * NC + c];
-#pragma unroll
-        for (int j = 0; j < NT; j++) {
-            rate[j] = __shfl_sync(FULL, crate[j], tr);
-            cum[j] = __shfl_sync(FULL, ccum[j], tr);
-        }
-        sum = __shfl_sync(FULL, csum, tr);
-        if (__shfl_sync(FULL, cneg, tr)) {
-            err = ERR_NEGATIVE_STATE;
-            err_tr = tr;
-            err_t = t;
-            err_rate = 0.0;
-        }
-        if (__shfl_sync(FULL, cbad, tr)) {
-            err = ERR_INVALID_RATE;
-            err_tr = __shfl_sync(FULL, cbad_tr, tr);
-            err_t = t;
-            err_rate = __shfl_sync(FULL, cbad_rate, tr);
-        }
-        candidates();
-    }
-    return fired;
-}
-
-/* ------------------------------------------------------------------ */
 /* Event sampling on a node's compartments uu (src/solvers/             */
 /* SimInf_solver.c:62-324), drawing from the node's stream.             */
 /* ------------------------------------------------------------------ */
@@ -858,7 +686,7 @@ __global__ void k_init(DevState s, double tt0)
 template <class M>
 __device__ __forceinline__ void node_day(const DevState &s, long long g, int day, double tt,
                                          double next, const int *sS, const uint32_t *sG,
-                                         bool warp_mode, unsigned long long &fired)
+                                         unsigned long long &fired)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     const int node = (int) (g % s.Nn);
@@ -876,42 +704,29 @@ __device__ __forceinline__ void node_day(const DevState &s, long long g, int day
     int err = 0, err_tr = -1;
     double err_t = 0, err_rate = 0;
     si_rng r;
-    if (warp_mode) {
-        uint64_t ctr = s.ctr[g];
-        fired += ssa_day_warp<M>(u, rate, sum, t, v, ld, gdata_of(s, g), s.seed, (uint64_t) g, ctr,
-                                 next, sS, sG, err, err_tr, err_t, err_rate);
-        si_rng_init(&r, s.seed, (uint64_t) g, ctr);
-    } else {
-        si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
-        si_recip dc = si_recip_none();
-        fired += ssa_day<M>(u, rate, sum, t, v, ld, gdata_of(s, g), r, next, sS, sG, dc, err,
-                            err_tr, err_t, err_rate);
-    }
-    const bool writer = !warp_mode || (threadIdx.x & 31) == 0;
+    si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
+    si_recip dc = si_recip_none();
+    fired += ssa_day<M>(u, rate, sum, t, v, ld, gdata_of(s, g), r, next, sS, sG, dc, err, err_tr,
+                        err_t, err_rate);
     if (err) {
-        if (writer)
-            record_error(s, err, PHASE_SSA, day, g, err_tr, -1, err_t, err_rate);
+        record_error(s, err, PHASE_SSA, day, g, err_tr, -1, err_t, err_rate);
     } else {
         int e_code = 0, e_idx = -1;
         const bool upd = node_e1<NC>(s, u, node, day, r, g, tt, e_code, e_idx);
-        if (writer) {
-            if (upd)
-                s.update[g] = 1;
-            if (e_code)
-                record_error(s, e_code, PHASE_E1, day, g, -1, e_idx, tt, 0);
-        }
+        if (upd)
+            s.update[g] = 1;
+        if (e_code)
+            record_error(s, e_code, PHASE_E1, day, g, -1, e_idx, tt, 0);
     }
-    if (writer) {
 #pragma unroll
-        for (int c = 0; c < NC; c++)
-            s.u[g * NC + c] = u[c];
+    for (int c = 0; c < NC; c++)
+        s.u[g * NC + c] = u[c];
 #pragma unroll
-        for (int k = 0; k < NT; k++)
-            s.t_rate[(size_t) k * s.Ntot + g] = rate[k];
-        s.sum_rate[g] = sum;
-        s.t_time[g] = t;
-        s.ctr[g] = r.ctr;
-    }
+    for (int k = 0; k < NT; k++)
+        s.t_rate[(size_t) k * s.Ntot + g] = rate[k];
+    s.sum_rate[g] = sum;
+    s.t_time[g] = t;
+    s.ctr[g] = r.ctr;
 }
 
 template <class M>
@@ -931,33 +746,35 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
     const bool stop = load_flag(s.err_day) < day;
     if ((int) blockIdx.x < s.heavy_blocks) {
         if (M::RATES_TIME_INVARIANT && !stop) {
-            int n[HEAVY_CLASSES];
+            int n[HEAVY_CLASSES], total = 0;
 #pragma unroll
-            for (int c = 0; c < HEAVY_CLASSES; c++)
+            for (int c = 0; c < HEAVY_CLASSES; c++) {
                 n[c] = min(s.heavy_count[par * HEAVY_CLASSES + c], (int) MAX_HEAVY);
+                total += n[c];
+            }
+            const int lane = threadIdx.x & 31;
             for (;;) {
-                int idx = 0;
-                if ((threadIdx.x & 31) == 0)
-                    idx = atomicAdd(&s.heavy_next[par], 1);
-                idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
+                int base = 0;
+                if (lane == 0)
+                    base = atomicAdd(&s.heavy_next[par], 32);
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                if (base >= total)
+                    break;
+                int idx = base + lane;
                 int c = 0;
                 while (c < HEAVY_CLASSES && idx >= n[c]) {
                     idx -= n[c];
                     c++;
                 }
-                if (c == HEAVY_CLASSES)
-                    break;
-                unsigned long long f = 0;
-                node_day<M>(s, s.heavy_list[(par * HEAVY_CLASSES + c) * MAX_HEAVY + idx], day, tt,
-                            next, sS, sG, true, f);
-                if ((threadIdx.x & 31) == 0)
-                    fired += f;
+                if (c < HEAVY_CLASSES)
+                    node_day<M>(s, s.heavy_list[(par * HEAVY_CLASSES + c) * MAX_HEAVY + idx], day,
+                                tt, next, sS, sG, fired);
             }
         }
     } else {
         const long long g = (blockIdx.x - s.heavy_blocks) * (long long) blockDim.x + threadIdx.x;
         if (g < s.Ntot && !stop && !(s.heavy_mark[g] == day + 1))
-            node_day<M>(s, g, day, tt, next, sS, sG, false, fired);
+            node_day<M>(s, g, day, tt, next, sS, sG, fired);
     }
     add_fired(s, fired);
 }

@@ -26,11 +26,14 @@ namespace siminf {
 
 enum { MAX_NC = 16, MAX_NT = 32, MAX_ERR = 1024 };
 
-/* Nodes whose rate sum at the start of a day is at least heavy_rate run one
- * per warp: k_ssa_e1's first heavy_blocks blocks are persistent warps that
- * take heavy nodes from a per-day queue, heaviest class first (classes:
- * sum >= 16, 4 and 1 times heavy_rate).  At most MAX_HEAVY per class and
- * day; the rest take the thread-per-node path. */
+/* Nodes whose rate sum at the start of a day is at least heavy_rate are
+ * listed by k_pts_store (k_init for day 0) in a per-day queue, heaviest
+ * class first (classes: sum >= 16, 4 and 1 times heavy_rate).  k_ssa_e1's
+ * first heavy_blocks blocks are persistent warps that take 32 queued nodes
+ * at a time, one per lane, so the day's longest chains start together at
+ * the start of the kernel instead of wherever their node's block is
+ * scheduled.  At most MAX_HEAVY per class and day; the rest take the
+ * ordinary one-thread-per-node blocks. */
 enum { SSA_BLOCK = 128, HEAVY_CLASSES = 3, MAX_HEAVY = 4096 };
 
 enum { PHASE_INIT = 0, PHASE_SSA = 1, PHASE_E1 = 2, PHASE_E2 = 3, PHASE_PTS = 4 };

@@ -155,15 +155,17 @@ def test_gpu_conservation_full_scale_properties(gpu):
         assert change >= d_enter[k] - d_exit[k]
 
 
+@pytest.mark.parametrize("heavy_rate", [1, -1])
 @pytest.mark.parametrize("label,m", parity_cases(), ids=[c[0] for c in parity_cases()])
-def test_gpu_heavy_warp_path_matches_oracle(gpu, oracle_lib, label, m):
-    """heavy_rate = 1 sends every node with a rate sum >= 1 through the
-    warp-per-node SSA: still bit-exact."""
+def test_gpu_heavy_queue_matches_oracle(gpu, oracle_lib, label, m, heavy_rate):
+    """heavy_rate = 1 queues every node with a rate sum >= 1 for the heavy
+    warps (32 nodes to a warp, first in the day); -1 turns the queue off.
+    Both stay bit-exact."""
     import ctypes as C
     from siminf_gb300 import abi, native
     _, _, ho = run_oracle(m, threads=4)
     h = abi.build_args(m, 42)
-    opt = abi.Options(cap_transfers=0, heavy_rate=1)
+    opt = abi.Options(cap_transfers=0, heavy_rate=heavy_rate)
     code = native.lib().siminf_gpu_run_solver_ex(C.cast(h.ref(), C.c_void_p),
                                                  native.device_model(m.name).handle,
                                                  C.byref(opt))
