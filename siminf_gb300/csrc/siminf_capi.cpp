@@ -32,6 +32,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <atomic>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -139,6 +140,18 @@ struct siminf_gpu_plan {
     siminf_gpu_stats stats{};
     bool ran = false;
     int days_cap = 0;
+
+    /* E2 planning state: events of day d go to positions e2_day_off[d] ..
+     * e2_day_off[d + 1] of d_e2 and come from input range e2_lo[d] ..
+     * e2_hi[d]; day_waves[d] holds the day's wave sizes. */
+    int nsel = 0;
+    std::vector<long long> e2_day_off, e2_lo, e2_hi;
+    std::vector<std::vector<long long>> day_waves;
+    /* Streamed runs: the waves are planned on host threads while the GPU
+     * runs earlier days; the caller's arrays stay valid until the run. */
+    bool e2_pending = false;
+    siminf_gpu_solver_args args{};
+    std::unique_ptr<E2Rec[]> h_e2;
 };
 
 static int validate(const siminf_gpu_solver_args *a, const Launchers *L)
@@ -247,9 +260,11 @@ static void parallel(F &&f)
         x.join();
 }
 
-static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int nsel,
-                       std::vector<E1Rec> &e1, std::vector<int> &e1_ptr,
-                       std::vector<E2Rec> &e2)
+/* Pass over the schedule before any wave is planned: order check, planned
+ * failures, the E1 records bucketed by node, and per day the number of
+ * valid external transfers, their output offset and their input range. */
+static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int nsel,
+                     std::vector<E1Rec> &e1, std::vector<int> &e1_ptr)
 {
     const int Nn = a->Nn, ndays = p->ndays;
     const double tt0 = a->tspan[0];
@@ -341,10 +356,13 @@ static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int 
     for (auto &c : chunks)
         for (int d = 0; d < ndays; d++)
             day_cnt[d] += c.e2_per_day[d];
-    std::vector<long long> day_off(ndays + 1, 0);
+    std::vector<long long> &day_off = p->e2_day_off;
+    day_off.assign(ndays + 1, 0);
     for (int d = 0; d < ndays; d++)
         day_off[d + 1] = day_off[d] + day_cnt[d];
-    std::vector<long long> range_lo(ndays), range_hi(ndays);
+    std::vector<long long> &range_lo = p->e2_lo, &range_hi = p->e2_hi;
+    range_lo.assign(ndays, 0);
+    range_hi.assign(ndays, 0);
     for (int d = 0; d < ndays; d++) {
         /* times of day d: (tt_{d-1}, tt_d]; day 0 takes every time <= tt0 */
         auto first_after = [&](double x) {
@@ -363,67 +381,99 @@ static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int 
     }
     p->e1_count = e1.size();
     p->e2_count = day_off[ndays];
-    e2.resize(day_off[ndays]);
+    p->nsel = nsel;
+    p->day_waves.assign(ndays, std::vector<long long>());
+    return 0;
+}
 
-    /* Wave levels, one thread per day at a time: level = 1 + max(level of
-     * the last event with the same source, of any add into the source, of
-     * the last event whose source is our destination).  Then a stable
-     * counting sort of the day's events by level. */
-    std::vector<std::vector<long long>> day_waves(ndays);
-    std::atomic<int> next_day(0);
-    parallel([&](int, int) {
-        std::vector<int> excl(Nn, 0), add(Nn, 0), stamp(Nn, -1);
-        std::vector<int> level;
-        std::vector<long long> idx;
-        for (int d = next_day++; d < ndays; d = next_day++) {
-            level.clear();
-            idx.clear();
-            int maxl = 0;
-            for (long long i = range_lo[d]; i < range_hi[d]; i++) {
-                if (a->event[i] != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
-                    continue;
-                const int s = a->node[i] - 1, t = a->dest[i] - 1;
-                if (s < 0 || s >= Nn || t < 0 || t >= Nn || a->select[i] - 1 < 0 ||
-                    a->select[i] - 1 >= nsel)
-                    continue;
-                if (stamp[s] != d) {
-                    stamp[s] = d;
-                    excl[s] = add[s] = 0;
-                }
-                if (stamp[t] != d) {
-                    stamp[t] = d;
-                    excl[t] = add[t] = 0;
-                }
-                const int L = 1 + std::max(std::max(excl[s], add[s]), excl[t]);
-                excl[s] = L;
-                add[t] = std::max(add[t], L);
-                level.push_back(L);
-                idx.push_back(i);
-                maxl = std::max(maxl, L);
-            }
-            std::vector<long long> cnt(maxl + 2, 0);
-            for (int L : level)
-                cnt[L]++;
-            std::vector<long long> off(maxl + 2, day_off[d]);
-            for (int L = 1; L <= maxl; L++)
-                off[L + 1] = off[L] + cnt[L];
-            for (size_t k = 0; k < level.size(); k++) {
-                const long long i = idx[k];
-                e2[off[level[k]]++] = E2Rec{a->node[i] - 1, a->dest[i] - 1, a->n[i],
-                                            a->select[i] - 1, a->shift[i] - 1, (int) i,
-                                            a->proportion[i]};
-            }
-            day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
+/* Per-thread scratch of the wave planner (levels per node, stamped by day). */
+struct WaveTracker {
+    std::vector<int> excl, add, stamp, level;
+    std::vector<long long> idx;
+    explicit WaveTracker(int Nn) : excl(Nn, 0), add(Nn, 0), stamp(Nn, -1) {}
+};
+
+/* Wave levels of day d: level = 1 + max(level of the last event with the
+ * same source, of any add into the source, of the last event whose source
+ * is our destination).  Then a stable counting sort of the day's events by
+ * level into e2 (positions e2_day_off[d] ..), and the wave sizes into
+ * p->day_waves[d]. */
+static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
+                           WaveTracker &w, E2Rec *e2)
+{
+    const int Nn = a->Nn, nsel = p->nsel;
+    std::vector<int> &excl = w.excl, &add = w.add, &stamp = w.stamp, &level = w.level;
+    std::vector<long long> &idx = w.idx;
+    level.clear();
+    idx.clear();
+    int maxl = 0;
+    for (long long i = p->e2_lo[d]; i < p->e2_hi[d]; i++) {
+        if (a->event[i] != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
+            continue;
+        const int s = a->node[i] - 1, t = a->dest[i] - 1;
+        if (s < 0 || s >= Nn || t < 0 || t >= Nn || a->select[i] - 1 < 0 ||
+            a->select[i] - 1 >= nsel)
+            continue;
+        if (stamp[s] != d) {
+            stamp[s] = d;
+            excl[s] = add[s] = 0;
         }
-    });
-    p->day_wave.assign(ndays + 1, 0);
+        if (stamp[t] != d) {
+            stamp[t] = d;
+            excl[t] = add[t] = 0;
+        }
+        const int L = 1 + std::max(std::max(excl[s], add[s]), excl[t]);
+        excl[s] = L;
+        add[t] = std::max(add[t], L);
+        level.push_back(L);
+        idx.push_back(i);
+        maxl = std::max(maxl, L);
+    }
+    std::vector<long long> cnt(maxl + 2, 0);
+    for (int L : level)
+        cnt[L]++;
+    std::vector<long long> off(maxl + 2, p->e2_day_off[d]);
+    for (int L = 1; L <= maxl; L++)
+        off[L + 1] = off[L] + cnt[L];
+    for (size_t k = 0; k < level.size(); k++) {
+        const long long i = idx[k];
+        e2[off[level[k]]++] = E2Rec{a->node[i] - 1, a->dest[i] - 1, a->n[i], a->select[i] - 1,
+                                    a->shift[i] - 1, (int) i, a->proportion[i]};
+    }
+    p->day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
+}
+
+/* Wave offsets of every day, from day_waves. */
+static void plan_wave_index(siminf_gpu_plan *p)
+{
+    p->day_wave.assign(p->ndays + 1, 0);
     p->wave_ptr.clear();
     p->wave_ptr.push_back(0);
-    for (int d = 0; d < ndays; d++) {
-        for (long long c : day_waves[d])
+    for (int d = 0; d < p->ndays; d++) {
+        for (long long c : p->day_waves[d])
             p->wave_ptr.push_back(p->wave_ptr.back() + c);
         p->day_wave[d + 1] = (int) p->wave_ptr.size() - 1;
     }
+}
+
+/* The whole schedule: scan, then the waves of every day on the planner
+ * threads.  e2 receives p->e2_count records (left unset otherwise). */
+static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int nsel,
+                       std::vector<E1Rec> &e1, std::vector<int> &e1_ptr,
+                       std::unique_ptr<E2Rec[]> &e2)
+{
+    int rc = plan_scan(p, a, nsel, e1, e1_ptr);
+    if (rc)
+        return rc;
+    e2.reset(new E2Rec[p->e2_count > 0 ? p->e2_count : 1]);
+    std::atomic<int> next_day(0);
+    E2Rec *dst = e2.get();
+    parallel([&](int, int) {
+        WaveTracker w(a->Nn);
+        for (int d = next_day++; d < p->ndays; d = next_day++)
+            plan_day_waves(p, a, d, w, dst);
+    });
+    plan_wave_index(p);
     return 0;
 }
 
@@ -516,14 +566,23 @@ void siminf_gpu_plan_free(siminf_gpu_plan *p)
     delete p;
 }
 
+static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
+                            const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream);
+
+int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
+                              const siminf_gpu_options *opt, siminf_gpu_plan **out)
+{
+    return plan_create_impl(a, model, opt, out, false);
+}
+
 int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
                            siminf_gpu_plan **out)
 {
     return siminf_gpu_plan_create_ex(a, model, nullptr, out);
 }
 
-int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
-                              const siminf_gpu_options *opt, siminf_gpu_plan **out)
+static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
+                            const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream)
 {
     auto t0 = std::chrono::steady_clock::now();
     int rc;
@@ -575,10 +634,19 @@ int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_
     const int nsel = (a->len > 0 && a->jcE) ? INT_MAX : 0;
     std::vector<E1Rec> e1;
     std::vector<int> e1_ptr;
-    std::vector<E2Rec> e2;
-    if ((rc = plan_events(p, a, nsel, e1, e1_ptr, e2))) {
+    std::unique_ptr<E2Rec[]> e2;
+    rc = stream ? plan_scan(p, a, nsel, e1, e1_ptr) : plan_events(p, a, nsel, e1, e1_ptr, e2);
+    if (rc) {
         delete p;
         return rc;
+    }
+    if (stream && p->e2_count == 0)
+        plan_wave_index(p);
+    if (stream && p->e2_count > 0) {
+        /* the waves are planned during the first run, beside the GPU */
+        p->e2_pending = true;
+        p->args = *a;
+        p->h_e2.reset(new E2Rec[p->e2_count]);
     }
     p->stats.ms_plan = ms_since(t0);
     p->horizon = (p->e2_count == 0) && L->pts_local;
@@ -639,7 +707,12 @@ int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_
         s.e1_ptr = de1p;
         s.e1 = de1;
     }
-    if (!rc) rc = upload(&p->d_e2, e2.data(), e2.size(), own, st);
+    if (!rc) {
+        if (p->e2_pending)
+            rc = dalloc(&p->d_e2, (size_t) p->e2_count, own);
+        else
+            rc = upload(&p->d_e2, e2.get(), (size_t) p->e2_count, own, st);
+    }
     if (!rc) rc = upload(&p->d_days, p->days.data(), p->days.size(), own, st);
 
     /* state */
@@ -868,6 +941,93 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
     return e;
 }
 
+/* The first run of a streamed plan: host threads plan the external
+ * transfers' waves day by day while this thread copies each chunk of
+ * finished days to the device on a copy stream and queues the chunk's
+ * kernels behind it, so planning and copying overlap the GPU's work on
+ * earlier days.  The kernels and their order are those of launch_all. */
+static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t st)
+{
+    const Launchers *L = p->L;
+    const siminf_gpu_solver_args *a = &p->args;
+    const int ndays = p->ndays;
+    enum { CHUNK_DAYS = 8 };
+    cudaError_t e = L->init(s, p->tt0, st);
+    if (e != cudaSuccess)
+        return e;
+
+    std::unique_ptr<std::atomic<int>[]> done(new std::atomic<int>[ndays]);
+    for (int d = 0; d < ndays; d++)
+        done[d].store(0);
+    std::atomic<int> next_day(0), failed(0);
+    E2Rec *h = p->h_e2.get();
+    std::vector<std::thread> workers;
+    const int nthreads = std::max(1, planner_threads() - 1);
+    for (int t = 0; t < nthreads; t++)
+        workers.emplace_back([&]() {
+            try {
+                WaveTracker w(a->Nn);
+                for (int d = next_day++; d < ndays; d = next_day++) {
+                    plan_day_waves(p, a, d, w, h);
+                    done[d].store(1, std::memory_order_release);
+                }
+            } catch (...) {
+                failed.store(1);
+            }
+        });
+
+    cudaStream_t cs = nullptr;
+    e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (int d0 = 0; d0 < ndays && e == cudaSuccess; d0 += CHUNK_DAYS) {
+        const int d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
+        for (int d = d0; d < d1 && !failed.load(); d++)
+            while (!done[d].load(std::memory_order_acquire) && !failed.load())
+                std::this_thread::yield();
+        if (failed.load()) {
+            e = cudaErrorMemoryAllocation;
+            break;
+        }
+        const long long lo = p->e2_day_off[d0], hi = p->e2_day_off[d1];
+        if (hi > lo) {
+            cudaEvent_t ev;
+            e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            if (e == cudaSuccess) {
+                e = cudaMemcpyAsync(p->d_e2 + lo, h + lo, (size_t) (hi - lo) * sizeof(E2Rec),
+                                    cudaMemcpyHostToDevice, cs);
+                if (e == cudaSuccess)
+                    e = cudaEventRecord(ev, cs);
+                if (e == cudaSuccess)
+                    e = cudaStreamWaitEvent(st, ev, 0);
+                cudaEventDestroy(ev);
+            }
+        }
+        for (int d = d0; d < d1 && e == cudaSuccess; d++) {
+            const DayInfo &di = p->days[d];
+            e = L->ssa_e1(s, d, di.tt, di.next, st);
+            long long off = p->e2_day_off[d];
+            for (size_t w = 0; w < p->day_waves[d].size() && e == cudaSuccess; w++) {
+                const long long c = p->day_waves[d][w];
+                e = L->e2_wave(s, p->d_e2 + off, (int) c, d, di.tt, st);
+                off += c;
+            }
+            if (e == cudaSuccess)
+                e = L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
+            std::swap(s.vA, s.vB);
+        }
+    }
+    /* the planners finish their days either way; the copies must land
+     * before the host buffer may go */
+    for (auto &t : workers)
+        t.join();
+    if (cs) {
+        const cudaError_t e2 = cudaStreamSynchronize(cs);
+        if (e == cudaSuccess)
+            e = e2;
+        cudaStreamDestroy(cs);
+    }
+    return e;
+}
+
 extern "C" {
 
 static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
@@ -905,7 +1065,15 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
     if (e != cudaSuccess)
         return cuda_fail(e, "plan_run reset");
 
-    e = launch_all(p, s, st, kp);
+    if (p->e2_pending) {
+        e = launch_streamed(p, s, st);
+        p->e2_pending = false;
+        p->h_e2.reset();
+        plan_wave_index(p);
+        p->stats.e2_waves = (int) p->wave_ptr.size() - 1;
+    } else {
+        e = launch_all(p, s, st, kp);
+    }
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     cudaEventRecord(ev1, st);
@@ -1005,7 +1173,7 @@ int siminf_gpu_schedule(const siminf_gpu_solver_args *a, int *days, int *waves,
         return rc;
     std::vector<E1Rec> e1;
     std::vector<int> e1_ptr;
-    std::vector<E2Rec> e2;
+    std::unique_ptr<E2Rec[]> e2;
     rc = plan_events(&p, a, a->len > 0 ? INT_MAX : 0, e1, e1_ptr, e2);
     if (rc)
         return rc;
@@ -1183,7 +1351,9 @@ static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *mode
                       const siminf_gpu_options *opt)
 {
     siminf_gpu_plan *p = nullptr;
-    int rc = siminf_gpu_plan_create_ex(args, model, opt, &p);
+    /* streamed: the external transfers' waves are planned and copied
+     * while the GPU runs the earlier days */
+    int rc = plan_create_impl(args, model, opt, &p, true);
     if (rc)
         return rc;
     rc = siminf_gpu_plan_run(p, nullptr);
