@@ -729,12 +729,11 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     if (!rc) rc = dalloc(&s.fired, 1, own);
     if (!rc) rc = dalloc(&s.heavy_list, (size_t) 2 * HEAVY_CLASSES * MAX_HEAVY, own);
     if (!rc) rc = dalloc(&s.heavy_count, (size_t) 2 * HEAVY_CLASSES, own);
-    if (!rc) rc = dalloc(&s.heavy_next, 2, own);
+    if (!rc) rc = dalloc(&s.queue_next, 4, own);
     if (!rc) rc = dalloc(&s.heavy_mark, (size_t) Ntot, own);
-    /* heavy-node path: threshold on the day-start rate sum (options, else
-     * SIMINF_HEAVY_RATE in the environment, 0 = off; default 8, the best
-     * of 8, 32 and 128 on the 10^6-node SEIR workload) and the number of
-     * persistent heavy blocks (SIMINF_HEAVY_BLOCKS, default 32) */
+    /* heavy part of the work queue: threshold on the day-start rate sum
+     * (options, else SIMINF_HEAVY_RATE in the environment, 0 = off;
+     * default 8, the best of 2 to 128 on the 10^6-node SEIR workload) */
     s.heavy_rate = 8.0;
     if (const char *ev = getenv("SIMINF_HEAVY_RATE"))
         s.heavy_rate = atof(ev);
@@ -742,11 +741,6 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
         s.heavy_rate = opt->heavy_rate;
     else if (opt && opt->heavy_rate < 0)
         s.heavy_rate = 0.0;
-    s.heavy_blocks = 32;
-    if (const char *ev = getenv("SIMINF_HEAVY_BLOCKS"))
-        s.heavy_blocks = std::max(0, atoi(ev));
-    if (!(s.heavy_rate > 0))
-        s.heavy_blocks = 0;
     if (!rc) {
         s.err_day = s.err_count + 1;
         s.err_day_pre_e2 = s.err_count + 2;
@@ -1049,7 +1043,7 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s.heavy_count, 0, 2 * HEAVY_CLASSES * sizeof(int), st);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(s.heavy_next, 0, 2 * sizeof(int), st);
+        e = cudaMemsetAsync(s.queue_next, 0, 4 * sizeof(unsigned long long), st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s.heavy_mark, 0, (size_t) s.Ntot * sizeof(int), st);
     if (e == cudaSuccess)

@@ -145,164 +145,191 @@ __device__ __forceinline__ void philox_block(const si_rng &r, uint64_t blk, uint
     si_philox4x32_10(&b0, &b1, &b2, &b3, r.k0, r.k1);
 }
 
+/* The SSA state of one node during its day, held by one thread. */
 template <class M>
-__device__ __forceinline__ unsigned ssa_day(int (&u)[M::NC], double (&rate)[M::NT], double &sum,
-                                            double &t, const double *v, const double *ld,
-                                            const double *gd, si_rng &r, double next,
-                                            const int *sS, const uint32_t *sG, si_recip &dc,
-                                            int &err, int &err_tr, double &err_t,
-                                            double &err_rate)
+struct SsaLane {
+    int u[M::NC];
+    double rate[M::NT], cum[M::NT];
+    double sum, t, L, U, tau;
+    uint64_t c;                       /* draw index of the next waiting time */
+    uint32_t q0, q1, q2, q3;          /* Philox block (c + 1) >> 2 */
+    unsigned fired;
+    int err, err_tr;
+    double err_t, err_rate;
+    si_recip dc;
+};
+
+/* Start the day of a node whose u, rate, sum and t are loaded and whose
+ * next draw is `c`; key holds the stream's key.  Returns true when nothing
+ * fires today (rate sum <= 0, or not finite after a recorded invalid rate,
+ * which would never reach `next`). */
+template <class M>
+__device__ __forceinline__ bool ssa_begin(SsaLane<M> &ln, const si_rng &key, uint64_t c,
+                                          double next)
+{
+    ln.fired = 0;
+    ln.c = c;
+    if (!si_finite_pos(ln.sum)) {
+        /* sum <= 0: nothing fires (ssm.c:148-151) */
+        if (!le_zero(si_double_bits(ln.sum)) && !ln.err) {
+            ln.err = ERR_INVALID_RATE;
+            ln.err_tr = -1;
+            ln.err_t = ln.t;
+            ln.err_rate = ln.sum;
+        }
+        ln.t = next;
+        return true;
+    }
+    prefix_sums<M>(ln.rate, ln.cum);
+    /* the pair of the first transition */
+    uint32_t p0, p1, p2, p3;
+    philox_block(key, c >> 2, p0, p1, p2, p3);
+    philox_block(key, (c + 1) >> 2, ln.q0, ln.q1, ln.q2, ln.q3);
+    ln.L = si_neglog_u32(word_of(p0, p1, p2, p3, (uint32_t) c & 3u));
+    ln.U = si_u32_to_uniform_pos(word_of(ln.q0, ln.q1, ln.q2, ln.q3, (uint32_t) (c + 1) & 3u));
+    ln.tau = si_div(ln.L, ln.sum);
+    return false;
+}
+
+/* One step of the direct method: the waiting time ends the day, or one
+ * transition fires.  Returns true when the node's day is over. */
+template <class M>
+__device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, double next,
+                                         const double *v, const double *ld, const double *gd,
+                                         const int *sS, const uint32_t *sG)
 {
     constexpr int NC = M::NC, NT = M::NT;
-    unsigned fired = 0;
-    uint64_t c = r.ctr;                       /* draw index of the next waiting time */
-    const uint64_t sbits = si_double_bits(sum);
-    if (!si_finite_pos(sum)) {
-        /* sum <= 0: nothing fires (ssm.c:148-151); a non-finite sum after an
-         * invalid rate, which is recorded, would never reach `next`. */
-        if (!le_zero(sbits) && !err) {
-            err = ERR_INVALID_RATE;
-            err_tr = -1;
-            err_t = t;
-            err_rate = sum;
-        }
-        t = next;
-        return 0;
+    const double tn = ln.tau + ln.t;
+    if (si_dge(tn, next)) {
+        ln.t = next;
+        ln.c += 1;                            /* the waiting time's draw was used */
+        return true;
     }
-    double cum[NT];
-    prefix_sums<M>(rate, cum);
+    ln.t = tn;
+    const double rnd = ln.U * ln.sum;
+    ln.c += 2;
 
-    /* the pair of the first transition */
-    uint32_t p0, p1, p2, p3, q0, q1, q2, q3;
-    philox_block(r, c >> 2, p0, p1, p2, p3);
-    philox_block(r, (c + 1) >> 2, q0, q1, q2, q3);
-    const uint32_t wl0 = word_of(p0, p1, p2, p3, (uint32_t) c & 3u);
-    const uint32_t wu0 = word_of(q0, q1, q2, q3, (uint32_t) (c + 1) & 3u);
-    double L = si_neglog_u32(wl0);
-    double U = si_u32_to_uniform_pos(wu0);
-    /* q holds block (c + 1) >> 2, the one the next pair may start in */
-    double tau = si_div(L, sum);
+    /* Draws of the next transition, off the chain. */
+    {
+        uint32_t n0, n1, n2, n3;
+        philox_block(key, (ln.c + 1) >> 2, n0, n1, n2, n3);
+        const uint32_t ci = (uint32_t) ln.c & 3u;
+        const uint32_t wl = (ci == 3u) ? ln.q3 : word_of(n0, n1, n2, n3, ci);
+        const uint32_t wu = word_of(n0, n1, n2, n3, (ci + 1u) & 3u);
+        ln.q0 = n0;
+        ln.q1 = n1;
+        ln.q2 = n2;
+        ln.q3 = n3;
+        ln.L = si_neglog_u32(wl);
+        ln.U = si_u32_to_uniform_pos(wu);
+    }
 
-    for (;;) {
-        const double tn = tau + t;
-        if (si_dge(tn, next)) {
-            t = next;
-            c += 1;                           /* the waiting time's draw was used */
-            break;
-        }
-        t = tn;
-        const double rnd = U * sum;
-        c += 2;
-
-        /* Draws of the next transition, off the chain. */
-        {
-            uint32_t n0, n1, n2, n3;
-            philox_block(r, (c + 1) >> 2, n0, n1, n2, n3);
-            const uint32_t ci = (uint32_t) c & 3u;
-            const uint32_t wl = (ci == 3u) ? word_of(q0, q1, q2, q3, 3u) : word_of(n0, n1, n2, n3, ci);
-            const uint32_t wu = word_of(n0, n1, n2, n3, (ci + 1u) & 3u);
-            q0 = n0;
-            q1 = n1;
-            q2 = n2;
-            q3 = n3;
-            L = si_neglog_u32(wl);
-            U = si_u32_to_uniform_pos(wu);
-        }
-
-        /* Inversion: the first k with !(rnd > cum[k]), else NT - 1. */
-        int tr = NT - 1;
+    /* Inversion: the first k with !(rnd > cum[k]), else NT - 1. */
+    int tr = NT - 1;
 #pragma unroll
-        for (int k = NT - 2; k >= 0; k--)
-            if (!si_dgt(rnd, cum[k]))
-                tr = k;
-        double rtr = rate[0];
+    for (int k = NT - 2; k >= 0; k--)
+        if (!si_dgt(rnd, ln.cum[k]))
+            tr = k;
+    double rtr = ln.rate[0];
+#pragma unroll
+    for (int k = 1; k < NT; k++)
+        if (tr == k)
+            rtr = ln.rate[k];
+    if (si_is_zero(rtr)) {
+        /* Back-scan to the first non-zero rate (ssm.c:171-189). */
+#pragma unroll
+        for (int k = NT - 1; k >= 1; k--)
+            if (tr == k && si_is_zero(ln.rate[k]))
+                tr = k - 1;
+        double r2 = ln.rate[0];
 #pragma unroll
         for (int k = 1; k < NT; k++)
             if (tr == k)
-                rtr = rate[k];
-        if (si_is_zero(rtr)) {
-            /* Back-scan to the first non-zero rate (ssm.c:171-189). */
-#pragma unroll
-            for (int k = NT - 1; k >= 1; k--)
-                if (tr == k && si_is_zero(rate[k]))
-                    tr = k - 1;
-            double r2 = rate[0];
-#pragma unroll
-            for (int k = 1; k < NT; k++)
-                if (tr == k)
-                    r2 = rate[k];
-            if (si_is_zero(r2)) {
-                sum = 0.0;
-                break;
-            }
+                r2 = ln.rate[k];
+        if (si_is_zero(r2)) {
+            ln.sum = 0.0;
+            return true;
         }
-
-        if (++fired > MAX_NODE_DAY_TRANSITIONS) {
-            /* Bounded work per node-day: a time step that stopped advancing
-             * t (a rate sum near the overflow threshold) ends the run
-             * with an error instead of spinning. */
-            err = ERR_TIMEOUT;
-            err_tr = tr;
-            err_t = t;
-            t = next;
-            break;
-        }
-        int neg = 0;
-#pragma unroll
-        for (int cc = 0; cc < NC; cc++) {
-            const int d = sS[tr * NC + cc];
-            u[cc] += d;
-            neg |= (d != 0) & (u[cc] < 0);
-        }
-        if (neg) {
-            err = ERR_NEGATIVE_STATE;
-            err_tr = tr;
-            err_t = t;
-            err_rate = 0.0;
-        }
-
-        /* Refresh the rates flagged in column tr of G, in row order. */
-        double delta = 0.0;
-        const uint32_t gm = sG[tr];
-        int bad = -1;
-        double bad_rate = 0.0;
-#pragma unroll
-        for (int k = 0; k < NT; k++) {
-            if (gm & (1u << k)) {
-                const double old = rate[k];
-                const double nr = M::rate(k, u, v, ld, gd, t, dc);
-                rate[k] = nr;
-                delta += nr - old;
-                if (si_bad_rate(nr)) {
-                    bad = k;
-                    bad_rate = nr;
-                }
-            }
-        }
-        if (bad >= 0) {
-            err = ERR_INVALID_RATE;
-            err_tr = bad;
-            err_t = t;
-            err_rate = bad_rate;
-        }
-        sum += delta;
-        prefix_sums<M>(rate, cum);
-
-        if (!si_finite_pos(sum)) {
-            if (!le_zero(si_double_bits(sum)) && !err) {
-                err = ERR_INVALID_RATE;
-                err_tr = -1;
-                err_t = t;
-                err_rate = sum;
-            }
-            t = next;
-            break;
-        }
-        tau = si_div(L, sum);
     }
-    r.ctr = c;
+
+    if (++ln.fired > MAX_NODE_DAY_TRANSITIONS) {
+        /* Bounded work per node-day: a time step that stopped advancing t
+         * (a rate sum near the overflow threshold) ends the run with an
+         * error instead of spinning. */
+        ln.err = ERR_TIMEOUT;
+        ln.err_tr = tr;
+        ln.err_t = ln.t;
+        ln.t = next;
+        return true;
+    }
+    int neg = 0;
+#pragma unroll
+    for (int cc = 0; cc < NC; cc++) {
+        const int d = sS[tr * NC + cc];
+        ln.u[cc] += d;
+        neg |= (d != 0) & (ln.u[cc] < 0);
+    }
+    if (neg) {
+        ln.err = ERR_NEGATIVE_STATE;
+        ln.err_tr = tr;
+        ln.err_t = ln.t;
+        ln.err_rate = 0.0;
+    }
+
+    /* Refresh the rates flagged in column tr of G, in row order. */
+    double delta = 0.0;
+    const uint32_t gm = sG[tr];
+    int bad = -1;
+    double bad_rate = 0.0;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        if (gm & (1u << k)) {
+            const double old = ln.rate[k];
+            const double nr = M::rate(k, ln.u, v, ld, gd, ln.t, ln.dc);
+            ln.rate[k] = nr;
+            delta += nr - old;
+            if (si_bad_rate(nr)) {
+                bad = k;
+                bad_rate = nr;
+            }
+        }
+    }
+    if (bad >= 0) {
+        ln.err = ERR_INVALID_RATE;
+        ln.err_tr = bad;
+        ln.err_t = ln.t;
+        ln.err_rate = bad_rate;
+    }
+    ln.sum += delta;
+    prefix_sums<M>(ln.rate, ln.cum);
+
+    if (!si_finite_pos(ln.sum)) {
+        if (!le_zero(si_double_bits(ln.sum)) && !ln.err) {
+            ln.err = ERR_INVALID_RATE;
+            ln.err_tr = -1;
+            ln.err_t = ln.t;
+            ln.err_rate = ln.sum;
+        }
+        ln.t = next;
+        return true;
+    }
+    ln.tau = si_div(ln.L, ln.sum);
+    return false;
+}
+
+/* A node's whole SSA day in one call (used where one thread keeps one
+ * node for the whole run). */
+template <class M>
+__device__ __forceinline__ unsigned ssa_day(SsaLane<M> &ln, si_rng &r, double next,
+                                            const double *v, const double *ld, const double *gd,
+                                            const int *sS, const uint32_t *sG)
+{
+    if (!ssa_begin<M>(ln, r, r.ctr, next))
+        while (!ssa_step<M>(ln, r, next, v, ld, gd, sS, sG)) {
+        }
+    r.ctr = ln.c;
     r.have = 0;
-    return fired;
+    return ln.fired;
 }
 
 /* ------------------------------------------------------------------ */
@@ -680,39 +707,22 @@ __global__ void k_init(DevState s, double tt0)
     push_heavy<M>(s, g, sum, 0);
 }
 
-/* One day of SSA and E1 events.  Blocks [0, HEAVY_BLOCKS) run the heavy
- * nodes listed for this day, one per warp; the remaining blocks run every
- * other (replicate, node) pair, one per thread. */
+/* The end of a node's day: its E1 events (or its SSA error) and the state
+ * written back. */
 template <class M>
-__device__ __forceinline__ void node_day(const DevState &s, long long g, int day, double tt,
-                                         double next, const int *sS, const uint32_t *sG,
-                                         unsigned long long &fired)
+__device__ __forceinline__ void node_finish(const DevState &s, SsaLane<M> &ln, si_rng &r,
+                                            long long g, int day, double tt,
+                                            unsigned long long &fired)
 {
-    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
-    const int node = (int) (g % s.Nn);
-    int u[NC];
-    double rate[NT];
-#pragma unroll
-    for (int c = 0; c < NC; c++)
-        u[c] = s.u[g * NC + c];
-#pragma unroll
-    for (int k = 0; k < NT; k++)
-        rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
-    double sum = s.sum_rate[g], t = s.t_time[g];
-    const double *v = s.vA + g * ND;
-    const double *ld = s.ldata + (size_t) node * s.Nld;
-    int err = 0, err_tr = -1;
-    double err_t = 0, err_rate = 0;
-    si_rng r;
-    si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
-    si_recip dc = si_recip_none();
-    fired += ssa_day<M>(u, rate, sum, t, v, ld, gdata_of(s, g), r, next, sS, sG, dc, err, err_tr,
-                        err_t, err_rate);
-    if (err) {
-        record_error(s, err, PHASE_SSA, day, g, err_tr, -1, err_t, err_rate);
+    constexpr int NC = M::NC, NT = M::NT;
+    r.ctr = ln.c;
+    r.have = 0;
+    fired += ln.fired;
+    if (ln.err) {
+        record_error(s, ln.err, PHASE_SSA, day, g, ln.err_tr, -1, ln.err_t, ln.err_rate);
     } else {
         int e_code = 0, e_idx = -1;
-        const bool upd = node_e1<NC>(s, u, node, day, r, g, tt, e_code, e_idx);
+        const bool upd = node_e1<NC>(s, ln.u, (int) (g % s.Nn), day, r, g, tt, e_code, e_idx);
         if (upd)
             s.update[g] = 1;
         if (e_code)
@@ -720,61 +730,137 @@ __device__ __forceinline__ void node_day(const DevState &s, long long g, int day
     }
 #pragma unroll
     for (int c = 0; c < NC; c++)
-        s.u[g * NC + c] = u[c];
+        s.u[g * NC + c] = ln.u[c];
 #pragma unroll
     for (int k = 0; k < NT; k++)
-        s.t_rate[(size_t) k * s.Ntot + g] = rate[k];
-    s.sum_rate[g] = sum;
-    s.t_time[g] = t;
+        s.t_rate[(size_t) k * s.Ntot + g] = ln.rate[k];
+    s.sum_rate[g] = ln.sum;
+    s.t_time[g] = ln.t;
     s.ctr[g] = r.ctr;
 }
 
+/* One day of SSA and E1 events for every (replicate, node): a persistent
+ * grid whose threads take nodes from the day's work queue, one node per
+ * thread at a time.  The queue has two parts: the heavy nodes (rate sum >=
+ * heavy_rate at the start of the day, heaviest class first) and then every
+ * other node in index order.  Heavy nodes go out 32 to a warp, and a warp
+ * that holds one takes nothing more until they are all done: the day lasts
+ * as long as its longest chain, and work started beside it in the same
+ * warp would stretch that chain.  Ordinary nodes go out lane by lane: a
+ * thread whose node's day is over takes the next entry at once, so the
+ * lanes of a warp keep stepping transitions instead of waiting for the
+ * warp's busiest node.  One atomic per warp hands out the entries. */
 template <class M>
 __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, double tt,
                                                          double next)
 {
-    constexpr int NC = M::NC, NT = M::NT;
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     __shared__ int sS[NT * NC];
     __shared__ uint32_t sG[NT];
     load_model_smem<M>(s, sS, sG);
     const int par = day & 1, npar = (day + 1) & 1;
     if (blockIdx.x == 0 && threadIdx.x < HEAVY_CLASSES)
         s.heavy_count[npar * HEAVY_CLASSES + threadIdx.x] = 0;  /* filled by this day's pts */
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        s.heavy_next[npar] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < 2)
+        s.queue_next[npar * 2 + threadIdx.x] = 0;
     unsigned long long fired = 0;
-    const bool stop = load_flag(s.err_day) < day;
-    if ((int) blockIdx.x < s.heavy_blocks) {
-        if (M::RATES_TIME_INVARIANT && !stop) {
-            int n[HEAVY_CLASSES], total = 0;
+    if (load_flag(s.err_day) < day) {
+        add_fired(s, fired);
+        return;
+    }
+    int n[HEAVY_CLASSES];
+    unsigned long long H = 0;
 #pragma unroll
-            for (int c = 0; c < HEAVY_CLASSES; c++) {
-                n[c] = min(s.heavy_count[par * HEAVY_CLASSES + c], (int) MAX_HEAVY);
-                total += n[c];
-            }
-            const int lane = threadIdx.x & 31;
-            for (;;) {
-                int base = 0;
-                if (lane == 0)
-                    base = atomicAdd(&s.heavy_next[par], 32);
-                base = __shfl_sync(0xFFFFFFFFu, base, 0);
-                if (base >= total)
-                    break;
-                int idx = base + lane;
-                int c = 0;
-                while (c < HEAVY_CLASSES && idx >= n[c]) {
-                    idx -= n[c];
-                    c++;
+    for (int c = 0; c < HEAVY_CLASSES; c++) {
+        n[c] = min(s.heavy_count[par * HEAVY_CLASSES + c], (int) MAX_HEAVY);
+        H += (unsigned long long) n[c];
+    }
+    const unsigned long long Ntot = (unsigned long long) s.Ntot;
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xFFFFFFFFu;
+
+    SsaLane<M> ln;
+    si_rng r;
+    long long g = -1;
+    bool alive = true, need = true, done = false, heavy = false;
+    bool heavy_left = H > 0;         /* warp-uniform: the heavy part may have entries */
+    const double *v = nullptr, *ld = nullptr, *gd = nullptr;
+    for (;;) {
+        /* hand queue entries to the lanes without a node */
+        const unsigned want = __ballot_sync(FULL, alive && need);
+        const bool holds_heavy = __any_sync(FULL, alive && !need && heavy);
+        const bool from_heavy = heavy_left;
+        if (want && !holds_heavy) {
+            const int leader = __ffs(want) - 1;
+            unsigned long long base = 0;
+            if (lane == leader)
+                base = atomicAdd(&s.queue_next[par * 2 + (from_heavy ? 0 : 1)],
+                                 (unsigned long long) __popc(want));
+            base = __shfl_sync(FULL, base, leader);
+            long long cand = -1;
+            bool empty = false;
+            if (alive && need) {
+                const unsigned long long pos = base + __popc(want & ((1u << lane) - 1u));
+                if (from_heavy) {
+                    if (pos < H) {
+                        int idx = (int) pos, c = 0;
+                        while (c < HEAVY_CLASSES - 1 && idx >= n[c]) {
+                            idx -= n[c];
+                            c++;
+                        }
+                        cand = s.heavy_list[(par * HEAVY_CLASSES + c) * MAX_HEAVY + idx];
+                    } else {
+                        empty = true;
+                    }
+                } else if (pos >= Ntot) {
+                    alive = false;
+                } else if (s.heavy_mark[pos] != day + 1) {
+                    cand = (long long) pos;     /* heavy ones come from the heavy part */
                 }
-                if (c < HEAVY_CLASSES)
-                    node_day<M>(s, s.heavy_list[(par * HEAVY_CLASSES + c) * MAX_HEAVY + idx], day,
-                                tt, next, sS, sG, fired);
+            }
+            if (from_heavy && __any_sync(FULL, empty))
+                heavy_left = false;
+            if (cand >= 0) {
+                g = cand;
+                heavy = from_heavy;
+                const int node = (int) (g % s.Nn);
+#pragma unroll
+                for (int c = 0; c < NC; c++)
+                    ln.u[c] = s.u[g * NC + c];
+#pragma unroll
+                for (int k = 0; k < NT; k++)
+                    ln.rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
+                ln.sum = s.sum_rate[g];
+                ln.t = s.t_time[g];
+                ln.err = 0;
+                ln.err_tr = -1;
+                ln.err_t = 0.0;
+                ln.err_rate = 0.0;
+                ln.dc = si_recip_none();
+                si_rng_init(&r, s.seed, (uint64_t) g, 0);
+                v = s.vA + g * ND;
+                ld = s.ldata + (size_t) node * s.Nld;
+                gd = gdata_of(s, g);
+                done = ssa_begin<M>(ln, r, s.ctr[g], next);
+                need = false;
             }
         }
-    } else {
-        const long long g = (blockIdx.x - s.heavy_blocks) * (long long) blockDim.x + threadIdx.x;
-        if (g < s.Ntot && !stop && !(s.heavy_mark[g] == day + 1))
-            node_day<M>(s, g, day, tt, next, sS, sG, fired);
+        if (!__any_sync(FULL, alive))
+            break;
+        if (alive && !need) {
+            if (done) {
+                node_finish<M>(s, ln, r, g, day, tt, fired);
+                need = true;
+                heavy = false;
+            } else if (heavy) {
+                /* a heavy warp has nothing else to do: the whole day in a
+                 * tight loop */
+                while (!done)
+                    done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG);
+            } else {
+                done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG);
+            }
+        }
     }
     add_fired(s, fired);
 }
@@ -882,7 +968,7 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
  * external transfer couples nodes and the post-time-step function reads
  * only its own node. */
 template <class M>
-__global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days, int ndays)
+__global__ void __launch_bounds__(256, 2) k_horizon(DevState s, const DayInfo *days, int ndays)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     __shared__ int sS[NT * NC];
@@ -892,40 +978,41 @@ __global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days
     unsigned long long fired = 0;
     if (g < s.Ntot) {
         const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
-        int u[NC];
-        double rate[NT];
+        SsaLane<M> ln;
 #pragma unroll
         for (int c = 0; c < NC; c++)
-            u[c] = s.u[g * NC + c];
+            ln.u[c] = s.u[g * NC + c];
 #pragma unroll
         for (int k = 0; k < NT; k++)
-            rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
-        double sum = s.sum_rate[g], t = s.t_time[g];
+            ln.rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
+        ln.sum = s.sum_rate[g];
+        ln.t = s.t_time[g];
+        ln.dc = si_recip_none();
         si_rng r;
         si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
         double *v = s.vA + g * ND, *vn = s.vB + g * ND;
         const double *ld = s.ldata + (size_t) node * s.Nld;
         const double *gd = gdata_of(s, g);
-        si_recip dc = si_recip_none();
         for (int d = 0; d < ndays; d++) {
             if (load_flag(s.err_day) < d)
                 break;
             const DayInfo di = days[d];
-            int err = 0, err_tr = -1;
-            double err_t = 0, err_rate = 0;
-            fired += ssa_day<M>(u, rate, sum, t, v, ld, gd, r, di.next, sS, sG, dc, err,
-                                err_tr, err_t, err_rate);
-            if (err) {
-                record_error(s, err, PHASE_SSA, d, g, err_tr, -1, err_t, err_rate);
+            ln.err = 0;
+            ln.err_tr = -1;
+            ln.err_t = 0.0;
+            ln.err_rate = 0.0;
+            fired += ssa_day<M>(ln, r, di.next, v, ld, gd, sS, sG);
+            if (ln.err) {
+                record_error(s, ln.err, PHASE_SSA, d, g, ln.err_tr, -1, ln.err_t, ln.err_rate);
                 break;
             }
             int e_code = 0, e_idx = -1;
-            bool upd = node_e1<NC>(s, u, node, d, r, g, di.tt, e_code, e_idx);
+            bool upd = node_e1<NC>(s, ln.u, node, d, r, g, di.tt, e_code, e_idx);
             if (e_code) {
                 record_error(s, e_code, PHASE_E1, d, g, -1, e_idx, di.tt, 0);
                 break;
             }
-            const int rc = M::pts(vn, u, v, ld, gd, node, di.tt);
+            const int rc = M::pts(vn, ln.u, v, ld, gd, node, di.tt);
             if (rc < 0) {
                 record_error(s, rc, PHASE_PTS, d, g, -1, -1, di.tt, 0);
                 break;
@@ -935,32 +1022,32 @@ __global__ void __launch_bounds__(256) k_horizon(DevState s, const DayInfo *days
                 bool bad = false;
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
-                    const double old = rate[k];
-                    const double nr = M::rate(k, u, vn, ld, gd, di.tt, dc);
-                    rate[k] = nr;
+                    const double old = ln.rate[k];
+                    const double nr = M::rate(k, ln.u, vn, ld, gd, di.tt, ln.dc);
+                    ln.rate[k] = nr;
                     delta += nr - old;
                     if (!isfinite(nr) || nr < 0.0) {
                         record_error(s, ERR_INVALID_RATE, PHASE_PTS, d, g, k, -1, di.tt, nr);
                         bad = true;
                     }
                 }
-                sum += delta;
+                ln.sum += delta;
                 if (bad)
                     break;
             }
-            store_columns<NC, ND>(s, rep, node, u, vn, di.c0, di.c1);
+            store_columns<NC, ND>(s, rep, node, ln.u, vn, di.c0, di.c1);
             double *tmp = v;
             v = vn;
             vn = tmp;
         }
 #pragma unroll
         for (int c = 0; c < NC; c++)
-            s.u[g * NC + c] = u[c];
+            s.u[g * NC + c] = ln.u[c];
 #pragma unroll
         for (int k = 0; k < NT; k++)
-            s.t_rate[(size_t) k * s.Ntot + g] = rate[k];
-        s.sum_rate[g] = sum;
-        s.t_time[g] = t;
+            s.t_rate[(size_t) k * s.Ntot + g] = ln.rate[k];
+        s.sum_rate[g] = ln.sum;
+        s.t_time[g] = ln.t;
         s.ctr[g] = r.ctr;
     }
     add_fired(s, fired);
@@ -1116,10 +1203,25 @@ struct Launch {
         k_horizon<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, days, ndays);
         return cudaGetLastError();
     }
+    /* k_ssa_e1 is persistent: as many blocks as can be resident at once
+     * (looked up once per model), fewer for small models. */
+    static int ssa_resident_blocks()
+    {
+        static int blocks = 0;
+        if (!blocks) {
+            int dev = 0, nsm = 1, per = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ssa_e1<M>, SSA_BLOCK, 0);
+            blocks = nsm * (per > 0 ? per : 1);
+        }
+        return blocks;
+    }
     static cudaError_t ssa_e1(const DevState &s, int day, double tt, double next, cudaStream_t st)
     {
-        k_ssa_e1<M><<<s.heavy_blocks + blocks_for(s.Ntot, SSA_BLOCK), SSA_BLOCK, 0, st>>>(
-            s, day, tt, next);
+        const long long need = (long long) blocks_for(s.Ntot, SSA_BLOCK);
+        const int grid = (int) (need < ssa_resident_blocks() ? need : ssa_resident_blocks());
+        k_ssa_e1<M><<<grid, SSA_BLOCK, 0, st>>>(s, day, tt, next);
         return cudaGetLastError();
     }
     static cudaError_t e2_wave(const DevState &s, const E2Rec *ev, int count, int day, double tt,

@@ -290,8 +290,7 @@ extern "C" int siminf_gpu_run_solver_ssm_noalloc(siminf_gpu_solver_args *a,
     s.err_day = &ctl->err_day;
     s.err_day_pre_e2 = &ctl->err_day_pre_e2;
     s.fired = &ctl->fired;
-    s.heavy_rate = 0.0;          /* the horizon kernel has no heavy-node path */
-    s.heavy_blocks = 0;
+    s.heavy_rate = 0.0;          /* the horizon kernel has no work queue */
     DayInfo *d_days = (DayInfo *) (base + lo.days);
 
     /* Dense S (Nt rows of Nc) and the G column masks, built on the stack. */

@@ -26,15 +26,14 @@ namespace siminf {
 
 enum { MAX_NC = 16, MAX_NT = 32, MAX_ERR = 1024 };
 
-/* Nodes whose rate sum at the start of a day is at least heavy_rate are
- * listed by k_pts_store (k_init for day 0) in a per-day queue, heaviest
- * class first (classes: sum >= 16, 4 and 1 times heavy_rate).  k_ssa_e1's
- * first heavy_blocks blocks are persistent warps that take 32 queued nodes
- * at a time, one per lane, so the day's longest chains start together at
- * the start of the kernel instead of wherever their node's block is
- * scheduled.  At most MAX_HEAVY per class and day; the rest take the
- * ordinary one-thread-per-node blocks. */
-enum { SSA_BLOCK = 128, HEAVY_CLASSES = 3, MAX_HEAVY = 4096 };
+/* k_ssa_e1 is a persistent grid fed by a per-day work queue of nodes: first
+ * the heavy nodes (rate sum >= heavy_rate at the start of the day, listed by
+ * k_pts_store or k_init in classes sum >= 16, 4 and 1 times heavy_rate,
+ * heaviest first), then every node in index order, heavy ones skipped.  So
+ * the day's longest chains start first, and a thread whose node is done
+ * takes the next one.  At most MAX_HEAVY nodes per class and day are
+ * listed; the rest come in index order. */
+enum { SSA_BLOCK = 128, HEAVY_CLASSES = 3, MAX_HEAVY = 32768 };
 
 enum { PHASE_INIT = 0, PHASE_SSA = 1, PHASE_E1 = 2, PHASE_E2 = 3, PHASE_PTS = 4 };
 
@@ -123,10 +122,9 @@ struct DevState {
      * list[((d & 1) * HEAVY_CLASSES + class) * MAX_HEAVY + i] */
     int *heavy_list;
     int *heavy_count;       /* [2][HEAVY_CLASSES] */
-    int *heavy_next;        /* [2]: queue position */
+    unsigned long long *queue_next;  /* [day parity][heavy, ordinary]: next queue entries */
     int *heavy_mark;        /* per g: day + 1 when listed for that day */
-    double heavy_rate;      /* <= 0 disables the heavy path */
-    int heavy_blocks;
+    double heavy_rate;      /* <= 0: no heavy part in the queue */
 };
 
 }  // namespace siminf
