@@ -203,6 +203,39 @@ int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args,
                              const siminf_gpu_options *options);
 
 /*
+ * Many independent models of one device model in one run -- different node
+ * counts, tspan lengths (prefixes of one grid from the same tspan[0]),
+ * events, parameters (ldata/gdata) and seeds -- each reduced on the device
+ * to its prevalence series (sum over its nodes of the compartments in
+ * prevalence_num_mask over those in prevalence_den_mask, at every tspan
+ * point) and the L2 distance of that series to a target.  Replaces the
+ * simulate-then-measure loop of the reference's ABC samplers
+ * (R/abc.R:589-628 for gdata proposals, :675-729 for ldata proposals),
+ * which calls run() once per proposal.  Each model's trajectory is the one
+ * siminf_gpu_run_solver_ssm gives it alone with its own seed; the models
+ * must share E and N (the model's select and shift matrices).  Returns 0
+ * or an error code; an error in one model stops the batch and the status
+ * names the model.
+ */
+typedef struct siminf_gpu_batch_job {
+    siminf_gpu_solver_args *args;   /* one model, Nrep = 1; its U/V are not written */
+    const double *target;           /* tlen prevalence values, or NULL */
+    double *prevalence;             /* out: tlen values, or NULL */
+    double *distance;               /* out: L2 distance to target (0 without one), or NULL */
+} siminf_gpu_batch_job;
+
+typedef struct siminf_gpu_batch_options {
+    unsigned prevalence_num_mask;   /* compartments (bit c) summed in the numerator */
+    unsigned prevalence_den_mask;   /* compartments summed in the denominator */
+    int cap_transfers;              /* as in siminf_gpu_options */
+    int heavy_rate;                 /* as in siminf_gpu_options */
+    int reserved[4];
+} siminf_gpu_batch_options;
+
+int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs, const siminf_gpu_model *model,
+                         const siminf_gpu_batch_options *options);
+
+/*
  * siminf_gpu_run_solver_ssm without allocating: no counterpart in the
  * reference, which allocates its solver state on every run.  For callers
  * that cannot allocate when they run a trajectory: a process whose device

@@ -135,6 +135,27 @@ class PfilterArgs(C.Structure):
     ]
 
 
+class BatchJob(C.Structure):
+    """siminf_gpu_batch_job."""
+    _fields_ = [
+        ("args", C.c_void_p),
+        ("target", C.POINTER(C.c_double)),
+        ("prevalence", C.POINTER(C.c_double)),
+        ("distance", C.POINTER(C.c_double)),
+    ]
+
+
+class BatchOptions(C.Structure):
+    """siminf_gpu_batch_options."""
+    _fields_ = [
+        ("prevalence_num_mask", C.c_uint),
+        ("prevalence_den_mask", C.c_uint),
+        ("cap_transfers", C.c_int),
+        ("heavy_rate", C.c_int),
+        ("reserved", C.c_int * 4),
+    ]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("transitions", C.c_uint64),

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # reference's C (bit-identical trajectories).
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off"]
-SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp", "siminf_noalloc.cu"]
+SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp", "siminf_noalloc.cu", "siminf_batch.cu"]
 
 
 def nvcc():

@@ -106,54 +106,6 @@ double ms_since(std::chrono::steady_clock::time_point t0)
 
 }  // namespace
 
-/* A planned failure: an event the device cannot apply (bad node, dest or
- * kind) that the reference would reject when it reaches it. */
-struct PlannedErr {
-    int day, code, index, node, phase;
-};
-
-struct siminf_gpu_plan {
-    const Launchers *L = nullptr;
-    DevState s{};
-    cudaStream_t stream = nullptr;
-    std::vector<void *> owned;
-
-    int ndays = 0;
-    std::vector<DayInfo> days;
-    DayInfo *d_days = nullptr;
-    bool horizon = false;
-
-    /* E2 waves */
-    E2Rec *d_e2 = nullptr;
-    std::vector<long long> wave_ptr;    /* offsets into d_e2, one past the last */
-    std::vector<int> day_wave;          /* ndays + 1 */
-    uint64_t e1_count = 0, e2_count = 0;
-
-    std::vector<PlannedErr> planned;
-
-    /* host-side copies needed to write results back */
-    size_t U_len = 0, V_len = 0, prU_len = 0, prV_len = 0;
-    int *d_u0 = nullptr;            /* device copy of the initial state */
-    double *d_v0 = nullptr;
-    double tt0 = 0;
-
-    siminf_gpu_stats stats{};
-    bool ran = false;
-    int days_cap = 0;
-
-    /* E2 planning state: events of day d go to positions e2_day_off[d] ..
-     * e2_day_off[d + 1] of d_e2 and come from input range e2_lo[d] ..
-     * e2_hi[d]; day_waves[d] holds the day's wave sizes. */
-    int nsel = 0;
-    std::vector<long long> e2_day_off, e2_lo, e2_hi;
-    std::vector<std::vector<long long>> day_waves;
-    /* Streamed runs: the waves are planned on host threads while the GPU
-     * runs earlier days; the caller's arrays stay valid until the run. */
-    bool e2_pending = false;
-    siminf_gpu_solver_args args{};
-    std::unique_ptr<E2Rec[]> h_e2;
-};
-
 static int validate(const siminf_gpu_solver_args *a, const Launchers *L)
 {
     char msg[256];
@@ -203,7 +155,48 @@ static int validate(const siminf_gpu_solver_args *a, const Launchers *L)
     return 0;
 }
 
+extern "C" {
+static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
+                            const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream,
+                            bool no_output);
+static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, struct KernelProfile *kp);
+}
+static int make_days(siminf_gpu_plan *p, const siminf_gpu_solver_args *a);
+template <class T>
+static int upload_owned(siminf_gpu_plan *p, T **dst, const T *src, size_t n);
+
 namespace siminf {
+
+int plan_create_internal(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
+                         const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream,
+                         bool no_output)
+{
+    return plan_create_impl(a, model, opt, out, stream, no_output);
+}
+
+int plan_run_internal(siminf_gpu_plan *p, cudaStream_t st)
+{
+    return plan_run_impl(p, st, nullptr);
+}
+
+int plan_upload(siminf_gpu_plan *p, void **dst, const void *src, size_t bytes)
+{
+    unsigned char *d = nullptr;
+    const int rc = upload_owned(p, &d, (const unsigned char *) src, bytes);
+    *dst = d;
+    return rc;
+}
+
+int plan_days(const double *tspan, int tlen, std::vector<DayInfo> &days)
+{
+    siminf_gpu_plan p;
+    siminf_gpu_solver_args a{};
+    a.tspan = tspan;
+    a.tlen = tlen;
+    const int rc = make_days(&p, &a);
+    days = p.days;
+    return rc;
+}
 
 int capi_validate(const siminf_gpu_solver_args *a, const Launchers *L)
 {
@@ -227,6 +220,16 @@ int capi_cuda_fail(cudaError_t e, const char *what)
 }
 
 }  // namespace siminf
+
+template <class T>
+static int upload_owned(siminf_gpu_plan *p, T **dst, const T *src, size_t n)
+{
+    const int rc = upload(dst, src, n, p->owned, nullptr);
+    if (rc)
+        return rc;
+    const cudaError_t e = cudaStreamSynchronize(nullptr);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "upload");
+}
 
 /* Day index whose event pass applies an event at `time`. */
 static inline long long event_day(int time, double tt0)
@@ -567,7 +570,8 @@ void siminf_gpu_plan_free(siminf_gpu_plan *p)
 }
 
 static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
-                            const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream);
+                            const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream,
+                            bool no_output = false);
 
 int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
                               const siminf_gpu_options *opt, siminf_gpu_plan **out)
@@ -582,7 +586,8 @@ int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_mod
 }
 
 static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
-                            const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream)
+                            const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream,
+                            bool no_output)
 {
     auto t0 = std::chrono::steady_clock::now();
     int rc;
@@ -596,6 +601,14 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
         return SIMINF_GPU_ERR_NO_DEVICE;
     }
     const Launchers *L = model->L;
+    siminf_gpu_solver_args checked;
+    if (no_output && a) {
+        /* no U/V wanted: the output checks pass on a stand-in */
+        static int stand_in;
+        checked = *a;
+        checked.U = &stand_in;
+        a = &checked;
+    }
     if ((rc = validate(a, L)))
         return rc;
 
@@ -747,7 +760,7 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     }
 
     /* outputs */
-    if (!rc) {
+    if (!rc && !no_output) {
         if (a->U) {
             p->U_len = (size_t) Nn * Nc * (size_t) Nrep * tlen;
             rc = dalloc(&s.U, p->U_len, own);
@@ -762,7 +775,7 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
             s.irU = dir;
         }
     }
-    if (!rc && Nd > 0) {
+    if (!rc && Nd > 0 && !no_output) {
         if (a->V) {
             p->V_len = (size_t) Nn * Nd * (size_t) Nrep * tlen;
             rc = dalloc(&s.V, p->V_len, own);

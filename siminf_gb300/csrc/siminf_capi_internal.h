@@ -6,10 +6,14 @@
 #ifndef SIMINF_CAPI_INTERNAL_H
 #define SIMINF_CAPI_INTERNAL_H
 
+#include <memory>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "../../include/siminf_gb300.h"
 #include "siminf_launch.h"
+#include "siminf_plan.h"
 
 /* A device model: its name and the launchers of its kernels. */
 struct siminf_gpu_model {
@@ -17,7 +21,77 @@ struct siminf_gpu_model {
     const siminf::Launchers *L;
 };
 
+using siminf::DayInfo;
+using siminf::DevState;
+using siminf::E2Rec;
+using siminf::Launchers;
+
+/* A planned failure: an event the device cannot apply (bad node, dest or
+ * kind) that the reference would reject when it reaches it. */
+struct PlannedErr {
+    int day, code, index, node, phase;
+};
+
+struct siminf_gpu_plan {
+    const Launchers *L = nullptr;
+    DevState s{};
+    cudaStream_t stream = nullptr;
+    std::vector<void *> owned;
+
+    int ndays = 0;
+    std::vector<DayInfo> days;
+    DayInfo *d_days = nullptr;
+    bool horizon = false;
+
+    /* E2 waves */
+    E2Rec *d_e2 = nullptr;
+    std::vector<long long> wave_ptr;    /* offsets into d_e2, one past the last */
+    std::vector<int> day_wave;          /* ndays + 1 */
+    uint64_t e1_count = 0, e2_count = 0;
+
+    std::vector<PlannedErr> planned;
+
+    /* host-side copies needed to write results back */
+    size_t U_len = 0, V_len = 0, prU_len = 0, prV_len = 0;
+    int *d_u0 = nullptr;            /* device copy of the initial state */
+    double *d_v0 = nullptr;
+    double tt0 = 0;
+
+    siminf_gpu_stats stats{};
+    bool ran = false;
+    int days_cap = 0;
+
+    /* E2 planning state: events of day d go to positions e2_day_off[d] ..
+     * e2_day_off[d + 1] of d_e2 and come from input range e2_lo[d] ..
+     * e2_hi[d]; day_waves[d] holds the day's wave sizes. */
+    int nsel = 0;
+    std::vector<long long> e2_day_off, e2_lo, e2_hi;
+    std::vector<std::vector<long long>> day_waves;
+    /* Streamed runs: the waves are planned on host threads while the GPU
+     * runs earlier days; the caller's arrays stay valid until the run. */
+    bool e2_pending = false;
+    siminf_gpu_solver_args args{};
+    std::unique_ptr<E2Rec[]> h_e2;
+};
+
 namespace siminf {
+
+/* Create a plan: validate, plan the schedule and upload.  stream: leave
+ * the external transfers' waves to the first run, which plans them beside
+ * the GPU.  no_output: allocate no U/V (the caller reads results some
+ * other way), whatever args->U says. */
+int plan_create_internal(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
+                         const siminf_gpu_options *opt, siminf_gpu_plan **out, bool stream,
+                         bool no_output);
+
+/* Run a plan on stream st (waits for it; returns 0 or the run's error). */
+int plan_run_internal(siminf_gpu_plan *p, cudaStream_t st);
+
+/* Upload n elements into a new device buffer the plan owns. */
+int plan_upload(siminf_gpu_plan *p, void **dst, const void *src, size_t bytes);
+
+/* The day schedule of tspan (src/solvers/SimInf_solver_ssm.c:305-334). */
+int plan_days(const double *tspan, int tlen, std::vector<DayInfo> &days);
 
 /* The checks siminf_gpu_run_solver_ssm applies to its arguments. */
 int capi_validate(const siminf_gpu_solver_args *a, const Launchers *L);

@@ -73,7 +73,30 @@ __device__ __forceinline__ void record_error(const DevState &s, int code, int ph
 
 __device__ __forceinline__ const double *gdata_of(const DevState &s, long long g)
 {
+    if (s.job_of)
+        return s.gdata + (size_t) s.job_of[g] * s.gdata_stride;
     return s.gdata + (size_t) (g / s.Nn) * s.gdata_stride;
+}
+
+/* Key of node g's stream: (seed, replicate * Nn + node) for one model, the
+ * job's own seed and local node index in a batch. */
+__device__ __forceinline__ void stream_key(const DevState &s, long long g, uint64_t &seed,
+                                           uint64_t &sid)
+{
+    if (s.job_of) {
+        const int j = s.job_of[g];
+        seed = s.job_seed[j];
+        sid = (uint64_t) (g - s.job_node0[j]);
+    } else {
+        seed = s.seed;
+        sid = (uint64_t) g;
+    }
+}
+
+/* Node g's model has run all its days (batches only). */
+__device__ __forceinline__ bool job_over(const DevState &s, long long g, int day)
+{
+    return s.job_of && day >= s.job_ndays[s.job_of[g]];
 }
 
 __device__ __forceinline__ int load_flag(const int *p)
@@ -817,6 +840,8 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
                 } else if (s.heavy_mark[pos] != day + 1) {
                     cand = (long long) pos;     /* heavy ones come from the heavy part */
                 }
+                if (cand >= 0 && job_over(s, cand, day))
+                    cand = -1;                  /* its model has run all its days */
             }
             if (from_heavy && __any_sync(FULL, empty))
                 heavy_left = false;
@@ -837,7 +862,11 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
                 ln.err_t = 0.0;
                 ln.err_rate = 0.0;
                 ln.dc = si_recip_none();
-                si_rng_init(&r, s.seed, (uint64_t) g, 0);
+                {
+                    uint64_t seed, sid;
+                    stream_key(s, g, seed, sid);
+                    si_rng_init(&r, seed, sid, 0);
+                }
                 v = s.vA + g * ND;
                 ld = s.ldata + (size_t) node * s.Nld;
                 gd = gdata_of(s, g);
@@ -883,7 +912,11 @@ __global__ void __launch_bounds__(256) k_e2_wave(DevState s, const E2Rec *ev, in
     for (int c = 0; c < NC; c++)
         uu[c] = s.u[gs * NC + c];
     si_rng r;
-    si_rng_init(&r, s.seed, (uint64_t) gs, s.ctr[gs]);
+    {
+        uint64_t seed, sid;
+        stream_key(s, gs, seed, sid);
+        si_rng_init(&r, seed, sid, s.ctr[gs]);
+    }
     int err = sample_select<NC>(s, uu, e.select, e.n, e.proportion, ind, &r);
     s.ctr[gs] = r.ctr;
     if (err) {
@@ -925,13 +958,37 @@ __global__ void __launch_bounds__(256) k_e2_wave(DevState s, const E2Rec *ev, in
     s.update[gs] = 1;
 }
 
+/* Batches: node g's share of its job's prevalence sums at columns c0 ..
+ * c1 - 1 (integer sums, so the order of the additions does not matter). */
+template <int NC>
+__device__ __forceinline__ void add_prevalence(const DevState &s, long long g, const int (&u)[NC],
+                                               int c0, int c1)
+{
+    const int j = s.job_of[g];
+    unsigned long long num = 0, den = 0;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const unsigned long long x = (unsigned long long) (long long) u[c];
+        if (s.prev_num_mask & (1u << c))
+            num += x;
+        if (s.prev_den_mask & (1u << c))
+            den += x;
+    }
+    const int tl = s.job_tlen[j];
+    for (int col = c0; col < c1 && col < tl; col++) {
+        unsigned long long *p = s.prev + 2 * (s.job_col0[j] + col);
+        atomicAdd(p, num);
+        atomicAdd(p + 1, den);
+    }
+}
+
 template <class M>
 __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double tt, int c0, int c1,
                                                    const double *v_in, double *v_out)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (g >= s.Ntot || load_flag(s.err_day) < day)
+    if (g >= s.Ntot || load_flag(s.err_day) < day || job_over(s, g, day))
         return;
     const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
     int u[NC];
@@ -960,15 +1017,18 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
         s.sum_rate[g] += delta;
         s.update[g] = 0;
     }
-    push_heavy<M>(s, g, s.sum_rate[g], day + 1);
+    if (!job_over(s, g, day + 1))
+        push_heavy<M>(s, g, s.sum_rate[g], day + 1);
     store_columns<NC, ND>(s, rep, node, u, vo, c0, c1);
+    if (s.prev && c1 > c0)
+        add_prevalence<NC>(s, g, u, c0, c1);
 }
 
 /* Whole horizon of one (replicate, node) in one thread: valid when no
  * external transfer couples nodes and the post-time-step function reads
  * only its own node. */
 template <class M>
-__global__ void __launch_bounds__(256, 2) k_horizon(DevState s, const DayInfo *days, int ndays)
+__global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s, const DayInfo *days, int ndays)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     __shared__ int sS[NT * NC];
@@ -989,7 +1049,11 @@ __global__ void __launch_bounds__(256, 2) k_horizon(DevState s, const DayInfo *d
         ln.t = s.t_time[g];
         ln.dc = si_recip_none();
         si_rng r;
-        si_rng_init(&r, s.seed, (uint64_t) g, s.ctr[g]);
+        {
+            uint64_t seed, sid;
+            stream_key(s, g, seed, sid);
+            si_rng_init(&r, seed, sid, s.ctr[g]);
+        }
         double *v = s.vA + g * ND, *vn = s.vB + g * ND;
         const double *ld = s.ldata + (size_t) node * s.Nld;
         const double *gd = gdata_of(s, g);

@@ -125,6 +125,23 @@ struct DevState {
     unsigned long long *queue_next;  /* [day parity][heavy, ordinary]: next queue entries */
     int *heavy_mark;        /* per g: day + 1 when listed for that day */
     double heavy_rate;      /* <= 0: no heavy part in the queue */
+
+    /* Batches of independent models (siminf_gpu_run_batch); job_of is NULL
+     * for a single model.  Node g belongs to job j = job_of[g], whose nodes
+     * start at job_node0[j]: its stream key is (job_seed[j], g -
+     * job_node0[j]), as in a run of that model alone, its gdata row is j,
+     * and it runs job_ndays[j] days.  At every stored column col <
+     * job_tlen[j], the sums over the job's nodes of the compartments in
+     * prev_num_mask and prev_den_mask are added to prev[2 * (job_col0[j] +
+     * col)] and prev[2 * (job_col0[j] + col) + 1]. */
+    const int *job_of;
+    const long long *job_node0;
+    const uint64_t *job_seed;
+    const int *job_ndays;
+    const int *job_tlen;
+    const long long *job_col0;
+    unsigned long long *prev;
+    uint32_t prev_num_mask, prev_den_mask;
 };
 
 }  // namespace siminf

@@ -35,6 +35,9 @@ def lib():
         getattr(L, name).restype = C.c_int
     L.siminf_gpu_run_solver_ssm_noalloc.argtypes = [vp, vp, vp]
     L.siminf_gpu_run_solver_ssm_noalloc.restype = C.c_int
+    L.siminf_gpu_run_batch.argtypes = [C.POINTER(abi.BatchJob), C.c_int, vp,
+                                       C.POINTER(abi.BatchOptions)]
+    L.siminf_gpu_run_batch.restype = C.c_int
     L.siminf_gpu_run_solver_ex.argtypes = [vp, vp, C.POINTER(abi.Options)]
     L.siminf_gpu_run_solver_ex.restype = C.c_int
     L.siminf_gpu_plan_create_ex.argtypes = [vp, vp, C.POINTER(abi.Options), C.POINTER(vp)]
@@ -67,7 +70,7 @@ EXPORTS = (
     "siminf_gpu_last_stats", "siminf_gpu_plan_create", "siminf_gpu_plan_run",
     "siminf_gpu_plan_download", "siminf_gpu_plan_stats", "siminf_gpu_plan_free",
     "siminf_gpu_plan_profile", "siminf_gpu_schedule", "siminf_gpu_pfilter",
-    "siminf_gpu_run_solver_ssm_noalloc",
+    "siminf_gpu_run_solver_ssm_noalloc", "siminf_gpu_run_batch",
 )
 
 

@@ -97,3 +97,49 @@ def pfilter(model, n_particles, obs_time, obs, obs_compartment, detect_p, seed=4
                                                  native.device_model(m.name).handle,
                                                  C.byref(pa)))
     return PfilterResult(float(ll[0]), ess, anc, pa.ms_total)
+
+
+def compartment_mask(model, names_or_indices):
+    """Bit mask of compartments given by index or by u0 row position."""
+    mask = 0
+    for c in names_or_indices:
+        mask |= 1 << int(c)
+    return mask
+
+
+def run_batch(models, seeds, targets=None, numerator=(2,), denominator=None,
+              cap_transfers=False):
+    """Many independent models of one device model in one run
+    (siminf_gpu_run_batch): returns (prevalence series, distances).
+
+    Prevalence at tspan point k of model j is the sum over its nodes of the
+    compartments in ``numerator`` over the sum of those in ``denominator``
+    (default: all); the distance is the L2 norm of prevalence - target.
+    Each model's trajectory is the one run(model, seed) gives it alone; this
+    replaces the one-run-per-proposal loop of R/abc.R:589-628 / :675-729.
+    """
+    n = len(models)
+    name = models[0].name
+    holders = [abi.build_args(m, int(s)) for m, s in zip(models, seeds)]
+    prevs = [np.zeros(len(m.tspan)) for m in models]
+    dists = np.zeros(n)
+    tgts = [None] * n
+    jobs = (abi.BatchJob * n)()
+    dptr = C.POINTER(C.c_double)
+    for j in range(n):
+        jobs[j].args = C.cast(holders[j].ref(), C.c_void_p)
+        if targets is not None and targets[j] is not None:
+            tgts[j] = np.ascontiguousarray(targets[j], dtype=np.float64)
+            if len(tgts[j]) != len(models[j].tspan):
+                raise ValueError("target %d needs %d values" % (j, len(models[j].tspan)))
+            jobs[j].target = tgts[j].ctypes.data_as(dptr)
+        jobs[j].prevalence = prevs[j].ctypes.data_as(dptr)
+        jobs[j].distance = C.cast(C.c_void_p(dists.ctypes.data + 8 * j), dptr)
+    den = range(models[0].Nc) if denominator is None else denominator
+    opt = abi.BatchOptions(prevalence_num_mask=compartment_mask(models[0], numerator),
+                           prevalence_den_mask=compartment_mask(models[0], den),
+                           cap_transfers=int(bool(cap_transfers)))
+    code = native.lib().siminf_gpu_run_batch(jobs, n, native.device_model(name).handle,
+                                             C.byref(opt))
+    native.check(code)
+    return prevs, dists
