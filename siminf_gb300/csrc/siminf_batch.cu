@@ -19,10 +19,13 @@
  * the batch; the status names the model and its local node.
  */
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -82,6 +85,11 @@ extern "C" int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs,
                                     const siminf_gpu_batch_options *opt)
 {
     capi_clear_status();
+    const auto t0 = std::chrono::steady_clock::now();
+    auto ms_since = [](std::chrono::steady_clock::time_point a) {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a)
+            .count();
+    };
     if (!jobs || njobs < 1 || !model || !model->L)
         return fail(SIMINF_GPU_ERR_INVALID_MODEL, "no jobs or no device model");
     const Launchers *L = model->L;
@@ -198,10 +206,24 @@ extern "C" int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs,
     }
 
     /* Events: stable counting sort by (time, E2 after E1), each model's own
-     * order kept, events past a model's horizon dropped. */
-    long long nev = 0;
-    int tmin = INT_MAX, tmax = INT_MIN;
-    for (int j = 0; j < njobs; j++) {
+     * order kept, events past a model's horizon dropped.  Keys are counted
+     * per model on host threads, offsets run key-major then model-major,
+     * and every model then writes its own events. */
+    const int nthreads = std::max(1, std::min(njobs, (int) std::thread::hardware_concurrency()));
+    std::vector<int> jmin(njobs, INT_MAX), jmax(njobs, INT_MIN), jbad(njobs, 0);
+    std::vector<long long> jcount(njobs, 0);
+    auto for_jobs = [&](auto &&f) {
+        std::atomic<int> next(0);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nthreads; t++)
+            th.emplace_back([&]() {
+                for (int j = next++; j < njobs; j = next++)
+                    f(j);
+            });
+        for (auto &x : th)
+            x.join();
+    };
+    for_jobs([&](int j) {
         const siminf_gpu_solver_args *a = jobs[j].args;
         for (int i = 0; i < a->len; i++) {
             if (event_day(a->time[i]) >= ndays[j])
@@ -209,43 +231,60 @@ extern "C" int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs,
             const bool e2 = a->event[i] == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT;
             if (a->node[i] < 1 || a->node[i] > a->Nn ||
                 (e2 && (a->dest[i] < 1 || a->dest[i] > a->Nn))) {
-                snprintf(msg, sizeof(msg), "batch job %d: event %d names a node outside it", j,
-                         i + 1);
-                return fail(e2 ? SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS
-                               : SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, msg);
+                if (!jbad[j])
+                    jbad[j] = (e2 && a->node[i] >= 1 && a->node[i] <= a->Nn) ? -(i + 1) : i + 1;
+                continue;
             }
-            tmin = std::min(tmin, a->time[i]);
-            tmax = std::max(tmax, a->time[i]);
-            nev++;
+            jmin[j] = std::min(jmin[j], a->time[i]);
+            jmax[j] = std::max(jmax[j], a->time[i]);
+            jcount[j]++;
         }
+    });
+    long long nev = 0;
+    int tmin = INT_MAX, tmax = INT_MIN;
+    for (int j = 0; j < njobs; j++) {
+        if (jbad[j]) {
+            snprintf(msg, sizeof(msg), "batch job %d: event %d names a node outside it", j,
+                     std::abs(jbad[j]));
+            return fail(jbad[j] < 0 ? SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS
+                                    : SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, msg);
+        }
+        nev += jcount[j];
+        tmin = std::min(tmin, jmin[j]);
+        tmax = std::max(tmax, jmax[j]);
     }
     std::vector<int> ev_event(nev), ev_time(nev), ev_node(nev), ev_dest(nev), ev_n(nev),
         ev_select(nev), ev_shift(nev);
     std::vector<double> ev_prop(nev);
     if (nev > 0) {
         const long long nkeys = 2 * ((long long) tmax - tmin + 1);
-        if (nkeys > 100000000)
+        if (nkeys * njobs > 400000000LL)
             return fail(SIMINF_GPU_ERR_INVALID_MODEL, "batch event times span too wide a range");
-        std::vector<long long> off(nkeys + 1, 0);
         auto key = [&](const siminf_gpu_solver_args *a, int i) {
             return 2 * ((long long) a->time[i] - tmin) +
                    (a->event[i] == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT ? 1 : 0);
         };
-        for (int j = 0; j < njobs; j++) {
+        /* off[key * njobs + j]: first position of model j's events with key */
+        std::vector<long long> off((size_t) nkeys * njobs, 0);
+        for_jobs([&](int j) {
             const siminf_gpu_solver_args *a = jobs[j].args;
             for (int i = 0; i < a->len; i++)
                 if (event_day(a->time[i]) < ndays[j])
-                    off[key(a, i) + 1]++;
+                    off[(size_t) key(a, i) * njobs + j]++;
+        });
+        long long run = 0;
+        for (size_t k = 0; k < off.size(); k++) {
+            const long long c = off[k];
+            off[k] = run;
+            run += c;
         }
-        for (long long k = 0; k < nkeys; k++)
-            off[k + 1] += off[k];
-        for (int j = 0; j < njobs; j++) {
+        for_jobs([&](int j) {
             const siminf_gpu_solver_args *a = jobs[j].args;
             const int base = (int) node0[j];
             for (int i = 0; i < a->len; i++) {
                 if (event_day(a->time[i]) >= ndays[j])
                     continue;
-                const long long at = off[key(a, i)]++;
+                const long long at = off[(size_t) key(a, i) * njobs + j]++;
                 const bool e2 = a->event[i] == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT;
                 ev_event[at] = a->event[i];
                 ev_time[at] = a->time[i];
@@ -256,7 +295,7 @@ extern "C" int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs,
                 ev_select[at] = a->select[i];
                 ev_shift[at] = a->shift[i];
             }
-        }
+        });
     }
 
     siminf_gpu_solver_args m = *T;
@@ -291,8 +330,10 @@ extern "C" int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs,
     siminf_gpu_options o{};
     o.cap_transfers = opt ? opt->cap_transfers : 0;
     o.heavy_rate = opt ? opt->heavy_rate : 0;
+    const double ms_merge = ms_since(t0);
     siminf_gpu_plan *p = nullptr;
-    int rc = plan_create_internal(&m, model, &o, &p, false, true);
+    /* streamed: the external transfers' waves are planned beside the GPU */
+    int rc = plan_create_internal(&m, model, &o, &p, true, true);
     if (rc)
         return rc;
 
@@ -371,6 +412,11 @@ extern "C" int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs,
             }
         }
     }
+    siminf_gpu_stats st = p->stats;
+    st.ms_plan += ms_merge;
+    st.ms_upload += ms_merge;
+    st.ms_download = ms_since(t0) - st.ms_upload - st.ms_solve;
+    capi_set_stats(st);
     siminf_gpu_plan_free(p);
     return rc;
 }

@@ -209,6 +209,11 @@ void capi_set_status(int code, int node, int tr, int evi, double time, double ra
     set_status(code, node, tr, evi, time, rate, msg);
 }
 
+void capi_set_stats(const siminf_gpu_stats &st)
+{
+    g_stats = st;
+}
+
 void capi_clear_status()
 {
     memset(&g_status, 0, sizeof(g_status));

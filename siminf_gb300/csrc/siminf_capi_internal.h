@@ -101,6 +101,9 @@ void capi_set_status(int code, int node, int tr, int evi, double time, double ra
                      const char *msg);
 void capi_clear_status();
 
+/* Record the calling thread's run statistics (siminf_gpu_last_stats). */
+void capi_set_stats(const siminf_gpu_stats &st);
+
 /* Record a failed CUDA call; returns SIMINF_GPU_ERR_CUDA. */
 int capi_cuda_fail(cudaError_t e, const char *what);
 

@@ -25,6 +25,13 @@ examples that need R), so every workload is generated here from fixed seeds.
   reference would instead stop with "Unable to sample individuals for
   event."
   Seeds: 1 graph, 2 u0, 3 events.
+- ``abc_models`` -- the ABC workload over uneven models: SEIR as in
+  ``seir_events`` with node counts drawn from {100, 1000, 10000, 50000}
+  (weights 0.4, 0.3, 0.2, 0.1), tspan 1..T with T ~ U{60, 365}, events and
+  graph scaled to the node count (transfers per day = Nn / 2), parameters
+  from the priors beta ~ U(0.05, 0.5), epsilon ~ U(0.1, 0.5), gamma ~
+  U(0.02, 0.2).  The target is the prevalence I/N of one such model run
+  with seed 7.  Generated day-vectorised from one seed per model.
 - ``sise_pfilter`` -- the particle-filter workload: mparse SISe
   ("S -> upsilon*phi*S -> I", "I -> gamma*I -> S", phi <- phi*(1-0.03) +
   0.05*I/(S+I)), `nodes` nodes with S ~ Poisson(100), I ~ Bernoulli(0.05) *
@@ -96,6 +103,72 @@ def seir_events(nodes=1_000_000, days=365, transfers=500_000, p_enter=0.002, p_e
     ev["shift"] = np.zeros(total, np.int32)
     return M.SEIR(u0, np.arange(1, days + 1, dtype=float), beta=0.16, epsilon=0.25,
                   gamma=0.077, events=ev)
+
+
+def seir_events_fast(nodes, days, transfers, rng, beta=0.16, epsilon=0.25, gamma=0.077,
+                     p_enter=0.002, p_exit=0.002, tspan0=1):
+    """``seir_events`` generated with whole-horizon draws instead of a loop
+    over days (same distributions, different draws)."""
+    S = rng.poisson(300, nodes)
+    I = rng.poisson(3, nodes) * (rng.random(nodes) < 0.01)
+    u0 = np.vstack([S, np.zeros(nodes), I, np.zeros(nodes)]).astype(np.int32)
+    a = 1.1
+    edges = 4 * transfers
+    K = float(np.sqrt(edges))
+    w = (1.0 - rng.random(nodes) * (1.0 - K ** -a)) ** (-1.0 / a)
+    gsrc = rng.integers(0, nodes, edges).astype(np.int32)
+    gdst = rng.choice(nodes, size=edges, p=w / w.sum()).astype(np.int32)
+    same = gsrc == gdst
+    gdst[same] = (gdst[same] + 1) % nodes
+    t_days = np.arange(tspan0, tspan0 + days, dtype=np.int32)
+    ex_t, ex_n = np.nonzero(rng.random((days, nodes)) < p_exit)
+    en_t, en_n = np.nonzero(rng.random((days, nodes)) < p_enter)
+    pick = rng.integers(0, edges, (days, transfers))
+    tr_n = (1 + rng.poisson(3, (days, transfers))).astype(np.int32)
+    # per day: exits, enters, transfers (the order R/SimInf_events.R:398 gives)
+    kinds = [(ex_t, ex_n, 0), (en_t, en_n, 1)]
+    parts = {k: [] for k in ("event", "time", "node", "dest", "n", "select")}
+    order_key = []
+    for tt, nn, kind in kinds:
+        parts["event"].append(np.full(len(tt), kind, np.int32))
+        parts["time"].append(t_days[tt])
+        parts["node"].append((nn + 1).astype(np.int32))
+        parts["dest"].append(np.zeros(len(tt), np.int32))
+        parts["n"].append(np.ones(len(tt), np.int32))
+        parts["select"].append(np.full(len(tt), 2 if kind == 0 else 1, np.int32))
+        order_key.append(tt.astype(np.int64) * 3 + kind)
+    td = np.repeat(np.arange(days), transfers)
+    parts["event"].append(np.full(td.size, 3, np.int32))
+    parts["time"].append(t_days[td])
+    parts["node"].append(gsrc[pick.reshape(-1)] + 1)
+    parts["dest"].append(gdst[pick.reshape(-1)] + 1)
+    parts["n"].append(tr_n.reshape(-1))
+    parts["select"].append(np.full(td.size, 2, np.int32))
+    order_key.append(td.astype(np.int64) * 3 + 2)
+    order = np.argsort(np.concatenate(order_key), kind="stable")
+    ev = {k: np.concatenate(v)[order] for k, v in parts.items()}
+    ev["proportion"] = np.zeros(len(order))
+    ev["shift"] = np.zeros(len(order), np.int32)
+    return M.SEIR(u0, np.arange(tspan0, tspan0 + days, dtype=float), beta=beta,
+                  epsilon=epsilon, gamma=gamma, events=ev)
+
+
+def abc_models(n, seed=11, sizes=(100, 1000, 10000, 50000), weights=(0.4, 0.3, 0.2, 0.1),
+               day_range=(60, 365)):
+    """n proposals of the ABC workload (see module docstring): models and
+    their seeds, plus the target prevalence series (I/N of the seed-7
+    model over the longest tspan) cut to each model's tspan."""
+    rng = np.random.default_rng(seed)
+    models, seeds = [], []
+    for j in range(n):
+        Nn = int(rng.choice(sizes, p=weights))
+        T = int(rng.integers(day_range[0], day_range[1] + 1))
+        models.append(seir_events_fast(Nn, T, max(1, Nn // 2), rng,
+                                       beta=rng.uniform(0.05, 0.5),
+                                       epsilon=rng.uniform(0.1, 0.5),
+                                       gamma=rng.uniform(0.02, 0.2)))
+        seeds.append(int(rng.integers(1, 2 ** 62)))
+    return models, seeds
 
 
 def sise_pfilter(nodes=500, particles=4096, weeks=52, seed=7):
