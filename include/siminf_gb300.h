@@ -363,6 +363,63 @@ int siminf_gpu_plan_profile(siminf_gpu_plan *plan, void *cuda_stream, double ms[
 int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
 void siminf_gpu_plan_free(siminf_gpu_plan *plan);
 
+/*
+ * Serving: a request loop that runs simulations, particle filters and
+ * re-runs of device-resident plans as they arrive.  No counterpart in the
+ * reference, where each run() call simulates on the calling thread
+ * (R/run.R:178-283).  The server keeps `slots` requests on the GPU at once,
+ * each on its own stream with stream-ordered allocation, and admits a
+ * request when its estimated device bytes fit the HBM budget (oldest first;
+ * a younger one that fits may pass an older one waiting for memory).
+ * siminf_gpu_server_submit returns at once; the request and every buffer it
+ * points to must stay valid until siminf_gpu_server_wait reports it
+ * finished.  Results are those of the same call made alone
+ * (siminf_gpu_run_solver_ex, siminf_gpu_pfilter, siminf_gpu_plan_run).
+ */
+enum {
+    SIMINF_GPU_REQUEST_RUN = 0,         /* args + model + options: U/V written */
+    SIMINF_GPU_REQUEST_PFILTER = 1,     /* args + model + pfilter */
+    SIMINF_GPU_REQUEST_PLAN = 2         /* plan: run again, results stay on the device */
+};
+
+typedef struct siminf_gpu_request {
+    int kind;
+    siminf_gpu_solver_args *args;
+    const siminf_gpu_model *model;
+    siminf_gpu_options options;
+    siminf_gpu_pfilter_args *pfilter;
+    siminf_gpu_plan *plan;
+    long long bytes;                    /* device bytes to admit (0: estimated) */
+    /* set by the server */
+    int status;                         /* 0 or an error code */
+    int finished;
+    double ms_wait;                     /* from submission to the start on a slot */
+    double ms_run;                      /* on the slot */
+    long long submit_ns;
+    siminf_gpu_stats stats;             /* runs and plans */
+    char message[200];                  /* the error's diagnostics */
+} siminf_gpu_request;
+
+typedef struct siminf_gpu_server_options {
+    int slots;                          /* requests on the GPU at once (0: 8) */
+    int reserved0;
+    long long hbm_budget_bytes;         /* admission budget (0: 90% of free memory) */
+    int reserved[4];
+} siminf_gpu_server_options;
+
+typedef struct siminf_gpu_server siminf_gpu_server;
+
+int siminf_gpu_server_create(const siminf_gpu_server_options *options,
+                             siminf_gpu_server **out);
+int siminf_gpu_server_submit(siminf_gpu_server *server, siminf_gpu_request *request);
+/* 1 when the request has finished, 0 on timeout (timeout_ms < 0: wait). */
+int siminf_gpu_server_wait(siminf_gpu_server *server, siminf_gpu_request *request,
+                           double timeout_ms);
+int siminf_gpu_server_load(siminf_gpu_server *server, int *pending, int *running,
+                           long long *bytes_in_use);
+/* Finishes every submitted request, then stops the slots. */
+void siminf_gpu_server_free(siminf_gpu_server *server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -171,6 +171,39 @@ class Stats(C.Structure):
     ]
 
 
+class ServerOptions(C.Structure):
+    """siminf_gpu_server_options."""
+    _fields_ = [
+        ("slots", C.c_int),
+        ("reserved0", C.c_int),
+        ("hbm_budget_bytes", C.c_longlong),
+        ("reserved", C.c_int * 4),
+    ]
+
+
+class Request(C.Structure):
+    """siminf_gpu_request."""
+    _fields_ = [
+        ("kind", C.c_int),
+        ("args", C.c_void_p),
+        ("model", C.c_void_p),
+        ("options", Options),
+        ("pfilter", C.c_void_p),
+        ("plan", C.c_void_p),
+        ("bytes", C.c_longlong),
+        ("status", C.c_int),
+        ("finished", C.c_int),
+        ("ms_wait", C.c_double),
+        ("ms_run", C.c_double),
+        ("submit_ns", C.c_longlong),
+        ("stats", Stats),
+        ("message", C.c_char * 200),
+    ]
+
+
+REQUEST_RUN, REQUEST_PFILTER, REQUEST_PLAN = 0, 1, 2
+
+
 def csc(dense):
     """Dense matrix -> (ir, jc, pr) in compressed-sparse-column form, the
     storage of R's dgCMatrix slots i, p, x."""

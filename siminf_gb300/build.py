@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # reference's C (bit-identical trajectories).
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off"]
-SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp", "siminf_noalloc.cu", "siminf_batch.cu"]
+SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp", "siminf_noalloc.cu", "siminf_batch.cu",
+           "siminf_server.cpp"]
 
 
 def nvcc():

@@ -70,13 +70,20 @@ int cuda_fail(cudaError_t e, const char *what)
     return SIMINF_GPU_ERR_CUDA;
 }
 
+/* Where the calling thread's plans live: the stream their copies and
+ * kernels go to, and whether their buffers come from the stream-ordered
+ * allocator (no device-wide synchronisation when they are freed). */
+thread_local cudaStream_t g_plan_stream = nullptr;
+thread_local bool g_plan_async = false;
+
 template <class T>
 int dalloc(T **p, size_t n, std::vector<void *> &owned)
 {
     *p = nullptr;
     if (n == 0)
         n = 1;
-    cudaError_t e = cudaMalloc((void **) p, n * sizeof(T));
+    cudaError_t e = g_plan_async ? cudaMallocAsync((void **) p, n * sizeof(T), g_plan_stream)
+                                 : cudaMalloc((void **) p, n * sizeof(T));
     if (e != cudaSuccess) {
         *p = nullptr;
         return cuda_fail(e, "cudaMalloc");
@@ -174,6 +181,12 @@ int plan_create_internal(const siminf_gpu_solver_args *a, const siminf_gpu_model
     return plan_create_impl(a, model, opt, out, stream, no_output);
 }
 
+void plan_thread_stream(cudaStream_t stream, bool async)
+{
+    g_plan_stream = stream;
+    g_plan_async = async;
+}
+
 int plan_run_internal(siminf_gpu_plan *p, cudaStream_t st)
 {
     return plan_run_impl(p, st, nullptr);
@@ -229,10 +242,10 @@ int capi_cuda_fail(cudaError_t e, const char *what)
 template <class T>
 static int upload_owned(siminf_gpu_plan *p, T **dst, const T *src, size_t n)
 {
-    const int rc = upload(dst, src, n, p->owned, nullptr);
+    const int rc = upload(dst, src, n, p->owned, p->stream);
     if (rc)
         return rc;
-    const cudaError_t e = cudaStreamSynchronize(nullptr);
+    const cudaError_t e = cudaStreamSynchronize(p->stream);
     return e == cudaSuccess ? 0 : cuda_fail(e, "upload");
 }
 
@@ -569,8 +582,14 @@ void siminf_gpu_plan_free(siminf_gpu_plan *p)
 {
     if (!p)
         return;
-    for (void *q : p->owned)
-        cudaFree(q);
+    for (void *q : p->owned) {
+        if (p->async_alloc)
+            cudaFreeAsync(q, p->stream);
+        else
+            cudaFree(q);
+    }
+    if (p->async_alloc)
+        cudaStreamSynchronize(p->stream);
     delete p;
 }
 
@@ -669,8 +688,9 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     p->stats.ms_plan = ms_since(t0);
     p->horizon = (p->e2_count == 0) && L->pts_local;
 
-    cudaStream_t st = nullptr;
+    cudaStream_t st = g_plan_stream;
     p->stream = st;
+    p->async_alloc = g_plan_async;
     auto &own = p->owned;
     int *dS;
     uint32_t *dG;
@@ -1099,9 +1119,11 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
 
     int counts[3];
     unsigned long long fired = 0;
-    e = cudaMemcpy(counts, s.err_count, sizeof(counts), cudaMemcpyDeviceToHost);
+    e = cudaMemcpyAsync(counts, s.err_count, sizeof(counts), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
-        e = cudaMemcpy(&fired, s.fired, sizeof(fired), cudaMemcpyDeviceToHost);
+        e = cudaMemcpyAsync(&fired, s.fired, sizeof(fired), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
         return cuda_fail(e, "read counters");
     p->stats.transitions = fired;
@@ -1112,7 +1134,10 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
     std::vector<ErrRec> cands;
     if (counts[0] > 0) {
         cands.resize(std::min(counts[0], (int) MAX_ERR));
-        e = cudaMemcpy(cands.data(), s.err, cands.size() * sizeof(ErrRec), cudaMemcpyDeviceToHost);
+        e = cudaMemcpyAsync(cands.data(), s.err, cands.size() * sizeof(ErrRec),
+                            cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
         if (e != cudaSuccess)
             return cuda_fail(e, "read errors");
     }
@@ -1148,14 +1173,18 @@ int siminf_gpu_plan_download(siminf_gpu_plan *p, siminf_gpu_solver_args *a)
         return SIMINF_GPU_ERR_INVALID_MODEL;
     auto t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaSuccess;
+    const cudaStream_t st = p->stream;
+    const auto d2h = cudaMemcpyDeviceToHost;
     if (a->U && p->s.U)
-        e = cudaMemcpy(a->U, p->s.U, p->U_len * sizeof(int), cudaMemcpyDeviceToHost);
+        e = cudaMemcpyAsync(a->U, p->s.U, p->U_len * sizeof(int), d2h, st);
     else if (a->prU && p->s.prU)
-        e = cudaMemcpy(a->prU, p->s.prU, p->prU_len * sizeof(double), cudaMemcpyDeviceToHost);
+        e = cudaMemcpyAsync(a->prU, p->s.prU, p->prU_len * sizeof(double), d2h, st);
     if (e == cudaSuccess && a->V && p->s.V)
-        e = cudaMemcpy(a->V, p->s.V, p->V_len * sizeof(double), cudaMemcpyDeviceToHost);
+        e = cudaMemcpyAsync(a->V, p->s.V, p->V_len * sizeof(double), d2h, st);
     else if (e == cudaSuccess && a->prV && p->s.prV)
-        e = cudaMemcpy(a->prV, p->s.prV, p->prV_len * sizeof(double), cudaMemcpyDeviceToHost);
+        e = cudaMemcpyAsync(a->prV, p->s.prV, p->prV_len * sizeof(double), d2h, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
         return cuda_fail(e, "download");
     p->stats.ms_download = ms_since(t0);
@@ -1227,8 +1256,10 @@ static int plan_set_tspan(siminf_gpu_plan *p, const double *tspan, int tlen)
         p->d_days = d;
         p->days_cap = p->ndays;
     }
-    cudaError_t e = cudaMemcpy(p->d_days, p->days.data(), p->days.size() * sizeof(DayInfo),
-                               cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpyAsync(p->d_days, p->days.data(), p->days.size() * sizeof(DayInfo),
+                                    cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(p->stream);
     return e == cudaSuccess ? 0 : cuda_fail(e, "days upload");
 }
 
@@ -1293,14 +1324,15 @@ int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model 
     p->days_cap = p->ndays;
     double *d_lfact = nullptr, *d_w = nullptr, *d_loglik = nullptr, *d_ess = nullptr;
     int *d_anc = nullptr, *d_anc_out = nullptr, *d_obs = nullptr;
-    rc = upload(&d_lfact, lfact.data(), lfact.size(), p->owned, nullptr);
+    const cudaStream_t pst = p->stream;
+    rc = upload(&d_lfact, lfact.data(), lfact.size(), p->owned, pst);
     if (!rc) rc = dalloc(&d_w, (size_t) Np, p->owned);
     if (!rc) rc = dalloc(&d_anc, (size_t) Np, p->owned);
     if (!rc && pf->ancestors) rc = dalloc(&d_anc_out, (size_t) Np * pf->n_obs, p->owned);
-    if (!rc) rc = upload(&d_obs, pf->obs, (size_t) pf->n_obs * Nn, p->owned, nullptr);
+    if (!rc) rc = upload(&d_obs, pf->obs, (size_t) pf->n_obs * Nn, p->owned, pst);
     if (!rc) rc = dalloc(&d_loglik, 1, p->owned);
     if (!rc) rc = dalloc(&d_ess, (size_t) pf->n_obs, p->owned);
-    if (!rc && cudaMemset(d_loglik, 0, sizeof(double)) != cudaSuccess)
+    if (!rc && cudaMemsetAsync(d_loglik, 0, sizeof(double), pst) != cudaSuccess)
         rc = cuda_fail(cudaGetLastError(), "memset");
     const double logp = si_log(pf->detect_p), logq = si_log(1.0 - pf->detect_p);
     const double log_np = si_log((double) Np);
@@ -1320,7 +1352,7 @@ int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model 
         }
         if (i > 0) {
             cudaError_t e = pf_gather(p->s.U, p->s.V, prev_tlen, (long long) nu, (long long) nv,
-                                      d_anc, Np, p->d_u0, p->d_v0, nullptr);
+                                      d_anc, Np, p->d_u0, p->d_v0, pst);
             if (e != cudaSuccess) {
                 rc = cuda_fail(e, "pf_gather");
                 break;
@@ -1329,14 +1361,14 @@ int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model 
         if ((rc = plan_set_tspan(p, tsp, tlen)))
             break;
         p->s.seed = (uint64_t) pf->seed + ((uint64_t) i + 1) * 0x9E3779B97F4A7C15ULL;
-        if ((rc = plan_run_impl(p, nullptr, nullptr)))
+        if ((rc = plan_run_impl(p, pst, nullptr)))
             break;
         cudaError_t e = pf_weights(p->s.U, tlen, Nn, Nc, Np, d_obs + (size_t) i * Nn,
-                                   pf->obs_compartment, d_lfact, tablen, logp, logq, d_w, nullptr);
+                                   pf->obs_compartment, d_lfact, tablen, logp, logq, d_w, pst);
         if (e == cudaSuccess)
             e = pf_finalize(d_w, Np, log_np, d_loglik, d_ess, i, (uint64_t) pf->seed,
                             (((uint64_t) 1) << 62) + (uint64_t) i, d_anc,
-                            d_anc_out ? d_anc_out + (size_t) i * Np : nullptr, nullptr);
+                            d_anc_out ? d_anc_out + (size_t) i * Np : nullptr, pst);
         if (e != cudaSuccess) {
             rc = cuda_fail(e, "pf kernels");
             break;
@@ -1344,13 +1376,16 @@ int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model 
         prev_tlen = tlen;
     }
     if (!rc) {
-        cudaError_t e = cudaMemcpy(pf->loglik, d_loglik, sizeof(double), cudaMemcpyDeviceToHost);
+        cudaError_t e = cudaMemcpyAsync(pf->loglik, d_loglik, sizeof(double),
+                                        cudaMemcpyDeviceToHost, pst);
         if (e == cudaSuccess)
-            e = cudaMemcpy(pf->ess, d_ess, (size_t) pf->n_obs * sizeof(double),
-                           cudaMemcpyDeviceToHost);
+            e = cudaMemcpyAsync(pf->ess, d_ess, (size_t) pf->n_obs * sizeof(double),
+                                cudaMemcpyDeviceToHost, pst);
         if (e == cudaSuccess && pf->ancestors)
-            e = cudaMemcpy(pf->ancestors, d_anc_out, (size_t) pf->n_obs * Np * sizeof(int),
-                           cudaMemcpyDeviceToHost);
+            e = cudaMemcpyAsync(pf->ancestors, d_anc_out, (size_t) pf->n_obs * Np * sizeof(int),
+                                cudaMemcpyDeviceToHost, pst);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(pst);
         if (e != cudaSuccess)
             rc = cuda_fail(e, "pf results");
     }
@@ -1368,7 +1403,7 @@ static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *mode
     int rc = plan_create_impl(args, model, opt, &p, true);
     if (rc)
         return rc;
-    rc = siminf_gpu_plan_run(p, nullptr);
+    rc = plan_run_impl(p, p->stream, nullptr);
     if (!rc)
         rc = siminf_gpu_plan_download(p, args);
     g_stats = p->stats;

@@ -35,7 +35,8 @@ struct PlannedErr {
 struct siminf_gpu_plan {
     const Launchers *L = nullptr;
     DevState s{};
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      /* copies and kernels of create, run, download */
+    bool async_alloc = false;           /* buffers from the stream-ordered allocator */
     std::vector<void *> owned;
 
     int ndays = 0;
@@ -92,6 +93,11 @@ int plan_upload(siminf_gpu_plan *p, void **dst, const void *src, size_t bytes);
 
 /* The day schedule of tspan (src/solvers/SimInf_solver_ssm.c:305-334). */
 int plan_days(const double *tspan, int tlen, std::vector<DayInfo> &days);
+
+/* Plans created by the calling thread from now on put their copies and
+ * kernels on `stream` and, if async, take their buffers from the
+ * stream-ordered allocator on it (nullptr, false: the defaults). */
+void plan_thread_stream(cudaStream_t stream, bool async);
 
 /* The checks siminf_gpu_run_solver_ssm applies to its arguments. */
 int capi_validate(const siminf_gpu_solver_args *a, const Launchers *L);

@@ -38,6 +38,17 @@ def lib():
     L.siminf_gpu_run_batch.argtypes = [C.POINTER(abi.BatchJob), C.c_int, vp,
                                        C.POINTER(abi.BatchOptions)]
     L.siminf_gpu_run_batch.restype = C.c_int
+    L.siminf_gpu_server_create.argtypes = [C.POINTER(abi.ServerOptions), C.POINTER(vp)]
+    L.siminf_gpu_server_create.restype = C.c_int
+    L.siminf_gpu_server_submit.argtypes = [vp, C.POINTER(abi.Request)]
+    L.siminf_gpu_server_submit.restype = C.c_int
+    L.siminf_gpu_server_wait.argtypes = [vp, C.POINTER(abi.Request), C.c_double]
+    L.siminf_gpu_server_wait.restype = C.c_int
+    L.siminf_gpu_server_load.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_longlong)]
+    L.siminf_gpu_server_load.restype = C.c_int
+    L.siminf_gpu_server_free.argtypes = [vp]
+    L.siminf_gpu_server_free.restype = None
     L.siminf_gpu_run_solver_ex.argtypes = [vp, vp, C.POINTER(abi.Options)]
     L.siminf_gpu_run_solver_ex.restype = C.c_int
     L.siminf_gpu_plan_create_ex.argtypes = [vp, vp, C.POINTER(abi.Options), C.POINTER(vp)]
@@ -71,6 +82,8 @@ EXPORTS = (
     "siminf_gpu_plan_download", "siminf_gpu_plan_stats", "siminf_gpu_plan_free",
     "siminf_gpu_plan_profile", "siminf_gpu_schedule", "siminf_gpu_pfilter",
     "siminf_gpu_run_solver_ssm_noalloc", "siminf_gpu_run_batch",
+    "siminf_gpu_server_create", "siminf_gpu_server_submit", "siminf_gpu_server_wait",
+    "siminf_gpu_server_load", "siminf_gpu_server_free",
 )
 
 
