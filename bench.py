@@ -3,7 +3,14 @@ workload (1,000,000 nodes x 365 days, 730k enter/exit and 182.5M external
 transfer events), one JSON line on stdout.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--scale S] [--no-e2e] [--no-cpu]
+                  [--scale S] [--no-e2e] [--no-cpu] [--batch R] [--abc N]
+                  [--serve-seconds T] [--serve-rate R]
+
+Beside the plain run the line carries the batched forms: `batched` (R
+replicates of the workload in one plan), `abc` (N uneven ABC proposals as
+one batch with on-device distances, against one run per proposal) and
+`serve` (an open-loop request trace through the serving loop, p50/p99
+latency, against serving the same trace one request at a time).
 
 A step is one full run of the workload's horizon.  `value` times K steps of
 siminf_gpu_plan_run with every input already resident in HBM (CUDA events on
@@ -52,6 +59,11 @@ def parse():
     ap.add_argument("--batch", type=int, default=8,
                     help="replicates of the workload run as one batched plan (0/1: skip)")
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--abc", type=int, default=256,
+                    help="ABC proposals (uneven models) run as one batch and one by one (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=5.0,
+                    help="length of the open-loop serving trace (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="arrivals per second")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-scale", type=float, default=0.05,
                     help="workload fraction of the bounded CPU sample")
@@ -139,6 +151,133 @@ def cpu_baseline(scale, days, threads, seed=42):
     if code:
         raise RuntimeError("oracle failed with %d" % code)
     return res.node_days / dt, res.transitions / dt, dt, "port", res
+
+
+def abc_bench(n, seed=11):
+    """The ABC workload: n proposals over uneven models (node counts 100 to
+    50,000, 60 to 365 days, events scaled to size), run as one batch with the
+    prevalence distance on the device, and one run() per proposal."""
+    from siminf_gb300 import workloads
+    from siminf_gb300.run import run, run_batch
+    models, seeds = workloads.abc_models(n, seed=seed)
+    node_days = sum(m.Nn * len(m.tspan) for m in models)
+    tmax = max(len(m.tspan) for m in models)
+    target = np.linspace(0.0, 0.05, tmax)
+    targets = [target[:len(m.tspan)] for m in models]
+    run_batch(models, seeds, targets, cap_transfers=True)         # warm-up
+    ts = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        run_batch(models, seeds, targets, cap_transfers=True)
+        ts.append(time.perf_counter() - t0)
+    tb = min(ts)
+    t0 = time.perf_counter()
+    for m, sd in zip(models, seeds):
+        run(m, seed=sd, cap_transfers=True)
+    tp = time.perf_counter() - t0
+    return {"models": n, "node_days": int(node_days), "value": node_days / tb, "unit": UNIT,
+            "seconds": tb, "one_run_per_model_value": node_days / tp,
+            "one_run_per_model_seconds": tp, "vs_one_run_per_model": tp / tb,
+            "data": "synthetic ABC proposals: SEIR, node counts {100,1e3,1e4,5e4} w.p. "
+                    "{.4,.3,.2,.1}, 60-365 days, events scaled to size, prior draws; "
+                    "end to end through the C ABI (host buffers)"}
+
+
+def serve_bench(seconds, rate, seed=5):
+    """Open-loop Poisson arrivals of a request mix (60% SIR runs, 100-20,000
+    nodes log-uniform, 30-365 days; 30% particle filters on the SISe model,
+    256-4,096 particles; 10% SEIR-with-events runs, 10,000-200,000 nodes)
+    served by the request loop, and the same trace served one request at a
+    time (the plain path).  Particle filters use 40 nodes and 6 weekly
+    observations and SEIR runs 30 days so the trace stays inside a minute."""
+    from siminf_gb300 import model as M
+    from siminf_gb300 import workloads
+    from siminf_gb300.run import pfilter, run
+    from siminf_gb300.serve import Server
+    rng = np.random.default_rng(seed)
+    pool_sir = []
+    for _ in range(12):
+        n = int(np.exp(rng.uniform(np.log(100), np.log(20000))))
+        days = int(rng.integers(30, 366))
+        u0 = {"S": np.full(n, 99), "I": np.full(n, 5), "R": np.zeros(n, int)}
+        pool_sir.append(M.SIR_mparse(u0, np.arange(1, days + 1), 0.16, 0.077))
+    pool_pf = []
+    for k in range(4):
+        pm, gdata, t_obs, obs = workloads.sise_pfilter(nodes=40, particles=4096, weeks=6,
+                                                       seed=7 + k)
+        pool_pf.append((pm, gdata, t_obs, obs))
+    pool_seir = [workloads.seir_events_fast(n, 30, n // 2, rng) for n in (10000, 60000, 200000)]
+    trace, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        r = rng.random()
+        kind = "sir" if r < 0.6 else ("pf" if r < 0.9 else "seir")
+        trace.append((t, kind, int(rng.integers(0, 1 << 30)),
+                      int(rng.integers(256, 4097)) if kind == "pf" else 0,
+                      int(rng.integers(0, 12 if kind == "sir" else
+                                       (4 if kind == "pf" else 3)))))
+
+    def node_days(kind, np_, k):
+        if kind == "sir":
+            return pool_sir[k].Nn * len(pool_sir[k].tspan)
+        if kind == "pf":
+            return np_ * pool_pf[k][0].Nn * int(pool_pf[k][2][-1])
+        return pool_seir[k].Nn * len(pool_seir[k].tspan)
+
+    total_nd = sum(node_days(kind, n_p, k) for _, kind, _, n_p, k in trace)
+
+    def submit(srv, kind, sd, n_p, k):
+        if kind == "sir":
+            return srv.run(pool_sir[k], seed=sd)
+        if kind == "pf":
+            pm, gdata, t_obs, obs = pool_pf[k]
+            return srv.pfilter(pm, n_p, t_obs, obs, 1, 0.8, seed=sd, gdata=gdata[:n_p])
+        return srv.run(pool_seir[k], seed=sd, cap_transfers=True)
+
+    srv = Server(slots=8, hbm_budget_bytes=150 * 10 ** 9)
+    for kind, k in (("sir", 0), ("pf", 0), ("seir", 0)):
+        srv.wait(submit(srv, kind, 1, 256, k))                     # warm-up
+    t0 = time.perf_counter()
+    tickets = []
+    for at, kind, sd, n_p, k in trace:
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        tickets.append(submit(srv, kind, sd, n_p, k))
+    for tk in tickets:
+        srv.wait(tk)
+    served_s = time.perf_counter() - t0
+    lat = np.array([tk.latency_ms for tk in tickets])
+    srv.close()
+
+    # plain path: the same trace, one request at a time on the caller's thread
+    t0 = time.perf_counter()
+    plain_lat = []
+    for at, kind, sd, n_p, k in trace:
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        if kind == "sir":
+            run(pool_sir[k], seed=sd)
+        elif kind == "pf":
+            pm, gdata, t_obs, obs = pool_pf[k]
+            pfilter(pm, n_p, t_obs, obs, 1, 0.8, seed=sd, gdata=gdata[:n_p])
+        else:
+            run(pool_seir[k], seed=sd, cap_transfers=True)
+        plain_lat.append((time.perf_counter() - t0 - at) * 1e3)
+    plain_s = time.perf_counter() - t0
+    plain_lat = np.array(plain_lat)
+    return {"requests": len(trace), "rate_per_s": rate, "trace_seconds": seconds,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "value": total_nd / served_s, "unit": UNIT, "seconds": served_s,
+            "plain_p50_ms": float(np.percentile(plain_lat, 50)),
+            "plain_p99_ms": float(np.percentile(plain_lat, 99)),
+            "plain_value": total_nd / plain_s, "plain_seconds": plain_s,
+            "slots": 8, "hbm_budget_bytes": 150 * 10 ** 9,
+            "data": "synthetic request mix, open-loop Poisson arrivals; latency from "
+                    "submission to completion; plain = one request at a time"}
 
 
 def run_reference(args):
@@ -260,6 +399,10 @@ def run_ours(args):
         pb.close()
         del hb, mb
 
+    abc = abc_bench(args.abc) if args.abc > 0 and rank == 0 and world == 1 else None
+    serve = (serve_bench(args.serve_seconds, args.serve_rate)
+             if args.serve_seconds > 0 and rank == 0 and world == 1 else None)
+
     e2e = None
     if not args.no_e2e:
         opt = abi.Options(cap_transfers=1)
@@ -328,6 +471,8 @@ def run_ours(args):
                                  % ALGO_BYTES_PER_NODE_DAY},
             "kernels": prof["kernels"],
             "batched": batched,
+            "abc": abc,
+            "serve": serve,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "t_generate_s": t_gen,
