@@ -44,6 +44,11 @@ UNIT = "node-days/s"
 # Algorithmic HBM bytes per node-day of this workload: one U column entry
 # (4 compartments x 4 B) + events read (0.504 events per node-day x 36 B).
 ALGO_BYTES_PER_NODE_DAY = 16 + 0.504 * 36
+# DRAM traffic of one k_ssa_e1 launch (dram__bytes_read.sum +
+# dram__bytes_write.sum) from an ncu capture of the 250,000-node, 60-day
+# case of this workload (day 30: 20.4 MB read, 0 written), per node; the
+# traffic grows with the node count, so a launch of N nodes moves N times it.
+SSA_TRAFFIC_BYTES_PER_NODE = 20.408320e6 / 250_000
 
 
 def parse():
@@ -464,7 +469,11 @@ def run_ours(args):
             "clocks": clk.summary(),
             "roofline": {"bound": "hbm", "kernel": top["name"] if top else None,
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "frac": (achieved / peak) if achieved else None,
+                         "traffic": (SSA_TRAFFIC_BYTES_PER_NODE * nodes
+                                     if top and top["name"] == "k_ssa_e1" else None),
+                         "traffic_unit": "bytes per launch",
+                         "algorithmic_bytes_per_launch": (ALGO_BYTES_PER_NODE_DAY * nodes),
                          "peak_source": peak_kind,
                          "note": "algorithmic bytes = %.1f B/node-day x node-days per launch; "
                                  "the SSA kernel is bound by FP64 latency, not HBM"
