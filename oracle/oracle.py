@@ -91,6 +91,8 @@ def ref_lib():
         _ref = C.CDLL(REF_LIB)
         _ref.ref_run.restype = C.c_int
         _ref.ref_run.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+        _ref.shim_set_independent.argtypes = [C.c_int]
+        _ref.shim_set_independent.restype = None
     return _ref
 
 
@@ -102,9 +104,17 @@ def run(holder, model_name, threads=1, cap_transfers=False):
     return code, res
 
 
-def run_ref(holder, model_name, threads=1):
-    """Run the reference's unmodified solver sources; returns the code."""
-    return ref_lib().ref_run(C.cast(holder.ref(), C.c_void_p), model_name.encode(), int(threads))
+def run_ref(holder, model_name, threads=1, independent=False):
+    """Run the reference's unmodified solver sources; returns the code.
+    independent: draw from per-thread Mersenne twisters seeded as the
+    reference seeds its GSL generators, instead of the shared per-node
+    stream (for distribution tests rather than bit-exact ones)."""
+    lib_ = ref_lib()
+    lib_.shim_set_independent(int(bool(independent)))
+    try:
+        return lib_.ref_run(C.cast(holder.ref(), C.c_void_p), model_name.encode(), int(threads))
+    finally:
+        lib_.shim_set_independent(0)
 
 
 def si_log(x):

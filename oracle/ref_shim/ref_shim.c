@@ -11,6 +11,15 @@
  * for replicated models run with Nthread == Nrep, replicate i.  Its offset
  * turns the local `node` at a draw site into the global stream id
  * replicate * Nn + node, so draws match siminf_stream.h's keying.
+ *
+ * Independent mode (shim_set_independent(1)), for the distribution tests
+ * against the reference: every generator is instead a 32-bit Mersenne
+ * twister (M. Matsumoto and T. Nishimura, ACM TOMACS 8(1), 1998: the
+ * published MT19937 recurrence, tempering and initialisation), the master
+ * seeded with the run's seed and each thread's generator from the master,
+ * as the reference seeds its GSL generators (src/solvers/SimInf_solver.c:
+ * 474-477); uniforms are word / 2^32 with zero rejected, and the samplers
+ * draw from a stream keyed by two of the thread's words.
  */
 #include <stdarg.h>
 #include <stdint.h>
@@ -24,9 +33,54 @@
 #include "gsl/gsl_randist.h"
 #include "../../siminf_gb300/csrc/siminf_stream.h"
 
+enum { MT_N = 624, MT_M = 397 };
+
 struct gsl_rng {
     long offset;
+    uint32_t mt[MT_N];
+    int mti;
 };
+
+static void mt_seed(gsl_rng *r, uint32_t s)
+{
+    r->mt[0] = s;
+    for (int i = 1; i < MT_N; i++)
+        r->mt[i] = 1812433253u * (r->mt[i - 1] ^ (r->mt[i - 1] >> 30)) + (uint32_t) i;
+    r->mti = MT_N;
+}
+
+static uint32_t mt_next(gsl_rng *r)
+{
+    static const uint32_t mag01[2] = {0x0u, 0x9908b0dfu};
+    uint32_t y;
+    if (r->mti >= MT_N) {
+        int kk;
+        for (kk = 0; kk < MT_N - MT_M; kk++) {
+            y = (r->mt[kk] & 0x80000000u) | (r->mt[kk + 1] & 0x7fffffffu);
+            r->mt[kk] = r->mt[kk + MT_M] ^ (y >> 1) ^ mag01[y & 1u];
+        }
+        for (; kk < MT_N - 1; kk++) {
+            y = (r->mt[kk] & 0x80000000u) | (r->mt[kk + 1] & 0x7fffffffu);
+            r->mt[kk] = r->mt[kk + (MT_M - MT_N)] ^ (y >> 1) ^ mag01[y & 1u];
+        }
+        y = (r->mt[MT_N - 1] & 0x80000000u) | (r->mt[0] & 0x7fffffffu);
+        r->mt[MT_N - 1] = r->mt[MT_M - 1] ^ (y >> 1) ^ mag01[y & 1u];
+        r->mti = 0;
+    }
+    y = r->mt[r->mti++];
+    y ^= (y >> 11);
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= (y >> 18);
+    return y;
+}
+
+static int g_independent;
+
+void shim_set_independent(int on)
+{
+    g_independent = on;
+}
 
 static const gsl_rng_type type_mt = {"mt19937"};
 static const gsl_rng_type type_taus = {"taus2"};
@@ -72,6 +126,7 @@ gsl_rng *gsl_rng_alloc(const gsl_rng_type *T)
     if (!r)
         return NULL;
     const int k = g.allocs++;
+    mt_seed(r, (uint32_t) (g.seed ^ (g.seed >> 32)) + (uint32_t) k);
     if (k == 0) {
         r->offset = -1;                        /* master: never draws */
     } else {
@@ -82,12 +137,17 @@ gsl_rng *gsl_rng_alloc(const gsl_rng_type *T)
 }
 
 void gsl_rng_free(gsl_rng *r) { free(r); }
-void gsl_rng_set(const gsl_rng *r, unsigned long int s) { (void) r; (void) s; }
+void gsl_rng_set(const gsl_rng *r, unsigned long int s)
+{
+    if (g_independent)
+        mt_seed((gsl_rng *) r, (uint32_t) s);
+}
 unsigned long int gsl_rng_max(const gsl_rng *r) { (void) r; return 0xFFFFFFFFUL; }
 unsigned long int gsl_rng_uniform_int(const gsl_rng *r, unsigned long int n)
 {
-    (void) r; (void) n;
-    return 0;
+    if (!g_independent || n == 0)
+        return 0;
+    return (unsigned long int) mt_next((gsl_rng *) r) % n;
 }
 
 static si_rng *stream(const gsl_rng *r, long node)
@@ -95,19 +155,43 @@ static si_rng *stream(const gsl_rng *r, long node)
     return &g.streams[r->offset + node];
 }
 
+/* Independent mode: a stream keyed by two of the generator's words. */
+static si_rng independent_stream(const gsl_rng *r)
+{
+    si_rng s;
+    const uint64_t k = ((uint64_t) mt_next((gsl_rng *) r) << 32) | mt_next((gsl_rng *) r);
+    si_rng_init(&s, k, 0x5EEDull, 0);
+    return s;
+}
+
 double shim_uniform_pos(const gsl_rng *r, long node)
 {
+    if (g_independent) {
+        uint32_t w;
+        do
+            w = mt_next((gsl_rng *) r);
+        while (w == 0);
+        return (double) w / 4294967296.0;
+    }
     return si_uniform_pos(stream(r, node));
 }
 
 unsigned int shim_binomial(const gsl_rng *r, double p, unsigned int n, long node)
 {
+    if (g_independent) {
+        si_rng s = independent_stream(r);
+        return (unsigned int) si_binomial(&s, p, (int) n);
+    }
     return (unsigned int) si_binomial(stream(r, node), p, (int) n);
 }
 
 unsigned int shim_hypergeometric(const gsl_rng *r, unsigned int n1, unsigned int n2,
                                  unsigned int t, long node)
 {
+    if (g_independent) {
+        si_rng s = independent_stream(r);
+        return (unsigned int) si_hypergeometric(&s, (int) n1, (int) n2, (int) t);
+    }
     return (unsigned int) si_hypergeometric(stream(r, node), (int) n1, (int) n2, (int) t);
 }
 
