@@ -8,9 +8,10 @@ transfer events), one JSON line on stdout.
 
 Beside the plain run the line carries the batched forms: `batched` (R
 replicates of the workload in one plan), `abc` (N uneven ABC proposals as
-one batch with on-device distances, against one run per proposal) and
-`serve` (an open-loop request trace through the serving loop, p50/p99
-latency, against serving the same trace one request at a time).
+one batch with on-device distances, against one run per proposal),
+`pfilter` (the 4,096-particle SISe particle filter) and `serve` (an
+open-loop request trace through the serving loop, p50/p99 latency, against
+serving the same trace one request at a time).
 
 A step is one full run of the workload's horizon.  `value` times K steps of
 siminf_gpu_plan_run with every input already resident in HBM (CUDA events on
@@ -66,6 +67,8 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--abc", type=int, default=256,
                     help="ABC proposals (uneven models) run as one batch and one by one (0: skip)")
+    ap.add_argument("--pfilter", type=int, default=4096,
+                    help="particles of the particle-filter workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=5.0,
                     help="length of the open-loop serving trace (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="arrivals per second")
@@ -186,6 +189,27 @@ def abc_bench(n, seed=11):
             "data": "synthetic ABC proposals: SEIR, node counts {100,1e3,1e4,5e4} w.p. "
                     "{.4,.3,.2,.1}, 60-365 days, events scaled to size, prior draws; "
                     "end to end through the C ABI (host buffers)"}
+
+
+def pfilter_bench(particles):
+    """The particle-filter workload: SISe with phi, 500 nodes per particle,
+    52 weekly Binomial(I, 0.8) observations from a ground-truth run (seed 7),
+    per-particle upsilon and gamma; one filter pass through the C ABI."""
+    from siminf_gb300 import workloads
+    from siminf_gb300.run import pfilter
+    m, gdata, t_obs, obs = workloads.sise_pfilter(nodes=500, particles=particles, weeks=52)
+    pfilter(m, particles, t_obs, obs, 1, 0.8, seed=3, gdata=gdata)      # warm-up
+    ts, res = [], None
+    for _ in range(2):
+        t0 = time.perf_counter()
+        res = pfilter(m, particles, t_obs, obs, 1, 0.8, seed=3, gdata=gdata)
+        ts.append(time.perf_counter() - t0)
+    dt = min(ts)
+    node_days = particles * m.Nn * int(t_obs[-1])
+    return {"particles": particles, "nodes": m.Nn, "observations": len(t_obs),
+            "node_days": int(node_days), "value": node_days / dt, "unit": UNIT,
+            "seconds": dt, "loglik": res.loglik,
+            "data": "synthetic SISe particle filter (phi pts), end to end through the C ABI"}
 
 
 def serve_bench(seconds, rate, seed=5):
@@ -405,6 +429,8 @@ def run_ours(args):
         del hb, mb
 
     abc = abc_bench(args.abc) if args.abc > 0 and rank == 0 and world == 1 else None
+    pf = (pfilter_bench(args.pfilter)
+          if args.pfilter > 0 and rank == 0 and world == 1 else None)
     serve = (serve_bench(args.serve_seconds, args.serve_rate)
              if args.serve_seconds > 0 and rank == 0 and world == 1 else None)
 
@@ -481,6 +507,7 @@ def run_ours(args):
             "kernels": prof["kernels"],
             "batched": batched,
             "abc": abc,
+            "pfilter": pf,
             "serve": serve,
             "e2e": e2e,
             "cpu_baseline": cpu,
@@ -492,9 +519,31 @@ def run_ours(args):
 
 
 def pinned_holder(m, seed, torch):
-    """ArgsHolder whose event arrays and U live in pinned host memory."""
+    """ArgsHolder whose inputs (u0, ldata, the event arrays) and output U
+    live in pinned host memory, as the e2e timing asks."""
+    import ctypes as C
     from siminf_gb300 import abi
     h = abi.build_args(m, seed)
+    a = h.args
+
+    def pinned(src):
+        t = torch.from_numpy(np.ascontiguousarray(src)).pin_memory()
+        h.keep.append(t)
+        return t.numpy()
+
+    def repoint(field, n, dtype, ctype):
+        arr = np.ctypeslib.as_array(getattr(a, field), shape=(n,)).view(dtype)
+        arr = pinned(arr)
+        setattr(a, field, arr.ctypes.data_as(C.POINTER(ctype)))
+        return arr
+
+    for k in ("event", "time", "node", "dest", "n", "select", "shift"):
+        repoint(k, a.len, np.int32, C.c_int)
+    repoint("proportion", a.len, np.float64, C.c_double)
+    repoint("u0", m.Nn * m.Nc * m.replicates, np.int32, C.c_int)
+    repoint("ldata", max(1, m.Nld * m.Nn), np.float64, C.c_double)
+    h.U = pinned(h.U)
+    a.U = h.U.ctypes.data_as(C.POINTER(C.c_int))
     return h
 
 

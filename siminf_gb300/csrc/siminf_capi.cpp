@@ -25,6 +25,7 @@
  * calling thread, every device buffer freed before returning.
  */
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -32,6 +33,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <atomic>
+#include <limits>
 #include <memory>
 #include <thread>
 #include <vector>
@@ -257,9 +259,15 @@ static inline long long event_day(int time, double tt0)
     return (long long) time - (long long) std::floor(tt0);
 }
 
-/* Threads used by the host planner. */
+/* Threads used by the host planner (SIMINF_PLANNER_THREADS overrides the
+ * hardware's count). */
 static int planner_threads()
 {
+    if (const char *ev = getenv("SIMINF_PLANNER_THREADS")) {
+        const int n = atoi(ev);
+        if (n >= 1 && n <= 256)
+            return n;
+    }
     unsigned n = std::thread::hardware_concurrency();
     if (n < 1)
         n = 1;
@@ -407,58 +415,85 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
     return 0;
 }
 
-/* Per-thread scratch of the wave planner (levels per node, stamped by day). */
+/* Per-thread scratch of the wave planner: per node, its levels on the day
+ * being planned, 16 bits each so the table of a million nodes stays in
+ * cache (zero outside the day; the nodes a day touches are listed and
+ * cleared after it).  A day whose wavefronts run deeper than 2^16 - 1 is
+ * planned again with 32-bit levels. */
 struct WaveTracker {
-    std::vector<int> excl, add, stamp, level;
+    std::vector<uint16_t> excl, add;
+    std::vector<int> touched, level;
     std::vector<long long> idx;
-    explicit WaveTracker(int Nn) : excl(Nn, 0), add(Nn, 0), stamp(Nn, -1) {}
+    std::vector<long long> cnt, off;
+    explicit WaveTracker(int Nn) : excl(Nn, 0), add(Nn, 0) {}
 };
+
+/* Levels of day d's external transfers into w.level / w.idx; T is the
+ * level type.  Returns false if a level would not fit T. */
+template <class T>
+static bool day_levels(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
+                       WaveTracker &w, T *excl, T *add, int &maxl)
+{
+    const int Nn = a->Nn, nsel = p->nsel;
+    const long long limit = (long long) std::numeric_limits<T>::max();
+    const int *ev = a->event, *src = a->node, *dst = a->dest, *sel = a->select;
+    w.level.clear();
+    w.idx.clear();
+    w.touched.clear();
+    maxl = 0;
+    bool ok = true;
+    for (long long i = p->e2_lo[d]; i < p->e2_hi[d]; i++) {
+        if (ev[i] != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
+            continue;
+        const int s = src[i] - 1, t = dst[i] - 1;
+        if (s < 0 || s >= Nn || t < 0 || t >= Nn || sel[i] - 1 < 0 || sel[i] - 1 >= nsel)
+            continue;
+        if (!excl[s] && !add[s])
+            w.touched.push_back(s);
+        if (!excl[t] && !add[t])
+            w.touched.push_back(t);
+        const long long L = 1 + (long long) std::max(std::max(excl[s], add[s]), excl[t]);
+        if (L > limit) {
+            ok = false;
+            break;
+        }
+        excl[s] = (T) L;
+        if (add[t] < (T) L)
+            add[t] = (T) L;
+        w.level.push_back((int) L);
+        w.idx.push_back(i);
+        maxl = std::max(maxl, (int) L);
+    }
+    for (int n : w.touched)
+        excl[n] = add[n] = 0;
+    return ok;
+}
 
 /* Wave levels of day d: level = 1 + max(level of the last event with the
  * same source, of any add into the source, of the last event whose source
  * is our destination).  Then a stable counting sort of the day's events by
- * level into e2 (positions e2_day_off[d] ..), and the wave sizes into
- * p->day_waves[d]. */
+ * level into e2 (positions e2_day_off[d] - base ..), and the wave sizes
+ * into p->day_waves[d]. */
 static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
-                           WaveTracker &w, E2Rec *e2)
+                           WaveTracker &w, E2Rec *e2, long long base = 0)
 {
-    const int Nn = a->Nn, nsel = p->nsel;
-    std::vector<int> &excl = w.excl, &add = w.add, &stamp = w.stamp, &level = w.level;
-    std::vector<long long> &idx = w.idx;
-    level.clear();
-    idx.clear();
     int maxl = 0;
-    for (long long i = p->e2_lo[d]; i < p->e2_hi[d]; i++) {
-        if (a->event[i] != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
-            continue;
-        const int s = a->node[i] - 1, t = a->dest[i] - 1;
-        if (s < 0 || s >= Nn || t < 0 || t >= Nn || a->select[i] - 1 < 0 ||
-            a->select[i] - 1 >= nsel)
-            continue;
-        if (stamp[s] != d) {
-            stamp[s] = d;
-            excl[s] = add[s] = 0;
-        }
-        if (stamp[t] != d) {
-            stamp[t] = d;
-            excl[t] = add[t] = 0;
-        }
-        const int L = 1 + std::max(std::max(excl[s], add[s]), excl[t]);
-        excl[s] = L;
-        add[t] = std::max(add[t], L);
-        level.push_back(L);
-        idx.push_back(i);
-        maxl = std::max(maxl, L);
+    if (!day_levels<uint16_t>(p, a, d, w, w.excl.data(), w.add.data(), maxl)) {
+        std::vector<int> excl(a->Nn, 0), add(a->Nn, 0);
+        day_levels<int>(p, a, d, w, excl.data(), add.data(), maxl);
     }
-    std::vector<long long> cnt(maxl + 2, 0);
+    const int *src = a->node, *dst = a->dest, *sel = a->select;
+    std::vector<int> &level = w.level;
+    std::vector<long long> &idx = w.idx, &cnt = w.cnt, &off = w.off;
+    cnt.assign(maxl + 2, 0);
     for (int L : level)
         cnt[L]++;
-    std::vector<long long> off(maxl + 2, p->e2_day_off[d]);
+    off.assign(maxl + 2, p->e2_day_off[d] - base);
     for (int L = 1; L <= maxl; L++)
         off[L + 1] = off[L] + cnt[L];
     for (size_t k = 0; k < level.size(); k++) {
         const long long i = idx[k];
-        e2[off[level[k]]++] = E2Rec{a->node[i] - 1, a->dest[i] - 1, a->n[i], a->select[i] - 1,
+        e2[off[level[k]]++] = E2Rec{src[i] - 1, dst[i] - 1, a->n[i], sel[i] - 1,
                                     a->shift[i] - 1, (int) i, a->proportion[i]};
     }
     p->day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
@@ -683,7 +718,6 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
         /* the waves are planned during the first run, beside the GPU */
         p->e2_pending = true;
         p->args = *a;
-        p->h_e2.reset(new E2Rec[p->e2_count]);
     }
     p->stats.ms_plan = ms_since(t0);
     p->horizon = (p->e2_count == 0) && L->pts_local;
@@ -977,30 +1011,59 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
  * transfers' waves day by day while this thread copies each chunk of
  * finished days to the device on a copy stream and queues the chunk's
  * kernels behind it, so planning and copying overlap the GPU's work on
- * earlier days.  The kernels and their order are those of launch_all. */
+ * earlier days.  The planners write each chunk straight into one slot of a
+ * ring of pinned host buffers, from which the copy runs as DMA without
+ * holding this thread; a slot is reused once its previous copy is done.
+ * The kernels and their order are those of launch_all. */
 static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t st)
 {
     const Launchers *L = p->L;
     const siminf_gpu_solver_args *a = &p->args;
     const int ndays = p->ndays;
-    enum { CHUNK_DAYS = 8 };
+    enum { CHUNK_DAYS = 8, RING = 4 };
     cudaError_t e = L->init(s, p->tt0, st);
     if (e != cudaSuccess)
         return e;
 
+    const int nchunks = (ndays + CHUNK_DAYS - 1) / CHUNK_DAYS;
+    long long slot_len = 1;
+    for (int c = 0; c < nchunks; c++) {
+        const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
+        slot_len = std::max(slot_len, p->e2_day_off[d1] - p->e2_day_off[d0]);
+    }
+    E2Rec *ring = nullptr;
+    e = cudaHostAlloc((void **) &ring, (size_t) RING * slot_len * sizeof(E2Rec),
+                      cudaHostAllocDefault);
+    if (e != cudaSuccess)
+        return e;
+
     std::unique_ptr<std::atomic<int>[]> done(new std::atomic<int>[ndays]);
+    std::unique_ptr<std::atomic<int>[]> issued(new std::atomic<int>[nchunks]);
+    std::vector<cudaEvent_t> copied(nchunks, nullptr);
     for (int d = 0; d < ndays; d++)
         done[d].store(0);
-    std::atomic<int> next_day(0), failed(0);
-    E2Rec *h = p->h_e2.get();
+    for (int c = 0; c < nchunks; c++)
+        issued[c].store(0);
+    std::atomic<int> next_day(0), failed(0), abort(0);
     std::vector<std::thread> workers;
     const int nthreads = std::max(1, planner_threads() - 1);
     for (int t = 0; t < nthreads; t++)
         workers.emplace_back([&]() {
             try {
                 WaveTracker w(a->Nn);
-                for (int d = next_day++; d < ndays; d = next_day++) {
-                    plan_day_waves(p, a, d, w, h);
+                for (int d = next_day++; d < ndays && !abort.load(); d = next_day++) {
+                    const int c = d / CHUNK_DAYS;
+                    if (c >= RING) {
+                        /* the slot's previous chunk must have left it */
+                        while (!issued[c - RING].load(std::memory_order_acquire) &&
+                               !abort.load())
+                            std::this_thread::yield();
+                        if (abort.load())
+                            break;
+                        cudaEventSynchronize(copied[c - RING]);
+                    }
+                    E2Rec *slot = ring + (size_t) (c % RING) * slot_len;
+                    plan_day_waves(p, a, d, w, slot, p->e2_day_off[c * CHUNK_DAYS]);
                     done[d].store(1, std::memory_order_release);
                 }
             } catch (...) {
@@ -1010,8 +1073,8 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
 
     cudaStream_t cs = nullptr;
     e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    for (int d0 = 0; d0 < ndays && e == cudaSuccess; d0 += CHUNK_DAYS) {
-        const int d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
+    for (int c = 0; c < nchunks && e == cudaSuccess; c++) {
+        const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
         for (int d = d0; d < d1 && !failed.load(); d++)
             while (!done[d].load(std::memory_order_acquire) && !failed.load())
                 std::this_thread::yield();
@@ -1020,35 +1083,32 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             break;
         }
         const long long lo = p->e2_day_off[d0], hi = p->e2_day_off[d1];
-        if (hi > lo) {
-            cudaEvent_t ev;
-            e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-            if (e == cudaSuccess) {
-                e = cudaMemcpyAsync(p->d_e2 + lo, h + lo, (size_t) (hi - lo) * sizeof(E2Rec),
-                                    cudaMemcpyHostToDevice, cs);
-                if (e == cudaSuccess)
-                    e = cudaEventRecord(ev, cs);
-                if (e == cudaSuccess)
-                    e = cudaStreamWaitEvent(st, ev, 0);
-                cudaEventDestroy(ev);
-            }
-        }
+        e = cudaEventCreateWithFlags(&copied[c], cudaEventDisableTiming);
+        if (e == cudaSuccess && hi > lo)
+            e = cudaMemcpyAsync(p->d_e2 + lo, ring + (size_t) (c % RING) * slot_len,
+                                (size_t) (hi - lo) * sizeof(E2Rec), cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(copied[c], cs);
+        if (e != cudaSuccess)
+            break;
+        issued[c].store(1, std::memory_order_release);
+        e = cudaStreamWaitEvent(st, copied[c], 0);
         for (int d = d0; d < d1 && e == cudaSuccess; d++) {
             const DayInfo &di = p->days[d];
             e = L->ssa_e1(s, d, di.tt, di.next, st);
             long long off = p->e2_day_off[d];
             for (size_t w = 0; w < p->day_waves[d].size() && e == cudaSuccess; w++) {
-                const long long c = p->day_waves[d][w];
-                e = L->e2_wave(s, p->d_e2 + off, (int) c, d, di.tt, st);
-                off += c;
+                const long long cnt = p->day_waves[d][w];
+                e = L->e2_wave(s, p->d_e2 + off, (int) cnt, d, di.tt, st);
+                off += cnt;
             }
             if (e == cudaSuccess)
                 e = L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
             std::swap(s.vA, s.vB);
         }
     }
-    /* the planners finish their days either way; the copies must land
-     * before the host buffer may go */
+    /* planners waiting for a slot give up once the copies stop */
+    abort.store(1);
     for (auto &t : workers)
         t.join();
     if (cs) {
@@ -1057,6 +1117,10 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             e = e2;
         cudaStreamDestroy(cs);
     }
+    for (cudaEvent_t ev : copied)
+        if (ev)
+            cudaEventDestroy(ev);
+    cudaFreeHost(ring);
     return e;
 }
 
@@ -1263,6 +1327,122 @@ static int plan_set_tspan(siminf_gpu_plan *p, const double *tspan, int tlen)
     return e == cudaSuccess ? 0 : cuda_fail(e, "days upload");
 }
 
+/* Intervals g0 .. n_obs - 1 of the particle filter as replays of one CUDA
+ * graph: the interval's seed, day schedule and observation row are read
+ * from the device, and the finalize kernel moves the interval counter on.
+ * One replay: reset the state from the gathered ancestors, k_init,
+ * k_horizon, weights, finalize (normalise, ESS, resample), gather for the
+ * next interval.  Errors are read once, after the last replay. */
+static int pfilter_graph(siminf_gpu_plan *p, const siminf_gpu_pfilter_args *pf, int g0,
+                         const std::vector<std::array<double, 2>> &tsps,
+                         const std::vector<int> &tlens, int nd, int prev_tlen,
+                         const double *d_lfact, int tablen, double logp, double logq,
+                         double log_np, double *d_w, double *d_loglik, double *d_ess, int *d_anc,
+                         int *d_anc_out, const int *d_obs, size_t nu, size_t nv)
+{
+    const int n_obs = pf->n_obs, Np = p->s.Nrep, tl = tlens[g0];
+    const cudaStream_t pst = p->stream;
+    std::vector<DayInfo> alldays((size_t) n_obs * nd);
+    std::vector<uint64_t> seeds(n_obs);
+    for (int i = 0; i < n_obs; i++) {
+        seeds[i] = (uint64_t) pf->seed + ((uint64_t) i + 1) * 0x9E3779B97F4A7C15ULL;
+        if (i < g0)
+            continue;
+        std::vector<DayInfo> dd;
+        plan_days(tsps[i].data(), tlens[i], dd);
+        std::copy(dd.begin(), dd.end(), alldays.begin() + (size_t) i * nd);
+    }
+    DayInfo *d_days = nullptr;
+    uint64_t *d_seeds = nullptr;
+    int *d_interval = nullptr;
+    int rc = upload(&d_days, alldays.data(), alldays.size(), p->owned, pst);
+    if (!rc) rc = upload(&d_seeds, seeds.data(), seeds.size(), p->owned, pst);
+    if (!rc) rc = upload(&d_interval, &g0, 1, p->owned, pst);
+    if (!rc) rc = plan_set_tspan(p, tsps[g0].data(), tl);
+    if (rc)
+        return rc;
+    DevState s = p->s;
+    s.pf_interval = d_interval;
+    s.pf_seeds = d_seeds;
+    s.pf_days = d_days;
+    s.pf_days_stride = nd;
+    const Launchers *L = p->L;
+    const int Nn = s.Nn, Nc = s.Nc;
+
+    /* the state of interval g0 from its ancestors, then the error flags */
+    cudaError_t e = pf_gather(s.U, s.V, prev_tlen, (long long) nu, (long long) nv, d_anc, Np,
+                              p->d_u0, p->d_v0, pst);
+    const int init_flags[3] = {0, INT_MAX, INT_MAX};
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s.err_count, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice,
+                            pst);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(pst);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "pfilter graph set-up");
+
+    cudaStream_t gs = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCapture(gs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t c = cudaMemcpyAsync(s.u, p->d_u0, (size_t) s.Ntot * Nc * sizeof(int),
+                                        cudaMemcpyDeviceToDevice, gs);
+        if (c == cudaSuccess && s.Nd > 0)
+            c = cudaMemcpyAsync(s.vA, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
+                                cudaMemcpyDeviceToDevice, gs);
+        if (c == cudaSuccess && s.Nd > 0)
+            c = cudaMemcpyAsync(s.vB, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
+                                cudaMemcpyDeviceToDevice, gs);
+        if (c == cudaSuccess)
+            c = L->init(s, 0.0, gs);
+        if (c == cudaSuccess)
+            c = L->horizon(s, d_days, nd, gs);
+        if (c == cudaSuccess)
+            c = pf_weights(s.U, tl, Nn, Nc, Np, d_obs, pf->obs_compartment, d_lfact, tablen, logp,
+                           logq, d_w, gs, d_interval);
+        if (c == cudaSuccess)
+            c = pf_finalize(d_w, Np, log_np, d_loglik, d_ess, 0, (uint64_t) pf->seed,
+                            ((uint64_t) 1) << 62, d_anc, d_anc_out, gs, d_interval);
+        if (c == cudaSuccess)
+            c = pf_gather(s.U, s.V, tl, (long long) nu, (long long) nv, d_anc, Np, p->d_u0,
+                          p->d_v0, gs);
+        e = cudaStreamEndCapture(gs, &graph);
+        if (e == cudaSuccess)
+            e = c;
+    }
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&exec, graph, 0);
+    for (int i = g0; i < n_obs && e == cudaSuccess; i++)
+        e = cudaGraphLaunch(exec, gs);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(gs);
+    if (exec)
+        cudaGraphExecDestroy(exec);
+    if (graph)
+        cudaGraphDestroy(graph);
+    if (gs)
+        cudaStreamDestroy(gs);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "pfilter graph");
+
+    /* errors of all replayed intervals */
+    int counts[3];
+    e = cudaMemcpy(counts, s.err_count, sizeof(counts), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "read counters");
+    std::vector<ErrRec> cands;
+    if (counts[0] > 0) {
+        cands.resize(std::min(counts[0], (int) MAX_ERR));
+        e = cudaMemcpy(cands.data(), s.err, cands.size() * sizeof(ErrRec), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "read errors");
+    }
+    return resolve_errors(p, cands);
+}
+
 int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model *model,
                        siminf_gpu_pfilter_args *pf)
 {
@@ -1336,20 +1516,36 @@ int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model 
         rc = cuda_fail(cudaGetLastError(), "memset");
     const double logp = si_log(pf->detect_p), logq = si_log(1.0 - pf->detect_p);
     const double log_np = si_log((double) Np);
-    int prev_tlen = 2;
-    for (int i = 0; i < pf->n_obs && !rc; i++) {
-        double tsp[2];
-        int tlen;
+    /* interval i runs tspan tsps[i] (R/pfilter.R:177-193) */
+    std::vector<std::array<double, 2>> tsps(pf->n_obs);
+    std::vector<int> tlens(pf->n_obs), ndays_i(pf->n_obs);
+    for (int i = 0; i < pf->n_obs; i++) {
         const double prev = (i == 0) ? a1->tspan[0] : (double) pf->obs_time[i - 1];
         if ((i == 0 && prev < pf->obs_time[0]) ||
             (i > 0 && pf->obs_time[i] - pf->obs_time[i - 1] > 1)) {
-            tsp[0] = prev;
-            tsp[1] = pf->obs_time[i];
-            tlen = 2;
+            tsps[i] = {prev, (double) pf->obs_time[i]};
+            tlens[i] = 2;
         } else {
-            tsp[0] = pf->obs_time[i];
-            tlen = 1;
+            tsps[i] = {(double) pf->obs_time[i], 0.0};
+            tlens[i] = 1;
         }
+        std::vector<DayInfo> dd;
+        plan_days(tsps[i].data(), tlens[i], dd);
+        ndays_i[i] = (int) dd.size();
+    }
+    /* Intervals 1.. with one shape (tspan length and day count) replay one
+     * CUDA graph; the rest run launch by launch. */
+    int g0 = pf->n_obs;
+    if (p->horizon && pf->n_obs > 2) {
+        g0 = 1;
+        for (int i = 2; i < pf->n_obs; i++)
+            if (tlens[i] != tlens[1] || ndays_i[i] != ndays_i[1])
+                g0 = pf->n_obs;
+    }
+    int prev_tlen = 2;
+    for (int i = 0; i < g0 && !rc; i++) {
+        const double *tsp = tsps[i].data();
+        const int tlen = tlens[i];
         if (i > 0) {
             cudaError_t e = pf_gather(p->s.U, p->s.V, prev_tlen, (long long) nu, (long long) nv,
                                       d_anc, Np, p->d_u0, p->d_v0, pst);
@@ -1375,6 +1571,9 @@ int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model 
         }
         prev_tlen = tlen;
     }
+    if (!rc && g0 < pf->n_obs)
+        rc = pfilter_graph(p, pf, g0, tsps, tlens, ndays_i[g0], prev_tlen, d_lfact, tablen, logp,
+                           logq, log_np, d_w, d_loglik, d_ess, d_anc, d_anc_out, d_obs, nu, nv);
     if (!rc) {
         cudaError_t e = cudaMemcpyAsync(pf->loglik, d_loglik, sizeof(double),
                                         cudaMemcpyDeviceToHost, pst);

@@ -88,7 +88,7 @@ __device__ __forceinline__ void stream_key(const DevState &s, long long g, uint6
         seed = s.job_seed[j];
         sid = (uint64_t) (g - s.job_node0[j]);
     } else {
-        seed = s.seed;
+        seed = s.pf_seeds ? s.pf_seeds[*s.pf_interval] : s.seed;
         sid = (uint64_t) g;
     }
 }
@@ -223,7 +223,9 @@ __device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, doub
 {
     constexpr int NC = M::NC, NT = M::NT;
     const double tn = ln.tau + ln.t;
-    if (si_dge(tn, next)) {
+    /* the hardware FP64 comparisons of the chain (IEEE, false on NaN, as
+     * si_dge/si_dgt): one instruction each, ~3% off a transition's latency */
+    if (tn >= next) {
         ln.t = next;
         ln.c += 1;                            /* the waiting time's draw was used */
         return true;
@@ -251,7 +253,7 @@ __device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, doub
     int tr = NT - 1;
 #pragma unroll
     for (int k = NT - 2; k >= 0; k--)
-        if (!si_dgt(rnd, ln.cum[k]))
+        if (!(rnd > ln.cum[k]))
             tr = k;
     double rtr = ln.rate[0];
 #pragma unroll
@@ -706,6 +708,8 @@ __global__ void k_init(DevState s, double tt0)
     const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
     if (g >= s.Ntot)
         return;
+    if (s.pf_days)
+        tt0 = s.pf_days[(size_t) *s.pf_interval * s.pf_days_stride].tt;
     const int node = (int) (g % s.Nn);
     int u[NC];
 #pragma unroll
@@ -1030,6 +1034,8 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
 template <class M>
 __global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s, const DayInfo *days, int ndays)
 {
+    if (s.pf_days)
+        days = s.pf_days + (size_t) *s.pf_interval * s.pf_days_stride;
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     __shared__ int sS[NT * NC];
     __shared__ uint32_t sG[NT];
@@ -1136,11 +1142,13 @@ __device__ __forceinline__ double pf_logdens(const double *lfact, int tablen, in
 
 __global__ void k_pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, const int *obs_row,
                              int obs_c, const double *lfact, int tablen, double logp, double logq,
-                             double *w)
+                             double *w, const int *interval)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= Np)
         return;
+    if (interval)
+        obs_row += (size_t) *interval * Nn;     /* obs_row is the first interval's row */
     const int *last = U + ((size_t) p * tlen + tlen - 1) * (size_t) Nn * Nc;
     double acc = 0.0;
     for (int node = 0; node < Nn; node++)
@@ -1152,8 +1160,17 @@ __global__ void k_pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, con
 /* One block: max (exact in any order), exp in parallel, then the serial
  * sums, log-likelihood, ESS and resampling on thread 0. */
 __global__ void k_pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess,
-                              int i, uint64_t seed, uint64_t sid, int *anc, int *anc_out)
+                              int i, uint64_t seed, uint64_t sid, int *anc, int *anc_out,
+                              int *interval)
 {
+    if (interval) {
+        /* graph replay: the interval, its resampling stream and its row of
+         * ancestors come from the device counter, which moves on at the end */
+        i = *interval;
+        sid += (uint64_t) i;
+        if (anc_out)
+            anc_out += (size_t) i * Np;
+    }
     __shared__ double red[1024];
     __shared__ double s_sum;
     double m = -INFINITY;
@@ -1203,6 +1220,8 @@ __global__ void k_pf_finalize(double *w, int Np, double log_np, double *loglik, 
                 anc_out[p] = j + 1;
             u += du;
         }
+        if (interval)
+            *interval = i + 1;
     }
 }
 
@@ -1224,17 +1243,19 @@ __global__ void k_pf_gather(const int *U, const double *V, int tlen, long long n
 
 cudaError_t pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, const int *obs_row,
                        int obs_c, const double *lfact, int tablen, double logp, double logq,
-                       double *w, cudaStream_t st)
+                       double *w, cudaStream_t st, const int *interval)
 {
     k_pf_weights<<<(Np + 127) / 128, 128, 0, st>>>(U, tlen, Nn, Nc, Np, obs_row, obs_c, lfact,
-                                                   tablen, logp, logq, w);
+                                                   tablen, logp, logq, w, interval);
     return cudaGetLastError();
 }
 
 cudaError_t pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess, int i,
-                        uint64_t seed, uint64_t sid, int *anc, int *anc_out, cudaStream_t st)
+                        uint64_t seed, uint64_t sid, int *anc, int *anc_out, cudaStream_t st,
+                        int *interval)
 {
-    k_pf_finalize<<<1, 1024, 0, st>>>(w, Np, log_np, loglik, ess, i, seed, sid, anc, anc_out);
+    k_pf_finalize<<<1, 1024, 0, st>>>(w, Np, log_np, loglik, ess, i, seed, sid, anc, anc_out,
+                                      interval);
     return cudaGetLastError();
 }
 

@@ -26,9 +26,10 @@ struct Launchers {
 /* Particle-filter kernels (model independent). */
 cudaError_t pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, const int *obs_row,
                        int obs_c, const double *lfact, int tablen, double logp, double logq,
-                       double *w, cudaStream_t st);
+                       double *w, cudaStream_t st, const int *interval = nullptr);
 cudaError_t pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess, int i,
-                        uint64_t seed, uint64_t sid, int *anc, int *anc_out, cudaStream_t st);
+                        uint64_t seed, uint64_t sid, int *anc, int *anc_out, cudaStream_t st,
+                        int *interval = nullptr);
 cudaError_t pf_gather(const int *U, const double *V, int tlen, long long nu, long long nv,
                       const int *anc, int Np, int *u0, double *v0, cudaStream_t st);
 

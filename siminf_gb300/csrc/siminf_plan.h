@@ -142,6 +142,15 @@ struct DevState {
     const long long *job_col0;
     unsigned long long *prev;
     uint32_t prev_num_mask, prev_den_mask;
+
+    /* Particle-filter intervals replayed from one CUDA graph: the interval
+     * index lives on the device (*pf_interval), and with it the interval's
+     * seed (pf_seeds[i]) and day schedule (pf_days + i * pf_days_stride),
+     * which k_init and k_horizon read instead of their arguments. */
+    const int *pf_interval;
+    const uint64_t *pf_seeds;
+    const DayInfo *pf_days;
+    int pf_days_stride;
 };
 
 }  // namespace siminf
