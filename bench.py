@@ -191,6 +191,35 @@ def abc_bench(n, seed=11):
                     "end to end through the C ABI (host buffers)"}
 
 
+def sir_plain_bench(threads):
+    """The small plain case: mparse SIR, 1,000 nodes of (S=99, I=5, R=0),
+    beta=0.16, gamma=0.077, tspan 1:150, no events, seed 42; run() end to
+    end against the oracle port on the host cores.  Latency-bound (one
+    k_horizon launch); reported, not optimised for."""
+    from siminf_gb300 import abi, workloads
+    from siminf_gb300.run import run
+    from oracle import oracle
+    m = workloads.sir_plain()
+    run(m, seed=42)
+    ts = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        r = run(m, seed=42)
+        ts.append(time.perf_counter() - t0)
+    dt = min(ts)
+    node_days = m.Nn * len(m.tspan)
+    h = abi.build_args(m, 42)
+    t0 = time.perf_counter()
+    code, res = oracle.run(h, m.name, threads)
+    dc = time.perf_counter() - t0
+    return {"nodes": m.Nn, "days": len(m.tspan), "value": node_days / dt, "unit": UNIT,
+            "ms": dt * 1e3, "transitions": int(r.stats.transitions),
+            "cpu_baseline": {"value": node_days / dc, "unit": UNIT, "ms": dc * 1e3,
+                             "cores": threads, "kind": "port",
+                             "sample": "the whole case"},
+            "data": "synthetic SIR (mparse) 1,000 nodes x 150 days, end to end"}
+
+
 def pfilter_bench(particles):
     """The particle-filter workload: SISe with phi, 500 nodes per particle,
     52 weekly Binomial(I, 0.8) observations from a ground-truth run (seed 7),
@@ -366,6 +395,12 @@ def run_ours(args):
     plan = native.Plan(holder, m.name, cap_transfers=True)
     st = plan.stats()
     node_days = nodes * st.days
+    # the library's autotuner picks the work queue's heavy threshold on the
+    # first 120 days (results do not depend on it)
+    tune = plan.tune(probe_days=120, stream=C.c_void_p(stream.cuda_stream))
+    autotune = {"probe_days": tune.probe_days,
+                "heavy_rate_candidates": list(tune.heavy_rate),
+                "ms": list(tune.ms), "chosen_heavy_rate": tune.heavy_rate[tune.chosen]}
 
     def barrier():
         torch.cuda.synchronize()
@@ -428,6 +463,7 @@ def run_ours(args):
         pb.close()
         del hb, mb
 
+    sir = sir_plain_bench(os.cpu_count() or 1) if rank == 0 and world == 1 else None
     abc = abc_bench(args.abc) if args.abc > 0 and rank == 0 and world == 1 else None
     pf = (pfilter_bench(args.pfilter)
           if args.pfilter > 0 and rank == 0 and world == 1 else None)
@@ -505,7 +541,9 @@ def run_ours(args):
                                  "the SSA kernel is bound by FP64 latency, not HBM"
                                  % ALGO_BYTES_PER_NODE_DAY},
             "kernels": prof["kernels"],
+            "autotune": autotune,
             "batched": batched,
+            "sir_plain": sir,
             "abc": abc,
             "pfilter": pf,
             "serve": serve,

@@ -361,6 +361,25 @@ int siminf_gpu_plan_download(siminf_gpu_plan *plan, siminf_gpu_solver_args *args
 int siminf_gpu_plan_profile(siminf_gpu_plan *plan, void *cuda_stream, double ms[8],
                             long long launches[8]);
 int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
+
+/*
+ * Autotuner (no counterpart in the reference): times the plan's first
+ * probe_days days (0: 16) for each candidate threshold of the heavy part of
+ * the SSA work queue (rate sum from which a node is queued first and run 32
+ * to a warp; 0 turns the part off), keeps the fastest in the plan, and
+ * reports the times.  Results never depend on the threshold; only the
+ * order in which nodes are simulated does.
+ */
+#define SIMINF_GPU_TUNE_CANDIDATES 4
+typedef struct siminf_gpu_tune_result {
+    double heavy_rate[SIMINF_GPU_TUNE_CANDIDATES];
+    double ms[SIMINF_GPU_TUNE_CANDIDATES];     /* device time of the probe days */
+    int chosen;                                 /* index of the kept candidate */
+    int probe_days;
+} siminf_gpu_tune_result;
+
+int siminf_gpu_plan_tune(siminf_gpu_plan *plan, void *cuda_stream, int probe_days,
+                         siminf_gpu_tune_result *out);
 void siminf_gpu_plan_free(siminf_gpu_plan *plan);
 
 /*

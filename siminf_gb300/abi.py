@@ -171,6 +171,16 @@ class Stats(C.Structure):
     ]
 
 
+class TuneResult(C.Structure):
+    """siminf_gpu_tune_result."""
+    _fields_ = [
+        ("heavy_rate", C.c_double * 4),
+        ("ms", C.c_double * 4),
+        ("chosen", C.c_int),
+        ("probe_days", C.c_int),
+    ]
+
+
 class ServerOptions(C.Structure):
     """siminf_gpu_server_options."""
     _fields_ = [

@@ -985,12 +985,13 @@ static cudaError_t timed(KernelProfile *kp, int kind, cudaStream_t st, F &&launc
 static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, KernelProfile *kp)
 {
     const Launchers *L = p->L;
+    const int ndays = p->max_days > 0 ? std::min(p->max_days, p->ndays) : p->ndays;
     cudaError_t e = timed(kp, 0, st, [&] { return L->init(s, p->tt0, st); });
     if (e != cudaSuccess)
         return e;
     if (p->horizon)
-        return timed(kp, 4, st, [&] { return L->horizon(s, p->d_days, p->ndays, st); });
-    for (int d = 0; d < p->ndays && e == cudaSuccess; d++) {
+        return timed(kp, 4, st, [&] { return L->horizon(s, p->d_days, ndays, st); });
+    for (int d = 0; d < ndays && e == cudaSuccess; d++) {
         const DayInfo &di = p->days[d];
         e = timed(kp, 1, st, [&] { return L->ssa_e1(s, d, di.tt, di.next, st); });
         for (int w = p->day_wave[d]; w < p->day_wave[d + 1] && e == cudaSuccess; w++) {
@@ -1211,6 +1212,34 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
 int siminf_gpu_plan_run(siminf_gpu_plan *p, void *cuda_stream)
 {
     return plan_run_impl(p, (cudaStream_t) cuda_stream, nullptr);
+}
+
+int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
+                         siminf_gpu_tune_result *out)
+{
+    if (!p || p->e2_pending)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    static const double cand[SIMINF_GPU_TUNE_CANDIDATES] = {0.0, 2.0, 8.0, 32.0};
+    const cudaStream_t st = (cudaStream_t) cuda_stream;
+    const double saved = p->s.heavy_rate;
+    p->max_days = probe_days > 0 ? probe_days : 16;
+    siminf_gpu_tune_result r{};
+    int best = -1, rc = plan_run_impl(p, st, nullptr);     /* warm-up */
+    for (int k = 0; k < SIMINF_GPU_TUNE_CANDIDATES && !rc; k++) {
+        p->s.heavy_rate = cand[k];
+        rc = plan_run_impl(p, st, nullptr);
+        r.heavy_rate[k] = cand[k];
+        r.ms[k] = p->stats.ms_solve;
+        if (!rc && (best < 0 || r.ms[k] < r.ms[best]))
+            best = k;
+    }
+    p->max_days = 0;
+    p->s.heavy_rate = (best >= 0) ? cand[best] : saved;
+    r.chosen = best;
+    r.probe_days = std::min(probe_days > 0 ? probe_days : 16, p->ndays);
+    if (out)
+        *out = r;
+    return rc;
 }
 
 int siminf_gpu_plan_profile(siminf_gpu_plan *p, void *cuda_stream, double ms[8],

@@ -61,6 +61,7 @@ struct siminf_gpu_plan {
     siminf_gpu_stats stats{};
     bool ran = false;
     int days_cap = 0;
+    int max_days = 0;                   /* > 0: runs stop after this many days (tuning) */
 
     /* E2 planning state: events of day d go to positions e2_day_off[d] ..
      * e2_day_off[d + 1] of d_e2 and come from input range e2_lo[d] ..

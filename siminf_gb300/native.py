@@ -68,6 +68,8 @@ def lib():
     L.siminf_gpu_plan_download.argtypes = [vp, vp]
     L.siminf_gpu_plan_download.restype = C.c_int
     L.siminf_gpu_plan_stats.argtypes = [vp, C.POINTER(abi.Stats)]
+    L.siminf_gpu_plan_tune.argtypes = [vp, vp, C.c_int, C.POINTER(abi.TuneResult)]
+    L.siminf_gpu_plan_tune.restype = C.c_int
     L.siminf_gpu_plan_free.argtypes = [vp]
     L.siminf_gpu_plan_free.restype = None
     _lib = L
@@ -83,7 +85,7 @@ EXPORTS = (
     "siminf_gpu_plan_profile", "siminf_gpu_schedule", "siminf_gpu_pfilter",
     "siminf_gpu_run_solver_ssm_noalloc", "siminf_gpu_run_batch",
     "siminf_gpu_server_create", "siminf_gpu_server_submit", "siminf_gpu_server_wait",
-    "siminf_gpu_server_load", "siminf_gpu_server_free",
+    "siminf_gpu_server_load", "siminf_gpu_server_free", "siminf_gpu_plan_tune",
 )
 
 
@@ -167,6 +169,13 @@ class Plan:
 
     def download(self):
         check(lib().siminf_gpu_plan_download(self.handle, C.cast(self.holder.ref(), C.c_void_p)))
+
+    def tune(self, probe_days=16, stream=None):
+        """Autotune the work queue's heavy threshold on the first
+        probe_days days (siminf_gpu_plan_tune); returns the TuneResult."""
+        r = abi.TuneResult()
+        check(lib().siminf_gpu_plan_tune(self.handle, stream, int(probe_days), C.byref(r)))
+        return r
 
     def stats(self):
         st = abi.Stats()

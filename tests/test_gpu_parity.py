@@ -172,3 +172,42 @@ def test_gpu_heavy_queue_matches_oracle(gpu, oracle_lib, label, m, heavy_rate):
     assert code == 0
     assert np.array_equal(h.U, ho.U), label
     assert np.array_equal(h.V, ho.V), label
+
+
+def test_gpu_crn_option_same_streams(gpu):
+    """crn = 1 (SimInf_run_solver_mssm_crn, one generator per replicate and
+    node) is what every run here does already: each (replicate, node) draws
+    from its own stream, so crn = 1 and crn = 0 give the same trajectories."""
+    import ctypes as C
+    from siminf_gb300 import abi, native
+    label, m = [c for c in parity_cases() if c[0] == "seir_events_rep5"][0]
+    out = []
+    for crn in (0, 1):
+        h = abi.build_args(m, 42)
+        h.args.crn = crn
+        code = native.lib().siminf_gpu_run_solver_mssm(C.cast(h.ref(), C.c_void_p),
+                                                       native.device_model(m.name).handle)
+        assert code == 0
+        out.append(h.U.copy())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_gpu_autotune_keeps_results(gpu):
+    """siminf_gpu_plan_tune picks one of its candidate thresholds and the
+    tuned plan's trajectories are the untuned plan's."""
+    from siminf_gb300 import abi, native
+    label, m = [c for c in parity_cases() if c[0] == "seir_events_300x120"][0]
+    h1 = abi.build_args(m, 42)
+    p1 = native.Plan(h1, m.name)
+    p1.run()
+    p1.download()
+    h2 = abi.build_args(m, 42)
+    p2 = native.Plan(h2, m.name)
+    r = p2.tune(probe_days=10)
+    assert 0 <= r.chosen < 4 and r.probe_days == 10
+    assert r.heavy_rate[r.chosen] in (0.0, 2.0, 8.0, 32.0)
+    p2.run()
+    p2.download()
+    assert np.array_equal(h1.U, h2.U)
+    p1.close()
+    p2.close()

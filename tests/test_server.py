@@ -17,7 +17,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 STRUCTS = [("siminf_gpu_request", abi.Request), ("siminf_gpu_server_options", abi.ServerOptions),
            ("siminf_gpu_batch_job", abi.BatchJob), ("siminf_gpu_batch_options", abi.BatchOptions),
            ("siminf_gpu_pfilter_args", abi.PfilterArgs), ("siminf_gpu_options", abi.Options),
-           ("siminf_gpu_stats", abi.Stats), ("siminf_gpu_solver_args", abi.SolverArgs)]
+           ("siminf_gpu_stats", abi.Stats), ("siminf_gpu_solver_args", abi.SolverArgs),
+           ("siminf_gpu_tune_result", abi.TuneResult)]
 
 
 def test_struct_layouts_match_the_header():
