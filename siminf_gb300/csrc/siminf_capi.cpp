@@ -171,6 +171,17 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
 static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, struct KernelProfile *kp);
 }
 static int make_days(siminf_gpu_plan *p, const siminf_gpu_solver_args *a);
+/* Something a run depends on changed: the next run goes launch by launch
+ * and a later unchanged one captures a new graph. */
+static void plan_changed(siminf_gpu_plan *p)
+{
+    p->runs_unchanged = 0;
+    if (p->run_graph) {
+        cudaGraphExecDestroy(p->run_graph);
+        p->run_graph = nullptr;
+    }
+}
+
 template <class T>
 static int upload_owned(siminf_gpu_plan *p, T **dst, const T *src, size_t n);
 
@@ -617,6 +628,8 @@ void siminf_gpu_plan_free(siminf_gpu_plan *p)
 {
     if (!p)
         return;
+    if (p->run_graph)
+        cudaGraphExecDestroy(p->run_graph);
     for (void *q : p->owned) {
         if (p->async_alloc)
             cudaFreeAsync(q, p->stream);
@@ -1125,22 +1138,17 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
     return e;
 }
 
-extern "C" {
-
-static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
+/* The reset at the start of every run: error counters, transition counter,
+ * work queues, the state from u0/v0. */
+static cudaError_t reset_run(siminf_gpu_plan *p, const DevState &s, cudaStream_t st,
+                             bool from_device)
 {
-    if (!p)
-        return SIMINF_GPU_ERR_INVALID_MODEL;
-    memset(&g_status, 0, sizeof(g_status));
-    DevState s = p->s;
-    cudaError_t e;
-    cudaEvent_t ev0, ev1;
-    cudaEventCreate(&ev0);
-    cudaEventCreate(&ev1);
-    cudaEventRecord(ev0, st);
-
-    const int init_flags[3] = {0, INT_MAX, INT_MAX};
-    e = cudaMemcpyAsync(s.err_count, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice, st);
+    static const int init_flags[3] = {0, INT_MAX, INT_MAX};
+    cudaError_t e = from_device
+                        ? cudaMemcpyAsync(s.err_count, p->d_init_flags, sizeof(init_flags),
+                                          cudaMemcpyDeviceToDevice, st)
+                        : cudaMemcpyAsync(s.err_count, init_flags, sizeof(init_flags),
+                                          cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s.fired, 0, sizeof(unsigned long long), st);
     if (e == cudaSuccess)
@@ -1159,10 +1167,80 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
             e = cudaMemcpyAsync(s.vB, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
                                 cudaMemcpyDeviceToDevice, st);
     }
-    if (e != cudaSuccess)
-        return cuda_fail(e, "plan_run reset");
+    return e;
+}
 
-    if (p->e2_pending) {
+/* A graph of one whole run (reset + launch_all), captured on a side stream;
+ * false when it cannot be built (the run then goes launch by launch). */
+static bool build_run_graph(siminf_gpu_plan *p, const DevState &s)
+{
+    if (p->run_graph) {
+        cudaGraphExecDestroy(p->run_graph);
+        p->run_graph = nullptr;
+    }
+    if (!p->d_init_flags) {
+        static const int init_flags[3] = {0, INT_MAX, INT_MAX};
+        if (upload(&p->d_init_flags, init_flags, 3, p->owned, p->stream) ||
+            cudaStreamSynchronize(p->stream) != cudaSuccess)
+            return false;
+    }
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+        return false;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t c = reset_run(p, s, cs, true);
+        if (c == cudaSuccess)
+            c = launch_all(p, s, cs, nullptr);
+        e = cudaStreamEndCapture(cs, &graph);
+        if (e == cudaSuccess)
+            e = c;
+    }
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&p->run_graph, graph, 0);
+    if (graph)
+        cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) {
+        cudaGetLastError();             /* clear the sticky-free capture error */
+        p->run_graph = nullptr;
+        return false;
+    }
+    return true;
+}
+
+extern "C" {
+
+static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
+{
+    if (!p)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    memset(&g_status, 0, sizeof(g_status));
+    DevState s = p->s;
+    cudaError_t e;
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, st);
+
+    /* a run that repeats the previous one unchanged replays its graph */
+    const char *g_env = getenv("SIMINF_RUN_GRAPH");
+    const bool graphs = !(g_env && g_env[0] == '0');
+    const bool replay = graphs && !kp && !p->e2_pending && p->runs_unchanged >= 1 &&
+                        (p->run_graph || build_run_graph(p, s));
+    p->runs_unchanged++;
+    if (replay) {
+        e = cudaGraphLaunch(p->run_graph, st);
+    } else {
+        e = reset_run(p, s, st, false);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "plan_run reset");
+    }
+
+    if (replay) {
+        /* the graph holds the whole run */
+    } else if (p->e2_pending) {
         e = launch_streamed(p, s, st);
         p->e2_pending = false;
         p->h_e2.reset();
@@ -1223,10 +1301,12 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
     const cudaStream_t st = (cudaStream_t) cuda_stream;
     const double saved = p->s.heavy_rate;
     p->max_days = probe_days > 0 ? probe_days : 16;
+    plan_changed(p);
     siminf_gpu_tune_result r{};
     int best = -1, rc = plan_run_impl(p, st, nullptr);     /* warm-up */
     for (int k = 0; k < SIMINF_GPU_TUNE_CANDIDATES && !rc; k++) {
         p->s.heavy_rate = cand[k];
+        plan_changed(p);
         rc = plan_run_impl(p, st, nullptr);
         r.heavy_rate[k] = cand[k];
         r.ms[k] = p->stats.ms_solve;
@@ -1235,6 +1315,7 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
     }
     p->max_days = 0;
     p->s.heavy_rate = (best >= 0) ? cand[best] : saved;
+    plan_changed(p);
     r.chosen = best;
     r.probe_days = std::min(probe_days > 0 ? probe_days : 16, p->ndays);
     if (out)
@@ -1342,6 +1423,7 @@ static int plan_set_tspan(siminf_gpu_plan *p, const double *tspan, int tlen)
         return rc;
     p->s.tlen = tlen;
     p->tt0 = tspan[0];
+    plan_changed(p);
     if (p->days_cap < p->ndays) {
         DayInfo *d = nullptr;
         if ((rc = dalloc(&d, (size_t) p->ndays, p->owned)))

@@ -62,6 +62,11 @@ struct siminf_gpu_plan {
     bool ran = false;
     int days_cap = 0;
     int max_days = 0;                   /* > 0: runs stop after this many days (tuning) */
+    /* A run that repeats the previous one unchanged replays it from a CUDA
+     * graph (the reset copies and every kernel launch of the run). */
+    cudaGraphExec_t run_graph = nullptr;
+    int runs_unchanged = 0;             /* runs since the last change of the plan */
+    int *d_init_flags = nullptr;        /* {0, INT_MAX, INT_MAX}: the error counters' reset */
 
     /* E2 planning state: events of day d go to positions e2_day_off[d] ..
      * e2_day_off[d + 1] of d_e2 and come from input range e2_lo[d] ..

@@ -211,3 +211,22 @@ def test_gpu_autotune_keeps_results(gpu):
     assert np.array_equal(h1.U, h2.U)
     p1.close()
     p2.close()
+
+
+@pytest.mark.parametrize("name", ["seir_events_rep5", "sise_200x199"])
+def test_gpu_plan_rerun_graph(gpu, oracle_lib, name):
+    """A plan run again unchanged replays its run from a CUDA graph; every
+    run gives the oracle's trajectories."""
+    from siminf_gb300 import abi, native
+    m = dict(parity_cases())[name]
+    _, _, ho = run_oracle(m, threads=4)
+    h = abi.build_args(m, 42)
+    p = native.Plan(h, m.name)
+    for _ in range(3):
+        h.U[:] = -1
+        p.run()
+        p.download()
+        assert np.array_equal(h.U, ho.U)
+        if m.Nd:
+            assert np.array_equal(h.V, ho.V)
+    p.close()
