@@ -518,11 +518,26 @@ SI_HD double si_neglog_u32_tab(uint32_t w)
     return si_u128_to_double_at(hi, lo, p, 64);
 }
 
+#ifdef __CUDACC__
+/* The rare hand-over to si_log, kept out of line on the device: it is
+ * taken by 1 word in 256, and inlined it would double the code of the SSA
+ * step that every warp keeps in its instruction cache. */
+static __device__ __noinline__ double si_neglog_slow(uint32_t w)
+{
+    return -si_log(si_u32_to_uniform_pos(w));
+}
+#endif
+
 SI_HD double si_neglog_u32(uint32_t w)
 {
     const uint64_t x = 2 * (uint64_t) w + 1;
-    if (x >= ((uint64_t) 1 << 33) - ((uint64_t) 1 << 25))
+    if (x >= ((uint64_t) 1 << 33) - ((uint64_t) 1 << 25)) {
+#ifdef __CUDA_ARCH__
+        return si_neglog_slow(w);
+#else
         return -si_log(si_u32_to_uniform_pos(w));
+#endif
+    }
     return si_neglog_u32_tab(w);
 }
 
