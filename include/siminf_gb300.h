@@ -203,6 +203,14 @@ int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args,
                              const siminf_gpu_options *options);
 
 /*
+ * No counterpart in the reference.  The run entry points keep the pinned
+ * host buffers through which they stage external transfers (at most four,
+ * 4 GiB in all) for the next run, and copy U/V back during the run when
+ * those arrays are pinned.  This frees the kept buffers.
+ */
+void siminf_gpu_release_cached(void);
+
+/*
  * Many independent models of one device model in one run -- different node
  * counts, tspan lengths (prefixes of one grid from the same tspan[0]),
  * events, parameters (ldata/gdata) and seeds -- each reduced on the device

@@ -35,6 +35,7 @@
 #include <atomic>
 #include <limits>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -111,6 +112,90 @@ int upload(T **p, const T *src, size_t n, std::vector<void *> &owned, cudaStream
 double ms_since(std::chrono::steady_clock::time_point t0)
 {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+/* Pinned host staging buffers kept between runs.  Pinning the half
+ * gigabyte that a streamed run of 10^6 nodes stages its external
+ * transfers through takes longer than several days of the GPU's work, so
+ * a buffer a run releases is kept for the next run: at most PINNED_KEEP
+ * buffers and PINNED_KEEP_BYTES in all, freed by
+ * siminf_gpu_release_cached. */
+enum { PINNED_KEEP = 4 };
+constexpr size_t PINNED_KEEP_BYTES = (size_t) 4 << 30;
+
+struct PinnedCache {
+    std::mutex mu;
+    std::vector<std::pair<void *, size_t>> free_list;
+};
+
+PinnedCache &pinned_cache()
+{
+    static PinnedCache c;
+    return c;
+}
+
+/* A pinned buffer of at least `bytes`: the smallest cached one that
+ * fits, else a new one. */
+cudaError_t pinned_acquire(size_t bytes, void **out, size_t *got)
+{
+    PinnedCache &c = pinned_cache();
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        int best = -1;
+        for (size_t i = 0; i < c.free_list.size(); i++)
+            if (c.free_list[i].second >= bytes &&
+                (best < 0 || c.free_list[i].second < c.free_list[best].second))
+                best = (int) i;
+        if (best >= 0) {
+            *out = c.free_list[best].first;
+            *got = c.free_list[best].second;
+            c.free_list.erase(c.free_list.begin() + best);
+            return cudaSuccess;
+        }
+    }
+    *got = bytes;
+    return cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+}
+
+/* Return a buffer of pinned_acquire: kept if the cache has room, the
+ * smallest buffers leaving first. */
+void pinned_release(void *ptr, size_t bytes)
+{
+    if (!ptr)
+        return;
+    PinnedCache &c = pinned_cache();
+    std::vector<void *> drop;
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        c.free_list.emplace_back(ptr, bytes);
+        std::sort(c.free_list.begin(), c.free_list.end(),
+                  [](const std::pair<void *, size_t> &x, const std::pair<void *, size_t> &y) {
+                      return x.second > y.second;
+                  });
+        size_t total = 0, keep = 0;
+        while (keep < c.free_list.size() && keep < PINNED_KEEP &&
+               total + c.free_list[keep].second <= PINNED_KEEP_BYTES)
+            total += c.free_list[keep++].second;
+        for (size_t i = keep; i < c.free_list.size(); i++)
+            drop.push_back(c.free_list[i].first);
+        c.free_list.resize(keep);
+    }
+    for (void *q : drop)
+        cudaFreeHost(q);
+}
+
+/* True if host pointer q is pinned (page-locked or registered), so that an
+ * asynchronous copy to it does not hold the calling thread. */
+bool host_pinned(const void *q)
+{
+    if (!q)
+        return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
 }
 
 }  // namespace
@@ -320,40 +405,58 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
         std::vector<PlannedErr> planned;
     };
     std::vector<Chunk> chunks(planner_threads());
+    const int E2 = SIMINF_GPU_EXTERNAL_TRANSFER_EVENT;
     parallel([&](int t, int n) {
         Chunk &c = chunks[t];
         c.e2_per_day.assign(ndays + 1, 0);
         const long long lo = len * t / n, hi = len * (t + 1) / n;
+        const int *time = a->time, *event = a->event, *node_ = a->node, *dest_ = a->dest,
+                  *select = a->select;
+        int pt = lo > 0 ? time[lo - 1] : INT_MIN, pk = lo > 0 ? event[lo - 1] : 0;
+        /* times are sorted, so the day changes rarely: it is recomputed
+         * when the time changes, and the day's count of valid transfers is
+         * kept in a register until then */
+        long long d = -1;
+        int d_time = 0;
+        long long run = 0;
         for (long long i = lo; i < hi; i++) {
-            const int tm = a->time[i], kind = a->event[i];
-            if (i > 0) {
-                const int pt = a->time[i - 1], pk = a->event[i - 1];
-                if (tm < pt || (tm == pt && pk == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT &&
-                                kind != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)) {
-                    if (c.bad < 0)
-                        c.bad = i;
-                }
+            const int tm = time[i], kind = event[i];
+            if (tm < pt || (tm == pt && pk == E2 && kind != E2)) {
+                if (c.bad < 0)
+                    c.bad = i;
             }
-            const long long d = event_day(tm, tt0);
+            pt = tm;
+            pk = kind;
+            if (d < 0 || tm != d_time) {
+                if (d >= 0 && d < ndays)
+                    c.e2_per_day[d] += run;
+                run = 0;
+                d = event_day(tm, tt0);
+                d_time = tm;
+            }
             if (d >= ndays)
                 continue;
-            const int node = a->node[i] - 1, dest = a->dest[i] - 1;
-            const int phase = kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT ? PHASE_E2 : PHASE_E1;
-            if (node < 0 || node >= Nn) {
-                c.planned.push_back({(int) d, SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, (int) i, node, phase});
-            } else if (kind < 0 || kind > 3) {
-                c.planned.push_back({(int) d, SIMINF_GPU_UNDEFINED_EVENT, (int) i, node, phase});
-            } else if (a->select[i] - 1 < 0 || a->select[i] - 1 >= nsel) {
-                c.planned.push_back({(int) d, SIMINF_GPU_ERR_SAMPLE_SELECT, (int) i, node, phase});
-            } else if (kind == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT) {
-                if (dest < 0 || dest >= Nn)
-                    c.planned.push_back({(int) d, SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS, (int) i, node, phase});
-                else
-                    c.e2_per_day[d]++;
-            } else {
-                c.e1.push_back(i);
+            const unsigned node = (unsigned) (node_[i] - 1), dest = (unsigned) (dest_[i] - 1),
+                           sel = (unsigned) (select[i] - 1);
+            const bool ok = node < (unsigned) Nn && (unsigned) kind <= 3u && sel < (unsigned) nsel;
+            if (ok && kind == E2 && dest < (unsigned) Nn) {
+                run++;
+                continue;
             }
+            const int phase = kind == E2 ? PHASE_E2 : PHASE_E1;
+            if (node >= (unsigned) Nn)
+                c.planned.push_back({(int) d, SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, (int) i, (int) node, phase});
+            else if ((unsigned) kind > 3u)
+                c.planned.push_back({(int) d, SIMINF_GPU_UNDEFINED_EVENT, (int) i, (int) node, phase});
+            else if (sel >= (unsigned) nsel)
+                c.planned.push_back({(int) d, SIMINF_GPU_ERR_SAMPLE_SELECT, (int) i, (int) node, phase});
+            else if (kind == E2)
+                c.planned.push_back({(int) d, SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS, (int) i, (int) node, phase});
+            else
+                c.e1.push_back(i);
         }
+        if (d >= 0 && d < ndays)
+            c.e2_per_day[d] += run;
     });
     long long bad = -1;
     for (auto &c : chunks) {
@@ -426,57 +529,73 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
     return 0;
 }
 
-/* Per-thread scratch of the wave planner: per node, its levels on the day
- * being planned, 16 bits each so the table of a million nodes stays in
- * cache (zero outside the day; the nodes a day touches are listed and
- * cleared after it).  A day whose wavefronts run deeper than 2^16 - 1 is
- * planned again with 32-bit levels. */
+/* Per-thread scratch of the wave planner: per node, its two levels on
+ * the day being planned (the last event with the node as source, `excl`,
+ * and the last add into it, `add`), packed into one word so that an event
+ * touches one cache line per node: 16 bits each, so the table of a
+ * million nodes (4 MB) stays in cache.  Zero outside the day; the nodes a
+ * day touches are listed and cleared after it.  A day whose wavefronts run
+ * deeper than 2^16 - 1 is planned again with 32-bit levels. */
 struct WaveTracker {
-    std::vector<uint16_t> excl, add;
+    std::vector<uint32_t> lv;
     std::vector<int> touched, level;
     std::vector<long long> idx;
     std::vector<long long> cnt, off;
-    explicit WaveTracker(int Nn) : excl(Nn, 0), add(Nn, 0) {}
+    explicit WaveTracker(int Nn) : lv(Nn, 0) {}
 };
 
 /* Levels of day d's external transfers into w.level / w.idx; T is the
- * level type.  Returns false if a level would not fit T. */
-template <class T>
+ * level type and P packs two of them (excl low, add high).  Returns false
+ * if a level would not fit T. */
+template <class T, class P>
 static bool day_levels(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
-                       WaveTracker &w, T *excl, T *add, int &maxl)
+                       WaveTracker &w, P *lv, int &maxl)
 {
-    const int Nn = a->Nn, nsel = p->nsel;
+    constexpr int SH = 8 * sizeof(T);
+    constexpr P LO = ((P) 1 << SH) - 1;
+    constexpr long long PF = 16;            /* prefetch distance, in events */
+    const unsigned Nn = (unsigned) a->Nn, nsel = (unsigned) p->nsel;
     const long long limit = (long long) std::numeric_limits<T>::max();
     const int *ev = a->event, *src = a->node, *dst = a->dest, *sel = a->select;
+    const long long lo = p->e2_lo[d], hi = p->e2_hi[d];
     w.level.clear();
     w.idx.clear();
     w.touched.clear();
     maxl = 0;
     bool ok = true;
-    for (long long i = p->e2_lo[d]; i < p->e2_hi[d]; i++) {
+    for (long long i = lo; i < hi; i++) {
+        if (i + PF < hi) {
+            const unsigned ps = (unsigned) (src[i + PF] - 1), pd = (unsigned) (dst[i + PF] - 1);
+            __builtin_prefetch(lv + (ps < Nn ? ps : 0), 1);
+            __builtin_prefetch(lv + (pd < Nn ? pd : 0), 1);
+        }
         if (ev[i] != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)
             continue;
-        const int s = src[i] - 1, t = dst[i] - 1;
-        if (s < 0 || s >= Nn || t < 0 || t >= Nn || sel[i] - 1 < 0 || sel[i] - 1 >= nsel)
+        const unsigned s = (unsigned) (src[i] - 1), t = (unsigned) (dst[i] - 1);
+        if (s >= Nn || t >= Nn || (unsigned) (sel[i] - 1) >= nsel)
             continue;
-        if (!excl[s] && !add[s])
-            w.touched.push_back(s);
-        if (!excl[t] && !add[t])
-            w.touched.push_back(t);
-        const long long L = 1 + (long long) std::max(std::max(excl[s], add[s]), excl[t]);
+        const P vs = lv[s], vt = lv[t];
+        if (!vs)
+            w.touched.push_back((int) s);
+        if (!vt)
+            w.touched.push_back((int) t);
+        const long long es = (long long) (vs & LO), as = (long long) (vs >> SH),
+                        et = (long long) (vt & LO);
+        const long long L = 1 + std::max(std::max(es, as), et);
         if (L > limit) {
             ok = false;
             break;
         }
-        excl[s] = (T) L;
-        if (add[t] < (T) L)
-            add[t] = (T) L;
+        lv[s] = (vs & ~LO) | (P) L;
+        const P vt2 = lv[t];                /* re-read: s == t sees its own update */
+        if ((long long) (vt2 >> SH) < L)
+            lv[t] = (vt2 & LO) | ((P) L << SH);
         w.level.push_back((int) L);
         w.idx.push_back(i);
         maxl = std::max(maxl, (int) L);
     }
     for (int n : w.touched)
-        excl[n] = add[n] = 0;
+        lv[n] = 0;
     return ok;
 }
 
@@ -489,9 +608,9 @@ static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, 
                            WaveTracker &w, E2Rec *e2, long long base = 0)
 {
     int maxl = 0;
-    if (!day_levels<uint16_t>(p, a, d, w, w.excl.data(), w.add.data(), maxl)) {
-        std::vector<int> excl(a->Nn, 0), add(a->Nn, 0);
-        day_levels<int>(p, a, d, w, excl.data(), add.data(), maxl);
+    if (!day_levels<uint16_t>(p, a, d, w, w.lv.data(), maxl)) {
+        std::vector<uint64_t> lv(a->Nn, 0);
+        day_levels<uint32_t>(p, a, d, w, lv.data(), maxl);
     }
     const int *src = a->node, *dst = a->dest, *sel = a->select;
     std::vector<int> &level = w.level;
@@ -995,6 +1114,40 @@ static cudaError_t timed(KernelProfile *kp, int kind, cudaStream_t st, F &&launc
     return e;
 }
 
+/* Copies of columns [c_lo, c_hi) of every replicate's U and V (dense or
+ * sparse, column k of replicate r at k + r * tlen) to a's host arrays,
+ * queued on st. */
+static cudaError_t download_columns(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a,
+                                    int c_lo, int c_hi, cudaStream_t st)
+{
+    const DevState &s = p->s;
+    const size_t col_u = (size_t) s.Nn * s.Nc, col_v = (size_t) s.Nn * s.Nd;
+    const auto d2h = cudaMemcpyDeviceToHost;
+    cudaError_t e = cudaSuccess;
+    for (int r = 0; r < s.Nrep && c_hi > c_lo && e == cudaSuccess; r++) {
+        const size_t k0 = (size_t) r * s.tlen + c_lo, k1 = (size_t) r * s.tlen + c_hi;
+        if (a->U && s.U) {
+            e = cudaMemcpyAsync(a->U + k0 * col_u, s.U + k0 * col_u,
+                                (k1 - k0) * col_u * sizeof(int), d2h, st);
+        } else if (a->prU && s.prU) {
+            const size_t j0 = (size_t) a->jcU[k0], j1 = (size_t) a->jcU[k1];
+            if (j1 > j0)
+                e = cudaMemcpyAsync(a->prU + j0, s.prU + j0, (j1 - j0) * sizeof(double), d2h, st);
+        }
+        if (e != cudaSuccess)
+            break;
+        if (a->V && s.V && col_v) {
+            e = cudaMemcpyAsync(a->V + k0 * col_v, s.V + k0 * col_v,
+                                (k1 - k0) * col_v * sizeof(double), d2h, st);
+        } else if (a->prV && s.prV) {
+            const size_t j0 = (size_t) a->jcV[k0], j1 = (size_t) a->jcV[k1];
+            if (j1 > j0)
+                e = cudaMemcpyAsync(a->prV + j0, s.prV + j0, (j1 - j0) * sizeof(double), d2h, st);
+        }
+    }
+    return e;
+}
+
 static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, KernelProfile *kp)
 {
     const Launchers *L = p->L;
@@ -1028,6 +1181,8 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
  * earlier days.  The planners write each chunk straight into one slot of a
  * ring of pinned host buffers, from which the copy runs as DMA without
  * holding this thread; a slot is reused once its previous copy is done.
+ * With pinned output arrays (p->out_args) the columns of U/V each chunk
+ * finishes are copied back on a third stream while later days run.
  * The kernels and their order are those of launch_all. */
 static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t st)
 {
@@ -1046,8 +1201,8 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
         slot_len = std::max(slot_len, p->e2_day_off[d1] - p->e2_day_off[d0]);
     }
     E2Rec *ring = nullptr;
-    e = cudaHostAlloc((void **) &ring, (size_t) RING * slot_len * sizeof(E2Rec),
-                      cudaHostAllocDefault);
+    size_t ring_bytes = 0;
+    e = pinned_acquire((size_t) RING * slot_len * sizeof(E2Rec), (void **) &ring, &ring_bytes);
     if (e != cudaSuccess)
         return e;
 
@@ -1085,8 +1240,11 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             }
         });
 
-    cudaStream_t cs = nullptr;
+    cudaStream_t cs = nullptr, ds = nullptr;
+    std::vector<cudaEvent_t> stored;
     e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess && p->out_args)
+        e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking);
     for (int c = 0; c < nchunks && e == cudaSuccess; c++) {
         const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
         for (int d = d0; d < d1 && !failed.load(); d++)
@@ -1120,6 +1278,22 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
                 e = L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
             std::swap(s.vA, s.vB);
         }
+        /* the columns this chunk finished go back while later days run */
+        const int c_hi = p->days[d1 - 1].c1;
+        if (ds && e == cudaSuccess && c_hi > p->cols_sent) {
+            cudaEvent_t ev = nullptr;
+            e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            if (e == cudaSuccess) {
+                stored.push_back(ev);
+                e = cudaEventRecord(ev, st);
+            }
+            if (e == cudaSuccess)
+                e = cudaStreamWaitEvent(ds, ev, 0);
+            if (e == cudaSuccess)
+                e = download_columns(p, p->out_args, p->cols_sent, c_hi, ds);
+            if (e == cudaSuccess)
+                p->cols_sent = c_hi;
+        }
     }
     /* planners waiting for a slot give up once the copies stop */
     abort.store(1);
@@ -1131,10 +1305,18 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             e = e2;
         cudaStreamDestroy(cs);
     }
+    if (ds) {
+        const cudaError_t e2 = cudaStreamSynchronize(ds);
+        if (e == cudaSuccess)
+            e = e2;
+        cudaStreamDestroy(ds);
+    }
     for (cudaEvent_t ev : copied)
         if (ev)
             cudaEventDestroy(ev);
-    cudaFreeHost(ring);
+    for (cudaEvent_t ev : stored)
+        cudaEventDestroy(ev);
+    pinned_release(ring, ring_bytes);
     return e;
 }
 
@@ -1713,9 +1895,22 @@ static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *mode
     int rc = plan_create_impl(args, model, opt, &p, true);
     if (rc)
         return rc;
+    /* pinned outputs come back chunk by chunk during the run */
+    if (p->e2_pending && host_pinned(args->U ? (const void *) args->U : args->prU) &&
+        (p->s.Nd == 0 || host_pinned(args->V ? (const void *) args->V : args->prV)))
+        p->out_args = args;
     rc = plan_run_impl(p, p->stream, nullptr);
-    if (!rc)
+    if (!rc && p->out_args) {
+        auto t0 = std::chrono::steady_clock::now();
+        cudaError_t e = download_columns(p, args, p->cols_sent, p->s.tlen, p->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(p->stream);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "download");
+        p->stats.ms_download = ms_since(t0);
+    } else if (!rc) {
         rc = siminf_gpu_plan_download(p, args);
+    }
     g_stats = p->stats;
     siminf_gpu_plan_free(p);
     return rc;
@@ -1735,6 +1930,18 @@ int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args, const siminf_gpu_mode
                              const siminf_gpu_options *options)
 {
     return run_solver(args, model, options);
+}
+
+void siminf_gpu_release_cached(void)
+{
+    PinnedCache &c = pinned_cache();
+    std::vector<std::pair<void *, size_t>> drop;
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        drop.swap(c.free_list);
+    }
+    for (auto &b : drop)
+        cudaFreeHost(b.first);
 }
 
 }  /* extern "C" */

@@ -79,6 +79,11 @@ struct siminf_gpu_plan {
     bool e2_pending = false;
     siminf_gpu_solver_args args{};
     std::unique_ptr<E2Rec[]> h_e2;
+    /* Streamed runs with pinned output arrays: each chunk's finished
+     * columns of U/V go back to out_args while later days run; columns
+     * [0, cols_sent) of every replicate are copied or on their way. */
+    siminf_gpu_solver_args *out_args = nullptr;
+    int cols_sent = 0;
 };
 
 namespace siminf {

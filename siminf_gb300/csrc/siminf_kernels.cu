@@ -47,7 +47,8 @@ enum { ERR_NEGATIVE_STATE = -1, ERR_UNDEFINED_EVENT = -3, ERR_SAMPLE_SELECT = -8
 
 enum { EV_EXIT = 0, EV_ENTER = 1, EV_INTERNAL = 2, EV_EXTERNAL = 3 };
 
-__device__ __forceinline__ void record_error(const DevState &s, int code, int phase, int day,
+/* Out of line: errors are rare, and every kernel calls this. */
+__device__ __noinline__ void record_error(const DevState &s, int code, int phase, int day,
                                              long long g, int tr, int evi, double time,
                                              double rate)
 {
@@ -569,16 +570,51 @@ __device__ int apply_e1(const DevState &s, int *uu, const E1Rec &e, si_rng *r)
     }
 }
 
-/* The node's E1 events of `day`, in array order.  Returns true when an
- * event was applied (the node is then flagged for a rate refresh). */
+/* The E1 events of one node-day, applied out of line: about one node-day
+ * in 250 has any, and inlined, the samplers they use would sit in the
+ * code of the SSA loop that every warp of k_ssa_e1 runs.  State and
+ * stream counter go in and out by value, so the caller's copies stay in
+ * registers. */
 template <int NC>
-__device__ bool node_e1(const DevState &s, int (&u)[NC], int node, int day, si_rng &r,
-                        long long g, double tt, int &err_code, int &err_event)
+struct E1Out {
+    int u[NC];
+    uint64_t ctr;
+    int err_code, err_event;
+    bool any;
+};
+
+template <int NC>
+__device__ __noinline__ E1Out<NC> node_e1_apply(const DevState &s, E1Out<NC> o, si_rng r, int lo,
+                                                int end, int day)
+{
+    for (int k = lo; k < end; k++) {
+        const E1Rec e = s.e1[k];
+        if (e.day != day)
+            break;
+        const int err = apply_e1<NC>(s, o.u, e, &r);
+        o.any = true;
+        if (err) {
+            o.err_code = err;
+            o.err_event = e.index;
+            break;
+        }
+    }
+    o.ctr = r.ctr;
+    return o;
+}
+
+/* The node's E1 events of `day` (src/solvers/SimInf_solver.c:658-822), in
+ * array order, applied to u with draws from r.  Returns true when an event
+ * was applied (the node is then flagged for a rate refresh).  A node's
+ * events are stored in day order: the day's first is found by bisection. */
+template <int NC>
+__device__ __forceinline__ bool node_e1(const DevState &s, int (&u)[NC], int node, int day,
+                                        si_rng &r, long long g, double tt, int &err_code,
+                                        int &err_event)
 {
     int lo = s.e1_ptr[node], hi = s.e1_ptr[node + 1];
     if (lo == hi)
         return false;
-    /* first event with e.day >= day */
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if (s.e1[mid].day < day)
@@ -589,27 +625,25 @@ __device__ bool node_e1(const DevState &s, int (&u)[NC], int node, int day, si_r
     const int end = s.e1_ptr[node + 1];
     if (lo >= end || s.e1[lo].day != day)
         return false;
-    int uu[NC];
+    E1Out<NC> o;
 #pragma unroll
     for (int c = 0; c < NC; c++)
-        uu[c] = u[c];
-    bool any = false;
-    for (int k = lo; k < end; k++) {
-        const E1Rec e = s.e1[k];
-        if (e.day != day)
-            break;
-        const int err = apply_e1<NC>(s, uu, e, &r);
-        any = true;
-        if (err) {
-            err_code = err;
-            err_event = e.index;
-            break;
-        }
+        o.u[c] = u[c];
+    o.ctr = r.ctr;
+    o.err_code = 0;
+    o.err_event = -1;
+    o.any = false;
+    o = node_e1_apply<NC>(s, o, r, lo, end, day);
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+        u[c] = o.u[c];
+    r.ctr = o.ctr;
+    r.have = 0;
+    if (o.err_code) {
+        err_code = o.err_code;
+        err_event = o.err_event;
     }
-#pragma unroll
-    for (int c = 0; c < NC; c++)
-        u[c] = uu[c];
-    return any;
+    return o.any;
 }
 
 /* Store the node's U/V entries for columns [c0, c1) of its replicate. */
@@ -885,13 +919,13 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
                 node_finish<M>(s, ln, r, g, day, tt, fired);
                 need = true;
                 heavy = false;
-            } else if (heavy) {
-                /* a heavy warp has nothing else to do: the whole day in a
-                 * tight loop */
-                while (!done)
-                    done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG);
             } else {
-                done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG);
+                /* one step; a heavy warp has nothing else to do and runs
+                 * its whole day in this loop (one call site of the step
+                 * keeps the loop's code small) */
+                do
+                    done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG);
+                while (heavy && !done);
             }
         }
     }

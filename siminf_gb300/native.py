@@ -72,6 +72,8 @@ def lib():
     L.siminf_gpu_plan_tune.restype = C.c_int
     L.siminf_gpu_plan_free.argtypes = [vp]
     L.siminf_gpu_plan_free.restype = None
+    L.siminf_gpu_release_cached.argtypes = []
+    L.siminf_gpu_release_cached.restype = None
     _lib = L
     return L
 
@@ -86,6 +88,7 @@ EXPORTS = (
     "siminf_gpu_run_solver_ssm_noalloc", "siminf_gpu_run_batch",
     "siminf_gpu_server_create", "siminf_gpu_server_submit", "siminf_gpu_server_wait",
     "siminf_gpu_server_load", "siminf_gpu_server_free", "siminf_gpu_plan_tune",
+    "siminf_gpu_release_cached",
 )
 
 

@@ -230,3 +230,61 @@ def test_gpu_plan_rerun_graph(gpu, oracle_lib, name):
         if m.Nd:
             assert np.array_equal(h.V, ho.V)
     p.close()
+
+
+def _pin_outputs(h, torch):
+    """Move the holder's output arrays into pinned host memory."""
+    import ctypes as C
+    for name, ctype in (("U", C.c_int), ("V", C.c_double), ("prU", C.c_double),
+                        ("prV", C.c_double)):
+        arr = getattr(h, name)
+        if arr is None:
+            continue
+        t = torch.from_numpy(arr).pin_memory()
+        h.keep.append(t)
+        pinned = t.numpy()
+        setattr(h, name, pinned)
+        setattr(h.args, name, pinned.ctypes.data_as(C.POINTER(ctype)))
+
+
+@pytest.mark.parametrize("name", ["seir_events_300x120", "seir_events_rep5", "sise3_events"])
+def test_gpu_pinned_outputs_streamed_back(gpu, oracle_lib, name):
+    """With pinned U/V a run with external transfers copies each chunk of
+    finished columns back while later days run (a third stream); the
+    arrays hold the oracle's trajectories, for every replicate."""
+    import ctypes as C
+    from siminf_gb300 import abi, native
+    torch = pytest.importorskip("torch")
+    m = dict(parity_cases())[name]
+    _, _, ho = run_oracle(m, threads=4)
+    for _ in range(2):                      # the second run reuses the kept staging buffer
+        h = abi.build_args(m, 42)
+        _pin_outputs(h, torch)
+        h.U[:] = -1
+        code = native.lib().siminf_gpu_run_solver_ex(C.cast(h.ref(), C.c_void_p),
+                                                     native.device_model(m.name).handle, None)
+        assert code == 0
+        assert np.array_equal(h.U, ho.U), name
+        if m.Nd:
+            assert np.array_equal(h.V, ho.V), name
+    native.lib().siminf_gpu_release_cached()
+
+
+def test_gpu_pinned_sparse_outputs_streamed_back(gpu, oracle_lib):
+    """The same with sparse U over a random pattern of 5 replicates."""
+    import ctypes as C
+    from siminf_gb300 import abi, native
+    torch = pytest.importorskip("torch")
+    m = dict(parity_cases())["seir_events_rep5"]
+    rng = np.random.default_rng(11)
+    nrow, ncol = m.Nn * m.Nc, m.replicates * len(m.tspan)
+    iu, ju = np.nonzero(rng.random((nrow, ncol)) < 0.05)
+    U_sp = sparse_pattern(iu + 1, ju + 1, nrow, ncol)
+    _, _, ho = run_oracle(m, U_sparse=U_sp)
+    h = abi.build_args(m, 42, U_sparse=U_sp)
+    _pin_outputs(h, torch)
+    h.prU[:] = -1
+    code = native.lib().siminf_gpu_run_solver_ex(C.cast(h.ref(), C.c_void_p),
+                                                 native.device_model(m.name).handle, None)
+    assert code == 0
+    assert np.array_equal(h.prU, ho.prU)
