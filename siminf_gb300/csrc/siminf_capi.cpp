@@ -114,9 +114,9 @@ double ms_since(std::chrono::steady_clock::time_point t0)
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-/* Pinned host staging buffers kept between runs.  Pinning the half
- * gigabyte that a streamed run of 10^6 nodes stages its external
- * transfers through takes longer than several days of the GPU's work, so
+/* Pinned host staging buffers kept between runs.  Pinning the gigabyte
+ * that a streamed run of 10^6 nodes stages its external transfers
+ * through takes longer than several days of the GPU's work, so
  * a buffer a run releases is kept for the next run: at most PINNED_KEEP
  * buffers and PINNED_KEEP_BYTES in all, freed by
  * siminf_gpu_release_cached. */
@@ -400,6 +400,7 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
      * event with its predecessor, so chunk borders are covered. */
     struct Chunk {
         long long bad = -1;
+        int max_select = 0, max_shift = 0;
         std::vector<long long> e1;
         std::vector<long long> e2_per_day;
         std::vector<PlannedErr> planned;
@@ -411,7 +412,8 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
         c.e2_per_day.assign(ndays + 1, 0);
         const long long lo = len * t / n, hi = len * (t + 1) / n;
         const int *time = a->time, *event = a->event, *node_ = a->node, *dest_ = a->dest,
-                  *select = a->select;
+                  *select = a->select, *shift = a->shift;
+        int msel = 0, mshift = 0;
         int pt = lo > 0 ? time[lo - 1] : INT_MIN, pk = lo > 0 ? event[lo - 1] : 0;
         /* times are sorted, so the day changes rarely: it is recomputed
          * when the time changes, and the day's count of valid transfers is
@@ -427,6 +429,8 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
             }
             pt = tm;
             pk = kind;
+            msel = std::max(msel, select[i]);
+            mshift = std::max(mshift, shift[i]);
             if (d < 0 || tm != d_time) {
                 if (d >= 0 && d < ndays)
                     c.e2_per_day[d] += run;
@@ -457,11 +461,16 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
         }
         if (d >= 0 && d < ndays)
             c.e2_per_day[d] += run;
+        c.max_select = msel;
+        c.max_shift = mshift;
     });
     long long bad = -1;
+    p->max_select = p->max_shift = 0;
     for (auto &c : chunks) {
         if (c.bad >= 0 && (bad < 0 || c.bad < bad))
             bad = c.bad;
+        p->max_select = std::max(p->max_select, c.max_select);
+        p->max_shift = std::max(p->max_shift, c.max_shift);
         p->planned.insert(p->planned.end(), c.planned.begin(), c.planned.end());
     }
     if (bad >= 0) {
@@ -875,12 +884,9 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     s.gdata = dgd;
     if (!rc && a->len > 0) {
         /* E and N have as many columns as the largest select and shift
-         * the events use (the struct carries no column counts). */
-        int maxsel = 0, maxshift = 0;
-        for (int i = 0; i < a->len; i++) {
-            maxsel = std::max(maxsel, a->select[i]);
-            maxshift = std::max(maxshift, a->shift[i]);
-        }
+         * the events use (the struct carries no column counts; the
+         * schedule scan found both). */
+        const int maxsel = p->max_select, maxshift = p->max_shift;
         const int ncolE = maxsel;
         const int nnzE = a->jcE[ncolE];
         int *dirE, *djcE;
@@ -1189,7 +1195,7 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
     const Launchers *L = p->L;
     const siminf_gpu_solver_args *a = &p->args;
     const int ndays = p->ndays;
-    enum { CHUNK_DAYS = 8, RING = 4 };
+    enum { CHUNK_DAYS = 8, RING = 8 };
     cudaError_t e = L->init(s, p->tt0, st);
     if (e != cudaSuccess)
         return e;
@@ -1223,10 +1229,13 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
                 for (int d = next_day++; d < ndays && !abort.load(); d = next_day++) {
                     const int c = d / CHUNK_DAYS;
                     if (c >= RING) {
-                        /* the slot's previous chunk must have left it */
+                        /* the slot's previous chunk must have left it;
+                         * planners that wait sleep (blocking-sync events,
+                         * short naps), so the launching thread keeps a
+                         * core */
                         while (!issued[c - RING].load(std::memory_order_acquire) &&
                                !abort.load())
-                            std::this_thread::yield();
+                            std::this_thread::sleep_for(std::chrono::microseconds(50));
                         if (abort.load())
                             break;
                         cudaEventSynchronize(copied[c - RING]);
@@ -1255,7 +1264,7 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             break;
         }
         const long long lo = p->e2_day_off[d0], hi = p->e2_day_off[d1];
-        e = cudaEventCreateWithFlags(&copied[c], cudaEventDisableTiming);
+        e = cudaEventCreateWithFlags(&copied[c], cudaEventDisableTiming | cudaEventBlockingSync);
         if (e == cudaSuccess && hi > lo)
             e = cudaMemcpyAsync(p->d_e2 + lo, ring + (size_t) (c % RING) * slot_len,
                                 (size_t) (hi - lo) * sizeof(E2Rec), cudaMemcpyHostToDevice, cs);

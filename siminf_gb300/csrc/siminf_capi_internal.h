@@ -72,6 +72,7 @@ struct siminf_gpu_plan {
      * e2_day_off[d + 1] of d_e2 and come from input range e2_lo[d] ..
      * e2_hi[d]; day_waves[d] holds the day's wave sizes. */
     int nsel = 0;
+    int max_select = 0, max_shift = 0;  /* largest select / shift of any event */
     std::vector<long long> e2_day_off, e2_lo, e2_hi;
     std::vector<std::vector<long long>> day_waves;
     /* Streamed runs: the waves are planned on host threads while the GPU
