@@ -185,6 +185,12 @@ int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args,
  * warp (results are identical either way); 0 takes the default (8), a
  * negative value turns the queue off.
  *
+ * two_pass: a tuning knob, not a semantic option -- each day first
+ * finishes, one node per thread, every node whose day has no transition,
+ * and steps only the others in the work queue (results are identical
+ * either way).  It pays where most node-days are quiet and the plan holds
+ * many nodes, which is when the default turns it on.
+ *
  * gdata_per_replicate: args->gdata holds one gdata vector per replicate
  * (Nrep rows of the model's gdata length); replicate r reads row r.  The
  * reference shares one gdata among replicates; particle filters and ABC
@@ -194,7 +200,8 @@ typedef struct siminf_gpu_options {
     int cap_transfers;
     int heavy_rate;     /* rate sum from which a node is queued first (0 = default 8, < 0 = off) */
     int gdata_per_replicate;
-    int reserved[5];
+    int two_pass;       /* > 0 on, < 0 off, 0 = on from 4,000,000 nodes (all replicates) */
+    int reserved[4];
 } siminf_gpu_options;
 
 /* siminf_gpu_run_solver_mssm with options (NULL = all zero). */

@@ -939,7 +939,7 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     if (!rc) rc = dalloc(&s.fired, 1, own);
     if (!rc) rc = dalloc(&s.heavy_list, (size_t) 2 * HEAVY_CLASSES * MAX_HEAVY, own);
     if (!rc) rc = dalloc(&s.heavy_count, (size_t) 2 * HEAVY_CLASSES, own);
-    if (!rc) rc = dalloc(&s.queue_next, 4, own);
+    if (!rc) rc = dalloc(&s.queue_next, 6, own);
     if (!rc) rc = dalloc(&s.heavy_mark, (size_t) Ntot, own);
     /* heavy part of the work queue: threshold on the day-start rate sum
      * (options, else SIMINF_HEAVY_RATE in the environment, 0 = off;
@@ -951,6 +951,15 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
         s.heavy_rate = opt->heavy_rate;
     else if (opt && opt->heavy_rate < 0)
         s.heavy_rate = 0.0;
+    /* two-pass days (options, else SIMINF_TWO_PASS, else from 4,000,000
+     * nodes: below that the day's longest chain, not its many quiet
+     * nodes, sets its length) */
+    s.two_pass = Ntot >= 4000000;
+    if (const char *ev = getenv("SIMINF_TWO_PASS"))
+        s.two_pass = atoi(ev) > 0;
+    if (opt && opt->two_pass)
+        s.two_pass = opt->two_pass > 0;
+    if (!rc) rc = dalloc(&s.active, (size_t) Ntot, own);
     if (!rc) {
         s.err_day = s.err_count + 1;
         s.err_day_pre_e2 = s.err_count + 2;
@@ -1345,7 +1354,7 @@ static cudaError_t reset_run(siminf_gpu_plan *p, const DevState &s, cudaStream_t
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s.heavy_count, 0, 2 * HEAVY_CLASSES * sizeof(int), st);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(s.queue_next, 0, 4 * sizeof(unsigned long long), st);
+        e = cudaMemsetAsync(s.queue_next, 0, 6 * sizeof(unsigned long long), st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s.heavy_mark, 0, (size_t) s.Ntot * sizeof(int), st);
     if (e == cudaSuccess)

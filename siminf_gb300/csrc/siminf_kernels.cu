@@ -646,6 +646,53 @@ __device__ __forceinline__ bool node_e1(const DevState &s, int (&u)[NC], int nod
     return o.any;
 }
 
+/* The NC compartments of one node, loaded or stored with 16-byte (NC a
+ * multiple of 4) or 8-byte (NC even) accesses: a node's block of u or of a
+ * U column starts at a multiple of NC ints from a 256-byte aligned base. */
+template <int NC>
+__device__ __forceinline__ void load_u(const int *p, int (&u)[NC])
+{
+    if constexpr (NC % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; c += 4) {
+            const int4 w = *reinterpret_cast<const int4 *>(p + c);
+            u[c] = w.x;
+            u[c + 1] = w.y;
+            u[c + 2] = w.z;
+            u[c + 3] = w.w;
+        }
+    } else if constexpr (NC % 2 == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; c += 2) {
+            const int2 w = *reinterpret_cast<const int2 *>(p + c);
+            u[c] = w.x;
+            u[c + 1] = w.y;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            u[c] = p[c];
+    }
+}
+
+template <int NC>
+__device__ __forceinline__ void store_u(int *p, const int (&u)[NC])
+{
+    if constexpr (NC % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; c += 4)
+            *reinterpret_cast<int4 *>(p + c) = make_int4(u[c], u[c + 1], u[c + 2], u[c + 3]);
+    } else if constexpr (NC % 2 == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; c += 2)
+            *reinterpret_cast<int2 *>(p + c) = make_int2(u[c], u[c + 1]);
+    } else {
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            p[c] = u[c];
+    }
+}
+
 /* Store the node's U/V entries for columns [c0, c1) of its replicate. */
 template <int NC, int ND>
 __device__ __forceinline__ void store_columns(const DevState &s, int rep, int node,
@@ -655,10 +702,7 @@ __device__ __forceinline__ void store_columns(const DevState &s, int rep, int no
     for (int col = c0; col < c1; col++) {
         const size_t ccol = (size_t) rep * s.tlen + col;
         if (s.U) {
-            int *dst = s.U + ccol * (size_t) s.Nn * NC + (size_t) node * NC;
-#pragma unroll
-            for (int c = 0; c < NC; c++)
-                dst[c] = u[c];
+            store_u<NC>(s.U + ccol * (size_t) s.Nn * NC + (size_t) node * NC, u);
         } else if (s.jcU) {
             /* rows of this node in the sorted CSC column */
             int lo = s.jcU[ccol], hi = s.jcU[ccol + 1];
@@ -719,36 +763,57 @@ __device__ __forceinline__ void load_model_smem(const DevState &s, int *sS, uint
 
 /* List g as heavy for `day` when its rate sum promises many transitions
  * in one unit of time (only for models whose rates ignore t). */
+/* The heavy class of a node whose rate sum at the start of a day is
+ * `sum`: 0 for sum >= 16 h, 1 for >= 4 h, 2 for >= h (h = heavy_rate),
+ * -1 for a node that is not heavy or a model whose rates depend on time. */
 template <class M>
-__device__ __forceinline__ void push_heavy(const DevState &s, long long g, double sum, int day)
+__device__ __forceinline__ int heavy_class(const DevState &s, double sum)
 {
     if (!M::RATES_TIME_INVARIANT || !(s.heavy_rate > 0.0))
-        return;
+        return -1;
     if (!si_dge(sum, s.heavy_rate) || !si_finite_pos(sum))
-        return;
-    const int cls = si_dge(sum, 16.0 * s.heavy_rate) ? 0 : si_dge(sum, 4.0 * s.heavy_rate) ? 1 : 2;
-    const int q = (day & 1) * HEAVY_CLASSES + cls;
-    const int slot = atomicAdd(&s.heavy_count[q], 1);
-    if (slot < MAX_HEAVY) {
-        s.heavy_list[q * MAX_HEAVY + slot] = (int) g;
-        s.heavy_mark[g] = day + 1;
+        return -1;
+    return si_dge(sum, 16.0 * s.heavy_rate) ? 0 : si_dge(sum, 4.0 * s.heavy_rate) ? 1 : 2;
+}
+
+/* Warp-wide (every lane of the warp calls it): lanes with cls >= 0 append
+ * their node to heavy list cls of `day`, with one atomic per class present
+ * in the warp; a list that is full takes nothing more. */
+__device__ __forceinline__ void push_heavy_warp(const DevState &s, long long g, int cls, int day)
+{
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < HEAVY_CLASSES; c++) {
+        const unsigned m = __ballot_sync(FULL, cls == c);
+        if (!m)
+            continue;
+        const int q = (day & 1) * HEAVY_CLASSES + c;
+        const int leader = __ffs(m) - 1;
+        int base = MAX_HEAVY;
+        if (lane == leader && load_flag(&s.heavy_count[q]) < MAX_HEAVY)
+            base = atomicAdd(&s.heavy_count[q], __popc(m));
+        base = __shfl_sync(FULL, base, leader);
+        if (cls == c) {
+            const int slot = base + __popc(m & ((1u << lane) - 1u));
+            if (slot < MAX_HEAVY) {
+                s.heavy_list[q * MAX_HEAVY + slot] = (int) g;
+                s.heavy_mark[g] = day + 1;
+            }
+        }
     }
 }
 
+/* k_init for one (replicate, node); returns its heavy class on day 0. */
 template <class M>
-__global__ void k_init(DevState s, double tt0)
+__device__ __forceinline__ int init_node(const DevState &s, long long g, double tt0)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
-    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (g >= s.Ntot)
-        return;
     if (s.pf_days)
         tt0 = s.pf_days[(size_t) *s.pf_interval * s.pf_days_stride].tt;
     const int node = (int) (g % s.Nn);
     int u[NC];
-#pragma unroll
-    for (int c = 0; c < NC; c++)
-        u[c] = s.u[g * NC + c];
+    load_u<NC>(s.u + g * NC, u);
     const double *v = s.vA + g * ND;
     const double *ld = s.ldata + (size_t) node * s.Nld;
     si_recip dc = si_recip_none();
@@ -765,7 +830,17 @@ __global__ void k_init(DevState s, double tt0)
     s.t_time[g] = tt0;
     s.ctr[g] = 0;
     s.update[g] = 0;
-    push_heavy<M>(s, g, sum, 0);
+    return heavy_class<M>(s, sum);
+}
+
+template <class M>
+__global__ void k_init(DevState s, double tt0)
+{
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    int cls = -1;
+    if (g < s.Ntot)
+        cls = init_node<M>(s, g, tt0);
+    push_heavy_warp(s, g, cls, 0);
 }
 
 /* The end of a node's day: its E1 events (or its SSA error) and the state
@@ -789,15 +864,88 @@ __device__ __forceinline__ void node_finish(const DevState &s, SsaLane<M> &ln, s
         if (e_code)
             record_error(s, e_code, PHASE_E1, day, g, -1, e_idx, tt, 0);
     }
-#pragma unroll
-    for (int c = 0; c < NC; c++)
-        s.u[g * NC + c] = ln.u[c];
+    store_u<NC>(s.u + g * NC, ln.u);
 #pragma unroll
     for (int k = 0; k < NT; k++)
         s.t_rate[(size_t) k * s.Ntot + g] = ln.rate[k];
     s.sum_rate[g] = ln.sum;
     s.t_time[g] = ln.t;
     s.ctr[g] = r.ctr;
+}
+
+/* The first pass of a two-pass day, one ordinary node (not in the day's
+ * heavy lists) per thread: a node whose day has no transition -- rate sum
+ * 0, or a first waiting time that passes the end of the day -- finishes
+ * here (its E1 events, state written back), with the warp's lanes in step;
+ * a node with a transition is listed in s.active for k_ssa_e1, which draws
+ * the same first waiting time again (same draw index) and steps it.  The
+ * draws and comparisons are those of ssa_begin and ssa_step. */
+template <class M>
+__global__ void __launch_bounds__(256) k_quick(DevState s, int day, double tt, double next)
+{
+    constexpr int NC = M::NC;
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    bool listed = false;
+    if (g < s.Ntot && load_flag(s.err_day) >= day && s.heavy_mark[g] != day + 1 &&
+        !job_over(s, g, day)) {
+        const double sum = s.sum_rate[g], t = s.t_time[g];
+        uint64_t c = s.ctr[g];
+        si_rng r;
+        {
+            uint64_t seed, sid;
+            stream_key(s, g, seed, sid);
+            si_rng_init(&r, seed, sid, 0);
+        }
+        int err = 0;
+        if (!si_finite_pos(sum)) {
+            /* nothing fires (src/solvers/SimInf_solver_ssm.c:148-151) */
+            if (!le_zero(si_double_bits(sum)))
+                err = ERR_INVALID_RATE;
+        } else {
+            uint32_t p0, p1, p2, p3;
+            philox_block(r, c >> 2, p0, p1, p2, p3);
+            const double tau = si_div(si_neglog_u32(word_of(p0, p1, p2, p3, (uint32_t) c & 3u)), sum);
+            if (tau + t >= next)
+                c += 1;                         /* the waiting time's draw was used */
+            else
+                listed = true;
+        }
+        if (!listed) {
+            if (err) {
+                record_error(s, err, PHASE_SSA, day, g, -1, -1, t, sum);
+            } else {
+                const int node = (int) (g % s.Nn);
+                if (s.e1_ptr[node] != s.e1_ptr[node + 1]) {
+                    int u[NC];
+                    load_u<NC>(s.u + g * NC, u);
+                    r.ctr = c;
+                    r.have = 0;
+                    int e_code = 0, e_idx = -1;
+                    if (node_e1<NC>(s, u, node, day, r, g, tt, e_code, e_idx)) {
+                        s.update[g] = 1;
+                        store_u<NC>(s.u + g * NC, u);
+                    }
+                    if (e_code)
+                        record_error(s, e_code, PHASE_E1, day, g, -1, e_idx, tt, 0);
+                    c = r.ctr;
+                }
+            }
+            s.t_time[g] = next;
+            s.ctr[g] = c;
+        }
+    }
+    /* list the nodes with a transition, one atomic per warp */
+    const unsigned FULL = 0xFFFFFFFFu;
+    const unsigned m = __ballot_sync(FULL, listed);
+    if (m) {
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        unsigned long long base = 0;
+        if (lane == leader)
+            base = atomicAdd(&s.queue_next[4 + (day & 1)], (unsigned long long) __popc(m));
+        base = __shfl_sync(FULL, base, leader);
+        if (listed)
+            s.active[base + __popc(m & ((1u << lane) - 1u))] = (int) g;
+    }
 }
 
 /* One day of SSA and E1 events for every (replicate, node): a persistent
@@ -824,6 +972,8 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
         s.heavy_count[npar * HEAVY_CLASSES + threadIdx.x] = 0;  /* filled by this day's pts */
     if (blockIdx.x == 0 && threadIdx.x < 2)
         s.queue_next[npar * 2 + threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 2)
+        s.queue_next[4 + npar] = 0;                     /* filled by the next k_quick */
     unsigned long long fired = 0;
     if (load_flag(s.err_day) < day) {
         add_fired(s, fired);
@@ -836,7 +986,10 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
         n[c] = min(s.heavy_count[par * HEAVY_CLASSES + c], (int) MAX_HEAVY);
         H += (unsigned long long) n[c];
     }
-    const unsigned long long Ntot = (unsigned long long) s.Ntot;
+    /* the ordinary part: every node in index order, or on two-pass days
+     * the nodes k_quick listed */
+    const unsigned long long Ntot = s.two_pass ? s.queue_next[4 + par]
+                                               : (unsigned long long) s.Ntot;
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
 
@@ -875,6 +1028,8 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
                     }
                 } else if (pos >= Ntot) {
                     alive = false;
+                } else if (s.two_pass) {
+                    cand = s.active[pos];
                 } else if (s.heavy_mark[pos] != day + 1) {
                     cand = (long long) pos;     /* heavy ones come from the heavy part */
                 }
@@ -887,9 +1042,7 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
                 g = cand;
                 heavy = from_heavy;
                 const int node = (int) (g % s.Nn);
-#pragma unroll
-                for (int c = 0; c < NC; c++)
-                    ln.u[c] = s.u[g * NC + c];
+                load_u<NC>(s.u + g * NC, ln.u);
 #pragma unroll
                 for (int k = 0; k < NT; k++)
                     ln.rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
@@ -1020,19 +1173,16 @@ __device__ __forceinline__ void add_prevalence(const DevState &s, long long g, c
     }
 }
 
+/* k_pts_store for one (replicate, node); returns its heavy class on the
+ * next day. */
 template <class M>
-__global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double tt, int c0, int c1,
-                                                   const double *v_in, double *v_out)
+__device__ __forceinline__ int pts_node(const DevState &s, long long g, int day, double tt,
+                                        int c0, int c1, const double *v_in, double *v_out)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
-    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (g >= s.Ntot || load_flag(s.err_day) < day || job_over(s, g, day))
-        return;
     const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
     int u[NC];
-#pragma unroll
-    for (int c = 0; c < NC; c++)
-        u[c] = s.u[g * NC + c];
+    load_u<NC>(s.u + g * NC, u);
     const double *vi = v_in + g * ND;
     double *vo = v_out + g * ND;
     const double *ld = s.ldata + (size_t) node * s.Nld;
@@ -1055,11 +1205,21 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
         s.sum_rate[g] += delta;
         s.update[g] = 0;
     }
-    if (!job_over(s, g, day + 1))
-        push_heavy<M>(s, g, s.sum_rate[g], day + 1);
     store_columns<NC, ND>(s, rep, node, u, vo, c0, c1);
     if (s.prev && c1 > c0)
         add_prevalence<NC>(s, g, u, c0, c1);
+    return job_over(s, g, day + 1) ? -1 : heavy_class<M>(s, s.sum_rate[g]);
+}
+
+template <class M>
+__global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double tt, int c0, int c1,
+                                                   const double *v_in, double *v_out)
+{
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    int cls = -1;
+    if (g < s.Ntot && load_flag(s.err_day) >= day && !job_over(s, g, day))
+        cls = pts_node<M>(s, g, day, tt, c0, c1, v_in, v_out);
+    push_heavy_warp(s, g, cls, day + 1);
 }
 
 /* Whole horizon of one (replicate, node) in one thread: valid when no
@@ -1079,9 +1239,7 @@ __global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s,
     if (g < s.Ntot) {
         const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
         SsaLane<M> ln;
-#pragma unroll
-        for (int c = 0; c < NC; c++)
-            ln.u[c] = s.u[g * NC + c];
+        load_u<NC>(s.u + g * NC, ln.u);
 #pragma unroll
         for (int k = 0; k < NT; k++)
             ln.rate[k] = s.t_rate[(size_t) k * s.Ntot + g];
@@ -1144,9 +1302,7 @@ __global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s,
             v = vn;
             vn = tmp;
         }
-#pragma unroll
-        for (int c = 0; c < NC; c++)
-            s.u[g * NC + c] = ln.u[c];
+        store_u<NC>(s.u + g * NC, ln.u);
 #pragma unroll
         for (int k = 0; k < NT; k++)
             s.t_rate[(size_t) k * s.Ntot + g] = ln.rate[k];
@@ -1338,6 +1494,12 @@ struct Launch {
     }
     static cudaError_t ssa_e1(const DevState &s, int day, double tt, double next, cudaStream_t st)
     {
+        if (s.two_pass) {
+            k_quick<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, next);
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess)
+                return e;
+        }
         const long long need = (long long) blocks_for(s.Ntot, SSA_BLOCK);
         const int grid = (int) (need < ssa_resident_blocks() ? need : ssa_resident_blocks());
         k_ssa_e1<M><<<grid, SSA_BLOCK, 0, st>>>(s, day, tt, next);

@@ -122,9 +122,16 @@ struct DevState {
      * list[((d & 1) * HEAVY_CLASSES + class) * MAX_HEAVY + i] */
     int *heavy_list;
     int *heavy_count;       /* [2][HEAVY_CLASSES] */
-    unsigned long long *queue_next;  /* [day parity][heavy, ordinary]: next queue entries */
+    unsigned long long *queue_next;  /* [day parity][heavy, ordinary]: next queue entries,
+                                      * then [4 + day parity]: length of `active` */
     int *heavy_mark;        /* per g: day + 1 when listed for that day */
     double heavy_rate;      /* <= 0: no heavy part in the queue */
+
+    /* Two-pass days: k_quick finishes every ordinary node whose day has no
+     * transition and lists the others in `active` (Ntot entries), the
+     * ordinary part of k_ssa_e1's queue. */
+    int two_pass;
+    int *active;
 
     /* Batches of independent models (siminf_gpu_run_batch); job_of is NULL
      * for a single model.  Node g belongs to job j = job_of[g], whose nodes

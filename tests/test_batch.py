@@ -57,7 +57,9 @@ def test_batch_rejects_mixed_tspan_start(oracle_lib):
 
 
 @pytest.mark.gpu
-def test_batch_matches_oracle_and_alone(gpu, oracle_lib):
+@pytest.mark.parametrize("two_pass", ["-1", "1"])
+def test_batch_matches_oracle_and_alone(gpu, oracle_lib, monkeypatch, two_pass):
+    monkeypatch.setenv("SIMINF_TWO_PASS", two_pass)
     from siminf_gb300.run import run_batch
     models = batch_models()
     seeds = [11, 12, 13, 2 ** 33 + 1, 99]

@@ -103,6 +103,20 @@ def test_gpu_error_codes(gpu, label, m, code):
     assert got == code
 
 
+@pytest.mark.parametrize("label,m,code", error_cases(), ids=[c[0] for c in error_cases()])
+def test_gpu_error_codes_two_pass(gpu, label, m, code):
+    """The reference's error codes when quiet node-days finish in the first
+    pass of a two-pass day."""
+    import ctypes as C
+    from siminf_gb300 import abi, native
+    h = abi.build_args(m, 42)
+    opt = abi.Options(two_pass=1)
+    got = native.lib().siminf_gpu_run_solver_ex(C.cast(h.ref(), C.c_void_p),
+                                                native.device_model(m.name).handle,
+                                                C.byref(opt))
+    assert got == code
+
+
 def test_gpu_unsorted_events_rejected(gpu):
     from siminf_gb300 import model as M
     m = M.SIR({"S": [5, 5], "I": [0, 0], "R": [0, 0]}, [1, 2, 3], 0.0, 0.0,
@@ -155,17 +169,19 @@ def test_gpu_conservation_full_scale_properties(gpu):
         assert change >= d_enter[k] - d_exit[k]
 
 
+@pytest.mark.parametrize("two_pass", [-1, 1])
 @pytest.mark.parametrize("heavy_rate", [1, -1])
 @pytest.mark.parametrize("label,m", parity_cases(), ids=[c[0] for c in parity_cases()])
-def test_gpu_heavy_queue_matches_oracle(gpu, oracle_lib, label, m, heavy_rate):
+def test_gpu_heavy_queue_matches_oracle(gpu, oracle_lib, label, m, heavy_rate, two_pass):
     """heavy_rate = 1 queues every node with a rate sum >= 1 for the heavy
     warps (32 nodes to a warp, first in the day); -1 turns the queue off.
-    Both stay bit-exact."""
+    two_pass = 1 finishes the quiet node-days in a first pass and queues
+    only the others; -1 queues every node.  All stay bit-exact."""
     import ctypes as C
     from siminf_gb300 import abi, native
     _, _, ho = run_oracle(m, threads=4)
     h = abi.build_args(m, 42)
-    opt = abi.Options(cap_transfers=0, heavy_rate=heavy_rate)
+    opt = abi.Options(cap_transfers=0, heavy_rate=heavy_rate, two_pass=two_pass)
     code = native.lib().siminf_gpu_run_solver_ex(C.cast(h.ref(), C.c_void_p),
                                                  native.device_model(m.name).handle,
                                                  C.byref(opt))
