@@ -62,7 +62,7 @@ def parse():
                     help="fraction of the 1e6 nodes / 5e5 transfers per day (1.0 = full)")
     ap.add_argument("--days", type=int, default=365)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--batch", type=int, default=8,
+    ap.add_argument("--batch", type=int, default=16,
                     help="replicates of the workload run as one batched plan (0/1: skip)")
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--abc", type=int, default=256,
@@ -395,12 +395,11 @@ def run_ours(args):
     plan = native.Plan(holder, m.name, cap_transfers=True)
     st = plan.stats()
     node_days = nodes * st.days
-    # the library's autotuner picks the work queue's heavy threshold on the
-    # first 120 days (results do not depend on it)
+    # the library's autotuner picks the work queue's layout (heavy
+    # threshold, one- or two-pass days) on the first 120 days (results do
+    # not depend on it)
     tune = plan.tune(probe_days=120, stream=C.c_void_p(stream.cuda_stream))
-    autotune = {"probe_days": tune.probe_days,
-                "heavy_rate_candidates": list(tune.heavy_rate),
-                "ms": list(tune.ms), "chosen_heavy_rate": tune.heavy_rate[tune.chosen]}
+    autotune = tune_summary(tune)
 
     def barrier():
         torch.cuda.synchronize()
@@ -427,7 +426,8 @@ def run_ours(args):
     ms_step = ms / args.steps
     value = node_days * world / (ms_step / 1e3)
     transitions_per_s = st.transitions * world / (ms_step / 1e3)
-    launches = 1 + (1 if st.e2_waves == 0 else 2 * st.days + st.e2_waves)
+    launches = 1 + (1 if st.e2_waves == 0 else
+                    (3 if autotune["chosen_two_pass"] else 2) * st.days + st.e2_waves)
 
     # dominant kernel: per-kernel device time from the library's own
     # per-launch events (one step), see roofline below
@@ -442,6 +442,7 @@ def run_ours(args):
         mb = m.replicate(args.batch)
         hb = abi.build_args(mb, seed)
         pb = native.Plan(hb, mb.name, cap_transfers=True)
+        tune_b = tune_summary(pb.tune(probe_days=60, stream=C.c_void_p(stream.cuda_stream)))
         pb.run(C.c_void_p(stream.cuda_stream))
         barrier()
         b0 = torch.cuda.Event(enable_timing=True)
@@ -457,7 +458,7 @@ def run_ours(args):
         batched = {"replicates": args.batch, "value": vb, "unit": UNIT, "ms_per_step": msb,
                    "steps": args.batch_steps, "warmup": 1,
                    "transitions_per_s": stb.transitions * world / (msb / 1e3),
-                   "vs_plain": vb / value,
+                   "vs_plain": vb / value, "autotune": tune_b,
                    "data": "%d replicates of the same synthetic workload in one plan "
                            "(mssm), inputs resident" % args.batch}
         pb.close()
@@ -583,6 +584,15 @@ def pinned_holder(m, seed, torch):
     h.U = pinned(h.U)
     a.U = h.U.ctypes.data_as(C.POINTER(C.c_int))
     return h
+
+
+def tune_summary(tune):
+    """The autotuner's candidates, probe times and choice."""
+    return {"probe_days": tune.probe_days,
+            "candidates": [{"heavy_rate": tune.heavy_rate[k], "two_pass": tune.two_pass[k],
+                            "ms": tune.ms[k]} for k in range(len(tune.ms))],
+            "chosen_heavy_rate": tune.heavy_rate[tune.chosen],
+            "chosen_two_pass": tune.two_pass[tune.chosen]}
 
 
 def plan_kernel_profile(plan, C, stream):

@@ -379,15 +379,17 @@ int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
 
 /*
  * Autotuner (no counterpart in the reference): times the plan's first
- * probe_days days (0: 16) for each candidate threshold of the heavy part of
- * the SSA work queue (rate sum from which a node is queued first and run 32
- * to a warp; 0 turns the part off), keeps the fastest in the plan, and
- * reports the times.  Results never depend on the threshold; only the
- * order in which nodes are simulated does.
+ * probe_days days (0: 16) for each candidate layout of the SSA work queue
+ * -- the threshold of its heavy part (rate sum from which a node is queued
+ * first and run 32 to a warp; 0 turns the part off: 0, 2, 8, 32) with
+ * one-pass and with two-pass days (siminf_gpu_options.two_pass) -- keeps
+ * the fastest in the plan, and reports the times.  Results never depend on
+ * the layout; only the order in which nodes are simulated does.
  */
-#define SIMINF_GPU_TUNE_CANDIDATES 4
+#define SIMINF_GPU_TUNE_CANDIDATES 8
 typedef struct siminf_gpu_tune_result {
     double heavy_rate[SIMINF_GPU_TUNE_CANDIDATES];
+    int two_pass[SIMINF_GPU_TUNE_CANDIDATES];   /* 1: two-pass days */
     double ms[SIMINF_GPU_TUNE_CANDIDATES];     /* device time of the probe days */
     int chosen;                                 /* index of the kept candidate */
     int probe_days;

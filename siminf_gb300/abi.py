@@ -175,8 +175,9 @@ class Stats(C.Structure):
 class TuneResult(C.Structure):
     """siminf_gpu_tune_result."""
     _fields_ = [
-        ("heavy_rate", C.c_double * 4),
-        ("ms", C.c_double * 4),
+        ("heavy_rate", C.c_double * 8),
+        ("two_pass", C.c_int * 8),
+        ("ms", C.c_double * 8),
         ("chosen", C.c_int),
         ("probe_days", C.c_int),
     ]

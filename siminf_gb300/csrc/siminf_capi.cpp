@@ -1497,24 +1497,28 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
 {
     if (!p || p->e2_pending)
         return SIMINF_GPU_ERR_INVALID_MODEL;
-    static const double cand[SIMINF_GPU_TUNE_CANDIDATES] = {0.0, 2.0, 8.0, 32.0};
+    static const double cand[4] = {0.0, 2.0, 8.0, 32.0};
     const cudaStream_t st = (cudaStream_t) cuda_stream;
     const double saved = p->s.heavy_rate;
+    const int saved_tp = p->s.two_pass;
     p->max_days = probe_days > 0 ? probe_days : 16;
     plan_changed(p);
     siminf_gpu_tune_result r{};
     int best = -1, rc = plan_run_impl(p, st, nullptr);     /* warm-up */
     for (int k = 0; k < SIMINF_GPU_TUNE_CANDIDATES && !rc; k++) {
-        p->s.heavy_rate = cand[k];
+        p->s.heavy_rate = cand[k % 4];
+        p->s.two_pass = k / 4;
         plan_changed(p);
         rc = plan_run_impl(p, st, nullptr);
-        r.heavy_rate[k] = cand[k];
+        r.heavy_rate[k] = cand[k % 4];
+        r.two_pass[k] = k / 4;
         r.ms[k] = p->stats.ms_solve;
         if (!rc && (best < 0 || r.ms[k] < r.ms[best]))
             best = k;
     }
     p->max_days = 0;
-    p->s.heavy_rate = (best >= 0) ? cand[best] : saved;
+    p->s.heavy_rate = (best >= 0) ? cand[best % 4] : saved;
+    p->s.two_pass = (best >= 0) ? best / 4 : saved_tp;
     plan_changed(p);
     r.chosen = best;
     r.probe_days = std::min(probe_days > 0 ? probe_days : 16, p->ndays);

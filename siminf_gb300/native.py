@@ -174,8 +174,9 @@ class Plan:
         check(lib().siminf_gpu_plan_download(self.handle, C.cast(self.holder.ref(), C.c_void_p)))
 
     def tune(self, probe_days=16, stream=None):
-        """Autotune the work queue's heavy threshold on the first
-        probe_days days (siminf_gpu_plan_tune); returns the TuneResult."""
+        """Autotune the work queue (heavy threshold, one- or two-pass days)
+        on the first probe_days days (siminf_gpu_plan_tune); returns the
+        TuneResult."""
         r = abi.TuneResult()
         check(lib().siminf_gpu_plan_tune(self.handle, stream, int(probe_days), C.byref(r)))
         return r

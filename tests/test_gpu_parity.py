@@ -209,8 +209,9 @@ def test_gpu_crn_option_same_streams(gpu):
 
 
 def test_gpu_autotune_keeps_results(gpu):
-    """siminf_gpu_plan_tune picks one of its candidate thresholds and the
-    tuned plan's trajectories are the untuned plan's."""
+    """siminf_gpu_plan_tune picks one of its candidate queue layouts
+    (heavy threshold x one- or two-pass days) and the tuned plan's
+    trajectories are the untuned plan's."""
     from siminf_gb300 import abi, native
     label, m = [c for c in parity_cases() if c[0] == "seir_events_300x120"][0]
     h1 = abi.build_args(m, 42)
@@ -220,8 +221,9 @@ def test_gpu_autotune_keeps_results(gpu):
     h2 = abi.build_args(m, 42)
     p2 = native.Plan(h2, m.name)
     r = p2.tune(probe_days=10)
-    assert 0 <= r.chosen < 4 and r.probe_days == 10
+    assert 0 <= r.chosen < 8 and r.probe_days == 10
     assert r.heavy_rate[r.chosen] in (0.0, 2.0, 8.0, 32.0)
+    assert list(r.two_pass) == [0] * 4 + [1] * 4
     p2.run()
     p2.download()
     assert np.array_equal(h1.U, h2.U)
