@@ -433,6 +433,7 @@ def run_ours(args):
     # per-launch events (one step), see roofline below
     prof = plan_kernel_profile(plan, C, stream)
     peak, peak_kind = measured_peaks()
+    reductions = reduce_bench(plan, peak) if rank == 0 else None
 
     # batched form: R replicates of the same workload in one device-resident
     # plan (the mssm layout), so one replicate's latency-bound tail overlaps
@@ -543,6 +544,7 @@ def run_ours(args):
                                  % ALGO_BYTES_PER_NODE_DAY},
             "kernels": prof["kernels"],
             "autotune": autotune,
+            "reductions": reductions,
             "batched": batched,
             "sir_plain": sir,
             "abc": abc,
@@ -584,6 +586,34 @@ def pinned_holder(m, seed, torch):
     h.U = pinned(h.U)
     a.U = h.U.ctypes.data_as(C.POINTER(C.c_int))
     return h
+
+
+def reduce_bench(plan, peak, reps=5):
+    """The trajectory consumers on the resident U of the headline run:
+    level-1 prevalence (I ~ .) and the long-format trajectory of I over
+    every node; kernel time (CUDA events), achieved HBM GB/s against the
+    measured peak, and the whole call with the result's copy to the host."""
+    from siminf_gb300.trajectory import _outputs, prevalence_device, trajectory_device
+    dU, _, ncol = _outputs(plan)
+    a = plan.holder.args
+    out = {}
+    runs = {"prevalence_level1": lambda: prevalence_device(dU, a.Nn, a.Nc, ncol, 0b0100,
+                                                           0b1111, 1),
+            "trajectory_I": lambda: trajectory_device(dU, a.Nn, a.Nc, ncol, [3])}
+    for name, fn in runs.items():
+        fn()
+        best = None
+        for _ in range(reps):
+            _, st = fn()
+            if best is None or st.ms_kernel < best.ms_kernel:
+                best = st
+        moved = best.bytes_read + best.bytes_written
+        gbs = moved / (best.ms_kernel / 1e3) / 1e9
+        out[name] = {"ms_kernel": best.ms_kernel, "ms_total": best.ms_total,
+                     "bytes_read": best.bytes_read, "bytes_written": best.bytes_written,
+                     "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
+                     "bound": "hbm"}
+    return out
 
 
 def tune_summary(tune):

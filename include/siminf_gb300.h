@@ -456,6 +456,87 @@ int siminf_gpu_server_load(siminf_gpu_server *server, int *pending, int *running
 /* Finishes every submitted request, then stops the slots. */
 void siminf_gpu_server_free(siminf_gpu_server *server);
 
+/*
+ * Trajectory consumers on the device, reading U or V where a run left them
+ * in HBM (a plan's outputs, siminf_gpu_plan_outputs, or any device copy of
+ * a dense U/V): the caller copies back the series it asks for, not the
+ * trajectory.  U is (Nn * Nc) x ncol and V (Nn * Nd) x ncol, column-major
+ * as the solver writes them (ncol = Nrep * tlen, replicate-major).  Node
+ * identifiers are one-based (NULL: every node in order); outputs are host
+ * arrays; the call waits for its stream.
+ */
+typedef struct siminf_gpu_reduce_stats {
+    double ms_kernel;           /* device time of the reduction kernels */
+    double ms_total;            /* the whole call, copies included */
+    long long bytes_read;       /* U/V bytes the kernels read */
+    long long bytes_written;    /* output bytes */
+} siminf_gpu_reduce_stats;
+
+/*
+ * The long format of SimInf_trajectory for dense U
+ * (src/misc/SimInf_trajectory.c:566-620, SimInf_u_dense2df): for each of
+ * the n_compartments one-based compartments, ncol * n rows (n = n_id, or
+ * Nn), row col * n + l holding node id[l] in column col.  out receives
+ * n_compartments such columns, one after the other.
+ */
+int siminf_gpu_trajectory_u(const int *d_U, int Nn, int Nc, int ncol,
+                            const int *compartments, int n_compartments,
+                            const int *id, int n_id, int *out, void *cuda_stream,
+                            siminf_gpu_reduce_stats *stats);
+
+/* The same for dense V (SimInf_v_dense2df, src/misc/SimInf_trajectory.c:652-706). */
+int siminf_gpu_trajectory_v(const double *d_V, int Nn, int Nd, int ncol,
+                            const int *variables, int n_variables,
+                            const int *id, int n_id, double *out, void *cuda_stream,
+                            siminf_gpu_reduce_stats *stats);
+
+/*
+ * prevalence(model, formula, level, index) (R/prevalence.R:72-96): cases
+ * and population are bit masks of zero-based compartments (the formula's
+ * left- and right-hand sides); the optional condition (the formula's
+ * "| ..." part) is a postfix program of n_condition (operator, argument)
+ * pairs over the node's compartments, evaluated in 64-bit integers;
+ * comparisons and logical operators give 0 or 1, and the program must end
+ * in one.  Where it is false a node counts neither as a case nor in the
+ * population.  Level 1: sum(cases) / sum(population) per column; level 2:
+ * #(cases > 0) / #(population > 0); level 3: cases / population per node,
+ * out[col * n + l].  0 / 0 gives NaN as in R.
+ */
+enum {
+    SIMINF_GPU_COND_COMPARTMENT = 1,    /* push u[argument] (zero-based) */
+    SIMINF_GPU_COND_CONST = 2,          /* push the argument */
+    SIMINF_GPU_COND_ADD = 3,
+    SIMINF_GPU_COND_SUB = 4,
+    SIMINF_GPU_COND_MUL = 5,
+    SIMINF_GPU_COND_NEG = 6,            /* unary minus */
+    SIMINF_GPU_COND_EQ = 7,
+    SIMINF_GPU_COND_NE = 8,
+    SIMINF_GPU_COND_LT = 9,
+    SIMINF_GPU_COND_LE = 10,
+    SIMINF_GPU_COND_GT = 11,
+    SIMINF_GPU_COND_GE = 12,
+    SIMINF_GPU_COND_AND = 13,
+    SIMINF_GPU_COND_OR = 14,
+    SIMINF_GPU_COND_NOT = 15
+};
+
+typedef struct siminf_gpu_prevalence_spec {
+    unsigned int cases;                 /* bit c: compartment c is a case */
+    unsigned int population;            /* bit c: compartment c is in the population */
+    int level;                          /* 1, 2 or 3 */
+    int n_condition;                    /* 0: no condition */
+    const int *condition;               /* 2 * n_condition ints: (operator, argument) */
+} siminf_gpu_prevalence_spec;
+
+int siminf_gpu_prevalence(const int *d_U, int Nn, int Nc, int ncol,
+                          const siminf_gpu_prevalence_spec *spec,
+                          const int *id, int n_id, double *out, void *cuda_stream,
+                          siminf_gpu_reduce_stats *stats);
+
+/* The device U/V of a plan that has run (d_V NULL without V), and ncol. */
+int siminf_gpu_plan_outputs(const siminf_gpu_plan *plan, const int **d_U,
+                            const double **d_V, int *ncol);
+
 #ifdef __cplusplus
 }
 #endif

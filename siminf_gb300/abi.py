@@ -183,6 +183,23 @@ class TuneResult(C.Structure):
     ]
 
 
+class ReduceStats(C.Structure):
+    """siminf_gpu_reduce_stats."""
+    _fields_ = [("ms_kernel", C.c_double), ("ms_total", C.c_double),
+                ("bytes_read", C.c_longlong), ("bytes_written", C.c_longlong)]
+
+
+class PrevalenceSpec(C.Structure):
+    """siminf_gpu_prevalence_spec."""
+    _fields_ = [("cases", C.c_uint), ("population", C.c_uint), ("level", C.c_int),
+                ("n_condition", C.c_int), ("condition", C.POINTER(C.c_int))]
+
+
+# Operators of a prevalence condition (SIMINF_GPU_COND_*).
+COND_OPS = {"compartment": 1, "const": 2, "+": 3, "-": 4, "*": 5, "neg": 6, "==": 7,
+            "!=": 8, "<": 9, "<=": 10, ">": 11, ">=": 12, "&": 13, "|": 14, "!": 15}
+
+
 class ServerOptions(C.Structure):
     """siminf_gpu_server_options."""
     _fields_ = [

@@ -74,6 +74,20 @@ def lib():
     L.siminf_gpu_plan_free.restype = None
     L.siminf_gpu_release_cached.argtypes = []
     L.siminf_gpu_release_cached.restype = None
+    pi = C.POINTER(C.c_int)
+    L.siminf_gpu_trajectory_u.argtypes = [vp, C.c_int, C.c_int, C.c_int, pi, C.c_int, pi,
+                                          C.c_int, pi, vp, C.POINTER(abi.ReduceStats)]
+    L.siminf_gpu_trajectory_u.restype = C.c_int
+    L.siminf_gpu_trajectory_v.argtypes = [vp, C.c_int, C.c_int, C.c_int, pi, C.c_int, pi,
+                                          C.c_int, C.POINTER(C.c_double), vp,
+                                          C.POINTER(abi.ReduceStats)]
+    L.siminf_gpu_trajectory_v.restype = C.c_int
+    L.siminf_gpu_prevalence.argtypes = [vp, C.c_int, C.c_int, C.c_int,
+                                        C.POINTER(abi.PrevalenceSpec), pi, C.c_int,
+                                        C.POINTER(C.c_double), vp, C.POINTER(abi.ReduceStats)]
+    L.siminf_gpu_prevalence.restype = C.c_int
+    L.siminf_gpu_plan_outputs.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), pi]
+    L.siminf_gpu_plan_outputs.restype = C.c_int
     _lib = L
     return L
 
@@ -88,7 +102,8 @@ EXPORTS = (
     "siminf_gpu_run_solver_ssm_noalloc", "siminf_gpu_run_batch",
     "siminf_gpu_server_create", "siminf_gpu_server_submit", "siminf_gpu_server_wait",
     "siminf_gpu_server_load", "siminf_gpu_server_free", "siminf_gpu_plan_tune",
-    "siminf_gpu_release_cached",
+    "siminf_gpu_release_cached", "siminf_gpu_trajectory_u", "siminf_gpu_trajectory_v",
+    "siminf_gpu_prevalence", "siminf_gpu_plan_outputs",
 )
 
 
