@@ -154,7 +154,7 @@ cudaError_t pinned_acquire(size_t bytes, void **out, size_t *got)
         }
     }
     *got = bytes;
-    return cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+    return cudaHostAlloc(out, bytes, cudaHostAllocPortable);
 }
 
 /* Return a buffer of pinned_acquire: kept if the cache has room, the
