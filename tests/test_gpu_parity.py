@@ -306,3 +306,32 @@ def test_gpu_pinned_sparse_outputs_streamed_back(gpu, oracle_lib):
                                                  native.device_model(m.name).handle, None)
     assert code == 0
     assert np.array_equal(h.prU, ho.prU)
+
+
+def test_gpu_two_pass_and_reductions_at_scale(gpu, monkeypatch):
+    """At 10% of the headline size, 4 replicates: two-pass days give the
+    trajectories of one-pass days, and the device prevalence and trajectory
+    of the resident U equal numpy's on the downloaded U."""
+    from oracle import trajectory as ref
+    from siminf_gb300 import abi, native, workloads
+    from siminf_gb300.trajectory import prevalence, trajectory
+    m = workloads.seir_events(nodes=100_000, days=60, transfers=50_000).replicate(4)
+    out = []
+    for tp in ("-1", "1"):
+        monkeypatch.setenv("SIMINF_TWO_PASS", tp)
+        h = abi.build_args(m, 11)
+        p = native.Plan(h, m.name, cap_transfers=True)
+        p.run()
+        p.download()
+        out.append(h.U.copy())
+        if tp == "1":
+            ncol = m.replicates * len(m.tspan)
+            for level in (1, 2):
+                got = prevalence(p, "I ~ . | S > 250", level=level)
+                want = ref.prevalence(h.U, m.Nn, m.Nc, ncol, 0b0100, 0b1111, level,
+                                      lambda S, E, I, R: S > 250, None, ["S", "E", "I", "R"])
+                assert np.array_equal(got, want)
+            tr = trajectory(p, ["E"])
+            assert np.array_equal(tr["E"], ref.trajectory(h.U, m.Nn, m.Nc, ncol, [2])[0])
+        p.close()
+    assert np.array_equal(out[0], out[1])
