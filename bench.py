@@ -434,6 +434,7 @@ def run_ours(args):
     prof = plan_kernel_profile(plan, C, stream)
     peak, peak_kind = measured_peaks()
     reductions = reduce_bench(plan, peak) if rank == 0 else None
+    event_sort = events_bench(m, peak) if rank == 0 and world == 1 else None
 
     # batched form: R replicates of the same workload in one device-resident
     # plan (the mssm layout), so one replicate's latency-bound tail overlaps
@@ -545,6 +546,7 @@ def run_ours(args):
             "kernels": prof["kernels"],
             "autotune": autotune,
             "reductions": reductions,
+            "event_sort": event_sort,
             "batched": batched,
             "sir_plain": sir,
             "abc": abc,
@@ -614,6 +616,37 @@ def reduce_bench(plan, peak, reps=5):
                      "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
                      "bound": "hbm"}
     return out
+
+
+def events_bench(m, peak, frac=0.1, seed=3):
+    """The event table's ordering (SimInf_events, R/SimInf_events.R:396)
+    on the device: the first tenth of the headline schedule, shuffled, sorted
+    by siminf_gpu_sort_events; against numpy's stable lexsort of the same
+    table on one host core."""
+    from siminf_gb300.events import COLUMNS, sort_events
+    n = int(len(m.events["time"]) * frac)
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(n)
+    ev = {k: np.asarray(m.events[k])[:n][perm] for k in COLUMNS}
+    sort_events(ev)
+    best = None
+    for _ in range(3):
+        _, st = sort_events(ev, stats=True)
+        if best is None or st.ms_kernel < best.ms_kernel:
+            best = st
+    t0 = time.perf_counter()
+    order = np.lexsort((ev["select"], ev["event"], ev["time"]))
+    _ = {k: v[order] for k, v in ev.items()}
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    moved = best.bytes_read + best.bytes_written
+    gbs = moved / (best.ms_kernel / 1e3) / 1e9
+    return {"events": n, "ms_kernel": best.ms_kernel, "ms_total": best.ms_total,
+            "bytes_moved": moved, "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
+            "bound": "hbm",
+            "cpu_baseline": {"ms": cpu_ms, "cores": 1, "kind": "numpy stable lexsort",
+                             "sample": "the same %d shuffled events" % n},
+            "data": "first tenth of the headline schedule, shuffled; the sort kernels "
+                    "(ms_kernel) and the call with every column's copies (ms_total)"}
 
 
 def tune_summary(tune):

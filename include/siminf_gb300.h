@@ -533,6 +533,18 @@ int siminf_gpu_prevalence(const int *d_U, int Nn, int Nc, int ncol,
                           const int *id, int n_id, double *out, void *cuda_stream,
                           siminf_gpu_reduce_stats *stats);
 
+/*
+ * The ordering SimInf_events gives a scheduled-event table
+ * (R/SimInf_events.R:396): events sorted by (time, event, select), equal
+ * keys in input order, done on the device (an LSD radix sort of the packed
+ * key and the input position, then a gather of every column).  The len
+ * events of the eight host columns are reordered in place; the solver
+ * entry points expect this order.  No counterpart in the reference's C.
+ */
+int siminf_gpu_sort_events(long long len, int *event, int *time, int *node, int *dest,
+                           int *n, double *proportion, int *select, int *shift,
+                           void *cuda_stream, siminf_gpu_reduce_stats *stats);
+
 /* The device U/V of a plan that has run (d_V NULL without V), and ncol. */
 int siminf_gpu_plan_outputs(const siminf_gpu_plan *plan, const int **d_U,
                             const double **d_V, int *ncol);

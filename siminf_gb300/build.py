@@ -4,9 +4,9 @@ The library is the C ABI of include/siminf_gb300.h: siminf_kernels.cu (the
 kernels, one instantiation per shipped model), siminf_capi.cpp (planning
 and the exported entry points), siminf_noalloc.cu (the allocation-free
 solver entry point and its static scratch), siminf_batch.cu (batches of
-uneven models), siminf_server.cpp (the request loop) and siminf_reduce.cu
-(trajectory and prevalence on the device), compiled in parallel and linked
-with nvcc.
+uneven models), siminf_server.cpp (the request loop), siminf_reduce.cu (trajectory and
+prevalence on the device) and siminf_events.cu (the event table's ordering
+on the device), compiled in parallel and linked with nvcc.
 
     python -m siminf_gb300.build
 """
@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off"]
 SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp", "siminf_noalloc.cu", "siminf_batch.cu",
-           "siminf_server.cpp", "siminf_reduce.cu"]
+           "siminf_server.cpp", "siminf_reduce.cu", "siminf_events.cu"]
 
 
 def nvcc():

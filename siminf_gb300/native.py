@@ -88,6 +88,10 @@ def lib():
     L.siminf_gpu_prevalence.restype = C.c_int
     L.siminf_gpu_plan_outputs.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), pi]
     L.siminf_gpu_plan_outputs.restype = C.c_int
+    L.siminf_gpu_sort_events.argtypes = [C.c_longlong, pi, pi, pi, pi, pi,
+                                         C.POINTER(C.c_double), pi, pi, vp,
+                                         C.POINTER(abi.ReduceStats)]
+    L.siminf_gpu_sort_events.restype = C.c_int
     _lib = L
     return L
 
@@ -103,7 +107,7 @@ EXPORTS = (
     "siminf_gpu_server_create", "siminf_gpu_server_submit", "siminf_gpu_server_wait",
     "siminf_gpu_server_load", "siminf_gpu_server_free", "siminf_gpu_plan_tune",
     "siminf_gpu_release_cached", "siminf_gpu_trajectory_u", "siminf_gpu_trajectory_v",
-    "siminf_gpu_prevalence", "siminf_gpu_plan_outputs",
+    "siminf_gpu_prevalence", "siminf_gpu_plan_outputs", "siminf_gpu_sort_events",
 )
 
 
