@@ -1173,13 +1173,17 @@ __device__ __forceinline__ void add_prevalence(const DevState &s, long long g, c
     }
 }
 
-/* k_pts_store for one (replicate, node); returns its heavy class on the
- * next day. */
+enum { NEEDS_REFRESH = -2 };
+
+/* k_pts_store for one (replicate, node): post-time-step function, U/V
+ * columns, prevalence.  Returns NEEDS_REFRESH when its rates must be
+ * recomputed (an event touched it, or the post-time-step function changed
+ * v), else its heavy class on the next day. */
 template <class M>
 __device__ __forceinline__ int pts_node(const DevState &s, long long g, int day, double tt,
                                         int c0, int c1, const double *v_in, double *v_out)
 {
-    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    constexpr int NC = M::NC, ND = M::ND;
     const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
     int u[NC];
     load_u<NC>(s.u + g * NC, u);
@@ -1188,26 +1192,44 @@ __device__ __forceinline__ int pts_node(const DevState &s, long long g, int day,
     const double *ld = s.ldata + (size_t) node * s.Nld;
     const double *gd = gdata_of(s, g);
     const int rc = M::pts(vo, u, vi, ld, gd, node, tt);
-    if (rc < 0) {
-        record_error(s, rc, PHASE_PTS, day, g, -1, -1, tt, 0);
-    } else if (rc > 0 || s.update[g]) {
-        si_recip dc = si_recip_none();
-        double delta = 0.0;
-#pragma unroll
-        for (int k = 0; k < NT; k++) {
-            const double old = s.t_rate[(size_t) k * s.Ntot + g];
-            const double nr = M::rate(k, u, vo, ld, gd, tt, dc);
-            s.t_rate[(size_t) k * s.Ntot + g] = nr;
-            delta += nr - old;
-            if (si_bad_rate(nr))
-                record_error(s, ERR_INVALID_RATE, PHASE_PTS, day, g, k, -1, tt, nr);
-        }
-        s.sum_rate[g] += delta;
-        s.update[g] = 0;
-    }
     store_columns<NC, ND>(s, rep, node, u, vo, c0, c1);
     if (s.prev && c1 > c0)
         add_prevalence<NC>(s, g, u, c0, c1);
+    if (rc < 0)
+        record_error(s, rc, PHASE_PTS, day, g, -1, -1, tt, 0);
+    else if (rc > 0 || s.update[g])
+        return NEEDS_REFRESH;
+    return job_over(s, g, day + 1) ? -1 : heavy_class<M>(s, s.sum_rate[g]);
+}
+
+/* The rate refresh of the day's end (src/solvers/SimInf_solver_ssm.c:
+ * 285-306): every rate recomputed with v_new at tt, their changes added to
+ * the rate sum in transition order.  Returns the heavy class on the next
+ * day. */
+template <class M>
+__device__ __forceinline__ int refresh_node(const DevState &s, long long g, int day, double tt,
+                                            const double *v_out)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    const int node = (int) (g % s.Nn);
+    int u[NC];
+    load_u<NC>(s.u + g * NC, u);
+    const double *vo = v_out + g * ND;
+    const double *ld = s.ldata + (size_t) node * s.Nld;
+    const double *gd = gdata_of(s, g);
+    si_recip dc = si_recip_none();
+    double delta = 0.0;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        const double old = s.t_rate[(size_t) k * s.Ntot + g];
+        const double nr = M::rate(k, u, vo, ld, gd, tt, dc);
+        s.t_rate[(size_t) k * s.Ntot + g] = nr;
+        delta += nr - old;
+        if (si_bad_rate(nr))
+            record_error(s, ERR_INVALID_RATE, PHASE_PTS, day, g, k, -1, tt, nr);
+    }
+    s.sum_rate[g] += delta;
+    s.update[g] = 0;
     return job_over(s, g, day + 1) ? -1 : heavy_class<M>(s, s.sum_rate[g]);
 }
 
@@ -1215,11 +1237,34 @@ template <class M>
 __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double tt, int c0, int c1,
                                                    const double *v_in, double *v_out)
 {
-    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    /* The block's nodes whose rates need a refresh are gathered first and
+     * refreshed by the block's first threads: the refresh is FP64 work,
+     * and the FP64 pipe issues a warp instruction at the same cost however
+     * few of its lanes are active. */
+    __shared__ int listed[256];
+    __shared__ int nlisted;
+    if (threadIdx.x == 0)
+        nlisted = 0;
+    __syncthreads();
+    const long long g0 = blockIdx.x * (long long) blockDim.x;
+    const long long g = g0 + threadIdx.x;
     int cls = -1;
-    if (g < s.Ntot && load_flag(s.err_day) >= day && !job_over(s, g, day))
+    if (g < s.Ntot && load_flag(s.err_day) >= day && !job_over(s, g, day)) {
         cls = pts_node<M>(s, g, day, tt, c0, c1, v_in, v_out);
+        if (cls == NEEDS_REFRESH) {
+            listed[atomicAdd(&nlisted, 1)] = threadIdx.x;
+            cls = -1;
+        }
+    }
     push_heavy_warp(s, g, cls, day + 1);
+    __syncthreads();
+    long long gr = -1;
+    int cls2 = -1;
+    if (threadIdx.x < nlisted) {
+        gr = g0 + listed[threadIdx.x];
+        cls2 = refresh_node<M>(s, gr, day, tt, v_out);
+    }
+    push_heavy_warp(s, gr, cls2, day + 1);
 }
 
 /* Whole horizon of one (replicate, node) in one thread: valid when no
