@@ -671,7 +671,7 @@ def plan_kernel_profile(plan, C, stream):
     lib.siminf_gpu_plan_profile.restype = C.c_int
     native.check(lib.siminf_gpu_plan_profile(plan.handle, C.c_void_p(stream.cuda_stream),
                                              prof, cnt))
-    names = ["k_init", "k_ssa_e1", "k_e2_wave", "k_pts_store", "k_horizon"]
+    names = ["k_init", "k_ssa_e1", "k_e2_wave", "k_pts_store", "k_horizon", "k_quick"]
     kernels = {n: {"ms": prof[i], "launches": int(cnt[i])} for i, n in enumerate(names)
                if cnt[i] > 0}
     total = sum(k["ms"] for k in kernels.values()) or 1.0

@@ -371,8 +371,9 @@ int siminf_gpu_plan_run(siminf_gpu_plan *plan, void *cuda_stream);
 int siminf_gpu_plan_download(siminf_gpu_plan *plan, siminf_gpu_solver_args *args);
 /* plan_run with a CUDA event pair around every launch: device milliseconds
  * and launch counts per kernel kind, [0] initialisation, [1] SSA + E1,
- * [2] E2 wavefront, [3] post time step + store, [4] whole-horizon kernel
- * (entries 5..7 are zero).  For profiling; slower than plan_run. */
+ * [2] E2 wavefront, [3] post time step + store, [4] whole-horizon kernel,
+ * [5] first pass of a two-pass day (entries 6..7 are zero).  For
+ * profiling; slower than plan_run. */
 int siminf_gpu_plan_profile(siminf_gpu_plan *plan, void *cuda_stream, double ms[8],
                             long long launches[8]);
 int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);

@@ -1103,7 +1103,7 @@ static int resolve_errors(siminf_gpu_plan *p, std::vector<ErrRec> &cands)
 }
 
 /* Per-kernel-kind device time of one run: [0] init, [1] ssa_e1, [2] e2_wave,
- * [3] pts_store, [4] horizon. */
+ * [3] pts_store, [4] horizon, [5] quick. */
 struct KernelProfile {
     cudaEvent_t a, b;
     double ms[8];
@@ -1174,7 +1174,10 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
         return timed(kp, 4, st, [&] { return L->horizon(s, p->d_days, ndays, st); });
     for (int d = 0; d < ndays && e == cudaSuccess; d++) {
         const DayInfo &di = p->days[d];
-        e = timed(kp, 1, st, [&] { return L->ssa_e1(s, d, di.tt, di.next, st); });
+        if (s.two_pass)
+            e = timed(kp, 5, st, [&] { return L->quick(s, d, di.tt, di.next, st); });
+        if (e == cudaSuccess)
+            e = timed(kp, 1, st, [&] { return L->ssa_e1(s, d, di.tt, di.next, st); });
         for (int w = p->day_wave[d]; w < p->day_wave[d + 1] && e == cudaSuccess; w++) {
             const long long off = p->wave_ptr[w];
             const int cnt = (int) (p->wave_ptr[w + 1] - off);
@@ -1285,7 +1288,10 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
         e = cudaStreamWaitEvent(st, copied[c], 0);
         for (int d = d0; d < d1 && e == cudaSuccess; d++) {
             const DayInfo &di = p->days[d];
-            e = L->ssa_e1(s, d, di.tt, di.next, st);
+            if (s.two_pass)
+                e = L->quick(s, d, di.tt, di.next, st);
+            if (e == cudaSuccess)
+                e = L->ssa_e1(s, d, di.tt, di.next, st);
             long long off = p->e2_day_off[d];
             for (size_t w = 0; w < p->day_waves[d].size() && e == cudaSuccess; w++) {
                 const long long cnt = p->day_waves[d][w];

@@ -1537,14 +1537,13 @@ struct Launch {
         }
         return blocks;
     }
+    static cudaError_t quick(const DevState &s, int day, double tt, double next, cudaStream_t st)
+    {
+        k_quick<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, next);
+        return cudaGetLastError();
+    }
     static cudaError_t ssa_e1(const DevState &s, int day, double tt, double next, cudaStream_t st)
     {
-        if (s.two_pass) {
-            k_quick<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, next);
-            const cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess)
-                return e;
-        }
         const long long need = (long long) blocks_for(s.Ntot, SSA_BLOCK);
         const int grid = (int) (need < ssa_resident_blocks() ? need : ssa_resident_blocks());
         k_ssa_e1<M><<<grid, SSA_BLOCK, 0, st>>>(s, day, tt, next);
@@ -1568,7 +1567,7 @@ struct Launch {
     static const Launchers *table()
     {
         static const Launchers t = {M::NC, M::NT, M::ND, M::NGD, M::PTS_LOCAL,
-                                    init, horizon, ssa_e1, e2_wave, pts_store};
+                                    init, horizon, quick, ssa_e1, e2_wave, pts_store};
         return &t;
     }
 };

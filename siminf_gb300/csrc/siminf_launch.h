@@ -16,6 +16,8 @@ struct Launchers {
     bool pts_local;     /* post-time-step reads only its own node */
     cudaError_t (*init)(const DevState &s, double tt0, cudaStream_t st);
     cudaError_t (*horizon)(const DevState &s, const DayInfo *days, int ndays, cudaStream_t st);
+    /* the first pass of a two-pass day (k_quick); ssa_e1 is the second */
+    cudaError_t (*quick)(const DevState &s, int day, double tt, double next, cudaStream_t st);
     cudaError_t (*ssa_e1)(const DevState &s, int day, double tt, double next, cudaStream_t st);
     cudaError_t (*e2_wave)(const DevState &s, const E2Rec *ev, int count, int day, double tt,
                            cudaStream_t st);
