@@ -60,6 +60,7 @@ enum {
     SIMINF_GPU_ERR_EVENT_SHIFT = -16,
     SIMINF_GPU_ERR_SHIFT_OUT_OF_BOUNDS = -17,
     SIMINF_GPU_ERR_INVALID_PROPORTION = -18,
+    SIMINF_GPU_ERR_AEM_REPLICATED_MODEL = -19,
     SIMINF_GPU_ERR_CUDA = -30,              /* a CUDA runtime call failed */
     SIMINF_GPU_ERR_EVENTS_UNSORTED = -31,   /* events not sorted by time, E1 before E2 */
     SIMINF_GPU_ERR_UNKNOWN_MODEL = -32,     /* no device model of that name */
@@ -117,7 +118,7 @@ typedef struct siminf_gpu_solver_args {
     const int *select;
     const int *shift;
     int Nthread;                /* ignored on the GPU */
-    int solver;                 /* 0 = ssm; 1 = aem is rejected */
+    int solver;                 /* 0 = ssm/mssm, 1 = aem (one replicate) */
     int crn;                    /* common random numbers (mssm) */
     int rng_type;               /* ignored: the GPU stream is Philox4x32-10 */
     unsigned long int seed;     /* Philox key */

@@ -63,7 +63,11 @@ int ref_run(const siminf_gpu_solver_args *ga, const char *model, int threads)
     }
     if (shim_configure((uint64_t) a.seed, a.Nn, a.Nthread, a.Nrep, threads))
         return -2;
-    const int err = (a.Nrep > 1) ? SimInf_run_solver_mssm(&a) : SimInf_run_solver_ssm(&a);
+    int err;
+    if (a.solver == 1)            /* aem: one replicate (src/SimInf.c:393-398) */
+        err = a.Nrep > 1 ? -19 : SimInf_run_solver_aem(&a);
+    else
+        err = (a.Nrep > 1) ? SimInf_run_solver_mssm(&a) : SimInf_run_solver_ssm(&a);
     shim_release();
     return err;
 }

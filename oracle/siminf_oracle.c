@@ -16,6 +16,10 @@
  *   - sparse store                  src/solvers/SimInf_solver.c:929-950,
  *                                   src/solvers/SimInf_solver_mssm.c:332-371
  *   - replicate loop (mssm)         src/solvers/SimInf_solver_mssm.c:105-384
+ *   - all-events method (aem)       src/solvers/SimInf_solver_aem.c:52-75
+ *                                   (calcTimes), :113-158 (initial times),
+ *                                   :179-307 (a node's day), :329-381
+ *                                   (rate refresh with time rescaling)
  *
  * Random draws come from siminf_stream.h, keyed by (seed, replicate * Nn +
  * node, draw index) instead of one GSL generator per thread, so results do
@@ -29,6 +33,7 @@
  * transfers run serially, as in the reference, so that this file doubles
  * as the CPU baseline.
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -69,6 +74,7 @@ typedef struct ctx {
     int Nn, Nc, Nt, Nd, Nld;
     uint64_t seed;
     int gdata_stride;           /* 0: one gdata; else replicate r uses gdata + r * stride */
+    int aem;                    /* all-events method instead of the direct method */
 } ctx;
 
 static const double *gdata_of(const ctx *c, int r)
@@ -89,6 +95,10 @@ typedef struct rep {
     double err_time, err_rate;
     size_t events_index;
     int *individuals;
+    /* aem: per (node, transition) the next event time, the time left
+     * when its rate fell to zero, and the draw index of its stream */
+    double *react_time, *react_inf;
+    uint64_t *react_ctr;
 } rep;
 
 static double now_seconds(void)
@@ -630,6 +640,169 @@ static void resolve_pts_errors(const ctx *c, rep *s)
     }
 }
 
+/* ------------------------------------------------------------------ */
+/* All-events method (src/solvers/SimInf_solver_aem.c).                */
+/* Transition j of node g draws from its own stream, keyed (seed,      */
+/* AEM_SID | (g * Nt + j)), where the reference gives every (node,     */
+/* transition) its own generator (:465-481).  The next event is the    */
+/* smallest time, the lowest transition among equal times, where the   */
+/* reference's binary heap (src/misc/binheap.c) may break an exact tie */
+/* the other way.                                                      */
+/* ------------------------------------------------------------------ */
+#define AEM_SID (1ULL << 63)
+
+static double aem_neglog(const ctx *c, int node, int j, uint64_t *ctr)
+{
+    si_rng rng;
+    si_rng_init(&rng, c->seed, AEM_SID | ((uint64_t) node * c->Nt + j), *ctr);
+    const double x = si_neglog_u32(si_next_u32(&rng));
+    *ctr = rng.ctr;
+    return x;
+}
+
+/* calcTimes (src/solvers/SimInf_solver_aem.c:52-75). */
+static void aem_calc_times(const ctx *c, int node, int j, double *time, double *inf,
+                           double tt, double old_rate, double new_rate, uint64_t *ctr)
+{
+    const double oldtime = *time;
+    if (isinf(oldtime)) {
+        if (*inf == 0.0)
+            *time = aem_neglog(c, node, j, ctr) / new_rate + tt;
+        else if (new_rate > 0.0)
+            *time = tt + (*inf / new_rate);
+    } else if (new_rate >= DBL_MIN) {
+        if (oldtime == tt)
+            *time = aem_neglog(c, node, j, ctr) / new_rate + tt;
+        else
+            *time = ((old_rate / new_rate) * (oldtime - tt)) + tt;
+    } else {
+        *inf = (oldtime - tt) * old_rate;
+        *time = INFINITY;
+    }
+}
+
+/* A rate of transition j refreshed at time t, then its event time. */
+static void aem_refresh(const ctx *c, rep *s, int r, int node, int j, const double *v,
+                        double t_rate_time, double t_calc)
+{
+    const siminf_gpu_solver_args *a = c->a;
+    const int Nc = c->Nc, Nt = c->Nt, Nld = c->Nld;
+    double *t_rate = &s->t_rate[(size_t) node * Nt];
+    const double old = t_rate[j];
+    const double rate = c->m->tr[j](&s->u[(size_t) node * Nc], v,
+                                    &a->ldata[(size_t) node * Nld], gdata_of(c, r),
+                                    t_rate_time);
+    t_rate[j] = rate;
+    if (!isfinite(rate) || rate < 0.0) {
+        s->node_err[node] = SIMINF_GPU_ERR_INVALID_RATE;
+        s->node_err_time[node] = t_rate_time;
+        s->node_err_rate[node] = rate;
+        s->node_err_tr[node] = j;
+    }
+    const size_t k = (size_t) node * Nt + j;
+    aem_calc_times(c, node, j, &s->react_time[k], &s->react_inf[k], t_calc, old, rate,
+                   &s->react_ctr[k]);
+}
+
+/* Initial rates and event times (src/solvers/SimInf_solver_aem.c:113-158). */
+static int aem_init_node(const ctx *c, rep *s, int r, int node, double tt)
+{
+    const siminf_gpu_solver_args *a = c->a;
+    const int Nc = c->Nc, Nt = c->Nt, Nd = c->Nd, Nld = c->Nld;
+    int err = 0;
+    for (int j = 0; j < Nt; j++) {
+        const double rate = c->m->tr[j](&s->u[(size_t) node * Nc], &s->v[(size_t) node * Nd],
+                                        &a->ldata[(size_t) node * Nld], gdata_of(c, r), tt);
+        const size_t k = (size_t) node * Nt + j;
+        s->t_rate[k] = rate;
+        if (!isfinite(rate) || rate < 0.0) {
+            s->node_err[node] = SIMINF_GPU_ERR_INVALID_RATE;
+            s->node_err_time[node] = tt;
+            s->node_err_rate[node] = rate;
+            s->node_err_tr[node] = j;
+            err = 1;
+        }
+        s->react_ctr[k] = 0;
+        s->react_inf[k] = 0.0;
+        s->react_time[k] = aem_neglog(c, node, j, &s->react_ctr[k]) / rate + tt;
+        if (s->react_time[k] <= 0.0)
+            s->react_time[k] = INFINITY;
+    }
+    s->t_time[node] = tt;
+    return err;
+}
+
+/* One node's day (src/solvers/SimInf_solver_aem.c:179-307).  Returns the
+ * number of transitions fired. */
+static uint64_t aem_node(const ctx *c, rep *s, int r, int node, double next)
+{
+    const siminf_gpu_solver_args *a = c->a;
+    const int Nc = c->Nc, Nt = c->Nt, Nd = c->Nd;
+    int *u = &s->u[(size_t) node * Nc];
+    const double *v = &s->v[(size_t) node * Nd];
+    const double *times = &s->react_time[(size_t) node * Nt];
+    uint64_t fired = 0;
+    for (;;) {
+        int tr = 0;
+        double t = times[0];
+        for (int j = 1; j < Nt; j++) {
+            if (times[j] < t) {
+                t = times[j];
+                tr = j;
+            }
+        }
+        s->t_time[node] = t;
+        if (isinf(t) || t >= next) {
+            s->t_time[node] = next;
+            break;
+        }
+        fired++;
+        for (int j = a->jcS[tr]; j < a->jcS[tr + 1]; j++) {
+            u[a->irS[j]] += a->prS[j];
+            if (u[a->irS[j]] < 0) {
+                s->node_err[node] = SIMINF_GPU_ERR_NEGATIVE_STATE;
+                s->node_err_time[node] = t;
+                s->node_err_rate[node] = 0;
+                s->node_err_tr[node] = tr;
+            }
+        }
+        for (int ii = a->jcG[tr]; ii < a->jcG[tr + 1]; ii++) {
+            const int j = a->irG[ii];
+            if (j != tr)
+                aem_refresh(c, s, r, node, j, v, t, t);
+        }
+        aem_refresh(c, s, r, node, tr, v, t, t);
+    }
+    if (g_node_fired)
+        g_node_fired[(size_t) r * c->Nn + node] += fired;
+    return fired;
+}
+
+/* Post time step and, where needed, every rate refreshed with v_new at tt
+ * and its event time rescaled at the node's time
+ * (src/solvers/SimInf_solver_aem.c:329-381).  Returns the pts rc. */
+static int aem_pts_node(const ctx *c, rep *s, int r, int node, double tt)
+{
+    const siminf_gpu_solver_args *a = c->a;
+    const int Nc = c->Nc, Nt = c->Nt, Nd = c->Nd, Nld = c->Nld;
+    const int rc = c->m->pts(&s->v_new[(size_t) node * Nd], &s->u[(size_t) node * Nc],
+                             &s->v[(size_t) node * Nd], &a->ldata[(size_t) node * Nld],
+                             gdata_of(c, r), node, tt);
+    if (rc < 0) {
+        s->node_err[node] = rc;
+        s->node_err_time[node] = tt;
+        s->node_err_tr[node] = -1;
+        s->node_err_rate[node] = 0;
+        return rc;
+    }
+    if (rc > 0 || s->update_node[node]) {
+        for (int j = 0; j < Nt; j++)
+            aem_refresh(c, s, r, node, j, &s->v_new[(size_t) node * Nd], tt, s->t_time[node]);
+        s->update_node[node] = 0;
+    }
+    return rc;
+}
+
 static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
                          oracle_result *res)
 {
@@ -656,6 +829,10 @@ static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
     /* Rates at the start (src/solvers/SimInf_solver_ssm.c:96-117). */
 #pragma omp parallel for schedule(static) if (parallel_nodes) reduction(|:any_err)
     for (int node = 0; node < Nn; node++) {
+        if (c->aem) {
+            any_err |= aem_init_node(c, s, r, node, tt);
+            continue;
+        }
         s->sum_t_rate[node] = 0.0;
         for (int j = 0; j < Nt; j++) {
             const double rate = c->m->tr[j](&s->u[(size_t) node * Nc], &s->v[(size_t) node * Nd],
@@ -685,7 +862,8 @@ static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
         uint64_t day_max = 0;
 #pragma omp parallel for schedule(static) if (parallel_nodes) reduction(+:fired) reduction(|:any_err) reduction(max:day_max)
         for (int node = 0; node < Nn; node++) {
-            const uint64_t f = ssa_node(c, s, r, node, next);
+            const uint64_t f = c->aem ? aem_node(c, s, r, node, next)
+                                      : ssa_node(c, s, r, node, next);
             fired += f;
             if (f > day_max)
                 day_max = f;
@@ -706,7 +884,10 @@ static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
         any_err = 0;
 #pragma omp parallel for schedule(static) if (parallel_nodes) reduction(|:any_err)
         for (int node = 0; node < Nn; node++) {
-            pts_node(c, s, r, node, tt);
+            if (c->aem)
+                aem_pts_node(c, s, r, node, tt);
+            else
+                pts_node(c, s, r, node, tt);
             any_err |= (s->node_err[node] != 0);
         }
         if (any_err)
@@ -746,7 +927,10 @@ static int rep_alloc(rep *s, int Nn, int Nc, int Nt, int Nd)
     s->node_err_rate = malloc((size_t) Nn * sizeof(double) + 8);
     s->node_err_tr = malloc((size_t) Nn * sizeof(int) + 4);
     s->individuals = malloc((size_t) Nc * sizeof(int) + 4);
-    return (s->u && s->v && s->v_new && s->t_rate && s->sum_t_rate && s->t_time &&
+    s->react_time = malloc((size_t) Nn * Nt * sizeof(double) + 8);
+    s->react_inf = malloc((size_t) Nn * Nt * sizeof(double) + 8);
+    s->react_ctr = malloc((size_t) Nn * Nt * sizeof(uint64_t) + 8);
+    return (s->react_time && s->react_inf && s->react_ctr && s->u && s->v && s->v_new && s->t_rate && s->sum_t_rate && s->t_time &&
             s->update_node && s->ctr && s->node_err && s->node_err_time &&
             s->node_err_rate && s->node_err_tr && s->individuals) ? 0 : -1;
 }
@@ -757,6 +941,7 @@ static void rep_free(rep *s)
     free(s->t_time); free(s->update_node); free(s->ctr); free(s->node_err);
     free(s->node_err_time); free(s->node_err_rate); free(s->node_err_tr);
     free(s->individuals);
+    free(s->react_time); free(s->react_inf); free(s->react_ctr);
 }
 
 /*
@@ -787,6 +972,11 @@ static int oracle_run_impl(const siminf_gpu_solver_args *args, const char *model
     c.Nd = args->Nd;
     c.Nld = args->Nld;
     c.seed = (uint64_t) args->seed;
+    c.aem = args->solver == 1;
+    if (args->solver != 0 && args->solver != 1)
+        return SIMINF_GPU_ERR_UNKNOWN_SOLVER;
+    if (c.aem && args->Nrep > 1)
+        return SIMINF_GPU_ERR_AEM_REPLICATED_MODEL;  /* src/SimInf.c:393-396 */
 #ifdef _OPENMP
     if (nthreads > 0)
         omp_set_num_threads(nthreads);

@@ -33,6 +33,7 @@ ERRORS = {
     -16: "'shift' is invalid.",
     -17: "'shift' is out of bounds.",
     -18: "Invalid proportion detected (< 0.0 or > 1.0).",
+    -19: "Cannot run the 'aem' solver on a replicated model.",
     -30: "A CUDA runtime call failed.",
     -31: "Events must be sorted by time, with E1 events before external transfers.",
     -32: "Unknown device model.",

@@ -64,3 +64,50 @@ def test_ks_seir_events_against_reference(oracle_lib):
                        n_e2_prop=1)
     m = M.SEIR(u0, np.array([5.0, 10.0, 15.0, 20.0]), 0.3, 0.25, 0.077, events=ev)
     _ks_all(m, seed_ours=7, seed_ref=8, nodes=(0, 5))
+
+
+def _ks_nodes(m, seed_ours, seed_ref):
+    """aem (one replicate only): a model of many identical, uncoupled nodes
+    gives one sample per node; the oracle's aem against the reference's
+    unmodified aem with independent generators, per compartment and tspan
+    point."""
+    stats = pytest.importorskip("scipy.stats")
+    from oracle import oracle
+    ho = abi.build_args(m, seed_ours, solver=1)
+    code, _ = oracle.run(ho, m.name, 8)
+    assert code == 0
+    hr = abi.build_args(m, seed_ref, solver=1)
+    assert oracle.run_ref(hr, m.name, 8, independent=True) == 0
+    tlen = len(m.tspan)
+    U_o = ho.U.reshape((m.Nn, m.Nc, tlen), order="F")
+    U_r = hr.U.reshape((m.Nn, m.Nc, tlen), order="F")
+    tests = []
+    for c in range(m.Nc):
+        for k in range(tlen):
+            a, b = U_o[:, c, k], U_r[:, c, k]
+            if a.min() == a.max() == b.min() == b.max():
+                continue
+            tests.append(stats.ks_2samp(a, b).pvalue)
+    level = 1e-3 / max(1, len(tests))
+    assert len(tests) > 0
+    assert min(tests) > level, (min(tests), level, len(tests))
+
+
+@pytest.mark.skipif(not _have_ref(), reason="the reference sources are not compiled here")
+def test_ks_sir_aem_against_reference(oracle_lib):
+    n = REPLICATES
+    u0 = {"S": np.full(n, 200), "I": np.full(n, 5), "R": np.zeros(n, int)}
+    m = M.SIR(u0, np.array([3.0, 6.0, 10.0, 15.0, 22.0, 30.0]), 0.16, 0.077)
+    _ks_nodes(m, seed_ours=11, seed_ref=12)
+
+
+@pytest.mark.skipif(not _have_ref(), reason="the reference sources are not compiled here")
+def test_ks_sise_aem_against_reference(oracle_lib):
+    """SISe: time-dependent rates and a post-time-step function that
+    changes phi every day, so every day ends with a rescaling refresh."""
+    n = REPLICATES
+    u0 = {"S": np.full(n, 120), "I": np.full(n, 6)}
+    m = M.SISe(u0, np.arange(1, 41, 4), phi=0.2, upsilon=0.02, gamma=0.1, alpha=1,
+               beta_t1=0.19, beta_t2=0.085, beta_t3=0.075, beta_t4=0.185, end_t1=10,
+               end_t2=20, end_t3=30, end_t4=365, epsilon=0.0005)
+    _ks_nodes(m, seed_ours=13, seed_ref=14)
