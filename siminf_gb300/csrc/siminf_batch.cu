@@ -103,6 +103,11 @@ extern "C" int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs,
         static int stand_in;
         a.U = &stand_in;                       /* the batch writes no U */
         int rc = jobs[j].args ? capi_validate(&a, L) : SIMINF_GPU_ERR_INVALID_MODEL;
+        if (!rc && a.solver != 0) {
+            capi_set_status(SIMINF_GPU_ERR_UNKNOWN_SOLVER, -1, -1, -1, 0, 0,
+                            "a batch runs the ssm solver");
+            rc = SIMINF_GPU_ERR_UNKNOWN_SOLVER;
+        }
         if (!rc && (a.Nrep != 1 || a.Nld != jobs[0].args->Nld))
             rc = SIMINF_GPU_ERR_INVALID_MODEL;
         if (rc) {

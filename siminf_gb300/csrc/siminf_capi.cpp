@@ -205,10 +205,15 @@ static int validate(const siminf_gpu_solver_args *a, const Launchers *L)
     char msg[256];
     if (!a || !L)
         return SIMINF_GPU_ERR_INVALID_MODEL;
-    if (a->solver != 0) {
-        set_status(SIMINF_GPU_ERR_UNKNOWN_SOLVER, -1, -1, -1, 0, 0,
-                   "the GPU path implements the ssm solver only");
+    if (a->solver != 0 && a->solver != 1) {
+        set_status(SIMINF_GPU_ERR_UNKNOWN_SOLVER, -1, -1, -1, 0, 0, "Invalid 'solver' value.");
         return SIMINF_GPU_ERR_UNKNOWN_SOLVER;
+    }
+    if (a->solver == 1 && a->Nrep > 1) {
+        /* src/SimInf.c:393-396 */
+        set_status(SIMINF_GPU_ERR_AEM_REPLICATED_MODEL, -1, -1, -1, 0, 0,
+                   "Cannot run the 'aem' solver on a replicated model.");
+        return SIMINF_GPU_ERR_AEM_REPLICATED_MODEL;
     }
     if (a->Nc != L->Nc || a->Nt != L->Nt || a->Nd != L->Nd || a->Nn < 1 || a->tlen < 1 ||
         (a->Nrep < 1) || !a->u0 || !a->tspan || !a->irG || !a->jcG || !a->irS || !a->jcS ||
@@ -861,7 +866,7 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
         p->args = *a;
     }
     p->stats.ms_plan = ms_since(t0);
-    p->horizon = (p->e2_count == 0) && L->pts_local;
+    p->horizon = (p->e2_count == 0) && L->pts_local && a->solver == 0;
 
     cudaStream_t st = g_plan_stream;
     p->stream = st;
@@ -954,11 +959,19 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     /* two-pass days (options, else SIMINF_TWO_PASS, else from 4,000,000
      * nodes: below that the day's longest chain, not its many quiet
      * nodes, sets its length) */
+    s.aem = a->solver == 1;
+    if (s.aem) {
+        if (!rc) rc = dalloc(&s.react_time, (size_t) Ntot * Nt, own);
+        if (!rc) rc = dalloc(&s.react_inf, (size_t) Ntot * Nt, own);
+        if (!rc) rc = dalloc(&s.react_ctr, (size_t) Ntot * Nt, own);
+    }
     s.two_pass = Ntot >= 4000000;
     if (const char *ev = getenv("SIMINF_TWO_PASS"))
         s.two_pass = atoi(ev) > 0;
     if (opt && opt->two_pass)
         s.two_pass = opt->two_pass > 0;
+    if (s.aem)
+        s.two_pass = 0;                 /* the work queue is the direct method's */
     if (!rc) rc = dalloc(&s.active, (size_t) Ntot, own);
     if (!rc) {
         s.err_day = s.err_count + 1;
@@ -1167,7 +1180,9 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
 {
     const Launchers *L = p->L;
     const int ndays = p->max_days > 0 ? std::min(p->max_days, p->ndays) : p->ndays;
-    cudaError_t e = timed(kp, 0, st, [&] { return L->init(s, p->tt0, st); });
+    cudaError_t e = timed(kp, 0, st, [&] {
+        return s.aem ? L->aem_init(s, p->tt0, st) : L->init(s, p->tt0, st);
+    });
     if (e != cudaSuccess)
         return e;
     if (p->horizon)
@@ -1177,7 +1192,10 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
         if (s.two_pass)
             e = timed(kp, 5, st, [&] { return L->quick(s, d, di.tt, di.next, st); });
         if (e == cudaSuccess)
-            e = timed(kp, 1, st, [&] { return L->ssa_e1(s, d, di.tt, di.next, st); });
+            e = timed(kp, 1, st, [&] {
+                return s.aem ? L->aem_day(s, d, di.tt, di.next, st)
+                             : L->ssa_e1(s, d, di.tt, di.next, st);
+            });
         for (int w = p->day_wave[d]; w < p->day_wave[d + 1] && e == cudaSuccess; w++) {
             const long long off = p->wave_ptr[w];
             const int cnt = (int) (p->wave_ptr[w + 1] - off);
@@ -1185,7 +1203,8 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
         }
         if (e == cudaSuccess)
             e = timed(kp, 3, st, [&] {
-                return L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
+                return s.aem ? L->aem_pts(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st)
+                             : L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
             });
         std::swap(s.vA, s.vB);
     }
@@ -1208,7 +1227,7 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
     const siminf_gpu_solver_args *a = &p->args;
     const int ndays = p->ndays;
     enum { CHUNK_DAYS = 8, RING = 8 };
-    cudaError_t e = L->init(s, p->tt0, st);
+    cudaError_t e = s.aem ? L->aem_init(s, p->tt0, st) : L->init(s, p->tt0, st);
     if (e != cudaSuccess)
         return e;
 
@@ -1291,7 +1310,8 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             if (s.two_pass)
                 e = L->quick(s, d, di.tt, di.next, st);
             if (e == cudaSuccess)
-                e = L->ssa_e1(s, d, di.tt, di.next, st);
+                e = s.aem ? L->aem_day(s, d, di.tt, di.next, st)
+                          : L->ssa_e1(s, d, di.tt, di.next, st);
             long long off = p->e2_day_off[d];
             for (size_t w = 0; w < p->day_waves[d].size() && e == cudaSuccess; w++) {
                 const long long cnt = p->day_waves[d][w];
@@ -1299,7 +1319,8 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
                 off += cnt;
             }
             if (e == cudaSuccess)
-                e = L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
+                e = s.aem ? L->aem_pts(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st)
+                          : L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
             std::swap(s.vA, s.vB);
         }
         /* the columns this chunk finished go back while later days run */
@@ -1770,11 +1791,11 @@ int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model 
     auto t0 = std::chrono::steady_clock::now();
     memset(&g_status, 0, sizeof(g_status));
     if (!a1 || !model || !pf || pf->n_particles < 1 || pf->n_obs < 1 || !pf->obs ||
-        !pf->obs_time || !pf->loglik || !pf->ess || a1->len > 0 ||
+        !pf->obs_time || !pf->loglik || !pf->ess || a1->len > 0 || a1->solver != 0 ||
         pf->obs_compartment < 0 || pf->obs_compartment >= a1->Nc ||
         !(pf->detect_p > 0.0 && pf->detect_p < 1.0)) {
         set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
-                   "invalid particle filter arguments (events are not supported)");
+                   "invalid particle filter arguments (events and the aem solver are not supported)");
         return SIMINF_GPU_ERR_INVALID_MODEL;
     }
     for (int i = 0; i < pf->n_obs; i++) {

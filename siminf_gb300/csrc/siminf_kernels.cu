@@ -27,6 +27,7 @@
  * Compiled with -fmad=false: every double operation rounds as in the
  * reference's C, which is what makes trajectories bit-identical.
  */
+#include <cfloat>
 #include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -1267,6 +1268,272 @@ __global__ void __launch_bounds__(256) k_pts_store(DevState s, int day, double t
     push_heavy_warp(s, gr, cls2, day + 1);
 }
 
+/* ------------------------------------------------------------------ */
+/* All-events method (src/solvers/SimInf_solver_aem.c), one thread per   */
+/* node.  Transition j of node g draws from its own stream, keyed (seed, */
+/* AEM_SID | (g * Nt + j)); the next event is the smallest event time,   */
+/* the lowest transition among equal times.                              */
+/* ------------------------------------------------------------------ */
+#define AEM_SID (1ULL << 63)
+
+__device__ __forceinline__ double aem_neglog(uint64_t seed, long long g, int Nt, int j,
+                                             uint64_t &ctr)
+{
+    si_rng r;
+    si_rng_init(&r, seed, AEM_SID | ((uint64_t) g * (uint64_t) Nt + (uint64_t) j), ctr);
+    const double x = si_neglog_u32(si_next_u32(&r));
+    ctr = r.ctr;
+    return x;
+}
+
+/* calcTimes (src/solvers/SimInf_solver_aem.c:52-75). */
+__device__ __forceinline__ void aem_calc_times(double &time, double &inf, double tt,
+                                               double old_rate, double new_rate, uint64_t seed,
+                                               long long g, int Nt, int j, uint64_t &ctr)
+{
+    const double oldtime = time;
+    if (isinf(oldtime)) {
+        if (inf == 0.0)
+            time = si_div(aem_neglog(seed, g, Nt, j, ctr), new_rate) + tt;
+        else if (new_rate > 0.0)
+            time = tt + si_div(inf, new_rate);
+    } else if (new_rate >= DBL_MIN) {
+        if (oldtime == tt)
+            time = si_div(aem_neglog(seed, g, Nt, j, ctr), new_rate) + tt;
+        else
+            time = (si_div(old_rate, new_rate) * (oldtime - tt)) + tt;
+    } else {
+        inf = (oldtime - tt) * old_rate;
+        time = si_bits_double(0x7FF0000000000000ULL);
+    }
+}
+
+/* Initial rates and event times (src/solvers/SimInf_solver_aem.c:113-158). */
+template <class M>
+__global__ void k_aem_init(DevState s, double tt0)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (g >= s.Ntot)
+        return;
+    const int node = (int) (g % s.Nn);
+    int u[NC];
+    load_u<NC>(s.u + g * NC, u);
+    const double *v = s.vA + g * ND;
+    const double *ld = s.ldata + (size_t) node * s.Nld;
+    si_recip dc = si_recip_none();
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        const double rate = M::rate(j, u, v, ld, gdata_of(s, g), tt0, dc);
+        const size_t k = (size_t) j * s.Ntot + g;
+        s.t_rate[k] = rate;
+        if (!isfinite(rate) || rate < 0.0)
+            record_error(s, ERR_INVALID_RATE, PHASE_INIT, 0, g, j, -1, tt0, rate);
+        uint64_t c = 0;
+        double t = si_div(aem_neglog(s.seed, g, NT, j, c), rate) + tt0;
+        if (t <= 0.0)
+            t = si_bits_double(0x7FF0000000000000ULL);
+        s.react_time[k] = t;
+        s.react_inf[k] = 0.0;
+        s.react_ctr[k] = c;
+    }
+    s.t_time[g] = tt0;
+    s.ctr[g] = 0;
+    s.update[g] = 0;
+}
+
+/* The state of one node's aem day, held by one thread. */
+template <class M>
+struct AemNode {
+    int u[M::NC];
+    double rate[M::NT], time[M::NT], inf[M::NT];
+    uint64_t ctr[M::NT];
+    int err, err_tr;
+    double err_t, err_rate;
+};
+
+/* Rate j refreshed at time t (rate functions) and its event time at tc
+ * (calcTimes), recording an invalid rate. */
+template <class M>
+__device__ __forceinline__ void aem_refresh(const DevState &s, AemNode<M> &a, long long g, int j,
+                                            const double *v, const double *ld, const double *gd,
+                                            double t, double tc, si_recip &dc)
+{
+    const double old = a.rate[j];
+    const double nr = M::rate(j, a.u, v, ld, gd, t, dc);
+    a.rate[j] = nr;
+    if (si_bad_rate(nr)) {
+        a.err = ERR_INVALID_RATE;
+        a.err_tr = j;
+        a.err_t = t;
+        a.err_rate = nr;
+    }
+    aem_calc_times(a.time[j], a.inf[j], tc, old, nr, s.seed, g, M::NT, j, a.ctr[j]);
+}
+
+/* One day of every node (src/solvers/SimInf_solver_aem.c:179-307), then
+ * the node's E1 events. */
+template <class M>
+__global__ void __launch_bounds__(128) k_aem_day(DevState s, int day, double tt, double next)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    __shared__ int sS[NT * NC];
+    __shared__ uint32_t sG[NT];
+    load_model_smem<M>(s, sS, sG);
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (g >= s.Ntot || load_flag(s.err_day) < day)
+        return;
+    const int node = (int) (g % s.Nn);
+    AemNode<M> a;
+    load_u<NC>(s.u + g * NC, a.u);
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        const size_t k = (size_t) j * s.Ntot + g;
+        a.rate[j] = s.t_rate[k];
+        a.time[j] = s.react_time[k];
+        a.inf[j] = s.react_inf[k];
+        a.ctr[j] = s.react_ctr[k];
+    }
+    a.err = 0;
+    a.err_tr = -1;
+    a.err_t = 0.0;
+    a.err_rate = 0.0;
+    const double *v = s.vA + g * ND;
+    const double *ld = s.ldata + (size_t) node * s.Nld;
+    const double *gd = gdata_of(s, g);
+    si_recip dc = si_recip_none();
+    unsigned fired = 0;
+    double t = next;
+    for (;;) {
+        int tr = 0;
+        double tmin = a.time[0];
+#pragma unroll
+        for (int j = 1; j < NT; j++)
+            if (a.time[j] < tmin) {
+                tmin = a.time[j];
+                tr = j;
+            }
+        if (isinf(tmin) || tmin >= next)
+            break;
+        t = tmin;
+        if (++fired > MAX_NODE_DAY_TRANSITIONS) {
+            a.err = ERR_TIMEOUT;
+            a.err_tr = tr;
+            a.err_t = t;
+            break;
+        }
+        int neg = 0;
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int d = sS[tr * NC + c];
+            a.u[c] += d;
+            neg |= (d != 0) & (a.u[c] < 0);
+        }
+        if (neg) {
+            a.err = ERR_NEGATIVE_STATE;
+            a.err_tr = tr;
+            a.err_t = t;
+            a.err_rate = 0.0;
+        }
+        /* the dependents in G's column (row order), then the transition
+         * that fired */
+        const uint32_t gm = sG[tr];
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+            if (j != tr && (gm & (1u << j)))
+                aem_refresh<M>(s, a, g, j, v, ld, gd, t, t, dc);
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+            if (j == tr)
+                aem_refresh<M>(s, a, g, j, v, ld, gd, t, t, dc);
+    }
+    if (fired)
+        atomicAdd(s.fired, (unsigned long long) fired);  /* per thread: lanes may have left */
+    si_rng r;
+    {
+        uint64_t seed, sid;
+        stream_key(s, g, seed, sid);
+        si_rng_init(&r, seed, sid, s.ctr[g]);
+    }
+    if (a.err) {
+        record_error(s, a.err, PHASE_SSA, day, g, a.err_tr, -1, a.err_t, a.err_rate);
+    } else {
+        int e_code = 0, e_idx = -1;
+        if (node_e1<NC>(s, a.u, node, day, r, g, tt, e_code, e_idx))
+            s.update[g] = 1;
+        if (e_code)
+            record_error(s, e_code, PHASE_E1, day, g, -1, e_idx, tt, 0);
+    }
+    store_u<NC>(s.u + g * NC, a.u);
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        const size_t k = (size_t) j * s.Ntot + g;
+        s.t_rate[k] = a.rate[j];
+        s.react_time[k] = a.time[j];
+        s.react_inf[k] = a.inf[j];
+        s.react_ctr[k] = a.ctr[j];
+    }
+    s.t_time[g] = next;
+    s.ctr[g] = r.ctr;
+}
+
+/* The day's end (src/solvers/SimInf_solver_aem.c:329-381): post-time-step
+ * function, U/V columns, and for a node an event touched or whose v
+ * changed, every rate recomputed with v_new at tt and its event time
+ * rescaled at the node's time (the end of the day). */
+template <class M>
+__global__ void __launch_bounds__(256) k_aem_pts(DevState s, int day, double tt, int c0, int c1,
+                                                 const double *v_in, double *v_out)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (g >= s.Ntot || load_flag(s.err_day) < day)
+        return;
+    const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
+    AemNode<M> a;
+    load_u<NC>(s.u + g * NC, a.u);
+    const double *vi = v_in + g * ND;
+    double *vo = v_out + g * ND;
+    const double *ld = s.ldata + (size_t) node * s.Nld;
+    const double *gd = gdata_of(s, g);
+    const int rc = M::pts(vo, a.u, vi, ld, gd, node, tt);
+    store_columns<NC, ND>(s, rep, node, a.u, vo, c0, c1);
+    if (rc < 0) {
+        record_error(s, rc, PHASE_PTS, day, g, -1, -1, tt, 0);
+        return;
+    }
+    if (rc == 0 && !s.update[g])
+        return;
+    const double tc = s.t_time[g];
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        const size_t k = (size_t) j * s.Ntot + g;
+        a.rate[j] = s.t_rate[k];
+        a.time[j] = s.react_time[k];
+        a.inf[j] = s.react_inf[k];
+        a.ctr[j] = s.react_ctr[k];
+    }
+    a.err = 0;
+    si_recip dc = si_recip_none();
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        aem_refresh<M>(s, a, g, j, vo, ld, gd, tt, tc, dc);
+        if (a.err) {
+            record_error(s, ERR_INVALID_RATE, PHASE_PTS, day, g, j, -1, tt, a.err_rate);
+            a.err = 0;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        const size_t k = (size_t) j * s.Ntot + g;
+        s.t_rate[k] = a.rate[j];
+        s.react_time[k] = a.time[j];
+        s.react_inf[k] = a.inf[j];
+        s.react_ctr[k] = a.ctr[j];
+    }
+    s.update[g] = 0;
+}
+
 /* Whole horizon of one (replicate, node) in one thread: valid when no
  * external transfer couples nodes and the post-time-step function reads
  * only its own node. */
@@ -1564,10 +1831,27 @@ struct Launch {
         k_pts_store<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, c0, c1, v_in, v_out);
         return cudaGetLastError();
     }
+    static cudaError_t aem_init(const DevState &s, double tt0, cudaStream_t st)
+    {
+        k_aem_init<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, tt0);
+        return cudaGetLastError();
+    }
+    static cudaError_t aem_day(const DevState &s, int day, double tt, double next, cudaStream_t st)
+    {
+        k_aem_day<M><<<blocks_for(s.Ntot, 128), 128, 0, st>>>(s, day, tt, next);
+        return cudaGetLastError();
+    }
+    static cudaError_t aem_pts(const DevState &s, int day, double tt, int c0, int c1,
+                               const double *v_in, double *v_out, cudaStream_t st)
+    {
+        k_aem_pts<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, day, tt, c0, c1, v_in, v_out);
+        return cudaGetLastError();
+    }
     static const Launchers *table()
     {
         static const Launchers t = {M::NC, M::NT, M::ND, M::NGD, M::PTS_LOCAL,
-                                    init, horizon, quick, ssa_e1, e2_wave, pts_store};
+                                    init, horizon, quick, ssa_e1, e2_wave, pts_store,
+                                    aem_init, aem_day, aem_pts};
         return &t;
     }
 };

@@ -23,6 +23,11 @@ struct Launchers {
                            cudaStream_t st);
     cudaError_t (*pts_store)(const DevState &s, int day, double tt, int c0, int c1,
                              const double *v_in, double *v_out, cudaStream_t st);
+    /* the all-events method's initialisation, day and day end */
+    cudaError_t (*aem_init)(const DevState &s, double tt0, cudaStream_t st);
+    cudaError_t (*aem_day)(const DevState &s, int day, double tt, double next, cudaStream_t st);
+    cudaError_t (*aem_pts)(const DevState &s, int day, double tt, int c0, int c1,
+                           const double *v_in, double *v_out, cudaStream_t st);
 };
 
 /* Particle-filter kernels (model independent). */

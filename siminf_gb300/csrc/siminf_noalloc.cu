@@ -206,6 +206,9 @@ extern "C" int siminf_gpu_run_solver_ssm_noalloc(siminf_gpu_solver_args *a,
     int rc = capi_validate(a, L);
     if (rc)
         return rc;
+    if (a->solver != 0)
+        return fail(SIMINF_GPU_ERR_UNKNOWN_SOLVER,
+                    "the allocation-free solver runs the ssm solver");
     if (a->Nrep != 1 || a->len > 0 || !a->U || !L->pts_local)
         return fail(SIMINF_GPU_ERR_INVALID_MODEL,
                     "the allocation-free solver runs one replicate without scheduled "

@@ -133,6 +133,13 @@ struct DevState {
     int two_pass;
     int *active;
 
+    /* All-events method (one replicate): per transition j of node g, in
+     * [j][Ntot] order, the next event time, the time left when its rate
+     * fell to zero, and the draw index of its own stream. */
+    int aem;
+    double *react_time, *react_inf;
+    uint64_t *react_ctr;
+
     /* Batches of independent models (siminf_gpu_run_batch); job_of is NULL
      * for a single model.  Node g belongs to job j = job_of[g], whose nodes
      * start at job_node0[j]: its stream key is (job_seed[j], g -

@@ -79,12 +79,12 @@ def _ks_nodes(m, seed_ours, seed_ref):
     hr = abi.build_args(m, seed_ref, solver=1)
     assert oracle.run_ref(hr, m.name, 8, independent=True) == 0
     tlen = len(m.tspan)
-    U_o = ho.U.reshape((m.Nn, m.Nc, tlen), order="F")
-    U_r = hr.U.reshape((m.Nn, m.Nc, tlen), order="F")
+    U_o = ho.U.reshape((m.Nc, m.Nn, tlen), order="F")     # [compartment, node, column]
+    U_r = hr.U.reshape((m.Nc, m.Nn, tlen), order="F")
     tests = []
     for c in range(m.Nc):
         for k in range(tlen):
-            a, b = U_o[:, c, k], U_r[:, c, k]
+            a, b = U_o[c, :, k], U_r[c, :, k]
             if a.min() == a.max() == b.min() == b.max():
                 continue
             tests.append(stats.ks_2samp(a, b).pvalue)
