@@ -435,6 +435,9 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     reductions = reduce_bench(plan, peak) if rank == 0 else None
     event_sort = events_bench(m, peak) if rank == 0 and world == 1 else None
+    aem = (aem_bench(m, node_days, torch, C, stream, os.cpu_count() or 1,
+                     0.0 if args.no_cpu else args.cpu_scale)
+           if rank == 0 and world == 1 else None)
 
     # batched form: R replicates of the same workload in one device-resident
     # plan (the mssm layout), so one replicate's latency-bound tail overlaps
@@ -547,6 +550,7 @@ def run_ours(args):
             "autotune": autotune,
             "reductions": reductions,
             "event_sort": event_sort,
+            "aem": aem,
             "batched": batched,
             "sir_plain": sir,
             "abc": abc,
@@ -647,6 +651,42 @@ def events_bench(m, peak, frac=0.1, seed=3):
                              "sample": "the same %d shuffled events" % n},
             "data": "first tenth of the headline schedule, shuffled; the sort kernels "
                     "(ms_kernel) and the call with every column's copies (ms_total)"}
+
+
+def aem_bench(m, node_days, torch, C, stream, threads, cpu_scale, seed=42):
+    """The all-events method (solver = 1, src/solvers/SimInf_solver_aem.c)
+    on the same workload, resident, with the oracle's aem on the host cores
+    over the CPU baseline's sample beside it."""
+    from siminf_gb300 import abi, native, workloads
+    h = abi.build_args(m, seed, solver=1)
+    p = native.Plan(h, m.name, cap_transfers=True)
+    p.run(C.c_void_p(stream.cuda_stream))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    p.run(C.c_void_p(stream.cuda_stream))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = p.stats()
+    p.close()
+    out = {"value": node_days / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+           "transitions_per_s": st.transitions / (ms / 1e3),
+           "data": "the headline workload under the aem solver, inputs resident"}
+    if cpu_scale > 0:
+        from oracle import oracle
+        oracle.build()
+        ms_ = workloads.seir_events(nodes=max(1, int(1_000_000 * cpu_scale)), days=365,
+                                    transfers=max(1, int(500_000 * cpu_scale)))
+        hc = abi.build_args(ms_, seed, solver=1)
+        t0 = time.perf_counter()
+        code, res = oracle.run(hc, ms_.name, threads, cap_transfers=True)
+        dt = time.perf_counter() - t0
+        if code == 0:
+            out["cpu_baseline"] = {"value": res.node_days / dt, "unit": UNIT, "cores": threads,
+                                   "kind": "port", "sample": "aem at %.3g scale, %.1f s"
+                                   % (cpu_scale, dt)}
+    return out
 
 
 def tune_summary(tune):
