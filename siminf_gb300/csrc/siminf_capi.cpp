@@ -960,6 +960,8 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
      * nodes: below that the day's longest chain, not its many quiet
      * nodes, sets its length) */
     s.aem = a->solver == 1;
+    if (s.aem && !(opt && opt->heavy_rate > 0) && !getenv("SIMINF_HEAVY_RATE"))
+        s.heavy_rate = 0.0;             /* aem: the heavy part is off unless asked for */
     if (s.aem) {
         if (!rc) rc = dalloc(&s.react_time, (size_t) Ntot * Nt, own);
         if (!rc) rc = dalloc(&s.react_inf, (size_t) Ntot * Nt, own);
@@ -1189,7 +1191,7 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
         return timed(kp, 4, st, [&] { return L->horizon(s, p->d_days, ndays, st); });
     for (int d = 0; d < ndays && e == cudaSuccess; d++) {
         const DayInfo &di = p->days[d];
-        if (s.two_pass)
+        if (s.two_pass && !s.aem)
             e = timed(kp, 5, st, [&] { return L->quick(s, d, di.tt, di.next, st); });
         if (e == cudaSuccess)
             e = timed(kp, 1, st, [&] {
@@ -1307,7 +1309,7 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
         e = cudaStreamWaitEvent(st, copied[c], 0);
         for (int d = d0; d < d1 && e == cudaSuccess; d++) {
             const DayInfo &di = p->days[d];
-            if (s.two_pass)
+            if (s.two_pass && !s.aem)
                 e = L->quick(s, d, di.tt, di.next, st);
             if (e == cudaSuccess)
                 e = s.aem ? L->aem_day(s, d, di.tt, di.next, st)
@@ -1534,18 +1536,18 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
     int best = -1, rc = plan_run_impl(p, st, nullptr);     /* warm-up */
     for (int k = 0; k < SIMINF_GPU_TUNE_CANDIDATES && !rc; k++) {
         p->s.heavy_rate = cand[k % 4];
-        p->s.two_pass = k / 4;
+        p->s.two_pass = p->s.aem ? 0 : k / 4;       /* two-pass days are the direct method's */
         plan_changed(p);
         rc = plan_run_impl(p, st, nullptr);
         r.heavy_rate[k] = cand[k % 4];
-        r.two_pass[k] = k / 4;
+        r.two_pass[k] = p->s.two_pass;
         r.ms[k] = p->stats.ms_solve;
         if (!rc && (best < 0 || r.ms[k] < r.ms[best]))
             best = k;
     }
     p->max_days = 0;
     p->s.heavy_rate = (best >= 0) ? cand[best % 4] : saved;
-    p->s.two_pass = (best >= 0) ? best / 4 : saved_tp;
+    p->s.two_pass = (best >= 0 && !p->s.aem) ? best / 4 : saved_tp;
     plan_changed(p);
     r.chosen = best;
     r.probe_days = std::min(probe_days > 0 ? probe_days : 16, p->ndays);

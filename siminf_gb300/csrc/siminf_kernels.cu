@@ -1310,18 +1310,31 @@ __device__ __forceinline__ void aem_calc_times(double &time, double &inf, double
 
 /* Initial rates and event times (src/solvers/SimInf_solver_aem.c:113-158). */
 template <class M>
+__device__ __forceinline__ int aem_init_node(const DevState &s, long long g, double tt0);
+
+template <class M>
 __global__ void k_aem_init(DevState s, double tt0)
 {
-    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (g >= s.Ntot)
-        return;
+    int cls = -1;
+    if (g < s.Ntot)
+        cls = aem_init_node<M>(s, g, tt0);
+    push_heavy_warp(s, g, cls, 0);
+}
+
+/* k_aem_init for one node; returns its heavy class on day 0 (from the sum
+ * of its rates, for the order of the work queue only). */
+template <class M>
+__device__ __forceinline__ int aem_init_node(const DevState &s, long long g, double tt0)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     const int node = (int) (g % s.Nn);
     int u[NC];
     load_u<NC>(s.u + g * NC, u);
     const double *v = s.vA + g * ND;
     const double *ld = s.ldata + (size_t) node * s.Nld;
     si_recip dc = si_recip_none();
+    double sum = 0.0;
 #pragma unroll
     for (int j = 0; j < NT; j++) {
         const double rate = M::rate(j, u, v, ld, gdata_of(s, g), tt0, dc);
@@ -1336,10 +1349,12 @@ __global__ void k_aem_init(DevState s, double tt0)
         s.react_time[k] = t;
         s.react_inf[k] = 0.0;
         s.react_ctr[k] = c;
+        sum += rate;
     }
     s.t_time[g] = tt0;
     s.ctr[g] = 0;
     s.update[g] = 0;
+    return heavy_class<M>(s, sum);
 }
 
 /* The state of one node's aem day, held by one thread. */
@@ -1371,84 +1386,65 @@ __device__ __forceinline__ void aem_refresh(const DevState &s, AemNode<M> &a, lo
     aem_calc_times(a.time[j], a.inf[j], tc, old, nr, s.seed, g, M::NT, j, a.ctr[j]);
 }
 
-/* One day of every node (src/solvers/SimInf_solver_aem.c:179-307), then
- * the node's E1 events. */
+/* One aem step of a node at its day (src/solvers/SimInf_solver_aem.c:
+ * 179-307): the transition with the smallest event time fires, then its
+ * dependents in G's column (row order) and itself get new rates and event
+ * times.  Returns true when the next event falls past the day's end. */
 template <class M>
-__global__ void __launch_bounds__(128) k_aem_day(DevState s, int day, double tt, double next)
+__device__ __forceinline__ bool aem_step(const DevState &s, AemNode<M> &a, long long g,
+                                         double next, const double *v, const double *ld,
+                                         const double *gd, const int *sS, const uint32_t *sG,
+                                         unsigned &fired, si_recip &dc)
 {
-    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
-    __shared__ int sS[NT * NC];
-    __shared__ uint32_t sG[NT];
-    load_model_smem<M>(s, sS, sG);
-    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (g >= s.Ntot || load_flag(s.err_day) < day)
-        return;
-    const int node = (int) (g % s.Nn);
-    AemNode<M> a;
-    load_u<NC>(s.u + g * NC, a.u);
+    constexpr int NC = M::NC, NT = M::NT;
+    int tr = 0;
+    double t = a.time[0];
 #pragma unroll
-    for (int j = 0; j < NT; j++) {
-        const size_t k = (size_t) j * s.Ntot + g;
-        a.rate[j] = s.t_rate[k];
-        a.time[j] = s.react_time[k];
-        a.inf[j] = s.react_inf[k];
-        a.ctr[j] = s.react_ctr[k];
+    for (int j = 1; j < NT; j++)
+        if (a.time[j] < t) {
+            t = a.time[j];
+            tr = j;
+        }
+    if (isinf(t) || t >= next)
+        return true;
+    if (++fired > MAX_NODE_DAY_TRANSITIONS) {
+        a.err = ERR_TIMEOUT;
+        a.err_tr = tr;
+        a.err_t = t;
+        return true;
     }
-    a.err = 0;
-    a.err_tr = -1;
-    a.err_t = 0.0;
-    a.err_rate = 0.0;
-    const double *v = s.vA + g * ND;
-    const double *ld = s.ldata + (size_t) node * s.Nld;
-    const double *gd = gdata_of(s, g);
-    si_recip dc = si_recip_none();
-    unsigned fired = 0;
-    double t = next;
-    for (;;) {
-        int tr = 0;
-        double tmin = a.time[0];
+    int neg = 0;
 #pragma unroll
-        for (int j = 1; j < NT; j++)
-            if (a.time[j] < tmin) {
-                tmin = a.time[j];
-                tr = j;
-            }
-        if (isinf(tmin) || tmin >= next)
-            break;
-        t = tmin;
-        if (++fired > MAX_NODE_DAY_TRANSITIONS) {
-            a.err = ERR_TIMEOUT;
-            a.err_tr = tr;
-            a.err_t = t;
-            break;
-        }
-        int neg = 0;
-#pragma unroll
-        for (int c = 0; c < NC; c++) {
-            const int d = sS[tr * NC + c];
-            a.u[c] += d;
-            neg |= (d != 0) & (a.u[c] < 0);
-        }
-        if (neg) {
-            a.err = ERR_NEGATIVE_STATE;
-            a.err_tr = tr;
-            a.err_t = t;
-            a.err_rate = 0.0;
-        }
-        /* the dependents in G's column (row order), then the transition
-         * that fired */
-        const uint32_t gm = sG[tr];
-#pragma unroll
-        for (int j = 0; j < NT; j++)
-            if (j != tr && (gm & (1u << j)))
-                aem_refresh<M>(s, a, g, j, v, ld, gd, t, t, dc);
-#pragma unroll
-        for (int j = 0; j < NT; j++)
-            if (j == tr)
-                aem_refresh<M>(s, a, g, j, v, ld, gd, t, t, dc);
+    for (int c = 0; c < NC; c++) {
+        const int d = sS[tr * NC + c];
+        a.u[c] += d;
+        neg |= (d != 0) & (a.u[c] < 0);
     }
-    if (fired)
-        atomicAdd(s.fired, (unsigned long long) fired);  /* per thread: lanes may have left */
+    if (neg) {
+        a.err = ERR_NEGATIVE_STATE;
+        a.err_tr = tr;
+        a.err_t = t;
+        a.err_rate = 0.0;
+    }
+    const uint32_t gm = sG[tr];
+#pragma unroll
+    for (int j = 0; j < NT; j++)
+        if (j != tr && (gm & (1u << j)))
+            aem_refresh<M>(s, a, g, j, v, ld, gd, t, t, dc);
+#pragma unroll
+    for (int j = 0; j < NT; j++)
+        if (j == tr)
+            aem_refresh<M>(s, a, g, j, v, ld, gd, t, t, dc);
+    return false;
+}
+
+/* The end of a node's aem day: its error, or its E1 events; the state
+ * written back with t = next. */
+template <class M>
+__device__ __forceinline__ void aem_finish(const DevState &s, AemNode<M> &a, long long g, int day,
+                                           double tt, double next)
+{
+    constexpr int NC = M::NC, NT = M::NT;
     si_rng r;
     {
         uint64_t seed, sid;
@@ -1459,7 +1455,7 @@ __global__ void __launch_bounds__(128) k_aem_day(DevState s, int day, double tt,
         record_error(s, a.err, PHASE_SSA, day, g, a.err_tr, -1, a.err_t, a.err_rate);
     } else {
         int e_code = 0, e_idx = -1;
-        if (node_e1<NC>(s, a.u, node, day, r, g, tt, e_code, e_idx))
+        if (node_e1<NC>(s, a.u, (int) (g % s.Nn), day, r, g, tt, e_code, e_idx))
             s.update[g] = 1;
         if (e_code)
             record_error(s, e_code, PHASE_E1, day, g, -1, e_idx, tt, 0);
@@ -1477,18 +1473,152 @@ __global__ void __launch_bounds__(128) k_aem_day(DevState s, int day, double tt,
     s.ctr[g] = r.ctr;
 }
 
+/* One day of every node under the all-events method, then its E1 events:
+ * a persistent grid fed by the day's work queue, as k_ssa_e1 -- first the
+ * heavy nodes (rate sum >= heavy_rate at the start of the day, listed by
+ * the previous day's end, heaviest class first), 32 to a warp that runs
+ * them to the day's end in a tight loop, then every other node in index
+ * order, lane by lane, a lane whose node's day is over taking the next
+ * node at once.  One atomic per warp hands out the entries. */
+template <class M>
+__global__ void __launch_bounds__(SSA_BLOCK, 4) k_aem_day(DevState s, int day, double tt,
+                                                          double next)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
+    __shared__ int sS[NT * NC];
+    __shared__ uint32_t sG[NT];
+    load_model_smem<M>(s, sS, sG);
+    const int par = day & 1, npar = (day + 1) & 1;
+    if (blockIdx.x == 0 && threadIdx.x < HEAVY_CLASSES)
+        s.heavy_count[npar * HEAVY_CLASSES + threadIdx.x] = 0;  /* filled by this day's end */
+    if (blockIdx.x == 0 && threadIdx.x < 2)
+        s.queue_next[npar * 2 + threadIdx.x] = 0;
+    unsigned long long fired = 0;
+    if (load_flag(s.err_day) < day) {
+        add_fired(s, fired);
+        return;
+    }
+    int n[HEAVY_CLASSES];
+    unsigned long long H = 0;
+#pragma unroll
+    for (int c = 0; c < HEAVY_CLASSES; c++) {
+        n[c] = min(s.heavy_count[par * HEAVY_CLASSES + c], (int) MAX_HEAVY);
+        H += (unsigned long long) n[c];
+    }
+    const unsigned long long Ntot = (unsigned long long) s.Ntot;
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xFFFFFFFFu;
+    AemNode<M> a;
+    long long g = -1;
+    bool alive = true, need = true, heavy = false;
+    bool heavy_left = H > 0;            /* warp-uniform: the heavy part may have entries */
+    unsigned nfired = 0;
+    const double *v = nullptr, *ld = nullptr, *gd = nullptr;
+    si_recip dc = si_recip_none();
+    for (;;) {
+        const unsigned want = __ballot_sync(FULL, alive && need);
+        const bool holds_heavy = __any_sync(FULL, alive && !need && heavy);
+        const bool from_heavy = heavy_left;
+        if (want && !holds_heavy) {
+            const int leader = __ffs(want) - 1;
+            unsigned long long base = 0;
+            if (lane == leader)
+                base = atomicAdd(&s.queue_next[par * 2 + (from_heavy ? 0 : 1)],
+                                 (unsigned long long) __popc(want));
+            base = __shfl_sync(FULL, base, leader);
+            long long cand = -1;
+            bool empty = false;
+            if (alive && need) {
+                const unsigned long long pos = base + __popc(want & ((1u << lane) - 1u));
+                if (from_heavy) {
+                    if (pos < H) {
+                        int idx = (int) pos, c = 0;
+                        while (c < HEAVY_CLASSES - 1 && idx >= n[c]) {
+                            idx -= n[c];
+                            c++;
+                        }
+                        cand = s.heavy_list[(par * HEAVY_CLASSES + c) * MAX_HEAVY + idx];
+                    } else {
+                        empty = true;
+                    }
+                } else if (pos >= Ntot) {
+                    alive = false;
+                } else if (s.heavy_mark[pos] != day + 1) {
+                    cand = (long long) pos;     /* heavy ones come from the heavy part */
+                }
+            }
+            if (from_heavy && __any_sync(FULL, empty))
+                heavy_left = false;
+            if (cand >= 0) {
+                g = cand;
+                heavy = from_heavy;
+                const int node = (int) (g % s.Nn);
+                load_u<NC>(s.u + g * NC, a.u);
+#pragma unroll
+                for (int j = 0; j < NT; j++) {
+                    const size_t k = (size_t) j * s.Ntot + g;
+                    a.rate[j] = s.t_rate[k];
+                    a.time[j] = s.react_time[k];
+                    a.inf[j] = s.react_inf[k];
+                    a.ctr[j] = s.react_ctr[k];
+                }
+                a.err = 0;
+                a.err_tr = -1;
+                a.err_t = 0.0;
+                a.err_rate = 0.0;
+                v = s.vA + g * ND;
+                ld = s.ldata + (size_t) node * s.Nld;
+                gd = gdata_of(s, g);
+                dc = si_recip_none();
+                nfired = 0;
+                need = false;
+            }
+        }
+        if (!__any_sync(FULL, alive))
+            break;
+        if (alive && !need) {
+            /* one event; a heavy warp has nothing else to do and runs its
+             * nodes' whole days in this loop */
+            bool done;
+            do
+                done = aem_step<M>(s, a, g, next, v, ld, gd, sS, sG, nfired, dc);
+            while (heavy && !done);
+            if (done) {
+                aem_finish<M>(s, a, g, day, tt, next);
+                fired += nfired;
+                need = true;
+                heavy = false;
+            }
+        }
+    }
+    add_fired(s, fired);
+}
+
 /* The day's end (src/solvers/SimInf_solver_aem.c:329-381): post-time-step
  * function, U/V columns, and for a node an event touched or whose v
  * changed, every rate recomputed with v_new at tt and its event time
  * rescaled at the node's time (the end of the day). */
 template <class M>
+__device__ __forceinline__ int aem_pts_node(const DevState &s, long long g, int day, double tt,
+                                            int c0, int c1, const double *v_in, double *v_out);
+
+template <class M>
 __global__ void __launch_bounds__(256) k_aem_pts(DevState s, int day, double tt, int c0, int c1,
                                                  const double *v_in, double *v_out)
 {
-    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (g >= s.Ntot || load_flag(s.err_day) < day)
-        return;
+    int cls = -1;
+    if (g < s.Ntot && load_flag(s.err_day) >= day)
+        cls = aem_pts_node<M>(s, g, day, tt, c0, c1, v_in, v_out);
+    push_heavy_warp(s, g, cls, day + 1);
+}
+
+/* k_aem_pts for one node; returns its heavy class on the next day. */
+template <class M>
+__device__ __forceinline__ int aem_pts_node(const DevState &s, long long g, int day, double tt,
+                                            int c0, int c1, const double *v_in, double *v_out)
+{
+    constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     const int rep = (int) (g / s.Nn), node = (int) (g % s.Nn);
     AemNode<M> a;
     load_u<NC>(s.u + g * NC, a.u);
@@ -1500,10 +1630,15 @@ __global__ void __launch_bounds__(256) k_aem_pts(DevState s, int day, double tt,
     store_columns<NC, ND>(s, rep, node, a.u, vo, c0, c1);
     if (rc < 0) {
         record_error(s, rc, PHASE_PTS, day, g, -1, -1, tt, 0);
-        return;
+        return -1;
     }
-    if (rc == 0 && !s.update[g])
-        return;
+    double sum = 0.0;
+    if (rc == 0 && !s.update[g]) {
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+            sum += s.t_rate[(size_t) j * s.Ntot + g];
+        return heavy_class<M>(s, sum);
+    }
     const double tc = s.t_time[g];
 #pragma unroll
     for (int j = 0; j < NT; j++) {
@@ -1530,8 +1665,10 @@ __global__ void __launch_bounds__(256) k_aem_pts(DevState s, int day, double tt,
         s.react_time[k] = a.time[j];
         s.react_inf[k] = a.inf[j];
         s.react_ctr[k] = a.ctr[j];
+        sum += a.rate[j];
     }
     s.update[g] = 0;
+    return heavy_class<M>(s, sum);
 }
 
 /* Whole horizon of one (replicate, node) in one thread: valid when no
@@ -1836,9 +1973,23 @@ struct Launch {
         k_aem_init<M><<<blocks_for(s.Ntot, 256), 256, 0, st>>>(s, tt0);
         return cudaGetLastError();
     }
+    static int aem_resident_blocks()
+    {
+        static int blocks = 0;
+        if (!blocks) {
+            int dev = 0, nsm = 1, per = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_aem_day<M>, SSA_BLOCK, 0);
+            blocks = nsm * (per > 0 ? per : 1);
+        }
+        return blocks;
+    }
     static cudaError_t aem_day(const DevState &s, int day, double tt, double next, cudaStream_t st)
     {
-        k_aem_day<M><<<blocks_for(s.Ntot, 128), 128, 0, st>>>(s, day, tt, next);
+        const long long need = (long long) blocks_for(s.Ntot, SSA_BLOCK);
+        const int grid = (int) (need < aem_resident_blocks() ? need : aem_resident_blocks());
+        k_aem_day<M><<<grid, SSA_BLOCK, 0, st>>>(s, day, tt, next);
         return cudaGetLastError();
     }
     static cudaError_t aem_pts(const DevState &s, int day, double tt, int c0, int c1,

@@ -37,13 +37,18 @@ def test_oracle_aem_conserves_population(oracle_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("heavy_rate", [0, 1, -1])
 @pytest.mark.parametrize("label,m", ONE_REPLICATE, ids=[c[0] for c in ONE_REPLICATE])
-def test_gpu_aem_matches_oracle(gpu, label, m):
+def test_gpu_aem_matches_oracle(gpu, label, m, heavy_rate):
+    """heavy_rate 1: every node with a rate sum >= 1 goes to the heavy
+    warps first; -1: no heavy part; 0: the default threshold."""
     from siminf_gb300 import native
     code_o, ho, res = run_oracle_aem(m)
     h = abi.build_args(m, 42, solver=1)
-    code = native.lib().siminf_gpu_run_solver_ssm(C.cast(h.ref(), C.c_void_p),
-                                                  native.device_model(m.name).handle)
+    opt = abi.Options(heavy_rate=heavy_rate)
+    code = native.lib().siminf_gpu_run_solver_ex(C.cast(h.ref(), C.c_void_p),
+                                                 native.device_model(m.name).handle,
+                                                 C.byref(opt))
     assert code == code_o == 0, label
     assert np.array_equal(h.U, ho.U), label
     if m.Nd:
