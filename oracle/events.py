@@ -1,5 +1,5 @@
 """CPU restatement of SimInf_events' ordering (test infrastructure only:
-the checker of siminf_gpu_sort_events).
+the oracle for siminf_gpu_sort_events).
 
 R/SimInf_events.R:396 orders the table by (time, event, select) with R's
 `order`, which leaves ties in their original order; numpy's lexsort is

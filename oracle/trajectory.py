@@ -1,5 +1,5 @@
 """CPU restatement of the trajectory consumers, in numpy (test
-infrastructure only: the checker of siminf_gpu_trajectory_u/_v and
+infrastructure only: the oracle for siminf_gpu_trajectory_u/_v and
 siminf_gpu_prevalence; only the test suite imports it).
 
 U (and V) are flat arrays in the solver's column-major layout: column col

@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(SORT_BLOCK) k_radix_scatter(const K *key, cons
                                                               uint32_t *pos_out)
 {
     __shared__ uint32_t before[RADIX];                    /* keys of earlier rounds */
-    __shared__ uint32_t wcnt[SORT_BLOCK / 32][RADIX];     /* this round, per warp */
+    __shared__ uint32_t wcnt[SORT_BLOCK / 32][RADIX];     /* the current 256 keys, per warp */
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     before[threadIdx.x] = 0;
     const long long base = blockIdx.x * (long long) SORT_TILE;
