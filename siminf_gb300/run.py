@@ -36,12 +36,20 @@ class Result:
         return cols[compartment::m.Nc, :]
 
 
-def run(model, seed=42, U_sparse=None, V_sparse=None, cap_transfers=False):
+SOLVERS = {"ssm": 0, "aem": 1}
+
+
+def run(model, seed=42, U_sparse=None, V_sparse=None, cap_transfers=False, solver="ssm"):
     """Simulate ``model`` on the GPU.  ``U_sparse``/``V_sparse`` are optional
     (ir, jc) CSC patterns over (Nn*Nc) x (Nrep*tlen) selecting which entries
     to record, as a punchcard does (R/punchcard.R:139-253).
-    ``cap_transfers`` enables the siminf_gpu_options extension of that name."""
-    holder = abi.build_args(model, seed, U_sparse=U_sparse, V_sparse=V_sparse)
+    ``cap_transfers`` enables the siminf_gpu_options extension of that name.
+    ``solver`` is "ssm" (the direct method) or "aem" (the all-events method,
+    one replicate), as in R's run(model, solver) (R/run.R:128-145)."""
+    if solver not in SOLVERS:
+        raise ValueError("Invalid 'solver' value.")
+    holder = abi.build_args(model, seed, U_sparse=U_sparse, V_sparse=V_sparse,
+                            solver=SOLVERS[solver])
     dm = native.device_model(model.name)
     if cap_transfers:
         opt = abi.Options(cap_transfers=1)

@@ -61,9 +61,10 @@ class Server:
         native.check(native.lib().siminf_gpu_server_submit(self.handle, C.byref(t.req)))
         return t
 
-    def run(self, model, seed=42, cap_transfers=False):
-        """A simulation run (siminf_gpu_run_solver_ex)."""
-        holder = abi.build_args(model, seed)
+    def run(self, model, seed=42, cap_transfers=False, solver="ssm"):
+        """A simulation run (siminf_gpu_run_solver_ex); solver "ssm" or "aem"."""
+        from .run import SOLVERS
+        holder = abi.build_args(model, seed, solver=SOLVERS[solver])
         t = Ticket(abi.REQUEST_RUN, model, holder)
         t.req.args = C.cast(holder.ref(), C.c_void_p)
         t.req.model = native.device_model(model.name).handle

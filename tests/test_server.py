@@ -105,3 +105,23 @@ def test_server_plan_continuation(gpu):
     assert np.array_equal(ref.U, want)
     srv.close()
     p.close()
+
+
+@pytest.mark.gpu
+def test_server_aem_requests_equal_alone(gpu):
+    """aem runs served beside ssm runs give what they give alone."""
+    from siminf_gb300.run import run
+    from siminf_gb300.serve import Server
+    cases = dict(parity_cases())
+    ms = [cases["seir_events_300x120"], cases["sise_200x199"], cases["sis_shift_weighted"]]
+    alone = [run(m, seed=21, solver="aem") for m in ms]
+    srv = Server(slots=3)
+    tickets = [srv.run(m, seed=21, solver="aem") for m in ms]
+    tickets += [srv.run(m, seed=21) for m in ms]
+    for t in tickets:
+        assert srv.wait(t)
+    for t, a in zip(tickets[:3], alone):
+        assert np.array_equal(t.U, a.U)
+    for t, m in zip(tickets[3:], ms):
+        assert np.array_equal(t.U, run(m, seed=21).U)
+    srv.close()
