@@ -1286,26 +1286,48 @@ __device__ __forceinline__ double aem_neglog(uint64_t seed, long long g, int Nt,
     return x;
 }
 
-/* calcTimes (src/solvers/SimInf_solver_aem.c:52-75). */
+/* calcTimes (src/solvers/SimInf_solver_aem.c:52-75), with its three
+ * quotients -- a new waiting time -log(u) / new_rate, a sleeping time
+ * inf / new_rate, a rescaling old_rate / new_rate -- formed by one division
+ * (one copy of the division's code in the kernel).  Addition commutes
+ * exactly, so tt + q and q + tt are the same double. */
 __device__ __forceinline__ void aem_calc_times(double &time, double &inf, double tt,
                                                double old_rate, double new_rate, uint64_t seed,
                                                long long g, int Nt, int j, uint64_t &ctr)
 {
     const double oldtime = time;
+    int kind;                           /* 0: q + tt, 1: q * (oldtime - tt) + tt, 2: none */
+    bool draw = false;
+    double num = 0.0;
     if (isinf(oldtime)) {
-        if (inf == 0.0)
-            time = si_div(aem_neglog(seed, g, Nt, j, ctr), new_rate) + tt;
-        else if (new_rate > 0.0)
-            time = tt + si_div(inf, new_rate);
+        if (inf == 0.0) {
+            draw = true;
+            kind = 0;
+        } else if (new_rate > 0.0) {
+            num = inf;
+            kind = 0;
+        } else {
+            kind = 2;
+        }
     } else if (new_rate >= DBL_MIN) {
-        if (oldtime == tt)
-            time = si_div(aem_neglog(seed, g, Nt, j, ctr), new_rate) + tt;
-        else
-            time = (si_div(old_rate, new_rate) * (oldtime - tt)) + tt;
+        if (oldtime == tt) {
+            draw = true;
+            kind = 0;
+        } else {
+            num = old_rate;
+            kind = 1;
+        }
     } else {
         inf = (oldtime - tt) * old_rate;
         time = si_bits_double(0x7FF0000000000000ULL);
+        return;
     }
+    if (kind == 2)
+        return;
+    if (draw)
+        num = aem_neglog(seed, g, Nt, j, ctr);
+    const double q = si_div(num, new_rate);
+    time = kind == 0 ? q + tt : (q * (oldtime - tt)) + tt;
 }
 
 /* Initial rates and event times (src/solvers/SimInf_solver_aem.c:113-158). */
