@@ -396,9 +396,10 @@ def run_ours(args):
     st = plan.stats()
     node_days = nodes * st.days
     # the library's autotuner picks the work queue's layout (heavy
-    # threshold, one- or two-pass days) on the first 120 days (results do
-    # not depend on it)
-    tune = plan.tune(probe_days=120, stream=C.c_void_p(stream.cuda_stream))
+    # threshold, one- or two-pass days) on the whole horizon: the epidemic
+    # peaks after the first months, where the heavy part matters (results
+    # do not depend on the layout)
+    tune = plan.tune(probe_days=args.days, stream=C.c_void_p(stream.cuda_stream))
     autotune = tune_summary(tune)
 
     def barrier():
@@ -426,12 +427,11 @@ def run_ours(args):
     ms_step = ms / args.steps
     value = node_days * world / (ms_step / 1e3)
     transitions_per_s = st.transitions * world / (ms_step / 1e3)
-    launches = 1 + (1 if st.e2_waves == 0 else
-                    (3 if autotune["chosen_two_pass"] else 2) * st.days + st.e2_waves)
-
     # dominant kernel: per-kernel device time from the library's own
-    # per-launch events (one step), see roofline below
+    # per-launch events (one step), see roofline below; its launch counts
+    # are the launches of one step
     prof = plan_kernel_profile(plan, C, stream)
+    launches = sum(k["launches"] for k in (prof["kernels"] or {}).values())
     peak, peak_kind = measured_peaks()
     reductions = reduce_bench(plan, peak) if rank == 0 else None
     event_sort = events_bench(m, peak) if rank == 0 and world == 1 else None
@@ -447,7 +447,7 @@ def run_ours(args):
         mb = m.replicate(args.batch)
         hb = abi.build_args(mb, seed)
         pb = native.Plan(hb, mb.name, cap_transfers=True)
-        tune_b = tune_summary(pb.tune(probe_days=60, stream=C.c_void_p(stream.cuda_stream)))
+        tune_b = tune_summary(pb.tune(probe_days=120, stream=C.c_void_p(stream.cuda_stream)))
         pb.run(C.c_void_p(stream.cuda_stream))
         barrier()
         b0 = torch.cuda.Event(enable_timing=True)
@@ -711,7 +711,7 @@ def plan_kernel_profile(plan, C, stream):
     lib.siminf_gpu_plan_profile.restype = C.c_int
     native.check(lib.siminf_gpu_plan_profile(plan.handle, C.c_void_p(stream.cuda_stream),
                                              prof, cnt))
-    names = ["k_init", "k_ssa_e1", "k_e2_wave", "k_pts_store", "k_horizon", "k_quick"]
+    names = ["k_init", "k_ssa_e1", "k_e2_wave+k_e2_tail", "k_pts_store", "k_horizon", "k_quick"]
     kernels = {n: {"ms": prof[i], "launches": int(cnt[i])} for i, n in enumerate(names)
                if cnt[i] > 0}
     total = sum(k["ms"] for k in kernels.values()) or 1.0
@@ -723,7 +723,7 @@ def plan_kernel_profile(plan, C, stream):
         st = plan.stats()
         nodes = plan.holder.args.Nn * plan.holder.args.Nrep
         launches = kernels[top_name]["launches"]
-        per_launch_nd = nodes * st.days / launches if top_name != "k_e2_wave" else 0
+        per_launch_nd = nodes * st.days / launches if top_name != "k_e2_wave+k_e2_tail" else 0
         top = {"name": top_name, "ms_per_launch": kernels[top_name]["ms"] / launches,
                "node_days_per_launch": per_launch_nd}
     return {"top": top, "kernels": kernels}

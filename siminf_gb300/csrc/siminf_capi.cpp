@@ -1178,6 +1178,35 @@ static cudaError_t download_columns(const siminf_gpu_plan *p, const siminf_gpu_s
     return e;
 }
 
+/* The wavefronts of one day: offsets into d_e2 and event counts.  The
+ * last ones, while each holds at most E2_TAIL_ITEMS events x replicates,
+ * run together in one block (k_e2_tail), up to E2_TAIL_WAVES per launch;
+ * the others, one launch each. */
+static cudaError_t launch_day_waves(const siminf_gpu_plan *p, const DevState &s,
+                                    const long long *off, const long long *cnt, int nw, int d,
+                                    double tt, cudaStream_t st, KernelProfile *kp)
+{
+    const Launchers *L = p->L;
+    int t = nw;
+    while (t > 0 && cnt[t - 1] * (long long) s.Nrep <= E2_TAIL_ITEMS)
+        t--;
+    if (nw - t < 2)
+        t = nw;                         /* a single small wave: its own launch */
+    cudaError_t e = cudaSuccess;
+    for (int w = 0; w < t && e == cudaSuccess; w++)
+        e = timed(kp, 2, st, [&] { return L->e2_wave(s, p->d_e2 + off[w], (int) cnt[w], d, tt, st); });
+    for (int w = t; w < nw && e == cudaSuccess; w += E2_TAIL_WAVES) {
+        E2Tail tail;
+        tail.n = std::min((int) E2_TAIL_WAVES, nw - w);
+        for (int k = 0; k < tail.n; k++) {
+            tail.off[k] = off[w + k];
+            tail.count[k] = (int) cnt[w + k];
+        }
+        e = timed(kp, 2, st, [&] { return L->e2_tail(s, p->d_e2, tail, d, tt, st); });
+    }
+    return e;
+}
+
 static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, KernelProfile *kp)
 {
     const Launchers *L = p->L;
@@ -1198,10 +1227,12 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
                 return s.aem ? L->aem_day(s, d, di.tt, di.next, st)
                              : L->ssa_e1(s, d, di.tt, di.next, st);
             });
-        for (int w = p->day_wave[d]; w < p->day_wave[d + 1] && e == cudaSuccess; w++) {
-            const long long off = p->wave_ptr[w];
-            const int cnt = (int) (p->wave_ptr[w + 1] - off);
-            e = timed(kp, 2, st, [&] { return L->e2_wave(s, p->d_e2 + off, cnt, d, di.tt, st); });
+        if (e == cudaSuccess) {
+            const int w0 = p->day_wave[d], nw = p->day_wave[d + 1] - w0;
+            std::vector<long long> cnt((size_t) nw);
+            for (int w = 0; w < nw; w++)
+                cnt[w] = p->wave_ptr[w0 + w + 1] - p->wave_ptr[w0 + w];
+            e = launch_day_waves(p, s, p->wave_ptr.data() + w0, cnt.data(), nw, d, di.tt, st, kp);
         }
         if (e == cudaSuccess)
             e = timed(kp, 3, st, [&] {
@@ -1314,11 +1345,16 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             if (e == cudaSuccess)
                 e = s.aem ? L->aem_day(s, d, di.tt, di.next, st)
                           : L->ssa_e1(s, d, di.tt, di.next, st);
-            long long off = p->e2_day_off[d];
-            for (size_t w = 0; w < p->day_waves[d].size() && e == cudaSuccess; w++) {
-                const long long cnt = p->day_waves[d][w];
-                e = L->e2_wave(s, p->d_e2 + off, (int) cnt, d, di.tt, st);
-                off += cnt;
+            if (e == cudaSuccess) {
+                const std::vector<long long> &cnt = p->day_waves[d];
+                std::vector<long long> off(cnt.size());
+                long long o = p->e2_day_off[d];
+                for (size_t w = 0; w < cnt.size(); w++) {
+                    off[w] = o;
+                    o += cnt[w];
+                }
+                e = launch_day_waves(p, s, off.data(), cnt.data(), (int) cnt.size(), d, di.tt,
+                                     st, nullptr);
             }
             if (e == cudaSuccess)
                 e = s.aem ? L->aem_pts(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st)

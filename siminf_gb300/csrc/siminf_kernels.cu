@@ -1086,18 +1086,15 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
     add_fired(s, fired);
 }
 
+/* One external transfer of one replicate (src/solvers/SimInf_solver.c:
+ * 824-902): sample from the source, add to the destination (atomics: adds
+ * into one destination commute within a wavefront), subtract from the
+ * source (exclusive to this event within its wavefront). */
 template <class M>
-__global__ void __launch_bounds__(256) k_e2_wave(DevState s, const E2Rec *ev, int count, int day,
-                                                 double tt)
+__device__ __forceinline__ void e2_apply(const DevState &s, const E2Rec &e, int rep, int day,
+                                         double tt)
 {
     constexpr int NC = M::NC;
-    const long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (i >= (long long) count * s.Nrep)
-        return;
-    if (load_flag(s.err_day) < day || load_flag(s.err_day_pre_e2) <= day)
-        return;
-    const int rep = (int) (i / count);
-    const E2Rec e = ev[i - (long long) rep * count];
     const long long gs = (long long) rep * s.Nn + e.src;
     const long long gd = (long long) rep * s.Nn + e.dst;
     int uu[NC], ind[NC];
@@ -1148,6 +1145,41 @@ __global__ void __launch_bounds__(256) k_e2_wave(DevState s, const E2Rec *ev, in
     }
     s.update[gd] = 1;
     s.update[gs] = 1;
+}
+
+template <class M>
+__global__ void __launch_bounds__(256) k_e2_wave(DevState s, const E2Rec *ev, int count, int day,
+                                                 double tt)
+{
+    const long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (i >= (long long) count * s.Nrep)
+        return;
+    if (load_flag(s.err_day) < day || load_flag(s.err_day_pre_e2) <= day)
+        return;
+    const int rep = (int) (i / count);
+    e2_apply<M>(s, ev[i - (long long) rep * count], rep, day, tt);
+}
+
+/* A day's last, small wavefronts in one block, in order, a barrier between
+ * two (the block's writes before it are visible to the block after it):
+ * one launch instead of one per wavefront.  Each holds at most
+ * E2_TAIL_ITEMS = 1024 events x replicates, one per thread. */
+template <class M>
+__global__ void __launch_bounds__(1024) k_e2_tail(DevState s, const E2Rec *ev, E2Tail tail,
+                                                  int day, double tt)
+{
+    if (load_flag(s.err_day) < day || load_flag(s.err_day_pre_e2) <= day)
+        return;                                     /* the same for every thread */
+    for (int w = 0; w < tail.n; w++) {
+        const int count = tail.count[w];
+        const E2Rec *wev = ev + tail.off[w];
+        const long long items = (long long) count * s.Nrep;
+        for (long long i = threadIdx.x; i < items; i += blockDim.x) {
+            const int rep = (int) (i / count);
+            e2_apply<M>(s, wev[i - (long long) rep * count], rep, day, tt);
+        }
+        __syncthreads();
+    }
 }
 
 /* Batches: node g's share of its job's prevalence sums at columns c0 ..
@@ -1975,6 +2007,12 @@ struct Launch {
         k_ssa_e1<M><<<grid, SSA_BLOCK, 0, st>>>(s, day, tt, next);
         return cudaGetLastError();
     }
+    static cudaError_t e2_tail(const DevState &s, const E2Rec *ev, const E2Tail &tail, int day,
+                               double tt, cudaStream_t st)
+    {
+        k_e2_tail<M><<<1, 1024, 0, st>>>(s, ev, tail, day, tt);
+        return cudaGetLastError();
+    }
     static cudaError_t e2_wave(const DevState &s, const E2Rec *ev, int count, int day, double tt,
                                cudaStream_t st)
     {
@@ -2024,7 +2062,7 @@ struct Launch {
     {
         static const Launchers t = {M::NC, M::NT, M::ND, M::NGD, M::PTS_LOCAL,
                                     init, horizon, quick, ssa_e1, e2_wave, pts_store,
-                                    aem_init, aem_day, aem_pts};
+                                    aem_init, aem_day, aem_pts, e2_tail};
         return &t;
     }
 };

@@ -28,6 +28,9 @@ struct Launchers {
     cudaError_t (*aem_day)(const DevState &s, int day, double tt, double next, cudaStream_t st);
     cudaError_t (*aem_pts)(const DevState &s, int day, double tt, int c0, int c1,
                            const double *v_in, double *v_out, cudaStream_t st);
+    /* a day's last, small wavefronts in one launch */
+    cudaError_t (*e2_tail)(const DevState &s, const E2Rec *ev, const E2Tail &tail, int day,
+                           double tt, cudaStream_t st);
 };
 
 /* Particle-filter kernels (model independent). */

@@ -57,6 +57,16 @@ struct E2Rec {          /* 32 bytes */
     double proportion;
 };
 
+/* A day's last, small wavefronts, run by one block (k_e2_tail): wave w
+ * holds count[w] events from off[w] of the wave list (at most
+ * E2_TAIL_WAVES waves of at most E2_TAIL_ITEMS events x replicates). */
+enum { E2_TAIL_WAVES = 32, E2_TAIL_ITEMS = 1024 };
+struct E2Tail {
+    int n;
+    int count[E2_TAIL_WAVES];
+    long long off[E2_TAIL_WAVES];
+};
+
 struct ErrRec {
     int code;
     int phase;
