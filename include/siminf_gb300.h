@@ -201,7 +201,7 @@ typedef struct siminf_gpu_options {
     int cap_transfers;
     int heavy_rate;     /* rate sum from which a node is queued first (0 = default 8, < 0 = off) */
     int gdata_per_replicate;
-    int two_pass;       /* > 0 on, < 0 off, 0 = on from 4,000,000 nodes (all replicates) */
+    int two_pass;       /* > 0 on, < 0 off, 0 = on from 500,000 nodes (all replicates) */
     int reserved[4];
 } siminf_gpu_options;
 

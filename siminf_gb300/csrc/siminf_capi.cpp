@@ -956,9 +956,6 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
         s.heavy_rate = opt->heavy_rate;
     else if (opt && opt->heavy_rate < 0)
         s.heavy_rate = 0.0;
-    /* two-pass days (options, else SIMINF_TWO_PASS, else from 4,000,000
-     * nodes: below that the day's longest chain, not its many quiet
-     * nodes, sets its length) */
     s.aem = a->solver == 1;
     if (s.aem && !(opt && opt->heavy_rate > 0) && !getenv("SIMINF_HEAVY_RATE"))
         s.heavy_rate = 0.0;             /* aem: the heavy part is off unless asked for */
@@ -967,7 +964,10 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
         if (!rc) rc = dalloc(&s.react_inf, (size_t) Ntot * Nt, own);
         if (!rc) rc = dalloc(&s.react_ctr, (size_t) Ntot * Nt, own);
     }
-    s.two_pass = Ntot >= 4000000;
+    /* two-pass days (options, else SIMINF_TWO_PASS, else from 500,000
+     * nodes: below that a day is short and the extra launch costs more
+     * than the quiet nodes it takes out of the work queue) */
+    s.two_pass = Ntot >= 500000;
     if (const char *ev = getenv("SIMINF_TWO_PASS"))
         s.two_pass = atoi(ev) > 0;
     if (opt && opt->two_pass)
