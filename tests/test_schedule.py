@@ -96,3 +96,28 @@ def test_schedule_headline_scale_properties():
     days, waves, e1, e2, wave = native.schedule(h)
     assert days == 365 and e2 == 365 * 10_000
     assert (wave[m.events["event"] == 3] >= 0).all()
+
+
+def test_schedule_self_transfers_and_deep_days():
+    """Transfers from a node to itself, chains that revisit few nodes (a
+    deep day), and both mixed with ordinary transfers: the levels follow
+    the serial rule."""
+    from siminf_gb300 import model as M
+    rng = np.random.default_rng(17)
+    Nn, days = 12, 6
+    ev = {k: [] for k in M.EVENT_FIELDS}
+    for t in range(1, days + 1):
+        for _ in range(300):
+            s_ = int(rng.integers(1, Nn + 1))
+            d_ = s_ if rng.random() < 0.2 else int(rng.integers(1, Nn + 1))
+            for key, val in zip(M.EVENT_FIELDS, (3, t, s_, d_, 1, 0.0, 2, 0)):
+                ev[key].append(val)
+    u0 = {"S": np.full(Nn, 500), "E": 0, "I": 0, "R": 0}
+    m = M.SEIR(u0, np.arange(1, days + 1), 0.0, 0.0, 0.0,
+               events=M.make_events(**{k: np.array(v) for k, v in ev.items()}))
+    h = abi.build_args(m, 1)
+    _, waves, _, e2, wave = native.schedule(h)
+    ref = reference_levels(m)
+    assert e2 == days * 300
+    assert np.array_equal(wave, ref)
+    assert waves > days * 50            # deep days: many wavefronts each
