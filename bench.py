@@ -432,6 +432,18 @@ def run_ours(args):
     # are the launches of one step
     prof = plan_kernel_profile(plan, C, stream)
     launches = sum(k["launches"] for k in (prof["kernels"] or {}).values())
+    # the run's critical path: every day lasts at least as long as its
+    # busiest node's chain of transitions (one recording run)
+    critical = None
+    if prof["kernels"] and "k_ssa_e1" in prof["kernels"]:
+        dmax = plan.day_max(C.c_void_p(stream.cuda_stream))
+        ssa_ms = prof["kernels"]["k_ssa_e1"]["ms"]
+        critical = {"transitions": int(dmax.sum()), "k_ssa_e1_ms": ssa_ms,
+                    "us_per_critical_transition": ssa_ms * 1e3 / max(1, int(dmax.sum())),
+                    "note": "sum over days of the most transitions one node fired that "
+                            "day; k_ssa_e1 time / that sum is the time per step of the "
+                            "busiest chain, which GB300's FP64 latency (64 cycles per "
+                            "dependent operation) bounds from below"}
     peak, peak_kind = measured_peaks()
     reductions = reduce_bench(plan, peak) if rank == 0 else None
     event_sort = events_bench(m, peak) if rank == 0 and world == 1 else None
@@ -548,6 +560,7 @@ def run_ours(args):
                                  % ALGO_BYTES_PER_NODE_DAY},
             "kernels": prof["kernels"],
             "autotune": autotune,
+            "critical_path": critical,
             "reductions": reductions,
             "event_sort": event_sort,
             "aem": aem,

@@ -370,6 +370,14 @@ int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *args,
                               siminf_gpu_plan **out);
 int siminf_gpu_plan_run(siminf_gpu_plan *plan, void *cuda_stream);
 int siminf_gpu_plan_download(siminf_gpu_plan *plan, siminf_gpu_solver_args *args);
+/* plan_run once recording, per day, the most transitions any node fired
+ * that day (day_max: one entry per day of the plan; the days' sum is the
+ * run's critical path: every day lasts at least as long as its busiest
+ * node's chain of transitions).  Recorded by the direct method's work
+ * queue; plans without external transfers and aem plans report zeros.
+ * For profiling. */
+int siminf_gpu_plan_day_max(siminf_gpu_plan *plan, void *cuda_stream, unsigned *day_max);
+
 /* plan_run with a CUDA event pair around every launch: device milliseconds
  * and launch counts per kernel kind, [0] initialisation, [1] SSA + E1,
  * [2] E2 wavefront, [3] post time step + store, [4] whole-horizon kernel,

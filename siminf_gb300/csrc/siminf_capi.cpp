@@ -1592,6 +1592,34 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
     return rc;
 }
 
+int siminf_gpu_plan_day_max(siminf_gpu_plan *p, void *cuda_stream, unsigned *day_max)
+{
+    if (!p || !day_max || p->e2_pending)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    const cudaStream_t st = (cudaStream_t) cuda_stream;
+    unsigned *d = nullptr;
+    cudaError_t e = cudaMalloc((void **) &d, (size_t) p->ndays * sizeof(unsigned));
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(d, 0, (size_t) p->ndays * sizeof(unsigned), st);
+    if (e != cudaSuccess) {
+        if (d)
+            cudaFree(d);
+        return cuda_fail(e, "day_max buffer");
+    }
+    p->s.day_max = d;
+    plan_changed(p);                    /* launch by launch, not from a graph */
+    int rc = plan_run_impl(p, st, nullptr);
+    p->s.day_max = nullptr;
+    plan_changed(p);
+    if (!rc) {
+        e = cudaMemcpy(day_max, d, (size_t) p->ndays * sizeof(unsigned), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "day_max copy");
+    }
+    cudaFree(d);
+    return rc;
+}
+
 int siminf_gpu_plan_profile(siminf_gpu_plan *p, void *cuda_stream, double ms[8],
                             long long launches[8])
 {

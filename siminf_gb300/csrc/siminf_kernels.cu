@@ -855,6 +855,8 @@ __device__ __forceinline__ void node_finish(const DevState &s, SsaLane<M> &ln, s
     r.ctr = ln.c;
     r.have = 0;
     fired += ln.fired;
+    if (s.day_max && ln.fired > *(volatile unsigned *) (s.day_max + day))
+        atomicMax(s.day_max + day, ln.fired);       /* profiling: the day's busiest node */
     if (ln.err) {
         record_error(s, ln.err, PHASE_SSA, day, g, ln.err_tr, -1, ln.err_t, ln.err_rate);
     } else {

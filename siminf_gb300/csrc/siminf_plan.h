@@ -143,6 +143,10 @@ struct DevState {
     int two_pass;
     int *active;
 
+    /* Profiling: per day, the most transitions any node fired that day
+     * (nullptr: not recorded). */
+    unsigned *day_max;
+
     /* All-events method (one replicate): per transition j of node g, in
      * [j][Ntot] order, the next event time, the time left when its rate
      * fell to zero, and the draw index of its own stream. */

@@ -6,6 +6,8 @@ visible, every entry point fails loudly.
 import ctypes as C
 import os
 
+import numpy as np
+
 from . import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -92,6 +94,8 @@ def lib():
                                          C.POINTER(C.c_double), pi, pi, vp,
                                          C.POINTER(abi.ReduceStats)]
     L.siminf_gpu_sort_events.restype = C.c_int
+    L.siminf_gpu_plan_day_max.argtypes = [vp, vp, C.POINTER(C.c_uint)]
+    L.siminf_gpu_plan_day_max.restype = C.c_int
     _lib = L
     return L
 
@@ -108,6 +112,7 @@ EXPORTS = (
     "siminf_gpu_server_load", "siminf_gpu_server_free", "siminf_gpu_plan_tune",
     "siminf_gpu_release_cached", "siminf_gpu_trajectory_u", "siminf_gpu_trajectory_v",
     "siminf_gpu_prevalence", "siminf_gpu_plan_outputs", "siminf_gpu_sort_events",
+    "siminf_gpu_plan_day_max",
 )
 
 
@@ -199,6 +204,14 @@ class Plan:
         r = abi.TuneResult()
         check(lib().siminf_gpu_plan_tune(self.handle, stream, int(probe_days), C.byref(r)))
         return r
+
+    def day_max(self, stream=None):
+        """Per day, the most transitions any node fired (one recording run,
+        siminf_gpu_plan_day_max)."""
+        out = np.zeros(self.stats().days, dtype=np.uint32)
+        check(lib().siminf_gpu_plan_day_max(self.handle, stream,
+                                            out.ctypes.data_as(C.POINTER(C.c_uint))))
+        return out
 
     def stats(self):
         st = abi.Stats()

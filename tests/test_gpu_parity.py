@@ -335,3 +335,24 @@ def test_gpu_two_pass_and_reductions_at_scale(gpu, monkeypatch):
             assert np.array_equal(tr["E"], ref.trajectory(h.U, m.Nn, m.Nc, ncol, [2])[0])
         p.close()
     assert np.array_equal(out[0], out[1])
+
+
+def test_gpu_day_max_matches_oracle(gpu, oracle_lib):
+    """The per-day busiest node's transition count (the run's critical
+    path), recorded on the GPU, equals the oracle's count of the same run."""
+    from oracle import oracle
+    from siminf_gb300 import abi, native
+    m = dict(parity_cases())["seir_events_300x120"]
+    h = abi.build_args(m, 42)
+    p = native.Plan(h, m.name)
+    got = p.day_max()
+    p.close()
+    want = np.zeros(len(got), dtype=np.uint64)
+    oracle.lib().oracle_set_day_max(want.ctypes.data)
+    try:
+        code, _ = oracle.run(abi.build_args(m, 42), m.name, 2)
+    finally:
+        oracle.lib().oracle_set_day_max(None)
+    assert code == 0
+    assert np.array_equal(got.astype(np.uint64), want)
+    assert want.sum() > 0
