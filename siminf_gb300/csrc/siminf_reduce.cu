@@ -119,7 +119,7 @@ struct PrevArgs {
     int level;
     const int2 *cond;
     int ncond;
-    unsigned long long *acc;    /* [ncol][2] for levels 1 and 2 */
+    unsigned long long *acc;    /* levels 1 and 2: [block][2] partial sums */
     double *out;                /* level 3: [ncol][n_id] */
 };
 
@@ -177,20 +177,31 @@ __global__ void __launch_bounds__(REDUCE_BLOCK) k_prevalence(PrevArgs a)
         }
     }
     if (a.level != 3) {
+        /* the block's partial sums, summed per column by k_prevalence_final
+         * in block order */
         tnum = block_sum(tnum, sh);
         tden = block_sum(tden, sh);
         if (threadIdx.x == 0) {
-            atomicAdd(&a.acc[2 * col], (unsigned long long) tnum);
-            atomicAdd(&a.acc[2 * col + 1], (unsigned long long) tden);
+            a.acc[2 * blockIdx.x] = (unsigned long long) tnum;
+            a.acc[2 * blockIdx.x + 1] = (unsigned long long) tden;
         }
     }
 }
 
-__global__ void k_prevalence_final(const unsigned long long *acc, long long ncol, double *out)
+/* Per column, the sums of its blocks' partial sums (chunks blocks per
+ * column, column-major in the grid), then the quotient. */
+__global__ void k_prevalence_final(const unsigned long long *acc, long long ncol,
+                                   long long chunks, double *out)
 {
     const long long col = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (col < ncol)
-        out[col] = (double) (long long) acc[2 * col] / (double) (long long) acc[2 * col + 1];
+    if (col >= ncol)
+        return;
+    unsigned long long num = 0, den = 0;
+    for (long long c = 0; c < chunks; c++) {
+        num += acc[2 * (col * chunks + c)];
+        den += acc[2 * (col * chunks + c) + 1];
+    }
+    out[col] = (double) (long long) num / (double) (long long) den;
 }
 
 /* One block: NODES_PER_BLOCK nodes of one column; T is int (U) or double
@@ -434,11 +445,8 @@ int siminf_gpu_prevalence(const int *d_U, int Nn, int Nc, int ncol,
                                 (size_t) spec->n_condition * sizeof(int2),
                                 cudaMemcpyHostToDevice, st);
     }
-    if (e == cudaSuccess && spec->level != 3) {
-        e = cudaMallocAsync((void **) &d_acc, (size_t) 2 * ncol * sizeof(unsigned long long), st);
-        if (e == cudaSuccess)
-            e = cudaMemsetAsync(d_acc, 0, (size_t) 2 * ncol * sizeof(unsigned long long), st);
-    }
+    if (e == cudaSuccess && spec->level != 3)
+        e = cudaMallocAsync((void **) &d_acc, (size_t) 2 * blocks * sizeof(unsigned long long), st);
     if (e == cudaSuccess)
         e = cudaEventCreate(&e0);
     if (e == cudaSuccess)
@@ -465,7 +473,8 @@ int siminf_gpu_prevalence(const int *d_U, int Nn, int Nc, int ncol,
             k_prevalence<0><<<(unsigned) blocks, REDUCE_BLOCK, 0, st>>>(a);
         e = cudaGetLastError();
         if (e == cudaSuccess && spec->level != 3) {
-            k_prevalence_final<<<(unsigned) ((ncol + 255) / 256), 256, 0, st>>>(d_acc, ncol, d_out);
+            k_prevalence_final<<<(unsigned) ((ncol + 255) / 256), 256, 0, st>>>(
+                d_acc, ncol, (nid + NODES_PER_BLOCK - 1) / NODES_PER_BLOCK, d_out);
             e = cudaGetLastError();
         }
         cudaEventRecord(e1, st);
