@@ -374,6 +374,26 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def replica_seed(rank):
+    """Each rank simulates its own replica of the workload with its own
+    seed: the path has no exchange between replicates."""
+    return 42 + rank
+
+
+def max_over_ranks(x, torch, world, device):
+    """The largest of every rank's x: a job's time is its slowest rank's."""
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, ms):
+    """Whole-job throughput: the units of every rank over the slowest
+    rank's time (ms)."""
+    return units_per_rank * world / (ms / 1e3)
+
+
 def run_ours(args):
     import ctypes as C
     import torch
@@ -386,7 +406,7 @@ def run_ours(args):
     build.build()
     nodes = max(1, int(1_000_000 * args.scale))
     transfers = max(1, int(500_000 * args.scale))
-    seed = 42 + rank
+    seed = replica_seed(rank)
     t_gen = time.perf_counter()
     m = workloads.seir_events(nodes=nodes, days=args.days, transfers=transfers)
     t_gen = time.perf_counter() - t_gen
@@ -420,13 +440,10 @@ def run_ours(args):
         barrier()
     ms = ev0.elapsed_time(ev1)
     st = plan.stats()
-    t_max = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_max, op=torch.distributed.ReduceOp.MAX)
-    ms = float(t_max.item())
+    ms = max_over_ranks(ms, torch, world, "cuda")
     ms_step = ms / args.steps
-    value = node_days * world / (ms_step / 1e3)
-    transitions_per_s = st.transitions * world / (ms_step / 1e3)
+    value = job_rate(node_days, world, ms_step)
+    transitions_per_s = job_rate(st.transitions, world, ms_step)
     # dominant kernel: per-kernel device time from the library's own
     # per-launch events (one step), see roofline below; its launch counts
     # are the launches of one step
@@ -504,11 +521,11 @@ def run_ours(args):
             native.check(lib.siminf_gpu_run_solver_ex(C.cast(pin.ref(), C.c_void_p), dm.handle,
                                                       C.byref(opt)))
         barrier()
-        dt = (time.perf_counter() - t0) / args.steps
+        dt = max_over_ranks((time.perf_counter() - t0) / args.steps, torch, world, "cuda")
         h2d = (m.u0.nbytes + sum(v.nbytes for v in m.events.values()) +
                m.ldata.nbytes)
         d2h = pin.U.nbytes
-        e2e = {"value": node_days * world / dt, "unit": UNIT,
+        e2e = {"value": job_rate(node_days, world, dt * 1e3), "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": dt * 1e3}
         estats = native.last_stats()
