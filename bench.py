@@ -12,6 +12,10 @@ one batch with on-device distances, against one run per proposal),
 `pfilter` (the 4,096-particle SISe particle filter) and `serve` (an
 open-loop request trace through the serving loop, p50/p99 latency, against
 serving the same trace one request at a time).
+The secondary legs time the "next" paths on their own inputs:
+`reductions` (prevalence and trajectory of the resident U), `event_sort`
+(the schedule's ordering), `individual_events` (the individual-event
+cleaner on a synthetic livestock register), `aem` (the all-events solver).
 
 A step is one full run of the workload's horizon.  `value` times K steps of
 siminf_gpu_plan_run with every input already resident in HBM (CUDA events on
@@ -464,6 +468,8 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     reductions = reduce_bench(plan, peak) if rank == 0 else None
     event_sort = events_bench(m, peak) if rank == 0 and world == 1 else None
+    individual = (individual_bench(peak, os.cpu_count() or 1, cpu=not args.no_cpu)
+                  if rank == 0 and world == 1 else None)
     aem = (aem_bench(m, node_days, torch, C, stream, os.cpu_count() or 1,
                      0.0 if args.no_cpu else args.cpu_scale)
            if rank == 0 and world == 1 else None)
@@ -580,6 +586,7 @@ def run_ours(args):
             "critical_path": critical,
             "reductions": reductions,
             "event_sort": event_sort,
+            "individual_events": individual,
             "aem": aem,
             "batched": batched,
             "sir_plain": sir,
@@ -681,6 +688,45 @@ def events_bench(m, peak, frac=0.1, seed=3):
                              "sample": "the same %d shuffled events" % n},
             "data": "first tenth of the headline schedule, shuffled; the sort kernels "
                     "(ms_kernel) and the call with every column's copies (ms_total)"}
+
+
+def individual_bench(peak, threads, cpu=True, n_ind=2_500_000, n_nodes=200_000, seed=7):
+    """The individual-event cleaner (SimInf_individual_events,
+    src/misc/SimInf_individual_events.c) on a synthetic livestock register
+    of n_ind animals (about 9.2e6 events, 185 MB of int32 columns, above the
+    L2) through siminf_gpu_individual_events; against the oracle's
+    restatement on all host cores (OpenMP over individuals, as the
+    reference's one task per individual)."""
+    from siminf_gb300.individual import longest_paths
+    from siminf_gb300.workloads import livestock_register
+    cols = livestock_register(n_ind, n_nodes, seed)
+    n = len(cols[0])
+    keep = longest_paths(*cols)
+    best = None
+    for _ in range(3):
+        _, st = longest_paths(*cols, stats=True)
+        if best is None or st.ms_kernel < best.ms_kernel:
+            best = st
+    moved = best.bytes_read + best.bytes_written
+    gbs = moved / (best.ms_kernel / 1e3) / 1e9
+    out = {"events": n, "individuals": n_ind, "kept": int(keep.sum()),
+           "events_per_s": n / (best.ms_kernel / 1e3),
+           "events_per_s_e2e": n / (best.ms_total / 1e3),
+           "ms_kernel": best.ms_kernel, "ms_total": best.ms_total, "bytes_moved": moved,
+           "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak, "bound": "hbm",
+           "data": "synthetic livestock register (%d animals, %d holdings, seed %d); "
+                   "the two kernels (ms_kernel) and the call with its copies of the five "
+                   "columns and keep (ms_total)" % (n_ind, n_nodes, seed)}
+    if cpu:
+        from oracle import oracle
+        oracle.build()
+        t0 = time.perf_counter()
+        want, _ = oracle.individual_events(*cols, threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"events_per_s": n / dt, "ms": dt * 1e3, "cores": threads,
+                               "kind": "port", "sample": "the same %d events" % n,
+                               "identical": bool(np.array_equal(want, keep))}
+    return out
 
 
 def aem_bench(m, node_days, torch, C, stream, threads, cpu_scale, seed=42):

@@ -555,6 +555,26 @@ int siminf_gpu_sort_events(long long len, int *event, int *time, int *node, int 
                            int *n, double *proportion, int *select, int *shift,
                            void *cuda_stream, siminf_gpu_reduce_stats *stats);
 
+/*
+ * SimInf_individual_events (src/misc/SimInf_individual_events.c:167-249):
+ * the cleaning of individual-based event data.  The len events of the host
+ * columns are sorted by (id, time, event, node, dest) with exact duplicates
+ * removed (R/SimInf_individual_events.R:397-410 does both before its C
+ * call); event is 0 (exit), 1 (enter) or 3 (external transfer) and dest is
+ * NA (INT_MIN) for the first two.  keep[i] becomes 1 for the events on each
+ * individual's longest consistent path and 0 for the rest, with the
+ * reference's search order and tie rule.  Runs on the device: one thread
+ * per individual over its slice of the columns.
+ * Returns 0, SIMINF_GPU_UNDEFINED_EVENT for an event type other than
+ * 0, 1 or 3 (message "'event[i]' is invalid." with the reference's
+ * one-based i; siminf_gpu_status.event_index holds it zero-based; keep is
+ * then all 0), SIMINF_GPU_ERR_INVALID_MODEL for a negative len, len above
+ * INT_MAX or a NULL column, or SIMINF_GPU_ERR_CUDA.
+ */
+int siminf_gpu_individual_events(long long len, const int *id, const int *event,
+                                 const int *time, const int *node, const int *dest,
+                                 int *keep, void *cuda_stream, siminf_gpu_reduce_stats *stats);
+
 /* The device U/V of a plan that has run (d_V NULL without V), and ncol. */
 int siminf_gpu_plan_outputs(const siminf_gpu_plan *plan, const int **d_U,
                             const double **d_V, int *ncol);

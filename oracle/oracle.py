@@ -179,3 +179,41 @@ def pfilter(model, n_particles, obs_time, obs, obs_compartment, detect_p, seed=4
                                 ess.ctypes.data_as(C.POINTER(C.c_double)),
                                 anc.ctypes.data_as(C.POINTER(C.c_int)))
     return code, float(ll[0]), ess, anc
+
+
+def _cols(id, event, time, node, dest):
+    return [np.ascontiguousarray(x, dtype=np.int32) for x in (id, event, time, node, dest)]
+
+
+def individual_events(id, event, time, node, dest, threads=1):
+    """The restated cleaning of individual events (oracle_individual.c) on
+    sorted, de-duplicated columns (dest NA = INT_MIN).  Returns (keep, bad):
+    keep an int32 0/1 array, bad the zero-based index of the first invalid
+    event type or -1."""
+    cols = _cols(id, event, time, node, dest)
+    n = len(cols[0])
+    keep = np.zeros(n, dtype=np.int32)
+    bad = C.c_longlong(-1)
+    f = lib().oracle_individual_events
+    f.restype = C.c_int
+    f.argtypes = [C.c_longlong] + [C.c_void_p] * 6 + [C.c_int, C.POINTER(C.c_longlong)]
+    code = f(n, *[c.ctypes.data for c in cols], keep.ctypes.data, int(threads), C.byref(bad))
+    if code not in (0, -1):
+        raise MemoryError("oracle_individual_events")
+    return keep, bad.value
+
+
+def ref_individual_events(id, event, time, node, dest, threads=1):
+    """SimInf_individual_events compiled unmodified (oracle/_ref); returns
+    (keep, message): message is the reference's error text, or None."""
+    cols = _cols(id, event, time, node, dest)
+    n = len(cols[0])
+    keep = np.zeros(n, dtype=np.int32)
+    msg = C.create_string_buffer(256)
+    f = ref_lib().ref_individual_events
+    f.restype = C.c_int
+    f.argtypes = [C.c_longlong] + [C.c_void_p] * 6 + [C.c_int, C.c_char_p, C.c_int]
+    code = f(n, *[c.ctypes.data for c in cols], keep.ctypes.data, int(threads), msg, 256)
+    if code == -2:
+        raise MemoryError("ref_individual_events")
+    return keep, (msg.value.decode() if code == -1 else None)

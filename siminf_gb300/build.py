@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off"]
 SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp", "siminf_noalloc.cu", "siminf_batch.cu",
-           "siminf_server.cpp", "siminf_reduce.cu", "siminf_events.cu"]
+           "siminf_server.cpp", "siminf_reduce.cu", "siminf_events.cu", "siminf_individual.cu"]
 
 
 def nvcc():

@@ -96,6 +96,9 @@ def lib():
     L.siminf_gpu_sort_events.restype = C.c_int
     L.siminf_gpu_plan_day_max.argtypes = [vp, vp, C.POINTER(C.c_uint)]
     L.siminf_gpu_plan_day_max.restype = C.c_int
+    L.siminf_gpu_individual_events.argtypes = [C.c_longlong, pi, pi, pi, pi, pi, pi, vp,
+                                               C.POINTER(abi.ReduceStats)]
+    L.siminf_gpu_individual_events.restype = C.c_int
     _lib = L
     return L
 
@@ -112,7 +115,7 @@ EXPORTS = (
     "siminf_gpu_server_load", "siminf_gpu_server_free", "siminf_gpu_plan_tune",
     "siminf_gpu_release_cached", "siminf_gpu_trajectory_u", "siminf_gpu_trajectory_v",
     "siminf_gpu_prevalence", "siminf_gpu_plan_outputs", "siminf_gpu_sort_events",
-    "siminf_gpu_plan_day_max",
+    "siminf_gpu_plan_day_max", "siminf_gpu_individual_events",
 )
 
 

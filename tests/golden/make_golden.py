@@ -15,6 +15,9 @@ Fixtures written:
   sise3_transfer_one.json  tests/sample_select.R:604-645  one E2 transfer, dense U
   sise3_transfer_three.json tests/sample_select.R:651-671 three moved, select S_1..S_3
   sise_punchcard_rep.json  tests/punchcard.R:364-410 replicates + sparse U/V
+  individual_events.json   tests/individual_events.R:199-690,1222-1256 every
+                           case that compares individual_events() with an
+                           expected table (input and expected columns)
 """
 import json
 import os
@@ -60,6 +63,98 @@ def after(lines, start, pattern):
         if re.search(pattern, lines[k]):
             return "\n".join(lines[k:])
     raise ValueError("pattern %r not found after line %d" % (pattern, start))
+
+
+def r_args(text):
+    """Split the argument list of an R call (text from after its opening
+    parenthesis) at top-level commas; returns (args, end index)."""
+    args, depth, cur, quote, k = [], 0, "", None, 0
+    while k < len(text):
+        ch = text[k]
+        if quote:
+            cur += ch
+            if ch == quote:
+                quote = None
+        elif ch in "\"'":
+            quote = ch
+            cur += ch
+        elif ch == "(":
+            depth += 1
+            cur += ch
+        elif ch == ")":
+            if depth == 0:
+                args.append(cur.strip())
+                return [a for a in args if a], k
+            depth -= 1
+            cur += ch
+        elif ch == "," and depth == 0:
+            args.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+        k += 1
+    raise ValueError("unbalanced call")
+
+
+def r_value(expr):
+    """An R literal vector: c(...), a scalar, integer(0), as.Date(...).
+    Returns a list of ints, floats, strings and None (NA)."""
+    expr = expr.strip()
+    if expr.startswith("as.Date("):
+        inner, _ = r_args(expr[len("as.Date("):])
+        return [{"date": v} for v in r_value(inner[0])]
+    if expr == "integer(0)":
+        return []
+    if expr.startswith("c("):
+        items, _ = r_args(expr[2:])
+        return [x for it in items for x in r_value(it)]
+    if expr in ("NA", "NA_integer_", "NA_character_", "NA_real_"):
+        return [None]
+    if expr[0] in "\"'":
+        return [expr[1:-1]]
+    if expr.endswith("L"):
+        return [int(expr[:-1])]
+    v = float(expr)
+    return [int(v) if v == int(v) else v]
+
+
+def r_data_frame(text):
+    """Columns of data.frame(name = vector, ...) starting at text."""
+    i = text.index("data.frame(") + len("data.frame(")
+    args, _ = r_args(text[i:])
+    out = {}
+    for a in args:
+        name, expr = a.split("=", 1)
+        out[name.strip()] = r_value(expr)
+    return out
+
+
+def individual_event_cases(lines, first, last):
+    """(line, input, expected) for each check of individual_events()
+    against an expected table in lines [first, last]."""
+    cases, events, expected, called = [], None, None, False
+    k = first - 1
+    while k < last:
+        line = lines[k]
+        m = re.match(r"^(events|events_exp|events_expected) <- data.frame\(", line)
+        if m:
+            df = r_data_frame("\n".join(lines[k:k + 40]))
+            if m.group(1) == "events":
+                events, expected, called = (df, None, False)
+            else:
+                expected = df
+        elif "individual_events(events)" in line and "u0_from" not in line:
+            called = True
+        if events is not None and called and set(events) == {"id", "event", "time",
+                                                             "node", "dest"}:
+            if re.match(r"^stopifnot\(identical\((events_obs|events_observed), "
+                        r"(events_exp|events_expected)\)\)", line) and expected:
+                cases.append({"line": k + 1, "input": events, "expected": expected})
+            elif re.match(r"^stopifnot\(identical\((events_obs, events|events, "
+                          r"as.data.frame\(individual_events\(events\)\))\)\)", line):
+                cases.append({"line": k + 1, "input": events, "expected": events})
+        k += 1
+    return cases
 
 
 def main(ref):
@@ -152,6 +247,12 @@ def main(ref):
         "V_x_expected": r_vector(after(pc, 400, r"result@V_sparse@x - c\(").replace(
             "stopifnot(all(abs(result@V_sparse@x - ", "")),
         "tol": 1e-8,
+    }
+
+    ie = read("individual_events.R")
+    fixtures["individual_events.json"] = {
+        "source": "tests/individual_events.R:199-690,1222-1256",
+        "cases": individual_event_cases(ie, 199, 690) + individual_event_cases(ie, 1222, 1256),
     }
 
     for name, fx in fixtures.items():

@@ -1,0 +1,212 @@
+"""Cleaning of individual-based event data (SimInf_individual_events,
+src/misc/SimInf_individual_events.c; individual_events(),
+R/SimInf_individual_events.R:383-436).
+
+CPU: the oracle's restatement against the reference's own test cases
+(tests/individual_events.R, lifted into tests/golden/individual_events.json)
+and against the reference's C file compiled unmodified (oracle/_ref, where
+it was built), plus the host-side checks and their messages.  GPU: the
+device path, bit-exact against the oracle on the golden cases, on random
+tables with deep searches and on a table larger than L2, and its error for
+an invalid event type."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from siminf_gb300 import individual as I
+from siminf_gb300.workloads import livestock_register
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+NA = I.NA
+
+
+def golden_cases():
+    with open(os.path.join(HERE, "golden", "individual_events.json")) as f:
+        return json.load(f)["cases"]
+
+
+def normalise(col, values):
+    out = []
+    for v in (values.tolist() if hasattr(values, "tolist") else values):
+        if isinstance(v, dict):
+            v = v["date"]
+        elif col == "time" and not isinstance(v, (int, str)):
+            v = str(v)
+        out.append(v)
+    return out
+
+
+def compare(out, expected, time_dates):
+    for col in ("id", "event", "time", "node", "dest"):
+        got = out[col]
+        if col == "time" and time_dates:
+            got = [str(np.datetime64(v, "D")) for v in got]
+        assert normalise(col, got) == normalise(col, expected[col]), col
+
+
+def random_table(rng, n_ind, max_events, n_nodes, t_max):
+    """Sorted, de-duplicated int32 columns of random individuals: few nodes
+    and times make long, tied and inconsistent paths likely."""
+    m = rng.integers(1, max_events + 1, size=n_ind)
+    n = int(m.sum())
+    id_ = np.repeat(np.arange(1, n_ind + 1), m)
+    event = rng.choice(np.array([0, 1, 3]), size=n, p=[0.25, 0.25, 0.5])
+    time = rng.integers(0, t_max, size=n)
+    node = rng.integers(1, n_nodes + 1, size=n)
+    dest = np.where(event == 3, rng.integers(1, n_nodes + 1, size=n), NA)
+    dkey = np.where(dest == NA, np.int64(1) << 40, dest)
+    o = np.lexsort((dkey, node, event, time, id_))
+    cols = [np.asarray(c)[o] for c in (id_, event, time, node, dest)]
+    same = np.ones(n - 1, dtype=bool)
+    for c in cols:
+        same &= c[1:] == c[:-1]
+    first = np.concatenate(([True], ~same))
+    return [np.ascontiguousarray(c[first], dtype=np.int32) for c in cols]
+
+
+# ---------------------------------------------------------------- CPU ---
+
+def test_golden_cases_through_the_oracle():
+    cases = golden_cases()
+    assert len(cases) >= 20
+    for c in cases:
+        prep = I.prepare(c["input"])
+        keep, bad = oracle.individual_events(*prep.keys)
+        assert bad == -1
+        compare(I.finish(prep, keep), c["expected"], prep.time_dates)
+
+
+def test_oracle_matches_the_reference_c_file():
+    if not oracle.ref_available():
+        pytest.skip("reference build not available")
+    rng = np.random.default_rng(11)
+    total = 0
+    for trial in range(150):
+        cols = random_table(rng, int(rng.integers(1, 40)), int(rng.integers(1, 16)),
+                            int(rng.integers(1, 5)), int(rng.integers(1, 12)))
+        k1, bad = oracle.individual_events(*cols, threads=2)
+        k2, msg = oracle.ref_individual_events(*cols, threads=2)
+        assert bad == -1 and msg is None
+        assert np.array_equal(k1, k2), trial
+        total += len(k1)
+    assert total > 5000
+
+
+def test_oracle_invalid_event_matches_the_reference_message():
+    cols = random_table(np.random.default_rng(3), 4, 5, 3, 5)
+    cols[1][2] = 2
+    keep, bad = oracle.individual_events(*cols)
+    assert bad == 2 and not keep.any()
+    if oracle.ref_available():
+        _, msg = oracle.ref_individual_events(*cols)
+        assert msg == "'event[3]' is invalid."
+
+
+def test_oracle_empty_and_single():
+    z = [np.zeros(0, np.int32)] * 5
+    keep, bad = oracle.individual_events(*z)
+    assert len(keep) == 0 and bad == -1
+    one = [np.array([v], np.int32) for v in (1, 3, 1, 1, 2)]
+    assert oracle.individual_events(*one)[0].tolist() == [1]
+
+
+@pytest.mark.parametrize("events, message", [
+    ({"id": [1], "event": [1], "time": [1], "node": [1]}, "Missing columns in 'events'."),
+    ({"id": [1, None], "event": [1, 0], "time": [1, 2], "node": [1, 1], "dest": [0, 0]},
+     "'id' must be an integer or character vector with non-NA values."),
+    ({"id": [1.5], "event": [1], "time": [1], "node": [1], "dest": [0]},
+     "'id' must be an integer or character vector with non-NA values."),
+    ({"id": [1], "event": [2], "time": [1], "node": [1], "dest": [0]},
+     "'event' must be an integer or character vector with non-NA values."),
+    ({"id": [1], "event": ["intTrans"], "time": [1], "node": [1], "dest": [0]},
+     "'event' type must be 'enter', 'exit', or 'extTrans'."),
+    ({"id": [1], "event": [1], "time": [1.2], "node": [1], "dest": [0]},
+     "'time' must be an integer or character vector with non-NA values."),
+    ({"id": [1], "event": [3], "time": [1], "node": [1], "dest": [None]},
+     "'node' or 'dest' contain NA values."),
+    ({"id": [1], "event": [3], "time": [1], "node": [1.1], "dest": [2]},
+     "'node' and 'dest' must both be integer or character."),
+    ({"id": [1], "event": [3], "time": [1], "node": [1], "dest": ["2"]},
+     "'node' and 'dest' must both be integer or character."),
+])
+def test_host_checks_give_the_reference_messages(events, message):
+    with pytest.raises(ValueError) as e:
+        I.prepare(events)
+    assert str(e.value) == message
+
+
+def test_prepare_orders_and_removes_repeats():
+    ev = {"id": [2, 1, 1, 1], "event": [1, 3, 1, 3], "time": [5, 2, 1, 2],
+          "node": [4, 1, 1, 1], "dest": [9, 2, 7, 2]}
+    p = I.prepare(ev)
+    ids, events, times, nodes, dests = (k.tolist() for k in p.keys)
+    assert ids == [1, 1, 2] and events == [1, 3, 1] and times == [1, 2, 5]
+    assert dests == [NA, 2, NA]              # dest is NA except for transfers
+    assert p.rows.tolist() == [2, 1, 0]
+
+
+def test_livestock_generator_is_sorted_and_mostly_consistent():
+    cols = livestock_register(2000, 50, seed=1)
+    keep, bad = oracle.individual_events(*cols)
+    assert bad == -1
+    assert 0.8 < keep.mean() <= 1.0
+
+
+# ---------------------------------------------------------------- GPU ---
+
+@pytest.mark.gpu
+def test_gpu_golden_cases():
+    for c in golden_cases():
+        prep = I.prepare(c["input"])
+        out = I.individual_events(c["input"])
+        compare(out, c["expected"], prep.time_dates)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed, n_ind, max_events, n_nodes, t_max", [
+    (1, 40, 12, 3, 8),        # deep searches, many ties
+    (2, 2000, 6, 4, 20),
+    (3, 5, 28, 2, 30),        # long single histories
+    (4, 30000, 4, 40, 400),
+])
+def test_gpu_matches_oracle_random(seed, n_ind, max_events, n_nodes, t_max):
+    cols = random_table(np.random.default_rng(seed), n_ind, max_events, n_nodes, t_max)
+    want, _ = oracle.individual_events(*cols, threads=4)
+    got = I.longest_paths(*cols)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.gpu
+def test_gpu_matches_oracle_larger_than_l2():
+    # ~10^7 events: the five int32 columns hold ~200 MB, above the 129 MB L2
+    cols = livestock_register(2_500_000, 200_000, seed=7)
+    assert len(cols[0]) > 9_000_000
+    want, _ = oracle.individual_events(*cols, threads=os.cpu_count() or 1)
+    got, st = I.longest_paths(*cols, stats=True)
+    assert np.array_equal(got, want)
+    assert st.ms_kernel > 0 and st.bytes_read == 20 * len(cols[0])
+
+
+@pytest.mark.gpu
+def test_gpu_invalid_event_type_is_the_reference_error():
+    from siminf_gb300 import abi, native
+    cols = random_table(np.random.default_rng(5), 10, 5, 3, 5)
+    cols[1][3] = 2
+    cols[1][7] = 5
+    with pytest.raises(abi.SimInfError) as e:
+        I.longest_paths(*cols)
+    assert e.value.code == -3
+    assert "'event[4]' is invalid." in str(e.value)
+    assert native.last_status().event_index == 3
+
+
+@pytest.mark.gpu
+def test_gpu_empty_and_single():
+    z = [np.zeros(0, np.int32)] * 5
+    assert len(I.longest_paths(*z)) == 0
+    for ev, keep in ((1, 1), (0, 1), (3, 1)):
+        one = [np.array([v], np.int32) for v in (1, ev, 1, 1, 2 if ev == 3 else NA)]
+        assert I.longest_paths(*one).tolist() == [keep]
