@@ -33,6 +33,8 @@ def normalise(col, values):
     for v in (values.tolist() if hasattr(values, "tolist") else values):
         if isinstance(v, dict):
             v = v["date"]
+        elif col == "dest" and v == NA:
+            v = None                          # R's NA_integer_ in an int32 column
         elif col == "time" and not isinstance(v, (int, str)):
             v = str(v)
         out.append(v)
@@ -146,6 +148,64 @@ def test_prepare_orders_and_removes_repeats():
     assert ids == [1, 1, 2] and events == [1, 3, 1] and times == [1, 2, 5]
     assert dests == [NA, 2, NA]              # dest is NA except for transfers
     assert p.rows.tolist() == [2, 1, 0]
+
+
+def test_vectorised_and_elementwise_paths_agree():
+    rng = np.random.default_rng(21)
+    for trial in range(20):
+        cols = random_table(rng, int(rng.integers(1, 300)), 8, 5, 30)
+        n = len(cols[0])
+        pick = rng.permutation(np.concatenate((np.arange(n),
+                                               rng.integers(0, n, size=n // 3))))  # repeats
+        ev = dict(zip(("id", "event", "time", "node", "dest"), (c[pick] for c in cols)))
+        ev["time"] = ev["time"].astype(np.float64)            # numeric columns of mixed types
+        ev["dest"] = np.where(ev["event"] == 3, ev["dest"], np.nan)
+        a = I.prepare(ev)
+        b = I.prepare({k: [None if isinstance(x, float) and np.isnan(x) else x
+                           for x in v.tolist()] for k, v in ev.items()}, elementwise=True)
+        assert a.arrays and not b.arrays
+        assert np.array_equal(a.rows, b.rows)
+        for x, y in zip(a.keys, b.keys):
+            assert np.array_equal(x, y)
+        for x, y in zip(a.keys, cols):
+            assert np.array_equal(x, y)                       # sorted, repeats gone
+
+
+def test_order_is_rs_order():
+    rng = np.random.default_rng(4)
+    for trial in range(30):
+        n = int(rng.integers(1, 4000))
+        keys = [rng.integers(-5, 5, n), rng.integers(-2 ** 40, 2 ** 40, n),
+                rng.integers(0, 3, n), rng.integers(0, 2 ** 31, n), rng.integers(0, 2, n)]
+        keys = [k.astype(np.int64) for k in keys]
+        assert np.array_equal(I._order(keys), np.lexsort(tuple(reversed(keys))))
+    sorted_keys = [np.sort(rng.integers(0, 9, 500)).astype(np.int64)]
+    assert np.array_equal(I._order(sorted_keys), np.arange(500))
+
+
+def test_vectorised_checks_and_rs_whole_numbers():
+    base = {"id": np.array([1, 1]), "event": np.array([1, 3]), "time": np.array([1.0, 2.0]),
+            "node": np.array([1, 1]), "dest": np.array([np.nan, 2.0])}
+    for col, value, message in [
+            ("id", np.array([1.0, np.nan]),
+             "'id' must be an integer or character vector with non-NA values."),
+            ("event", np.array([1, 2]),
+             "'event' must be an integer or character vector with non-NA values."),
+            ("time", np.array([1.0, 2.5]),
+             "'time' must be an integer or character vector with non-NA values."),
+            ("dest", np.array([0.0, np.nan]), "'node' or 'dest' contain NA values."),
+            ("node", np.array([1.0, 1.5]),
+             "'node' and 'dest' must both be integer or character.")]:
+        ev = dict(base, **{col: value})
+        with pytest.raises(ValueError) as e:
+            I.prepare(ev)
+        assert str(e.value) == message
+    # within sqrt(eps) of a whole number counts as whole, and is truncated
+    ev = dict(base, time=np.array([1.0, 2.9999999999]))
+    assert I.prepare(ev).keys[2].tolist() == [1, 2]
+    ev = {k: v.tolist() for k, v in ev.items()}
+    ev["dest"] = [None, 2.0]
+    assert I.prepare(ev, elementwise=True).keys[2].tolist() == [1, 2]
 
 
 def test_livestock_generator_is_sorted_and_mostly_consistent():
