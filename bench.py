@@ -24,8 +24,10 @@ siminf_gpu_run_solver_ex with host buffers (planning, host->device copies,
 solve, device->host copy of U inside the timed region).  The state (U alone
 is 5.84 GB) is far larger than the 129 MB L2, so no flush is needed between
 steps.  `--impl reference` times the reference algorithm on the host cores
-(the oracle's C port of the ssm solver with OpenMP, or the reference's own
-sources when they were compiled for this machine) on a bounded sample.
+(the oracle's C port of the ssm solver with OpenMP, whose parity with the
+reference's own sources is tested where those compile) on a bounded sample;
+the port, not those sources, because the workload needs capped transfer
+sizes, which the reference does not have.
 
 With N > 1 (torchrun) every rank runs an independent replica of the
 workload with its own seed (the path has no data exchange between
