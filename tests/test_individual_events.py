@@ -208,6 +208,23 @@ def test_vectorised_checks_and_rs_whole_numbers():
     assert I.prepare(ev, elementwise=True).keys[2].tolist() == [1, 2]
 
 
+def test_boundary_rejects_bad_tables_before_any_device_call():
+    """Argument checks of siminf_gpu_individual_events run on the host,
+    before any CUDA call, so they answer without a GPU."""
+    import ctypes as C
+    from siminf_gb300 import abi, native
+    L = native.lib()
+    st = abi.ReduceStats()
+    nul = C.POINTER(C.c_int)()
+    assert L.siminf_gpu_individual_events(-1, nul, nul, nul, nul, nul, nul, None,
+                                          C.byref(st)) == -9
+    assert "invalid individual event table" in native.last_status().message.decode()
+    assert L.siminf_gpu_individual_events(1 << 31, nul, nul, nul, nul, nul, nul, None,
+                                          None) == -9
+    assert L.siminf_gpu_individual_events(3, nul, nul, nul, nul, nul, nul, None, None) == -9
+    assert L.siminf_gpu_individual_events(0, nul, nul, nul, nul, nul, nul, None, None) == 0
+
+
 def test_livestock_generator_is_sorted_and_mostly_consistent():
     cols = livestock_register(2000, 50, seed=1)
     keep, bad = oracle.individual_events(*cols)
