@@ -715,7 +715,8 @@ def individual_bench(peak, threads, cpu=True, n_ind=2_500_000, n_nodes=200_000, 
            "events_per_s": n / (best.ms_kernel / 1e3),
            "events_per_s_e2e": n / (best.ms_total / 1e3),
            "ms_kernel": best.ms_kernel, "ms_total": best.ms_total, "bytes_moved": moved,
-           "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak, "bound": "hbm",
+           "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
+           "bound": "latency of the per-individual search; frac is against HBM",
            "data": "synthetic livestock register (%d animals, %d holdings, seed %d); "
                    "the two kernels (ms_kernel) and the call with its copies of the five "
                    "columns and keep (ms_total)" % (n_ind, n_nodes, seed)}

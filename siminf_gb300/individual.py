@@ -124,8 +124,9 @@ def check_time(time):
             raise ValueError(msg)
         return np.array([int(v) for v in time], dtype=np.int64), False
     if kind == "str":
-        try:
-            days = np.array(time, dtype="datetime64[D]").astype(np.int64)
+        try:       # as.Date's default formats: %Y-%m-%d and %Y/%m/%d
+            days = np.array([v.replace("/", "-") for v in time],
+                            dtype="datetime64[D]").astype(np.int64)
         except ValueError:
             raise ValueError(msg)
         return days, True
