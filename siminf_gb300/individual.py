@@ -23,6 +23,7 @@ sorts in the session's collation: the kept rows are the same, but
 individuals can come out in another order for mixed-case names.
 """
 import ctypes as C
+import re
 
 import numpy as np
 
@@ -54,15 +55,21 @@ def _is_na(x):
 
 
 def _kind(values):
-    """'str', 'num' or 'empty' for the non-NA values of a column."""
-    kinds = {isinstance(v, str) for v in values if not _is_na(v)}
+    """'num', 'str', 'logical' (R's TRUE/FALSE, not numeric there),
+    'mixed' or 'empty' for the non-NA values of a column."""
+    kinds = set()
+    for v in values:
+        if _is_na(v):
+            continue
+        if isinstance(v, (bool, np.bool_)):
+            kinds.add("logical")
+        elif isinstance(v, str):
+            kinds.add("str")
+        else:
+            kinds.add("num")
     if not kinds:
         return "empty"
-    if kinds == {True}:
-        return "str"
-    if kinds == {False}:
-        return "num"
-    return "mixed"
+    return kinds.pop() if len(kinds) == 1 else "mixed"
 
 
 # R's is_wholenumber (R/check_arguments.R:191-193): |x - round(x)| below
@@ -124,15 +131,35 @@ def check_time(time):
             raise ValueError(msg)
         return np.array([int(v) for v in time], dtype=np.int64), False
     if kind == "str":
-        try:       # as.Date's default formats: %Y-%m-%d and %Y/%m/%d
-            days = np.array([v.replace("/", "-") for v in time],
-                            dtype="datetime64[D]").astype(np.int64)
-        except ValueError:
-            raise ValueError(msg)
-        return days, True
+        return _dates(time, msg), True
     if kind == "empty":
         return np.zeros(0, dtype=np.int64), False
     raise ValueError(msg)
+
+
+_DATE = re.compile(r"\s*(\d{1,4})([-/])(\d{1,2})\2(\d{1,2})")
+
+
+def _dates(values, msg):
+    """Days since 1970-01-01 the way as.Date() reads strings: the format
+    (%Y-%m-%d or %Y/%m/%d) is the one the first value matches, and a value
+    it does not fit, or an impossible date, is NA."""
+    first = _DATE.match(values[0])
+    if not first:
+        raise ValueError("character string is not in a standard unambiguous format")
+    sep = first.group(2)
+    days = []
+    for v in values:
+        m = _DATE.match(v)
+        if not m or m.group(2) != sep:
+            raise ValueError(msg)
+        try:
+            d = np.datetime64("%04d-%02d-%02d" % (int(m.group(1)), int(m.group(3)),
+                                                  int(m.group(4))), "D")
+        except ValueError:
+            raise ValueError(msg)
+        days.append(d.astype(np.int64))
+    return np.array(days, dtype=np.int64)
 
 
 def check_nodes(event, node, dest):

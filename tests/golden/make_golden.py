@@ -17,7 +17,9 @@ Fixtures written:
   sise_punchcard_rep.json  tests/punchcard.R:364-410 replicates + sparse U/V
   individual_events.json   tests/individual_events.R:199-690,1222-1256 every
                            case that compares individual_events() with an
-                           expected table (input and expected columns)
+                           expected table (input and expected columns), and
+                           :84-330 every literal table it must reject, with
+                           the message
 """
 import json
 import os
@@ -110,6 +112,8 @@ def r_value(expr):
         return [x for it in items for x in r_value(it)]
     if expr in ("NA", "NA_integer_", "NA_character_", "NA_real_"):
         return [None]
+    if expr in ("TRUE", "FALSE"):
+        return [expr == "TRUE"]
     if expr[0] in "\"'":
         return [expr[1:-1]]
     if expr.endswith("L"):
@@ -153,6 +157,26 @@ def individual_event_cases(lines, first, last):
             elif re.match(r"^stopifnot\(identical\((events_obs, events|events, "
                           r"as.data.frame\(individual_events\(events\)\))\)\)", line):
                 cases.append({"line": k + 1, "input": events, "expected": events})
+        k += 1
+    return cases
+
+
+def individual_event_errors(lines, first, last):
+    """(line, input, message) for each data.frame that individual_events()
+    must reject with a message, in lines [first, last]."""
+    cases, events = [], None
+    k = first - 1
+    while k < last:
+        line = lines[k]
+        if line.startswith("events <- data.frame("):
+            events = r_data_frame("\n".join(lines[k:k + 40]))
+        elif line.startswith("events$"):
+            events = None                     # modified in place: not a literal table
+        elif line.startswith("res <- assertError(individual_events(events))") and events:
+            text = "\n".join(lines[k + 1:k + 6])
+            m = re.search(r'check_error\(\s*res,\s*"((?:[^"\\]|\\.)*)"', text)
+            if m:
+                cases.append({"line": k + 1, "input": events, "message": m.group(1)})
         k += 1
     return cases
 
@@ -253,6 +277,7 @@ def main(ref):
     fixtures["individual_events.json"] = {
         "source": "tests/individual_events.R:199-690,1222-1256",
         "cases": individual_event_cases(ie, 199, 690) + individual_event_cases(ie, 1222, 1256),
+        "errors": individual_event_errors(ie, 84, 330),
     }
 
     for name, fx in fixtures.items():

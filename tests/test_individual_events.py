@@ -140,6 +140,24 @@ def test_host_checks_give_the_reference_messages(events, message):
     assert str(e.value) == message
 
 
+def test_golden_rejections():
+    """Every literal table tests/individual_events.R:84-330 expects
+    individual_events() to reject, with its message."""
+    with open(os.path.join(HERE, "golden", "individual_events.json")) as f:
+        errors = json.load(f)["errors"]
+    assert len(errors) >= 10
+    for case in errors:
+        with pytest.raises(ValueError) as e:
+            I.prepare(case["input"])
+        assert str(e.value) == case["message"], case["line"]
+        # the same table as numpy arrays where numpy keeps the R types
+        arrays = {k: np.array(v) for k, v in case["input"].items()}
+        if all(a.dtype.kind in "iufbU" for a in arrays.values()):
+            with pytest.raises(ValueError) as e:
+                I.prepare(arrays)
+            assert str(e.value) == case["message"], case["line"]
+
+
 def test_prepare_orders_and_removes_repeats():
     ev = {"id": [2, 1, 1, 1], "event": [1, 3, 1, 3], "time": [5, 2, 1, 2],
           "node": [4, 1, 1, 1], "dest": [9, 2, 7, 2]}
