@@ -196,14 +196,23 @@ int siminf_gpu_run_solver_mssm(siminf_gpu_solver_args *args,
  * (Nrep rows of the model's gdata length); replicate r reads row r.  The
  * reference shares one gdata among replicates; particle filters and ABC
  * batches over parameter sets need one per replicate.
+ *
+ * max_node_day_transitions: the most transitions one node may fire in one
+ * unit of time; a node that would fire more stops the run with
+ * SIMINF_GPU_ERR_TIMEOUT instead of holding the GPU (the reference loops
+ * until its rate sum runs out).  0 takes the default, 2^28.
  */
 typedef struct siminf_gpu_options {
     int cap_transfers;
     int heavy_rate;     /* rate sum from which a node is queued first (0 = default 8, < 0 = off) */
     int gdata_per_replicate;
     int two_pass;       /* > 0 on, < 0 off, 0 = on from 500,000 nodes (all replicates) */
-    int reserved[4];
+    int max_node_day_transitions;   /* > 0: the bound; 0: 2^28 */
+    int reserved[3];
 } siminf_gpu_options;
+
+/* The default of siminf_gpu_options.max_node_day_transitions. */
+#define SIMINF_GPU_MAX_NODE_DAY_TRANSITIONS (1u << 28)
 
 /* siminf_gpu_run_solver_mssm with options (NULL = all zero). */
 int siminf_gpu_run_solver_ex(siminf_gpu_solver_args *args,
@@ -574,6 +583,24 @@ int siminf_gpu_sort_events(long long len, int *event, int *time, int *node, int 
 int siminf_gpu_individual_events(long long len, const int *id, const int *event,
                                  const int *time, const int *node, const int *dest,
                                  int *keep, void *cuda_stream, siminf_gpu_reduce_stats *stats);
+
+/*
+ * siminf_gpu_individual_events with a bound on each individual's search
+ * (no counterpart in the reference).  The depth-first search can take time
+ * exponential in an individual's event count -- branches that rejoin while
+ * the exits present cannot be reached, so nothing prunes it -- and here it
+ * holds a GPU thread.  max_steps bounds the candidate events one
+ * individual's search examines (<= 0: SIMINF_GPU_INDIVIDUAL_MAX_STEPS,
+ * which siminf_gpu_individual_events uses).  An individual that runs out
+ * keeps none of its events and the call returns SIMINF_GPU_ERR_TIMEOUT,
+ * siminf_gpu_status.event_index holding the zero-based first event of the
+ * lowest such individual; every other individual's keep is computed.
+ */
+#define SIMINF_GPU_INDIVIDUAL_MAX_STEPS (1LL << 26)
+int siminf_gpu_individual_events_ex(long long len, const int *id, const int *event,
+                                    const int *time, const int *node, const int *dest,
+                                    int *keep, long long max_steps, void *cuda_stream,
+                                    siminf_gpu_reduce_stats *stats);
 
 /* The device U/V of a plan that has run (d_V NULL without V), and ncol. */
 int siminf_gpu_plan_outputs(const siminf_gpu_plan *plan, const int **d_U,

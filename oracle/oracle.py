@@ -37,10 +37,11 @@ class OracleResult(C.Structure):
 
 
 def build(ref=None):
-    """Compile liboracle.so (and _ref when the reference tree exists)."""
+    """Compile liboracle.so, and _ref from the reference tree at `ref` (or
+    $SIMINF_REFERENCE) when one is given and present."""
     subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
-    ref_dir = ref or os.environ.get("SIMINF_REFERENCE", "/root/reference")
-    if os.path.isdir(os.path.join(ref_dir, "src", "solvers")):
+    ref_dir = ref or os.environ.get("SIMINF_REFERENCE")
+    if ref_dir and os.path.isdir(os.path.join(ref_dir, "src", "solvers")):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + ref_dir])
 
 

@@ -832,6 +832,9 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     s.Ntot = Ntot;
     s.seed = (uint64_t) a->seed;
     s.cap = opt ? (opt->cap_transfers != 0) : 0;
+    s.max_fired = (opt && opt->max_node_day_transitions > 0)
+                      ? (unsigned) opt->max_node_day_transitions
+                      : SIMINF_GPU_MAX_NODE_DAY_TRANSITIONS;
     p->tt0 = a->tspan[0];
 
     if ((rc = make_days(p, a))) {
@@ -1095,7 +1098,10 @@ static int resolve_errors(siminf_gpu_plan *p, std::vector<ErrRec> &cands)
         for (auto &e : c)
             if (e.phase == PHASE_PTS)
                 pts.push_back(e);
-        std::sort(pts.begin(), pts.end(), [](const ErrRec &x, const ErrRec &y) {
+        /* stable: one node's records stay in the order its thread wrote
+         * them (transition order), so the last one wins as in the
+         * reference's loop */
+        std::stable_sort(pts.begin(), pts.end(), [](const ErrRec &x, const ErrRec &y) {
             return x.node < y.node;
         });
         for (auto &e : pts) {
@@ -1484,10 +1490,24 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
     memset(&g_status, 0, sizeof(g_status));
     DevState s = p->s;
     cudaError_t e;
-    cudaEvent_t ev0, ev1;
-    cudaEventCreate(&ev0);
-    cudaEventCreate(&ev1);
-    cudaEventRecord(ev0, st);
+    /* the run's two timing events, destroyed on every return path */
+    struct EventPair {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~EventPair()
+        {
+            if (a)
+                cudaEventDestroy(a);
+            if (b)
+                cudaEventDestroy(b);
+        }
+    } ev;
+    e = cudaEventCreate(&ev.a);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&ev.b);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(ev.a, st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "plan_run events");
 
     /* a run that repeats the previous one unchanged replays its graph */
     const char *g_env = getenv("SIMINF_RUN_GRAPH");
@@ -1516,14 +1536,15 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
     }
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
-    cudaEventRecord(ev1, st);
-    e = cudaEventSynchronize(ev1);
+    e = cudaEventRecord(ev.b, st);
+    if (e == cudaSuccess)
+        e = cudaEventSynchronize(ev.b);
     if (e != cudaSuccess)
         return cuda_fail(e, "solver kernels");
     float ms = 0;
-    cudaEventElapsedTime(&ms, ev0, ev1);
-    cudaEventDestroy(ev0);
-    cudaEventDestroy(ev1);
+    e = cudaEventElapsedTime(&ms, ev.a, ev.b);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "solver time");
 
     int counts[3];
     unsigned long long fired = 0;

@@ -74,10 +74,16 @@ __host__ __device__ __forceinline__ bool ie_follows(const int *event, const int 
  * search: at each level the next branch is the first later event that may
  * follow the previous level's event; the search backs up when none is
  * left or the branch is an exit.  A lone root is kept when no path exists
- * yet: an exit if exits are present, else an enter or a transfer. */
-__host__ __device__ inline void ie_longest_path(const int *event, const int *time,
+ * yet: an exit if exits are present, else an enter or a transfer.
+ *
+ * The search can take time exponential in n (branches that rejoin, exits
+ * that no path reaches, so nothing prunes it); the reference runs it on a
+ * CPU, here it would hold a GPU thread.  budget bounds the candidate
+ * events examined; the function returns false when it runs out, with keep
+ * cleared. */
+__host__ __device__ inline bool ie_longest_path(const int *event, const int *time,
                                                 const int *node, const int *dest, int n,
-                                                int *path, int *keep)
+                                                int *path, int *keep, long long budget)
 {
     bool any_enter = false, any_exit = false;
     for (int i = 0; i < n; i++) {
@@ -104,6 +110,11 @@ __host__ __device__ inline void ie_longest_path(const int *event, const int *tim
             int j = path[depth] > 0 ? path[depth] : prev + 1;
             path[depth] = 0;
             for (; j < n; j++) {
+                if (--budget < 0) {
+                    for (int k = 0; k < n; k++)
+                        keep[k] = 0;
+                    return false;
+                }
                 if (!ie_follows(event, time, node, dest, prev, j))
                     continue;
                 path[depth] = j + 1;
@@ -126,13 +137,15 @@ __host__ __device__ inline void ie_longest_path(const int *event, const int *tim
             }
         }
     }
+    return true;
 }
 
 /* counts[0]: individuals listed so far; counts[1]: smallest index of an
- * invalid event type (IE_NONE when none).  A block takes IE_TILE events,
- * IE_ITEMS per thread in strides of the block, and appends its first
- * events with one atomic: a counter shared by every warp of the grid was
- * the kernel's bottleneck. */
+ * invalid event type (IE_NONE when none); counts[2]: smallest first event
+ * of an individual whose search ran out of steps (IE_NONE when none).  A
+ * block takes IE_TILE events, IE_ITEMS per thread in strides of the block,
+ * and appends its first events with one atomic: a counter shared by every
+ * warp of the grid was the kernel's bottleneck. */
 __global__ void __launch_bounds__(IE_BLOCK) k_indiv_starts(const int *__restrict__ id,
                                                            const int *__restrict__ event,
                                                            long long len, int *starts,
@@ -189,8 +202,9 @@ __global__ void __launch_bounds__(IE_BLOCK) k_indiv_paths(const int *__restrict_
                                                           const int *__restrict__ dest,
                                                           long long len,
                                                           const int *__restrict__ starts,
-                                                          const unsigned long long *counts,
-                                                          int *path, int *keep)
+                                                          unsigned long long *counts,
+                                                          int *path, int *keep,
+                                                          long long budget)
 {
     if (counts[1] != IE_NONE)
         return;
@@ -202,8 +216,9 @@ __global__ void __launch_bounds__(IE_BLOCK) k_indiv_paths(const int *__restrict_
         long long e = b + 1;
         while (e < len && id[e] == who)
             e++;
-        ie_longest_path(event + b, time + b, node + b, dest + b, (int) (e - b), path + b,
-                        keep + b);
+        if (!ie_longest_path(event + b, time + b, node + b, dest + b, (int) (e - b), path + b,
+                             keep + b, budget))
+            atomicMin(&counts[2], (unsigned long long) b);  /* the search gave up */
     }
 }
 
@@ -219,6 +234,16 @@ extern "C" int siminf_gpu_individual_events(long long len, const int *id, const 
                                             const int *time, const int *node, const int *dest,
                                             int *keep, void *cuda_stream,
                                             siminf_gpu_reduce_stats *stats)
+{
+    return siminf_gpu_individual_events_ex(len, id, event, time, node, dest, keep,
+                                           SIMINF_GPU_INDIVIDUAL_MAX_STEPS, cuda_stream, stats);
+}
+
+extern "C" int siminf_gpu_individual_events_ex(long long len, const int *id, const int *event,
+                                               const int *time, const int *node,
+                                               const int *dest, int *keep, long long max_steps,
+                                               void *cuda_stream,
+                                               siminf_gpu_reduce_stats *stats)
 {
     capi_clear_status();
     const cudaStream_t st = (cudaStream_t) cuda_stream;
@@ -238,7 +263,7 @@ extern "C" int siminf_gpu_individual_events(long long len, const int *id, const 
     unsigned long long *d_counts = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (e == cudaSuccess) e = cudaMallocAsync((void **) &d_cols, 8 * ib, st);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **) &d_counts, 2 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **) &d_counts, 3 * sizeof(unsigned long long), st);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     int *d_id = d_cols, *d_event = d_cols + len, *d_time = d_cols + 2 * len,
@@ -248,7 +273,9 @@ extern "C" int siminf_gpu_individual_events(long long len, const int *id, const 
     int *dev_col[5] = {d_id, d_event, d_time, d_node, d_dest};
     for (int c = 0; c < 5 && e == cudaSuccess; c++)
         e = cudaMemcpyAsync(dev_col[c], host[c], ib, cudaMemcpyHostToDevice, st);
-    unsigned long long counts[2] = {0, IE_NONE};
+    unsigned long long counts[3] = {0, IE_NONE, IE_NONE};
+    if (max_steps <= 0)
+        max_steps = SIMINF_GPU_INDIVIDUAL_MAX_STEPS;
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_counts, counts, sizeof(counts), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
@@ -261,7 +288,7 @@ extern "C" int siminf_gpu_individual_events(long long len, const int *id, const 
                                                               d_counts, d_keep);
         k_indiv_paths<<<(unsigned) grid, IE_BLOCK, 0, st>>>(d_id, d_event, d_time, d_node,
                                                             d_dest, len, d_starts, d_counts,
-                                                            d_path, d_keep);
+                                                            d_path, d_keep, max_steps);
         cudaEventRecord(e1, st);
         e = cudaGetLastError();
     }
@@ -295,6 +322,13 @@ extern "C" int siminf_gpu_individual_events(long long len, const int *id, const 
         char msg[96];
         snprintf(msg, sizeof(msg), "'event[%lld]' is invalid.", (long long) counts[1] + 1);
         return fail(SIMINF_GPU_UNDEFINED_EVENT, (long long) counts[1], msg);
+    }
+    if (counts[2] != IE_NONE) {
+        char msg[160];
+        snprintf(msg, sizeof(msg),
+                 "the search of the individual whose events start at 'event[%lld]' "
+                 "gave up after %lld steps.", (long long) counts[2] + 1, max_steps);
+        return fail(SIMINF_GPU_ERR_TIMEOUT, (long long) counts[2], msg);
     }
     return 0;
 }

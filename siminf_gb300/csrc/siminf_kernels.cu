@@ -43,8 +43,6 @@ enum { ERR_NEGATIVE_STATE = -1, ERR_UNDEFINED_EVENT = -3, ERR_SAMPLE_SELECT = -8
        ERR_INVALID_RATE = -11, ERR_EVENTS_N = -15, ERR_EVENT_SHIFT = -16,
        ERR_SHIFT_OUT_OF_BOUNDS = -17, ERR_INVALID_PROPORTION = -18, ERR_TIMEOUT = -33 };
 
-/* Upper bound on the transitions of one node in one unit of time. */
-#define MAX_NODE_DAY_TRANSITIONS (1u << 28)
 
 enum { EV_EXIT = 0, EV_ENTER = 1, EV_INTERNAL = 2, EV_EXTERNAL = 3 };
 
@@ -221,7 +219,7 @@ __device__ __forceinline__ bool ssa_begin(SsaLane<M> &ln, const si_rng &key, uin
 template <class M>
 __device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, double next,
                                          const double *v, const double *ld, const double *gd,
-                                         const int *sS, const uint32_t *sG)
+                                         const int *sS, const uint32_t *sG, unsigned max_fired)
 {
     constexpr int NC = M::NC, NT = M::NT;
     const double tn = ln.tau + ln.t;
@@ -279,7 +277,7 @@ __device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, doub
         }
     }
 
-    if (++ln.fired > MAX_NODE_DAY_TRANSITIONS) {
+    if (++ln.fired > max_fired) {
         /* Bounded work per node-day: a time step that stopped advancing t
          * (a rate sum near the overflow threshold) ends the run with an
          * error instead of spinning. */
@@ -349,10 +347,10 @@ __device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, doub
 template <class M>
 __device__ __forceinline__ unsigned ssa_day(SsaLane<M> &ln, si_rng &r, double next,
                                             const double *v, const double *ld, const double *gd,
-                                            const int *sS, const uint32_t *sG)
+                                            const int *sS, const uint32_t *sG, unsigned max_fired)
 {
     if (!ssa_begin<M>(ln, r, r.ctr, next))
-        while (!ssa_step<M>(ln, r, next, v, ld, gd, sS, sG)) {
+        while (!ssa_step<M>(ln, r, next, v, ld, gd, sS, sG, max_fired)) {
         }
     r.ctr = ln.c;
     r.have = 0;
@@ -1080,7 +1078,7 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
                  * its whole day in this loop (one call site of the step
                  * keeps the loop's code small) */
                 do
-                    done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG);
+                    done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG, s.max_fired);
                 while (heavy && !done);
             }
         }
@@ -1463,7 +1461,7 @@ __device__ __forceinline__ bool aem_step(const DevState &s, AemNode<M> &a, long 
         }
     if (isinf(t) || t >= next)
         return true;
-    if (++fired > MAX_NODE_DAY_TRANSITIONS) {
+    if (++fired > s.max_fired) {
         a.err = ERR_TIMEOUT;
         a.err_tr = tr;
         a.err_t = t;
@@ -1768,7 +1766,7 @@ __global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s,
             ln.err_tr = -1;
             ln.err_t = 0.0;
             ln.err_rate = 0.0;
-            fired += ssa_day<M>(ln, r, di.next, v, ld, gd, sS, sG);
+            fired += ssa_day<M>(ln, r, di.next, v, ld, gd, sS, sG, s.max_fired);
             if (ln.err) {
                 record_error(s, ln.err, PHASE_SSA, d, g, ln.err_tr, -1, ln.err_t, ln.err_rate);
                 break;

@@ -169,12 +169,13 @@ __global__ void k_noalloc_pick(const ErrRec *err, NoallocCtl *ctl)
             if (err[i].code != SIMINF_GPU_ERR_INVALID_RATE) {
                 if (other < 0 || err[i].node < err[other].node)
                     other = i;
-            } else if (last_rate < 0 || err[i].node > err[last_rate].node) {
+            } else if (last_rate < 0 || err[i].node >= err[last_rate].node) {
                 last_rate = i;
             }
         }
         /* in node order, the first error that is not an invalid rate,
-         * else the last invalid rate */
+         * else the last invalid rate: of the highest node, its last record
+         * (one thread records a node's rates in transition order) */
         if (other >= 0) {
             best = other;
         } else if (last_rate >= 0) {
@@ -269,6 +270,7 @@ extern "C" int siminf_gpu_run_solver_ssm_noalloc(siminf_gpu_solver_args *a,
     s.Ntot = Nn;
     s.seed = (uint64_t) a->seed;
     s.cap = 0;
+    s.max_fired = SIMINF_GPU_MAX_NODE_DAY_TRANSITIONS;
     s.S = (const int *) (base + lo.S);
     s.Gmask = (const uint32_t *) (base + lo.G);
     s.hasN = 0;

@@ -91,6 +91,8 @@ struct DevState {
     long long Ntot;
     uint64_t seed;
     int cap;                /* cap sampled sizes at what the node holds */
+    unsigned max_fired;     /* transitions one node may fire in one unit of
+                             * time before the run stops with a timeout */
 
     /* model matrices */
     const int *S;           /* dense, Nt rows of Nc */

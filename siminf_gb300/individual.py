@@ -23,6 +23,7 @@ sorts in the session's collation: the kept rows are the same, but
 individuals can come out in another order for mixed-case names.
 """
 import ctypes as C
+import datetime
 import re
 
 import numpy as np
@@ -34,10 +35,12 @@ EVENT_CODES = {"exit": 0, "enter": 1, "extTrans": 3}
 EVENT_NAMES = {v: k for k, v in EVENT_CODES.items()}
 
 
-def longest_paths(id, event, time, node, dest, stream=None, stats=False):
+def longest_paths(id, event, time, node, dest, stream=None, stats=False, max_steps=0):
     """siminf_gpu_individual_events on sorted, de-duplicated int32 columns
     (dest NA = INT_MIN): keep, a 0/1 int32 array (with the ReduceStats when
-    stats=True)."""
+    stats=True).  max_steps > 0 bounds each individual's search
+    (siminf_gpu_individual_events_ex); an individual whose search runs out
+    raises the library's timeout error."""
     cols = [np.ascontiguousarray(x, dtype=np.int32) for x in (id, event, time, node, dest)]
     n = len(cols[0])
     if any(len(c) != n for c in cols):
@@ -45,8 +48,9 @@ def longest_paths(id, event, time, node, dest, stream=None, stats=False):
     keep = np.zeros(n, dtype=np.int32)
     st = abi.ReduceStats()
     pi = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
-    native.check(native.lib().siminf_gpu_individual_events(
-        n, *[pi(c) for c in cols], pi(keep), stream, C.byref(st)))
+    native.check(native.lib().siminf_gpu_individual_events_ex(
+        n, *[pi(c) for c in cols], pi(keep), C.c_longlong(int(max_steps)), stream,
+        C.byref(st)))
     return (keep, st) if stats else keep
 
 
@@ -55,16 +59,19 @@ def _is_na(x):
 
 
 def _kind(values):
-    """'num', 'str', 'logical' (R's TRUE/FALSE, not numeric there),
-    'mixed' or 'empty' for the non-NA values of a column."""
+    """'num', 'str', 'logical' (R's TRUE/FALSE, not numeric there), 'date'
+    (numpy datetime64 or datetime.date values, R's Date), 'mixed' or
+    'empty' for the non-NA values of a column."""
     kinds = set()
     for v in values:
-        if _is_na(v):
+        if _is_na(v) or (isinstance(v, np.datetime64) and np.isnat(v)):
             continue
         if isinstance(v, (bool, np.bool_)):
             kinds.add("logical")
         elif isinstance(v, str):
             kinds.add("str")
+        elif isinstance(v, (np.datetime64, datetime.date)):
+            kinds.add("date")
         else:
             kinds.add("num")
     if not kinds:
@@ -123,9 +130,13 @@ def check_event(event):
 
 def check_time(time):
     msg = "'time' must be an integer or character vector with non-NA values."
-    if any(_is_na(v) for v in time):
+    if any(_is_na(v) or (isinstance(v, np.datetime64) and np.isnat(v)) for v in time):
         raise ValueError(msg)
     kind = _kind(time)
+    if kind == "date":
+        # Date columns: days since 1970-01-01, as R stores a Date
+        return np.array([np.datetime64(v, "D").astype(np.int64) for v in time],
+                        dtype=np.int64), True
     if kind == "num":
         if not _whole(time):
             raise ValueError(msg)
@@ -162,11 +173,15 @@ def _dates(values, msg):
     return np.array(days, dtype=np.int64)
 
 
-def check_nodes(event, node, dest):
+def check_nodes(event, node, dest, dest_kind=None):
+    """dest holds NA for every event but a transfer; dest_kind is the kind
+    of the caller's dest column before that (R checks the column's type)."""
     if any(_is_na(v) for v in node) or any(_is_na(d) for e, d in zip(event, dest) if e == 3):
         raise ValueError("'node' or 'dest' contain NA values.")
     msg = "'node' and 'dest' must both be integer or character."
     kn, kd = _kind(node), _kind(dest)
+    if dest_kind is not None and kd == "empty":
+        kd = dest_kind
     if kn in ("num", "empty") and kd in ("num", "empty"):
         if not _whole(node) or not _whole([d for e, d in zip(event, dest) if e == 3]):
             raise ValueError(msg)
@@ -310,8 +325,9 @@ def prepare(events, elementwise=False):
         id_code = check_id(raw["id"])
         event, event_named = check_event(raw["event"])
         time, time_dates = check_time(raw["time"])
+        dest_kind = _kind(raw["dest"])
         raw["dest"] = [d if e == 3 else None for e, d in zip(event, raw["dest"])]
-        node_code, dest_code = check_nodes(event, raw["node"], raw["dest"])
+        node_code, dest_code = check_nodes(event, raw["node"], raw["dest"], dest_kind)
 
     # order(id, time, event, node, dest), NA last; then drop exact repeats
     live = dest_code[dest_code != NA]

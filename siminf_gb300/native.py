@@ -61,6 +61,9 @@ def lib():
     L.siminf_gpu_schedule.restype = C.c_int
     L.siminf_gpu_pfilter.argtypes = [vp, vp, C.POINTER(abi.PfilterArgs)]
     L.siminf_gpu_pfilter.restype = C.c_int
+    L.siminf_gpu_individual_events_ex.argtypes = ([C.c_longlong] + [vp] * 6 +
+                                                  [C.c_longlong, vp, vp])
+    L.siminf_gpu_individual_events_ex.restype = C.c_int
     L.siminf_gpu_last_status.argtypes = [C.POINTER(abi.Status)]
     L.siminf_gpu_last_stats.argtypes = [C.POINTER(abi.Stats)]
     L.siminf_gpu_plan_create.argtypes = [vp, vp, C.POINTER(vp)]
@@ -116,6 +119,7 @@ EXPORTS = (
     "siminf_gpu_release_cached", "siminf_gpu_trajectory_u", "siminf_gpu_trajectory_v",
     "siminf_gpu_prevalence", "siminf_gpu_plan_outputs", "siminf_gpu_sort_events",
     "siminf_gpu_plan_day_max", "siminf_gpu_individual_events",
+    "siminf_gpu_individual_events_ex",
 )
 
 
@@ -185,11 +189,13 @@ class Plan:
     run() repeats the whole horizon on the GPU, download() fills the
     holder's U/V buffers."""
 
-    def __init__(self, holder, model_name, cap_transfers=False):
+    def __init__(self, holder, model_name, cap_transfers=False, **options):
+        """options: further siminf_gpu_options fields (heavy_rate,
+        two_pass, gdata_per_replicate, max_node_day_transitions)."""
         self.holder = holder
         self.model = device_model(model_name)
         h = C.c_void_p()
-        opt = abi.Options(cap_transfers=int(bool(cap_transfers)))
+        opt = abi.Options(cap_transfers=int(bool(cap_transfers)), **options)
         check(lib().siminf_gpu_plan_create_ex(C.cast(holder.ref(), C.c_void_p),
                                               self.model.handle, C.byref(opt), C.byref(h)))
         self.handle = h

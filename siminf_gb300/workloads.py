@@ -56,12 +56,14 @@ def sir_plain(nodes=1000, days=150):
 def powerlaw_graph(nodes, edges, seed=1, exponent=2.1, cutoff=None):
     """Fixed directed graph: uniform sources, destinations drawn with
     probability proportional to power-law weights with the given exponent
-    on [1, cutoff] (default cutoff sqrt(edges))."""
+    on [1, cutoff] (default cutoff sqrt(edges); np.inf: no cutoff, the
+    plain power law)."""
     rng = np.random.default_rng(seed)
     a = exponent - 1.0
     K = float(cutoff if cutoff is not None else np.sqrt(edges))
     u = rng.random(nodes)
-    w = (1.0 - u * (1.0 - K ** -a)) ** (-1.0 / a)      # truncated Pareto(a) on [1, K]
+    # truncated Pareto(a) on [1, K]; K = inf gives the untruncated law
+    w = (1.0 - u * (1.0 - (0.0 if np.isinf(K) else K ** -a))) ** (-1.0 / a)
     p = w / w.sum()
     src = rng.integers(0, nodes, edges).astype(np.int32)
     dst = rng.choice(nodes, size=edges, p=p).astype(np.int32)
@@ -71,16 +73,20 @@ def powerlaw_graph(nodes, edges, seed=1, exponent=2.1, cutoff=None):
 
 
 def seir_events(nodes=1_000_000, days=365, transfers=500_000, p_enter=0.002, p_exit=0.002,
-                graph_edges=None, seeds=(1, 2, 3)):
+                graph_edges=None, seeds=(1, 2, 3), transfer_n=None, cutoff=None):
     """Config 2 (see module docstring).  Events are produced in the order
-    R/SimInf_events.R:398 sorts them: by time, exits, enters, transfers."""
+    R/SimInf_events.R:398 sorts them: by time, exits, enters, transfers.
+    transfer_n: a fixed transfer size instead of 1 + Poisson(3) (n = 1 is
+    the balanced variant the reference runs without capping for a few
+    months); cutoff: the graph's power-law cutoff (powerlaw_graph)."""
     g_seed, u_seed, e_seed = seeds
     rng_u = np.random.default_rng(u_seed)
     S = rng_u.poisson(300, nodes)
     I = rng_u.poisson(3, nodes) * (rng_u.random(nodes) < 0.01)
     u0 = np.vstack([S, np.zeros(nodes), I, np.zeros(nodes)]).astype(np.int32)
 
-    gsrc, gdst = powerlaw_graph(nodes, graph_edges or 4 * transfers, seed=g_seed)
+    gsrc, gdst = powerlaw_graph(nodes, graph_edges or 4 * transfers, seed=g_seed,
+                                cutoff=cutoff)
     rng = np.random.default_rng(e_seed)
     chunks = {k: [] for k in ("event", "time", "node", "dest", "n", "select")}
     for t in range(1, days + 1):
@@ -88,6 +94,8 @@ def seir_events(nodes=1_000_000, days=365, transfers=500_000, p_enter=0.002, p_e
         en = np.nonzero(rng.random(nodes) < p_enter)[0].astype(np.int32)
         pick = rng.integers(0, len(gsrc), transfers)
         n = (1 + rng.poisson(3, transfers)).astype(np.int32)
+        if transfer_n is not None:
+            n[:] = transfer_n
         m = len(ex) + len(en) + transfers
         chunks["event"].append(np.concatenate([np.zeros(len(ex), np.int32),
                                                np.ones(len(en), np.int32),

@@ -287,5 +287,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SIMINF_REFERENCE",
-                                                               "/root/reference"))
+    if len(sys.argv) < 2 and not os.environ.get("SIMINF_REFERENCE"):
+        sys.exit("usage: make_golden.py REFERENCE_TREE (or set SIMINF_REFERENCE)")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ["SIMINF_REFERENCE"])

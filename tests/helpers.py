@@ -87,6 +87,33 @@ def run_gpu(m, seed=42, U_sparse=None, V_sparse=None):
     return code, h, native.last_stats()
 
 
+def pin_inputs_outputs(h, m, torch):
+    """Move the holder's inputs (u0, ldata, the event columns) and its U
+    into pinned host memory, as an end-to-end caller with pinned buffers
+    passes them."""
+    import ctypes as C
+    a = h.args
+
+    def pinned(src):
+        t = torch.from_numpy(np.ascontiguousarray(src)).pin_memory()
+        h.keep.append(t)
+        return t.numpy()
+
+    def repoint(field, n, dtype, ctype):
+        if n <= 0 or not getattr(a, field):
+            return
+        arr = pinned(np.ctypeslib.as_array(getattr(a, field), shape=(n,)).view(dtype))
+        setattr(a, field, arr.ctypes.data_as(C.POINTER(ctype)))
+
+    for k in ("event", "time", "node", "dest", "n", "select", "shift"):
+        repoint(k, a.len, np.int32, C.c_int)
+    repoint("proportion", a.len, np.float64, C.c_double)
+    repoint("u0", m.Nn * m.Nc * m.replicates, np.int32, C.c_int)
+    repoint("ldata", m.Nld * m.Nn, np.float64, C.c_double)
+    h.U = pinned(h.U)
+    a.U = h.U.ctypes.data_as(C.POINTER(C.c_int))
+
+
 def U_matrix(m, h):
     return h.U.reshape((m.Nn * m.Nc, m.replicates * len(m.tspan)), order="F")
 

@@ -9,6 +9,7 @@ it was built), plus the host-side checks and their messages.  GPU: the
 device path, bit-exact against the oracle on the golden cases, on random
 tables with deep searches and on a table larger than L2, and its error for
 an invalid event type."""
+import datetime
 import json
 import os
 
@@ -189,6 +190,33 @@ def test_vectorised_and_elementwise_paths_agree():
             assert np.array_equal(x, y)                       # sorted, repeats gone
 
 
+def test_dates_with_character_ids():
+    """Date times with character ids (or a list of datetime.date with
+    numeric ids) take the value-by-value path and are read as R's Date
+    columns: days since 1970-01-01, the same keys as numeric days."""
+    ids = ["b", "a", "a", "b"]
+    days = np.array(["2020-01-05", "2020-01-01", "2020-02-01", "2020-01-09"],
+                    dtype="datetime64[D]")
+    base = {"id": ids, "event": [1, 1, 0, 0], "node": [1, 2, 2, 1], "dest": [None] * 4}
+    a = I.prepare(dict(base, time=days))
+    assert a.time_dates
+    b = I.prepare(dict(base, time=[d.astype(object) for d in days]))
+    c = I.prepare(dict(base, time=days.astype(np.int64).tolist()))
+    for x, y, z in zip(a.keys, b.keys, c.keys):
+        assert np.array_equal(x, y) and np.array_equal(x, z)
+    d = I.prepare({"id": [2, 1], "event": [1, 0], "node": [1, 1], "dest": [0, 0],
+                   "time": [datetime.date(2020, 1, 2), datetime.date(2020, 1, 1)]})
+    assert d.time_dates and d.keys[2].tolist() == [18262, 18263]
+
+
+def test_character_nodes_with_numeric_dest_rejected():
+    """No transfers, character nodes and a numeric dest column: R's check
+    sees a numeric dest and rejects the table."""
+    with pytest.raises(ValueError, match="'node' and 'dest' must both be integer or character."):
+        I.prepare({"id": [1, 1], "event": ["enter", "exit"], "time": [1, 2],
+                   "node": ["x", "x"], "dest": [0, 0]})
+
+
 def test_order_is_rs_order():
     rng = np.random.default_rng(4)
     for trial in range(30):
@@ -296,6 +324,53 @@ def test_gpu_invalid_event_type_is_the_reference_error():
     assert e.value.code == -3
     assert "'event[4]' is invalid." in str(e.value)
     assert native.last_status().event_index == 3
+
+
+def exploding_individual(layers, who=2):
+    """One individual whose search has 2^layers paths and no pruning: it
+    enters at node 1, then at each layer moves to node a or node b and from
+    either on to the next layer's first node; its one exit is at a node no
+    path reaches, so no path is kept longer than the lone exit."""
+    rows = [(who, 1, 0, 1, NA)]
+    t, at = 1, 1
+    for k in range(layers):
+        a, b, nxt = 1000 + 3 * k, 1001 + 3 * k, 1002 + 3 * k
+        rows += [(who, 3, t + 1, at, a), (who, 3, t + 1, at, b),
+                 (who, 3, t + 2, a, nxt), (who, 3, t + 2, b, nxt)]
+        t, at = t + 2, nxt
+    rows.append((who, 0, t + 5, 999, NA))
+    rows.sort(key=lambda r: (r[0], r[2], r[1], r[3], r[4]))
+    return [np.array(c, np.int32) for c in zip(*rows)]
+
+
+@pytest.mark.gpu
+def test_gpu_search_budget_stops_an_exploding_individual():
+    """An individual with 2^20 paths and an unreachable exit: with a budget
+    of 10^4 steps its search gives up, the call returns the timeout error
+    naming its first event, and the other individuals' keep is the
+    oracle's; with the default budget a small case of the same shape
+    finishes and equals the oracle."""
+    from siminf_gb300 import abi, native
+    good = random_table(np.random.default_rng(8), 40, 8, 6, 30)
+    bad = exploding_individual(20, who=int(good[0].max()) + 1)
+    cols = [np.concatenate([g, b]) for g, b in zip(good, bad)]
+    want, _ = oracle.individual_events(*good)
+    n_good = len(good[0])
+    keep = np.zeros(len(cols[0]), np.int32)
+    pi = lambda a: a.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_int))
+    code = native.lib().siminf_gpu_individual_events_ex(
+        len(cols[0]), *[pi(c) for c in cols], pi(keep), 10_000, None, None)
+    assert code == -33
+    st = native.last_status()
+    assert st.event_index == n_good
+    assert np.array_equal(keep[:n_good], want)
+    assert not keep[n_good:].any()
+    small = exploding_individual(6)
+    got = I.longest_paths(*small)
+    assert np.array_equal(got, oracle.individual_events(*small)[0])
+    with pytest.raises(abi.SimInfError) as e:
+        I.longest_paths(*small, max_steps=50)
+    assert e.value.code == -33
 
 
 @pytest.mark.gpu

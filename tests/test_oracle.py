@@ -25,6 +25,25 @@ def test_oracle_matches_reference(oracle_lib, label, m, threads):
     assert res.transitions > 0 or label.startswith("sis_shift")
 
 
+@needs_ref
+def test_oracle_matches_reference_on_balanced_headline_sample(oracle_lib):
+    """The benchmark workload's generator at 5% scale (50,000 nodes, 25,000
+    transfers a day) for 120 days with transfers of one individual: the
+    variant the reference runs without capping.  The oracle, with every
+    host thread, equals the reference's unmodified solver bit for bit."""
+    import os
+    from siminf_gb300 import abi, workloads
+    m = workloads.seir_events(nodes=50_000, days=120, transfers=25_000, transfer_n=1)
+    threads = os.cpu_count() or 1
+    ho = abi.build_args(m, 42)
+    code_o, res = oracle.run(ho, m.name, threads)
+    hr = abi.build_args(m, 42)
+    code_r = oracle.run_ref(hr, m.name, threads)
+    assert code_o == code_r == 0
+    assert np.array_equal(ho.U, hr.U)
+    assert res.transitions > 100_000 and res.e2_events == 120 * 25_000
+
+
 def test_oracle_thread_count_invariance(oracle_lib):
     for label, m in parity_cases()[:4]:
         _, _, h1 = run_oracle(m, threads=1)

@@ -85,11 +85,40 @@ def test_noalloc_rejects_runs_beyond_scratch(gpu):
     _same(_sir(64, 30, 2), 3)        # the next call runs normally
 
 
+def _status():
+    st = native.last_status()
+    return st.error, st.node, st.transition, st.rate
+
+
 def test_noalloc_reports_the_solver_error(gpu):
     m = _sir(50, 20, 4, beta=-0.5)   # negative rates: invalid rate at start
     code_e, _ = _existing(m, 1)
+    st_e = _status()
     code_n, _ = _noalloc(m, 1)
     assert code_e == code_n == -11
+    assert _status() == st_e
+    _same(_sir(64, 30, 2), 3)
+
+
+def test_noalloc_reports_the_last_invalid_rate_of_a_node(gpu):
+    """Three invalid rates of every node at the first day's end (negative
+    upsilons once phi leaves 0): both entry points report the highest
+    node's last transition, the status the reference's refresh loop leaves
+    behind."""
+    rng = np.random.default_rng(2)
+    u0 = {k: (rng.poisson(20, 30) if k.startswith("S") else np.zeros(30, np.int64))
+          for k in ("S_1", "I_1", "S_2", "I_2", "S_3", "I_3")}
+    m = M.SISe3(u0, np.arange(1.0, 10.0), phi=0.0, upsilon_1=-0.01, upsilon_2=-0.02,
+                upsilon_3=-0.03, gamma_1=0.1, gamma_2=0.12, gamma_3=0.14, alpha=1.0,
+                beta_t1=0.19, beta_t2=0.085, beta_t3=0.075, beta_t4=0.185, end_t1=91,
+                end_t2=182, end_t3=273, end_t4=365, epsilon=1e-5)
+    code_e, _ = _existing(m, 1)
+    st_e = _status()
+    code_n, _ = _noalloc(m, 1)
+    st_n = _status()
+    assert code_e == code_n == -11
+    assert st_n == st_e
+    assert st_e[1] == m.Nn - 1 and st_e[2] == 4
     _same(_sir(64, 30, 2), 3)
 
 
