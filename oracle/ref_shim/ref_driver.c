@@ -64,10 +64,13 @@ int ref_run(const siminf_gpu_solver_args *ga, const char *model, int threads)
     if (shim_configure((uint64_t) a.seed, a.Nn, a.Nthread, a.Nrep, threads))
         return -2;
     int err;
-    if (a.solver == 1)            /* aem: one replicate (src/SimInf.c:393-398) */
+    /* the dispatch of src/SimInf.c:383-399 */
+    if (a.solver == 1)            /* aem: one replicate */
         err = a.Nrep > 1 ? -19 : SimInf_run_solver_aem(&a);
+    else if (a.Nrep > 1)
+        err = a.crn == 1 ? SimInf_run_solver_mssm_crn(&a) : SimInf_run_solver_mssm(&a);
     else
-        err = (a.Nrep > 1) ? SimInf_run_solver_mssm(&a) : SimInf_run_solver_ssm(&a);
+        err = SimInf_run_solver_ssm(&a);
     shim_release();
     return err;
 }

@@ -37,6 +37,7 @@ enum { MT_N = 624, MT_M = 397 };
 
 struct gsl_rng {
     long offset;
+    int crn;                /* one of mssm_crn's per-(replicate, node) generators */
     uint32_t mt[MT_N];
     int mti;
 };
@@ -92,6 +93,7 @@ static struct {
     int Nn, Nthread, Nrep, threads, verbose;
     int allocs;
     si_rng *streams;
+    si_rng *crn_streams;    /* replicated models: the SSA streams of mssm_crn */
 } g;
 
 int shim_configure(uint64_t seed, int Nn, int Nthread, int Nrep, int threads)
@@ -110,6 +112,15 @@ int shim_configure(uint64_t seed, int Nn, int Nthread, int Nrep, int threads)
         return -1;
     for (long i = 0; i < n; i++)
         si_rng_init(&g.streams[i], seed, (uint64_t) i, 0);
+    free(g.crn_streams);
+    g.crn_streams = NULL;
+    if (Nrep > 1) {
+        g.crn_streams = malloc((size_t) n * sizeof(si_rng));
+        if (!g.crn_streams)
+            return -1;
+        for (long i = 0; i < n; i++)
+            si_rng_init(&g.crn_streams[i], seed, SI_CRN_SID | (uint64_t) i, 0);
+    }
     return 0;
 }
 
@@ -117,6 +128,8 @@ void shim_release(void)
 {
     free(g.streams);
     g.streams = NULL;
+    free(g.crn_streams);
+    g.crn_streams = NULL;
 }
 
 gsl_rng *gsl_rng_alloc(const gsl_rng_type *T)
@@ -127,8 +140,16 @@ gsl_rng *gsl_rng_alloc(const gsl_rng_type *T)
         return NULL;
     const int k = g.allocs++;
     mt_seed(r, (uint32_t) (g.seed ^ (g.seed >> 32)) + (uint32_t) k);
+    r->crn = 0;
     if (k == 0) {
         r->offset = -1;                        /* master: never draws */
+    } else if (k - 1 >= g.Nthread) {
+        /* mssm_crn allocates one generator per (replicate, node) after the
+         * threads' event generators (src/solvers/SimInf_solver_mssm_crn.c:
+         * 459-473), replicate by replicate, node by node: the j-th is
+         * stream j = replicate * Nn + node */
+        r->crn = 1;
+        r->offset = k - 1 - g.Nthread;
     } else {
         const long i = k - 1;
         r->offset = (g.Nrep > 1) ? i * g.Nn : i * (g.Nn / g.Nthread);
@@ -152,6 +173,8 @@ unsigned long int gsl_rng_uniform_int(const gsl_rng *r, unsigned long int n)
 
 static si_rng *stream(const gsl_rng *r, long node)
 {
+    if (r->crn)
+        return &g.crn_streams[r->offset];      /* its own stream, whatever `node` says */
     return &g.streams[r->offset + node];
 }
 

@@ -75,6 +75,7 @@ typedef struct ctx {
     uint64_t seed;
     int gdata_stride;           /* 0: one gdata; else replicate r uses gdata + r * stride */
     int aem;                    /* all-events method instead of the direct method */
+    int crn;                    /* mssm_crn: SSA draws from a stream of their own */
 } ctx;
 
 static const double *gdata_of(const ctx *c, int r)
@@ -88,6 +89,7 @@ typedef struct rep {
     double *t_rate, *sum_t_rate, *t_time;
     int *update_node;
     uint64_t *ctr;              /* next draw index of each node's stream */
+    uint64_t *crn_ctr;          /* mssm_crn: next draw index of its SSA stream */
     int *node_err;              /* per-node error of the current phase */
     double *node_err_time, *node_err_rate;
     int *node_err_tr;
@@ -141,7 +143,13 @@ static uint64_t ssa_node(const ctx *c, rep *s, int r, int node, double next)
     uint64_t fired = 0;
     si_rng rng;
 
-    si_rng_init(&rng, c->seed, (uint64_t) r * c->Nn + node, s->ctr[node]);
+    /* mssm_crn (src/solvers/SimInf_solver_mssm_crn.c:185,196): the two
+     * draws of a transition come from a generator per (replicate, node),
+     * apart from the one the node's events draw from */
+    if (c->crn)
+        si_rng_init(&rng, c->seed, SI_CRN_SID | ((uint64_t) r * c->Nn + node), s->crn_ctr[node]);
+    else
+        si_rng_init(&rng, c->seed, (uint64_t) r * c->Nn + node, s->ctr[node]);
     for (;;) {
         double cum, rand, tau, delta = 0.0;
         int tr;
@@ -203,7 +211,10 @@ static uint64_t ssa_node(const ctx *c, rep *s, int r, int node, double next)
         }
         s->sum_t_rate[node] += delta;
     }
-    s->ctr[node] = rng.ctr;
+    if (c->crn)
+        s->crn_ctr[node] = rng.ctr;
+    else
+        s->ctr[node] = rng.ctr;
     if (g_node_fired)
         g_node_fired[(size_t) r * c->Nn + node] += fired;
     return fired;
@@ -822,6 +833,7 @@ static int run_replicate(const ctx *c, rep *s, int r, int parallel_nodes,
     }
     memset(s->update_node, 0, Nn * sizeof(int));
     memset(s->ctr, 0, Nn * sizeof(uint64_t));
+    memset(s->crn_ctr, 0, Nn * sizeof(uint64_t));
     memset(s->node_err, 0, Nn * sizeof(int));
     s->error = 0;
     s->events_index = 0;
@@ -922,6 +934,7 @@ static int rep_alloc(rep *s, int Nn, int Nc, int Nt, int Nd)
     s->t_time = malloc((size_t) Nn * sizeof(double) + 8);
     s->update_node = malloc((size_t) Nn * sizeof(int) + 4);
     s->ctr = malloc((size_t) Nn * sizeof(uint64_t) + 8);
+    s->crn_ctr = malloc((size_t) Nn * sizeof(uint64_t) + 8);
     s->node_err = malloc((size_t) Nn * sizeof(int) + 4);
     s->node_err_time = malloc((size_t) Nn * sizeof(double) + 8);
     s->node_err_rate = malloc((size_t) Nn * sizeof(double) + 8);
@@ -931,14 +944,14 @@ static int rep_alloc(rep *s, int Nn, int Nc, int Nt, int Nd)
     s->react_inf = malloc((size_t) Nn * Nt * sizeof(double) + 8);
     s->react_ctr = malloc((size_t) Nn * Nt * sizeof(uint64_t) + 8);
     return (s->react_time && s->react_inf && s->react_ctr && s->u && s->v && s->v_new && s->t_rate && s->sum_t_rate && s->t_time &&
-            s->update_node && s->ctr && s->node_err && s->node_err_time &&
+            s->update_node && s->ctr && s->crn_ctr && s->node_err && s->node_err_time &&
             s->node_err_rate && s->node_err_tr && s->individuals) ? 0 : -1;
 }
 
 static void rep_free(rep *s)
 {
     free(s->u); free(s->v); free(s->v_new); free(s->t_rate); free(s->sum_t_rate);
-    free(s->t_time); free(s->update_node); free(s->ctr); free(s->node_err);
+    free(s->t_time); free(s->update_node); free(s->ctr); free(s->crn_ctr); free(s->node_err);
     free(s->node_err_time); free(s->node_err_rate); free(s->node_err_tr);
     free(s->individuals);
     free(s->react_time); free(s->react_inf); free(s->react_ctr);
@@ -977,6 +990,9 @@ static int oracle_run_impl(const siminf_gpu_solver_args *args, const char *model
         return SIMINF_GPU_ERR_UNKNOWN_SOLVER;
     if (c.aem && args->Nrep > 1)
         return SIMINF_GPU_ERR_AEM_REPLICATED_MODEL;  /* src/SimInf.c:393-396 */
+    /* crn selects SimInf_run_solver_mssm_crn for replicated models only
+     * (src/SimInf.c:385-389) */
+    c.crn = !c.aem && args->Nrep > 1 && args->crn == 1;
 #ifdef _OPENMP
     if (nthreads > 0)
         omp_set_num_threads(nthreads);
@@ -1104,6 +1120,17 @@ static int pf_resample(const double *w, int n, double unif, int *idx)
         idx[i] = j;
         u += du;
     }
+    return 0;
+}
+
+/* pf_resample on its own, with one-based ancestors as the reference's
+ * function returns them; -1 on invalid weights. */
+int oracle_systematic_resampling(const double *w, int n, double unif, int *idx)
+{
+    if (pf_resample(w, n, unif, idx))
+        return -1;
+    for (int i = 0; i < n; i++)
+        idx[i] += 1;
     return 0;
 }
 

@@ -941,6 +941,11 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     if (!rc) rc = dalloc(&s.sum_rate, (size_t) Ntot, own);
     if (!rc) rc = dalloc(&s.t_time, (size_t) Ntot, own);
     if (!rc) rc = dalloc(&s.ctr, (size_t) Ntot, own);
+    /* crn = 1 selects SimInf_run_solver_mssm_crn for replicated models
+     * (src/SimInf.c:385-389): the SSA draws from a stream of its own */
+    s.crn_ctr = nullptr;
+    if (!rc && a->crn == 1 && Nrep > 1 && a->solver == 0)
+        rc = dalloc(&s.crn_ctr, (size_t) Ntot, own);
     if (!rc) rc = dalloc(&s.update, (size_t) Ntot, own);
     if (!rc) rc = dalloc(&s.err, (size_t) MAX_ERR, own);
     if (!rc) rc = dalloc(&s.err_count, 3, own);

@@ -828,6 +828,8 @@ __device__ __forceinline__ int init_node(const DevState &s, long long g, double 
     s.sum_rate[g] = sum;
     s.t_time[g] = tt0;
     s.ctr[g] = 0;
+    if (s.crn_ctr)
+        s.crn_ctr[g] = 0;
     s.update[g] = 0;
     return heavy_class<M>(s, sum);
 }
@@ -850,7 +852,15 @@ __device__ __forceinline__ void node_finish(const DevState &s, SsaLane<M> &ln, s
                                             unsigned long long &fired)
 {
     constexpr int NC = M::NC, NT = M::NT;
-    r.ctr = ln.c;
+    if (s.crn_ctr) {
+        /* common random numbers: the day's SSA draws came from the SSA's
+         * own stream; the events draw from the node's */
+        s.crn_ctr[g] = ln.c;
+        r.s1 &= ~SI_CRN_S1;
+        r.ctr = s.ctr[g];
+    } else {
+        r.ctr = ln.c;
+    }
     r.have = 0;
     fired += ln.fired;
     if (s.day_max && ln.fired > *(volatile unsigned *) (s.day_max + day))
@@ -890,12 +900,14 @@ __global__ void __launch_bounds__(256) k_quick(DevState s, int day, double tt, d
     if (g < s.Ntot && load_flag(s.err_day) >= day && s.heavy_mark[g] != day + 1 &&
         !job_over(s, g, day)) {
         const double sum = s.sum_rate[g], t = s.t_time[g];
-        uint64_t c = s.ctr[g];
+        uint64_t c = s.crn_ctr ? s.crn_ctr[g] : s.ctr[g];
         si_rng r;
         {
             uint64_t seed, sid;
             stream_key(s, g, seed, sid);
             si_rng_init(&r, seed, sid, 0);
+            if (s.crn_ctr)
+                r.s1 |= SI_CRN_S1;      /* the SSA's own stream */
         }
         int err = 0;
         if (!si_finite_pos(sum)) {
@@ -912,6 +924,13 @@ __global__ void __launch_bounds__(256) k_quick(DevState s, int day, double tt, d
                 listed = true;
         }
         if (!listed) {
+            if (s.crn_ctr) {
+                /* the SSA stream's counter is done for the day; c becomes
+                 * the node stream's, which the events draw from */
+                s.crn_ctr[g] = c;
+                c = s.ctr[g];
+                r.s1 &= ~SI_CRN_S1;
+            }
             if (err) {
                 record_error(s, err, PHASE_SSA, day, g, -1, -1, t, sum);
             } else {
@@ -1058,11 +1077,13 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
                     uint64_t seed, sid;
                     stream_key(s, g, seed, sid);
                     si_rng_init(&r, seed, sid, 0);
+                    if (s.crn_ctr)
+                        r.s1 |= SI_CRN_S1;      /* the SSA's own stream */
                 }
                 v = s.vA + g * ND;
                 ld = s.ldata + (size_t) node * s.Nld;
                 gd = gdata_of(s, g);
-                done = ssa_begin<M>(ln, r, s.ctr[g], next);
+                done = ssa_begin<M>(ln, r, s.crn_ctr ? s.crn_ctr[g] : s.ctr[g], next);
                 need = false;
             }
         }
@@ -1750,10 +1771,18 @@ __global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s,
         ln.t = s.t_time[g];
         ln.dc = si_recip_none();
         si_rng r;
+        uint64_t c_other = 0;       /* common random numbers: the other stream's counter */
         {
             uint64_t seed, sid;
             stream_key(s, g, seed, sid);
-            si_rng_init(&r, seed, sid, s.ctr[g]);
+            if (s.crn_ctr) {
+                /* r holds the SSA's own stream; the events switch to the node's */
+                si_rng_init(&r, seed, sid, s.crn_ctr[g]);
+                r.s1 |= SI_CRN_S1;
+                c_other = s.ctr[g];
+            } else {
+                si_rng_init(&r, seed, sid, s.ctr[g]);
+            }
         }
         double *v = s.vA + g * ND, *vn = s.vB + g * ND;
         const double *ld = s.ldata + (size_t) node * s.Nld;
@@ -1772,7 +1801,21 @@ __global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s,
                 break;
             }
             int e_code = 0, e_idx = -1;
+            if (s.crn_ctr) {
+                const uint64_t t = r.ctr;   /* to the node's stream */
+                r.ctr = c_other;
+                c_other = t;
+                r.s1 ^= SI_CRN_S1;
+                r.have = 0;
+            }
             bool upd = node_e1<NC>(s, ln.u, node, d, r, g, di.tt, e_code, e_idx);
+            if (s.crn_ctr) {
+                const uint64_t t = r.ctr;   /* back to the SSA's */
+                r.ctr = c_other;
+                c_other = t;
+                r.s1 ^= SI_CRN_S1;
+                r.have = 0;
+            }
             if (e_code) {
                 record_error(s, e_code, PHASE_E1, d, g, -1, e_idx, di.tt, 0);
                 break;
@@ -1811,7 +1854,12 @@ __global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s,
             s.t_rate[(size_t) k * s.Ntot + g] = ln.rate[k];
         s.sum_rate[g] = ln.sum;
         s.t_time[g] = ln.t;
-        s.ctr[g] = r.ctr;
+        if (s.crn_ctr) {
+            s.crn_ctr[g] = r.ctr;
+            s.ctr[g] = c_other;
+        } else {
+            s.ctr[g] = r.ctr;
+        }
     }
     add_fired(s, fired);
 }

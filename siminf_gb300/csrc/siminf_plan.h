@@ -110,6 +110,11 @@ struct DevState {
     double *t_rate, *sum_rate, *t_time;
     uint64_t *ctr;
     uint8_t *update;
+    /* common random numbers (mssm_crn, replicated models): the SSA draws of
+     * node g come from stream SI_CRN_SID | g, whose next draw index is
+     * crn_ctr[g]; ctr[g] then counts the draws of its events only.
+     * nullptr: the SSA and the events share stream g. */
+    uint64_t *crn_ctr;
 
     /* events */
     const int *e1_ptr;

@@ -163,7 +163,16 @@ SI_HD void si_philox4x32_10(uint32_t *c0, uint32_t *c1, uint32_t *c2,
 
 /* Draw i of stream sid under seed is word (i & 3) of
  * Philox4x32-10(counter = {i >> 2 (64 bits), sid (64 bits)},
- *               key = seed (64 bits)). */
+ *               key = seed (64 bits)).
+ *
+ * Stream ids: node g = replicate * Nn + node draws from sid g; with common
+ * random numbers (mssm_crn) its SSA draws come from sid SI_CRN_SID | g
+ * instead, so that they do not shift when its events draw; the
+ * all-events method's transition j uses 2^63 | (g * Nt + j) and particle
+ * filter interval i resamples from 2^62 + i.  SI_CRN_SID only sets bits
+ * of the high word s1. */
+#define SI_CRN_SID (3ULL << 61)
+#define SI_CRN_S1 ((uint32_t) (SI_CRN_SID >> 32))
 typedef struct si_rng {
     uint32_t k0, k1;            /* seed */
     uint32_t s0, s1;            /* stream id */

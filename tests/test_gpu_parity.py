@@ -190,22 +190,34 @@ def test_gpu_heavy_queue_matches_oracle(gpu, oracle_lib, label, m, heavy_rate, t
     assert np.array_equal(h.V, ho.V), label
 
 
-def test_gpu_crn_option_same_streams(gpu):
-    """crn = 1 (SimInf_run_solver_mssm_crn, one generator per replicate and
-    node) is what every run here does already: each (replicate, node) draws
-    from its own stream, so crn = 1 and crn = 0 give the same trajectories."""
+@pytest.mark.parametrize("name", ["sir_mparse_rep7", "seir_events_rep5"])
+@pytest.mark.parametrize("heavy_rate,two_pass", [(-1, -1), (1, 1), (1, -1)])
+def test_gpu_crn_matches_oracle(gpu, oracle_lib, name, heavy_rate, two_pass):
+    """crn = 1 on a replicated model (SimInf_run_solver_mssm_crn,
+    src/solvers/SimInf_solver_mssm_crn.c:185,196): the SSA draws from a
+    stream per (replicate, node) of its own, the events from the node's
+    stream.  Bit-exact with the oracle, which equals the reference's
+    mssm_crn compiled unmodified, on the whole-horizon kernel (no external
+    transfers) and the work queue in every layout; different from crn = 0."""
     import ctypes as C
+    from oracle import oracle
     from siminf_gb300 import abi, native
-    label, m = [c for c in parity_cases() if c[0] == "seir_events_rep5"][0]
-    out = []
-    for crn in (0, 1):
-        h = abi.build_args(m, 42)
-        h.args.crn = crn
-        code = native.lib().siminf_gpu_run_solver_mssm(C.cast(h.ref(), C.c_void_p),
-                                                       native.device_model(m.name).handle)
-        assert code == 0
-        out.append(h.U.copy())
-    assert np.array_equal(out[0], out[1])
+    m = dict(parity_cases())[name]
+    ho = abi.build_args(m, 42)
+    ho.args.crn = 1
+    assert oracle.run(ho, m.name, 4)[0] == 0
+    h = abi.build_args(m, 42)
+    h.args.crn = 1
+    opt = abi.Options(heavy_rate=heavy_rate, two_pass=two_pass)
+    code = native.lib().siminf_gpu_run_solver_ex(C.cast(h.ref(), C.c_void_p),
+                                                 native.device_model(m.name).handle,
+                                                 C.byref(opt))
+    assert code == 0
+    assert np.array_equal(h.U, ho.U)
+    h0 = abi.build_args(m, 42)
+    assert native.lib().siminf_gpu_run_solver_mssm(C.cast(h0.ref(), C.c_void_p),
+                                                   native.device_model(m.name).handle) == 0
+    assert not np.array_equal(h0.U, h.U)
 
 
 def test_gpu_autotune_keeps_results(gpu):

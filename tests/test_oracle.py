@@ -44,6 +44,29 @@ def test_oracle_matches_reference_on_balanced_headline_sample(oracle_lib):
     assert res.transitions > 100_000 and res.e2_events == 120 * 25_000
 
 
+@needs_ref
+@pytest.mark.parametrize("name", ["sir_mparse_rep7", "seir_events_rep5"])
+def test_oracle_crn_matches_reference(oracle_lib, name):
+    """crn = 1 on a replicated model runs the reference's mssm_crn solver
+    (src/solvers/SimInf_solver_mssm_crn.c): the SSA draws come from a
+    generator per (replicate, node), the events from the node's stream.
+    The oracle equals it bit for bit, and differs from crn = 0."""
+    from siminf_gb300 import abi
+    m = dict(parity_cases())[name]
+    out = {}
+    for crn in (0, 1):
+        ho = abi.build_args(m, 42)
+        ho.args.crn = crn
+        code_o, res = oracle.run(ho, m.name, 3)
+        hr = abi.build_args(m, 42)
+        hr.args.crn = crn
+        code_r = oracle.run_ref(hr, m.name, 3)
+        assert code_o == code_r == 0
+        assert np.array_equal(ho.U, hr.U)
+        out[crn] = ho.U.copy()
+    assert not np.array_equal(out[0], out[1])
+
+
 def test_oracle_thread_count_invariance(oracle_lib):
     for label, m in parity_cases()[:4]:
         _, _, h1 = run_oracle(m, threads=1)
