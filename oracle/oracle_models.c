@@ -271,6 +271,69 @@ static int pf_pts(double *v_new, const int *u, const double *v,
     return v[0] != v_new[0];
 }
 
+/* src/misc/SimInf_local_spread.c:43-71: neighbours' contribution to phi
+ * of node i; neighbors is (index, distance) pairs ended by index -1, phi
+ * and u point at the first node. */
+static double local_spread(const double *neighbors, const double *phi, const int *u,
+                           double N_i, double phi_i, int Nc, double D)
+{
+    double ls = 0.0;
+    const double phi_i_N_i = phi_i * N_i;
+    for (int j = (int) neighbors[0]; j >= 0; j = (int) neighbors[0]) {
+        double N_j = 0;
+        for (int k = j * Nc; k < (j + 1) * Nc; k++)
+            N_j += u[k];
+        if (N_j > 0.0)
+            ls += ((phi[j] * N_j - phi_i_N_i) * D) / (N_i * neighbors[1]);
+        neighbors += 2;
+    }
+    return ls;
+}
+
+/* SISe_sp, src/models/SISe_sp.c:108-160: the SISe rates; the post time
+ * step adds the local spread from the neighbours after end_t1..end_t4 in
+ * ldata; gdata = (upsilon, gamma, alpha, beta_t1..beta_t4, coupling).  It
+ * reads other nodes through offsets from its own node's u and v. */
+static int sise_sp_pts(double *v_new, const int *u, const double *v,
+                       const double *ldata, const double *gdata, int node, double t)
+{
+    const int day = (int) t % 365;
+    const double I_i = u[1];
+    const double N_i = u[0] + I_i;
+    const double phi = v[0];
+    v_new[0] = decay(phi, day, (int) ldata[0], (int) ldata[1], (int) ldata[2],
+                     (int) ldata[3], gdata[3], gdata[4], gdata[5], gdata[6]);
+    if (N_i > 0.0)
+        v_new[0] += gdata[2] * I_i / N_i +
+                    local_spread(&ldata[4], &v[-node], &u[-2 * node], N_i, phi, 2, gdata[7]);
+    if (!isfinite(v_new[0]))
+        return -7;
+    if (v_new[0] < 0.0)
+        return -10;
+    return phi != v_new[0];
+}
+
+/* SISe3_sp, src/models/SISe3_sp.c:207-255: the SISe3 rates with the local
+ * spread; gdata = (upsilon_1..3, gamma_1..3, alpha, beta_t1..4, coupling). */
+static int sise3_sp_pts(double *v_new, const int *u, const double *v,
+                        const double *ldata, const double *gdata, int node, double t)
+{
+    const int day = (int) t % 365;
+    const double I_i = u[1] + u[3] + u[5];
+    const double N_i = u[0] + u[2] + u[4] + I_i;
+    const double phi = v[0];
+    v_new[0] = decay(phi, day, (int) ldata[0], (int) ldata[1], (int) ldata[2],
+                     (int) ldata[3], gdata[7], gdata[8], gdata[9], gdata[10]);
+    if (N_i > 0.0)
+        v_new[0] += gdata[6] * I_i / N_i +
+                    local_spread(&ldata[4], &v[-node], &u[-6 * node], N_i, phi, 6, gdata[11]);
+    if (!isfinite(v_new[0]))
+        return -7;
+    if (v_new[0] < 0.0)
+        return -10;
+    return phi != v_new[0];
+}
+
 static const oracle_model models[] = {
     {"SIR", 3, 2, 0, {sir_s_to_i, sir_i_to_r}, pts_none},
     {"SEIR", 4, 3, 0, {seir_s_to_e, seir_e_to_i, seir_i_to_r}, pts_none},
@@ -279,12 +342,50 @@ static const oracle_model models[] = {
     {"SISe3", 6, 6, 1, {sise3_s1, sise3_i1, sise3_s2, sise3_i2, sise3_s3, sise3_i3}, sise3_pts},
     {"SIR_mparse", 3, 2, 0, {mp_sir_1, mp_sir_2}, pts_none},
     {"SISe_pf", 2, 2, 1, {pf_s_to_i, pf_i_to_s}, pf_pts},
+    {"SISe_sp", 2, 2, 1, {sise_s_to_i, sise_i_to_s}, sise_sp_pts},
+    {"SISe3_sp", 6, 6, 1, {sise3_s1, sise3_i1, sise3_s2, sise3_i2, sise3_s3, sise3_i3},
+     sise3_sp_pts},
 };
+
+/* Models registered at run time: host builds of generated model code,
+ * whose rate and post-time-step functions the test suite hands over. */
+enum { MAX_REGISTERED = 64 };
+static oracle_model registered[MAX_REGISTERED];
+static char registered_names[MAX_REGISTERED][64];
+static int n_registered;
+
+int oracle_register_model(const char *name, int Nc, int Nt, int Nd, const oracle_trfun *tr,
+                          oracle_ptsfun pts)
+{
+    if (Nt < 1 || Nt > 32 || strlen(name) >= 64)
+        return -1;
+    int k = 0;
+    while (k < n_registered && strcmp(registered_names[k], name) != 0)
+        k++;
+    if (k == n_registered) {
+        if (n_registered == MAX_REGISTERED)
+            return -1;
+        n_registered++;
+    }
+    strcpy(registered_names[k], name);
+    oracle_model *m = &registered[k];
+    m->name = registered_names[k];
+    m->Nc = Nc;
+    m->Nt = Nt;
+    m->Nd = Nd;
+    for (int j = 0; j < 32; j++)
+        m->tr[j] = j < Nt ? tr[j] : NULL;
+    m->pts = pts;
+    return 0;
+}
 
 const oracle_model *oracle_model_lookup(const char *name)
 {
     for (size_t i = 0; i < sizeof(models) / sizeof(models[0]); i++)
         if (strcmp(models[i].name, name) == 0)
             return &models[i];
+    for (int k = 0; k < n_registered; k++)
+        if (strcmp(registered_names[k], name) == 0)
+            return &registered[k];
     return NULL;
 }

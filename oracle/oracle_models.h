@@ -20,7 +20,7 @@ typedef int (*oracle_ptsfun)(double *v_new, const int *u, const double *v,
 typedef struct oracle_model {
     const char *name;
     int Nc, Nt, Nd;
-    oracle_trfun tr[8];
+    oracle_trfun tr[32];
     oracle_ptsfun pts;
 } oracle_model;
 

@@ -16,6 +16,8 @@ void shim_release(void);
 
 extern TRFun ref_SIR_tr[], ref_SEIR_tr[], ref_SIS_tr[], ref_SISe_tr[], ref_SISe3_tr[];
 extern PTSFun ref_SIR_pts, ref_SEIR_pts, ref_SIS_pts, ref_SISe_pts, ref_SISe3_pts;
+extern TRFun ref_SISe_sp_tr[], ref_SISe3_sp_tr[];
+extern PTSFun ref_SISe_sp_pts, ref_SISe3_sp_pts;
 
 _Static_assert(sizeof(SimInf_solver_args) == sizeof(siminf_gpu_solver_args),
                "siminf_gpu_solver_args must stay layout-identical to SimInf_solver_args");
@@ -23,7 +25,7 @@ _Static_assert(sizeof(SimInf_solver_args) == sizeof(siminf_gpu_solver_args),
 int ref_run(const siminf_gpu_solver_args *ga, const char *model, int threads)
 {
     SimInf_solver_args a;
-    TRFun tr[8];
+    TRFun tr[32];
     PTSFun pts;
     int Nt = ga->Nt;
 
@@ -37,13 +39,17 @@ int ref_run(const siminf_gpu_solver_args *ga, const char *model, int threads)
         memcpy(tr, ref_SISe_tr, 2 * sizeof(TRFun)); pts = ref_SISe_pts;
     } else if (strcmp(model, "SISe3") == 0) {
         memcpy(tr, ref_SISe3_tr, 6 * sizeof(TRFun)); pts = ref_SISe3_pts;
+    } else if (strcmp(model, "SISe_sp") == 0) {
+        memcpy(tr, ref_SISe_sp_tr, 2 * sizeof(TRFun)); pts = ref_SISe_sp_pts;
+    } else if (strcmp(model, "SISe3_sp") == 0) {
+        memcpy(tr, ref_SISe3_sp_tr, 6 * sizeof(TRFun)); pts = ref_SISe3_sp_pts;
     } else {
         /* mparse models have no source in the reference tree: use the
          * oracle's host versions of the generated code. */
         const oracle_model *m = oracle_model_lookup(model);
         if (!m)
             return -32;
-        for (int j = 0; j < Nt && j < 8; j++)
+        for (int j = 0; j < Nt && j < 32; j++)
             tr[j] = (TRFun) m->tr[j];
         pts = (PTSFun) m->pts;
     }

@@ -108,7 +108,9 @@ extern "C" int siminf_gpu_run_batch(siminf_gpu_batch_job *jobs, int njobs,
                             "a batch runs the ssm solver");
             rc = SIMINF_GPU_ERR_UNKNOWN_SOLVER;
         }
-        if (!rc && (a.Nrep != 1 || a.Nld != jobs[0].args->Nld))
+        /* a post-time-step that reads other nodes indexes them within its
+         * own model, which a batch's node numbering does not keep */
+        if (!rc && (a.Nrep != 1 || a.Nld != jobs[0].args->Nld || !L->pts_local))
             rc = SIMINF_GPU_ERR_INVALID_MODEL;
         if (rc) {
             snprintf(msg, sizeof(msg), "batch job %d: not a valid one-replicate model like job 0",

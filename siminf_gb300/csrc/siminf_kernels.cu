@@ -1245,7 +1245,11 @@ __device__ __forceinline__ int pts_node(const DevState &s, long long g, int day,
     double *vo = v_out + g * ND;
     const double *ld = s.ldata + (size_t) node * s.Nld;
     const double *gd = gdata_of(s, g);
-    const int rc = M::pts(vo, u, vi, ld, gd, node, tt);
+    /* a post-time-step function that reads other nodes (by offsets from
+     * its node, src/models/SISe_sp.c:127-134) gets the node's place in the
+     * replicate's arrays; every node's external transfers are done */
+    const int rc = M::PTS_LOCAL ? M::pts(vo, u, vi, ld, gd, node, tt)
+                                : M::pts(vo, s.u + g * NC, vi, ld, gd, node, tt);
     store_columns<NC, ND>(s, rep, node, u, vo, c0, c1);
     if (s.prev && c1 > c0)
         add_prevalence<NC>(s, g, u, c0, c1);
@@ -1701,7 +1705,8 @@ __device__ __forceinline__ int aem_pts_node(const DevState &s, long long g, int 
     double *vo = v_out + g * ND;
     const double *ld = s.ldata + (size_t) node * s.Nld;
     const double *gd = gdata_of(s, g);
-    const int rc = M::pts(vo, a.u, vi, ld, gd, node, tt);
+    const int rc = M::PTS_LOCAL ? M::pts(vo, a.u, vi, ld, gd, node, tt)
+                                : M::pts(vo, s.u + g * NC, vi, ld, gd, node, tt);
     store_columns<NC, ND>(s, rep, node, a.u, vo, c0, c1);
     if (rc < 0) {
         record_error(s, rc, PHASE_PTS, day, g, -1, -1, tt, 0);
@@ -2129,6 +2134,8 @@ const Launchers *launchers_for(const char *name)
         {"SISe3", Launch<ModelSISe3>::table},
         {"SIR_mparse", Launch<ModelSIRmparse>::table},
         {"SISe_pf", Launch<ModelSISePF>::table},
+        {"SISe_sp", Launch<ModelSISe_sp>::table},
+        {"SISe3_sp", Launch<ModelSISe3_sp>::table},
     };
     for (const Entry &e : entries) {
         const char *a = e.name, *b = name;

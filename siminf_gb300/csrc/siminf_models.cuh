@@ -218,6 +218,108 @@ struct ModelSISe3 {
     }
 };
 
+/* The spread of the environmental pressure phi from proximal nodes
+ * (src/misc/SimInf_local_spread.c:43-71): neighbors is the node's list of
+ * (index, distance) pairs ended by a negative index; phi and u point at
+ * the first node of the replicate, so the neighbours' current phi and
+ * compartments are read where every node of the replicate keeps them.
+ * Each neighbour j that holds individuals adds
+ * ((phi_j * N_j - phi_i * N_i) * D) / (N_i * distance), in list order. */
+__device__ __forceinline__ double local_spread(const double *neighbors, const double *phi,
+                                               const int *u, double N_i, double phi_i,
+                                               int Nc, double D)
+{
+    double ls = 0.0;
+    const double phi_i_N_i = phi_i * N_i;
+    int j = (int) neighbors[0];
+    while (j >= 0) {
+        double N_j = 0;
+        for (int k = j * Nc; k < (j + 1) * Nc; k++)
+            N_j += u[k];
+        if (N_j > 0.0)
+            ls += ((phi[j] * N_j - phi_i_N_i) * D) / (N_i * neighbors[1]);
+        neighbors += 2;
+        j = (int) neighbors[0];
+    }
+    return ls;
+}
+
+/* SISe_sp, src/models/SISe_sp.c:40-160: SISe whose post-time-step adds
+ * the local spread from the neighbours listed in ldata after end_t1..4.
+ * gdata = (upsilon, gamma, alpha, beta_t1..beta_t4, coupling), v = (phi).
+ * The post-time-step reads other nodes: u and v are the replicate's
+ * arrays at this node (PTS_LOCAL false), as in the reference. */
+struct ModelSISe_sp {
+    static constexpr int NC = 2, NT = 2, ND = 1;
+    static constexpr int NGD = 8;  /* gdata entries read */
+    static constexpr bool PTS_LOCAL = false;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
+                                                  const double *ldata, const double *gdata,
+                                                  double t, si_recip &dc)
+    {
+        if (k == 0)
+            return gdata[0] * v[0] * si_i2d(u[0]);
+        return gdata[1] * si_i2d(u[1]);
+    }
+    __device__ __forceinline__ static int pts(double *v_new, const int *u, const double *v,
+                                              const double *ldata, const double *gdata,
+                                              int node, double t)
+    {
+        const int day = (int) t % 365;
+        const double I_i = u[1];
+        const double N_i = u[0] + I_i;
+        const double phi = v[0];
+        v_new[0] = forward_euler_linear_decay(phi, day, (int) ldata[0], (int) ldata[1],
+                                              (int) ldata[2], (int) ldata[3], gdata[3],
+                                              gdata[4], gdata[5], gdata[6]);
+        if (N_i > 0.0)
+            v_new[0] += gdata[2] * I_i / N_i +
+                        local_spread(ldata + 4, v - node, u - 2 * node, N_i, phi, 2, gdata[7]);
+        if (!isfinite(v_new[0]))
+            return -7;          /* SIMINF_ERR_V_IS_NOT_FINITE */
+        if (v_new[0] < 0.0)
+            return -10;         /* SIMINF_ERR_V_IS_NEGATIVE */
+        return phi != v_new[0];
+    }
+};
+
+/* SISe3_sp, src/models/SISe3_sp.c:50-255: SISe3 with the local spread of
+ * SISe_sp.  gdata = (upsilon_1..3, gamma_1..3, alpha, beta_t1..beta_t4,
+ * coupling), ldata = (end_t1..end_t4, neighbours), v = (phi). */
+struct ModelSISe3_sp {
+    static constexpr int NC = 6, NT = 6, ND = 1;
+    static constexpr int NGD = 12;  /* gdata entries read */
+    static constexpr bool PTS_LOCAL = false;
+    static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
+                                                  const double *ldata, const double *gdata,
+                                                  double t, si_recip &dc)
+    {
+        return ModelSISe3::rate(k, u, v, ldata, gdata, t, dc);
+    }
+    __device__ __forceinline__ static int pts(double *v_new, const int *u, const double *v,
+                                              const double *ldata, const double *gdata,
+                                              int node, double t)
+    {
+        const int day = (int) t % 365;
+        const double I_i = u[1] + u[3] + u[5];
+        const double N_i = u[0] + u[2] + u[4] + I_i;
+        const double phi = v[0];
+        v_new[0] = forward_euler_linear_decay(phi, day, (int) ldata[0], (int) ldata[1],
+                                              (int) ldata[2], (int) ldata[3], gdata[7],
+                                              gdata[8], gdata[9], gdata[10]);
+        if (N_i > 0.0)
+            v_new[0] += gdata[6] * I_i / N_i +
+                        local_spread(ldata + 4, v - node, u - 6 * node, N_i, phi, 6, gdata[11]);
+        if (!isfinite(v_new[0]))
+            return -7;
+        if (v_new[0] < 0.0)
+            return -10;
+        return phi != v_new[0];
+    }
+};
+
 /* mparse SIR (R/C-generator.R:204-247 output for "S -> beta*S*I/N -> I",
  * "I -> gamma*I -> R", N <- S+I+R); gdata = (beta, gamma). */
 struct ModelSIRmparse {

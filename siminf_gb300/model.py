@@ -171,6 +171,98 @@ def SISe3(u0, tspan, phi, upsilon_1, upsilon_2, upsilon_3, gamma_1, gamma_2, gam
                        E=E, N=N, events=events)
 
 
+def distance_matrix(x, y, cutoff, min_dist=None):
+    """Euclidean distances between the nodes at (x, y) that are at most
+    cutoff apart, as the reference's distance_matrix() builds them
+    (src/misc/SimInf_distance_matrix.c:24-83): a CSC matrix (i, p, d) whose
+    column j lists node j's neighbours in node order; coincident nodes get
+    min_dist, which must then be given and > 0."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    n = len(x)
+    if n < 1 or len(y) != n:
+        raise ValueError("'x' and 'y' must be numeric vectors of one length > 0.")
+    if not np.isfinite(cutoff) or cutoff < 0:
+        raise ValueError("'cutoff' must be > 0.")
+    ii, pp, dd = [], [0], []
+    for col in range(n):
+        d = np.hypot(x[col] - x, y[col] - y)
+        if not np.isfinite(d).all():
+            raise ValueError("Invalid distance for i=%d." % col)
+        rows = np.nonzero(d <= cutoff)[0]
+        rows = rows[rows != col]
+        dist = d[rows]
+        if (dist <= 0).any():
+            if min_dist is None or not np.isfinite(min_dist) or min_dist < 0:
+                raise ValueError("Invalid 'min_dist' argument. Please provide 'min_dist' > 0.")
+            dist = np.where(dist <= 0, min_dist, dist)
+        ii.extend(rows.tolist())
+        dd.extend(dist.tolist())
+        pp.append(len(ii))
+    return (np.array(ii, dtype=np.int32), np.array(pp, dtype=np.int32),
+            np.array(dd, dtype=np.float64))
+
+
+def ldata_sp(data, distance, metric=1):
+    """Local data with the spatial coupling appended, as SimInf_ldata_sp
+    packs it (src/misc/SimInf_ldata.c:50-135): for each node its rows of
+    data, then (neighbour index, value) pairs and a (-1, 0) stop pair, zero
+    padded to the longest list.  value is the neighbour's degree (metric
+    0), the distance (1) or 1 / distance^2 (2)."""
+    data = np.asarray(data, dtype=np.float64)
+    if data.ndim == 1:
+        data = data.reshape(-1, 1)
+    ir, jc, d = distance
+    n = data.shape[1]
+    if len(jc) - 1 != n:
+        raise ValueError("The number of nodes in 'data' and 'distance' are not equal.")
+    degree = np.diff(jc)
+    nld = data.shape[0] + (int(degree.max(initial=0)) + 1) * 2
+    out = np.zeros((nld, n))
+    out[:data.shape[0], :] = data
+    for node in range(n):
+        k = data.shape[0]
+        for e in range(jc[node], jc[node + 1]):
+            out[k, node] = ir[e]
+            out[k + 1, node] = (degree[ir[e]] if metric == 0 else
+                                d[e] if metric == 1 else 1.0 / (d[e] * d[e]))
+            k += 2
+        out[k, node] = -1.0
+    return out
+
+
+def SISe_sp(u0, tspan, phi, upsilon, gamma, alpha, beta_t1, beta_t2, beta_t3, beta_t4,
+            end_t1, end_t2, end_t3, end_t4, coupling, distance, events=None):
+    """R/SISe_sp.R:139-183: SISe whose environmental pressure spreads to
+    proximal nodes; ldata = end_t1..end_t4 then the neighbours (distances)
+    of ldata_sp(metric 1), gdata = upsilon, gamma, alpha, beta_t1..beta_t4,
+    coupling.  distance is the (i, p, x) of distance_matrix()."""
+    u0 = _u0(u0, ("S", "I"))
+    n = u0.shape[1]
+    G = np.ones((2, 2), dtype=np.int32)
+    S = np.array([[-1, 1], [1, -1]], dtype=np.int32)
+    E = np.array([[1, 1], [0, 1]], dtype=np.float64)
+    ldata = ldata_sp(_rep_ldata(n, end_t1, end_t2, end_t3, end_t4), distance, 1)
+    gdata = np.array([upsilon, gamma, alpha, beta_t1, beta_t2, beta_t3, beta_t4, coupling],
+                     dtype=np.float64)
+    v0 = np.broadcast_to(np.asarray(phi, dtype=np.float64), (n,)).reshape(1, n)
+    return SimInfModel("SISe_sp", G, S, u0, tspan, v0=v0, ldata=ldata, gdata=gdata,
+                       E=E, events=events)
+
+
+def SISe3_sp(u0, tspan, phi, upsilon_1, upsilon_2, upsilon_3, gamma_1, gamma_2, gamma_3,
+             alpha, beta_t1, beta_t2, beta_t3, beta_t4, end_t1, end_t2, end_t3, end_t4,
+             coupling, distance, events=None):
+    """R/SISe3_sp.R: SISe3 with the spatial coupling of SISe_sp; gdata =
+    upsilon_1..3, gamma_1..3, alpha, beta_t1..beta_t4, coupling."""
+    m = SISe3(u0, tspan, phi, upsilon_1, upsilon_2, upsilon_3, gamma_1, gamma_2, gamma_3,
+              alpha, beta_t1, beta_t2, beta_t3, beta_t4, end_t1, end_t2, end_t3, end_t4,
+              coupling, events=events)
+    return SimInfModel("SISe3_sp", m.G, m.S, m.u0, tspan, v0=m.v0,
+                       ldata=ldata_sp(m.ldata, distance, 1), gdata=m.gdata, E=m.E, N=m.N,
+                       events=events)
+
+
 def SIR_mparse(u0, tspan, beta, gamma, events=None):
     """mparse(transitions = c("S -> beta*S*I/N -> I", "I -> gamma*I -> R",
     "N <- S+I+R"), compartments = c("S","I","R"), gdata = c(beta, gamma)).
@@ -211,5 +303,6 @@ def _u0(u0, names):
 
 
 __all__ = ["SimInfModel", "SIR", "SEIR", "SIS", "SISe", "SISe3", "SIR_mparse", "SISe_pf",
+           "SISe_sp", "SISe3_sp", "distance_matrix", "ldata_sp",
            "make_events", "empty_events", "EXIT_EVENT", "ENTER_EVENT",
            "INTERNAL_TRANSFER_EVENT", "EXTERNAL_TRANSFER_EVENT"]

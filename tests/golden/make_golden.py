@@ -273,6 +273,24 @@ def main(ref):
         "tol": 1e-8,
     }
 
+    # tests/ldata_sp.R: the distance matrix of (1..10, 1..10) with cutoff 3
+    # and the spatial ldata (end_t1..end_t4, then neighbour pairs) packed
+    # with each metric.
+    ls = read("ldata_sp.R")
+    fixtures["ldata_sp.json"] = {
+        "source": "tests/ldata_sp.R:34-66,147-226",
+        "x": list(range(1, 11)), "y": list(range(1, 11)), "cutoff": 3,
+        "end_t": [91, 182, 273, 365],
+        "d_i": r_vector(after(ls, 40, r"^d <- new\(")),
+        "d_p": r_vector(after(ls, 40, r"^\s+p = c\(")),
+        "d_x": r_vector(after(ls, 40, r"^\s+x = c\(")),
+        "ldata_degree": r_vector(after(ls, 145, r"^ldata_exp <- structure\(")),
+        "ldata_distance": r_vector(after(ls, 160, r"^ldata_exp <- structure\(")),
+        "ldata_inverse_square": r_vector(after(ls, 196, r"^ldata_exp <- structure\(")),
+        "dim": [14, 10],
+        "tol": 1e-8,
+    }
+
     ie = read("individual_events.R")
     fixtures["individual_events.json"] = {
         "source": "tests/individual_events.R:199-690,1222-1256",

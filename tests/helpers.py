@@ -215,4 +215,26 @@ def parity_cases():
     sis.N = np.array([[1], [0]], dtype=np.int32)
     sis.E = np.array([[1, 2], [0, 1]], dtype=np.float64)
     cases.append(("sis_shift_weighted", sis))
+    # spatial coupling: phi spreads between the nodes of a 12 x 12 grid
+    # within distance 1.5 (up to eight neighbours), with external
+    # transfers, so each post time step reads neighbours after the day's
+    # transfers; replicated, so the neighbours sit in the replicate's block
+    gx, gy = np.meshgrid(np.arange(12.0), np.arange(12.0))
+    dist = M.distance_matrix(gx.ravel(), gy.ravel(), 1.5)
+    n = 144
+    u0 = {"S": rng.poisson(200, n), "I": rng.poisson(2, n) * (rng.random(n) < 0.3)}
+    sp = M.SISe_sp(u0, np.arange(1, 91), phi=rng.uniform(0, 0.2, n), upsilon=0.015,
+                   gamma=0.1, alpha=0.8, beta_t1=0.19, beta_t2=0.085, beta_t3=0.075,
+                   beta_t4=0.185, end_t1=91, end_t2=182, end_t3=273, end_t4=365,
+                   coupling=0.05, distance=dist,
+                   events=random_events(rng, n, 90, n_e2=20, n_e2_prop=2))
+    cases.append(("sise_sp_grid_events", sp))
+    cases.append(("sise_sp_grid_rep3", sp.replicate(3)))
+    u0 = {k: rng.poisson(15, n) * (1 if k.startswith("S") else (rng.random(n) < 0.3))
+          for k in ("S_1", "I_1", "S_2", "I_2", "S_3", "I_3")}
+    cases.append(("sise3_sp_grid", M.SISe3_sp(
+        u0, np.arange(1, 61), phi=0.05, upsilon_1=0.01, upsilon_2=0.02, upsilon_3=0.03,
+        gamma_1=0.1, gamma_2=0.12, gamma_3=0.14, alpha=1.0, beta_t1=0.19, beta_t2=0.085,
+        beta_t3=0.075, beta_t4=0.185, end_t1=91, end_t2=182, end_t3=273, end_t4=365,
+        coupling=0.02, distance=dist)))
     return cases

@@ -24,7 +24,7 @@ def test_gpu_matches_oracle(gpu, oracle_lib, label, m):
 
 @pytest.mark.parametrize("seed", [1, 2, 3, 1234567, 2 ** 40 + 5])
 def test_gpu_seeds(gpu, oracle_lib, seed):
-    label, m = parity_cases()[-3]          # SEIR with all event kinds
+    m = dict(parity_cases())["seir_events_300x120"]     # SEIR with all event kinds
     _, _, ho = run_oracle(m, seed=seed, threads=4)
     code, hg, _ = run_gpu(m, seed=seed)
     assert code == 0 and np.array_equal(hg.U, ho.U)
