@@ -146,6 +146,21 @@ typedef struct siminf_gpu_model siminf_gpu_model;
  */
 int siminf_gpu_model_builtin(const char *name, siminf_gpu_model **out);
 
+/*
+ * A device model compiled from model C code: the mparse output of
+ * R/C-generator.R:204-297 (trFun1..trFunK and ptsFun) or a hand-written
+ * model file with TRFun/PTSFun functions (inst/include/SimInf.h:92-107),
+ * whose functions were compiled for the GPU with their signatures
+ * unchanged into a library of their own (siminf_gb300/devmodel.py does it
+ * with nvcc, caching the library by a digest of the C code as
+ * R/run.R:93-98 caches the host build).  Replaces the dyn.load of the
+ * compiled model in R/run.R:22-98 that SimInf_run then calls through
+ * tr_fun/pts_fun.  path names that library; it stays loaded until the
+ * process exits.  Returns 0 or SIMINF_GPU_ERR_UNKNOWN_MODEL (not found, or
+ * built against another version of this library).
+ */
+int siminf_gpu_model_load(const char *path, siminf_gpu_model **out);
+
 /* Number of transitions (Nt), compartments (Nc) and continuous state
  * variables (Nd) the model expects; any pointer may be NULL. */
 int siminf_gpu_model_dims(const siminf_gpu_model *model, int *Nc, int *Nt, int *Nd);

@@ -118,6 +118,59 @@ def run_ref(holder, model_name, threads=1, independent=False):
         lib_.shim_set_independent(0)
 
 
+MODELS_DIR = os.path.join(HERE, "_models")
+SHIM_DIR = os.path.join(HERE, "model_shim")
+_model_libs = []
+
+
+def register_c_model(name, c_code, Nc, Nt, Nd):
+    """Build model C code on the host with gcc, as R CMD SHLIB builds it for
+    the reference (R/run.R:22-73), against the stub R headers of
+    model_shim/include, and register its rate and post-time-step functions
+    under `name` with the oracle and, when built, with oracle/_ref, so that
+    run()/run_ref() can run the model."""
+    import hashlib
+    import re
+    key = hashlib.sha256(c_code.encode()).hexdigest()[:16]
+    os.makedirs(MODELS_DIR, exist_ok=True)
+    src = os.path.join(MODELS_DIR, "model_%s.c" % key)
+    so = os.path.join(MODELS_DIR, "model_%s.so" % key)
+    if not os.path.exists(so):
+        with open(src, "w") as f:
+            f.write(c_code)
+        m = re.search(r"(\w+)\s*\(\s*SEXP\s+\w+\s*,\s*SEXP\s+\w+\s*\)\s*\{", c_code)
+        if not m:
+            raise ValueError("model code without a run function")
+        wrap = os.path.join(MODELS_DIR, "capture_%s.c" % key)
+        with open(wrap, "w") as f:
+            f.write('#include "model_%s.c"\n'
+                    "int shim_model_capture(SEXP (*)(SEXP, SEXP), int, TRFun *, PTSFun *);\n"
+                    "int shim_model_entry(int nt, TRFun *tr, PTSFun *pts)\n"
+                    "{\n    return shim_model_capture(&%s, nt, tr, pts);\n}\n"
+                    % (key, m.group(1)))
+        tmp = so + ".%d.tmp" % os.getpid()
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11",
+                               "-ffp-contract=off", "-w", "-I", os.path.join(SHIM_DIR, "include"),
+                               "-DSIMINF_MODEL_RUN=shim_model_run",
+                               "-DSIMINF_R_INIT=R_init_shim_model",
+                               "-DSIMINF_FORCE_SYMBOLS=FALSE", wrap,
+                               os.path.join(SHIM_DIR, "model_shim.c"), "-o", tmp, "-lm"])
+        os.replace(tmp, so)
+    mlib = C.CDLL(so)
+    _model_libs.append(mlib)
+    tr = (C.c_void_p * 32)()
+    pts = C.c_void_p()
+    if mlib.shim_model_entry(Nt, tr, C.byref(pts)) != 0:
+        raise ValueError("the model code's run function passed no post-time-step function")
+    targets = [lib()] + ([ref_lib()] if ref_available() else [])
+    for L in targets:
+        f = L.oracle_register_model
+        f.restype = C.c_int
+        f.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        if f(name.encode(), Nc, Nt, Nd, C.cast(tr, C.c_void_p), pts) != 0:
+            raise ValueError("could not register model %s" % name)
+
+
 def si_log(x):
     return lib().oracle_si_log(float(x))
 

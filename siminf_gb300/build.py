@@ -70,7 +70,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    subprocess.check_call([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+    subprocess.check_call([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-ldl"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -40,6 +40,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 
 #include "../../include/siminf_gb300.h"
 #include "siminf_capi_internal.h"
@@ -721,6 +722,36 @@ int siminf_gpu_model_builtin(const char *name, siminf_gpu_model **out)
         return SIMINF_GPU_ERR_ALLOC_MEMORY_BUFFER;
     snprintf(m->name, sizeof(m->name), "%s", name);
     m->L = L;
+    *out = m;
+    return 0;
+}
+
+int siminf_gpu_model_load(const char *path, siminf_gpu_model **out)
+{
+    if (!path || !out)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    /* The library stays loaded for the life of the process: its kernels
+     * may sit in plans, captured graphs and streams of any thread. */
+    void *h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+    if (!h) {
+        const char *why = dlerror();
+        set_status(SIMINF_GPU_ERR_UNKNOWN_MODEL, -1, -1, -1, 0, 0, why ? why : path);
+        return SIMINF_GPU_ERR_UNKNOWN_MODEL;
+    }
+    auto abi = (int (*)(void)) dlsym(h, "siminf_model_abi");
+    auto table = (const Launchers *(*)(void)) dlsym(h, "siminf_model_launchers");
+    if (!abi || !table || abi() != SIMINF_MODEL_ABI) {
+        char msg[300];
+        snprintf(msg, sizeof(msg), "%s: not a device model library of this build", path);
+        set_status(SIMINF_GPU_ERR_UNKNOWN_MODEL, -1, -1, -1, 0, 0, msg);
+        return SIMINF_GPU_ERR_UNKNOWN_MODEL;
+    }
+    siminf_gpu_model *m = (siminf_gpu_model *) calloc(1, sizeof(siminf_gpu_model));
+    if (!m)
+        return SIMINF_GPU_ERR_ALLOC_MEMORY_BUFFER;
+    const char *base = strrchr(path, '/');
+    snprintf(m->name, sizeof(m->name), "%s", base ? base + 1 : path);
+    m->L = table();
     *out = m;
     return 0;
 }

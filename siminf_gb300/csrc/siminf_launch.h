@@ -46,6 +46,14 @@ cudaError_t pf_gather(const int *U, const double *V, int tlen, long long nu, lon
 /* The launcher table of a built-in device model, or nullptr. */
 const Launchers *launchers_for(const char *name);
 
+/* A device model compiled from model C code into a library of its own
+ * (siminf_gb300/devmodel.py) exports its launcher table and this version
+ * as siminf_model_launchers() and siminf_model_abi(); the loader compares
+ * the version with its own, which changes whenever the table or the device
+ * state it passes changes layout. */
+#define SIMINF_MODEL_ABI \
+    (20261204 + (int) sizeof(siminf::DevState) + (int) sizeof(siminf::Launchers))
+
 }  // namespace siminf
 
 #endif

@@ -28,6 +28,8 @@ def lib():
     vp = C.c_void_p
     L.siminf_gpu_model_builtin.argtypes = [C.c_char_p, C.POINTER(vp)]
     L.siminf_gpu_model_builtin.restype = C.c_int
+    L.siminf_gpu_model_load.argtypes = [C.c_char_p, C.POINTER(vp)]
+    L.siminf_gpu_model_load.restype = C.c_int
     L.siminf_gpu_model_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int)]
     L.siminf_gpu_model_free.argtypes = [vp]
@@ -119,7 +121,7 @@ EXPORTS = (
     "siminf_gpu_release_cached", "siminf_gpu_trajectory_u", "siminf_gpu_trajectory_v",
     "siminf_gpu_prevalence", "siminf_gpu_plan_outputs", "siminf_gpu_sort_events",
     "siminf_gpu_plan_day_max", "siminf_gpu_individual_events",
-    "siminf_gpu_individual_events_ex",
+    "siminf_gpu_individual_events_ex", "siminf_gpu_model_load",
 )
 
 
@@ -176,11 +178,34 @@ class DeviceModel:
 
 
 _models = {}
+_code_models = {}
+
+
+def register_model_code(name, c_code, Nc, Nt, Nd, Ngd, pts_local=None):
+    """Make `name` a device model compiled from model C code (devmodel),
+    compiled and loaded the first time an entry point asks for it."""
+    _code_models[name] = (c_code, Nc, Nt, Nd, Ngd, pts_local)
+
+
+def load_device_model(name, path):
+    """Load a device model library built by devmodel.compile
+    (siminf_gpu_model_load) and register it under `name`."""
+    dm = DeviceModel.__new__(DeviceModel)
+    dm.name = name
+    h = C.c_void_p()
+    check(lib().siminf_gpu_model_load(os.fsencode(path), C.byref(h)))
+    dm.handle = h
+    _models[name] = dm
+    return dm
 
 
 def device_model(name):
     if name not in _models:
-        _models[name] = DeviceModel(name)
+        if name in _code_models:
+            from . import devmodel
+            devmodel.load(name, *_code_models[name])
+        else:
+            _models[name] = DeviceModel(name)
     return _models[name]
 
 
