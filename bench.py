@@ -23,11 +23,15 @@ the launching stream); `e2e` times K calls of the C ABI entry point
 siminf_gpu_run_solver_ex with host buffers (planning, host->device copies,
 solve, device->host copy of U inside the timed region).  The state (U alone
 is 5.84 GB) is far larger than the 129 MB L2, so no flush is needed between
-steps.  `--impl reference` times the reference algorithm on the host cores
+steps.  `--impl reference` times the reference algorithm on every host core
 (the oracle's C port of the ssm solver with OpenMP, whose parity with the
-reference's own sources is tested where those compile) on a bounded sample;
-the port, not those sources, because the workload needs capped transfer
-sizes, which the reference does not have.
+reference's own sources is tested where those compile) on the same whole
+workload, one run per step; the port, not those sources, because the
+workload needs capped transfer sizes, which the reference does not have.
+`cpu_baseline` is one such run inside this arm.  `untruncated` runs the
+same generator with the destination power law left uncut, at a tenth of
+the size, on the GPU and on the host cores: there one hub's chain of
+transitions sets the length of every day.
 
 With N > 1 (torchrun) every rank runs an independent replica of the
 workload with its own seed (the path has no data exchange between
@@ -79,8 +83,11 @@ def parse():
                     help="length of the open-loop serving trace (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="arrivals per second")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-scale", type=float, default=0.05,
-                    help="workload fraction of the bounded CPU sample")
+    ap.add_argument("--cpu-scale", type=float, default=1.0,
+                    help="workload fraction of the CPU baseline's run (1.0: the whole "
+                         "workload, about 15 s on 16 cores)")
+    ap.add_argument("--no-untruncated", dest="untruncated", action="store_false",
+                    help="skip the run on the untruncated power-law graph")
     return ap.parse_args()
 
 
@@ -151,13 +158,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(scale, days, threads, seed=42):
-    """The reference algorithm on the host cores over a bounded sample of
-    the same workload; returns (node-days/s, transitions/s, seconds, kind)."""
+def cpu_baseline(scale, days, threads, seed=42, m=None):
+    """The reference algorithm on the host cores: one run of the workload
+    (the model m when given, else the workload at `scale` of its nodes and
+    transfers); returns (node-days/s, transitions/s, seconds, kind, result)."""
     from siminf_gb300 import abi, workloads
     from oracle import oracle
-    m = workloads.seir_events(nodes=max(1, int(1_000_000 * scale)), days=days,
-                              transfers=max(1, int(500_000 * scale)))
+    if m is None:
+        m = workloads.seir_events(nodes=max(1, int(1_000_000 * scale)), days=days,
+                                  transfers=max(1, int(500_000 * scale)))
     h = abi.build_args(m, seed)
     t0 = time.perf_counter()
     code, res = oracle.run(h, m.name, threads, cap_transfers=True)
@@ -344,38 +353,116 @@ def serve_bench(seconds, rate, seed=5):
                     "submission to completion; plain = one request at a time"}
 
 
+UNTRUNCATED_SCALE = 0.1
+
+
+def untruncated_workload():
+    """The headline generator with the destination power law left
+    untruncated (exponent 2.1 on [1, inf)), at a tenth of the nodes and
+    transfers: a few hubs collect most of the population and one node's
+    chain of transitions sets the length of every day."""
+    from siminf_gb300 import workloads
+    return workloads.seir_events(nodes=int(1_000_000 * UNTRUNCATED_SCALE),
+                                 transfers=int(500_000 * UNTRUNCATED_SCALE), cutoff=np.inf)
+
+
+def untruncated_cpu(threads, m=None):
+    m = m if m is not None else untruncated_workload()
+    v, tr, dt, kind, res = cpu_baseline(UNTRUNCATED_SCALE, 365, threads, m=m)
+    return {"value": v, "unit": UNIT, "ms": dt * 1e3, "cores": threads, "kind": kind,
+            "transitions": int(res.transitions)}
+
+
+def untruncated_bench(torch, C, stream, threads, cpu=True):
+    """The untruncated graph on the GPU (resident plan, tuned as the
+    headline) and on the host cores, with the run's critical path."""
+    from siminf_gb300 import abi, native
+    m = untruncated_workload()
+    h = abi.build_args(m, 42)
+    p = native.Plan(h, m.name, cap_transfers=True)
+    s = C.c_void_p(stream.cuda_stream)
+    p.run(s)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    p.run(s)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    dmax = p.day_max(s)
+    nd = m.Nn * p.stats().days
+    out = {"nodes": m.Nn, "days": 365, "transfers_per_day": int(500_000 * UNTRUNCATED_SCALE),
+           "value": nd / (ms / 1e3), "unit": UNIT, "ms": ms,
+           "critical_path_transitions": int(dmax.sum()),
+           "us_per_critical_transition": ms * 1e3 / max(1, int(dmax.sum())),
+           "graph": "destination weights power law 2.1 on [1, inf), no cutoff",
+           "cpu_baseline": untruncated_cpu(threads, m) if cpu else None}
+    p.close()
+    return out
+
+
+def workload_config(args, m, st_days, e2_waves=None):
+    """The config object both arms print for the headline workload."""
+    nodes = max(1, int(1_000_000 * args.scale))
+    transfers = max(1, int(500_000 * args.scale))
+    cfg = {"workload": "seir_events_%dx%d" % (nodes, args.days) if args.scale != 1.0
+           else "seir_events_1e6x365",
+           "nodes": nodes, "days": st_days, "transfers_per_day": transfers,
+           "events": int(len(m.events["event"])), "cap_transfers": True,
+           "graph": "uniform sources, destination weights power law 2.1 cut at sqrt(edges)"}
+    if e2_waves is not None:
+        cfg["e2_waves"] = e2_waves
+    return cfg
+
+
 def run_reference(args):
+    """The reference arm: the reference algorithm (the oracle's C port of
+    the ssm solver with OpenMP over nodes and the serial external-transfer
+    phase, bit-identical to the reference's own sources where those
+    compile) on every host core, on the same full workload as the GPU arm:
+    one step is one whole run of the horizon.  A CPU run has nothing to
+    warm up beyond its first (page faults, the thread pool), so at most one
+    warm-up run is made whatever --warmup says, which keeps the arm within
+    minutes at about 15 s per run on 16 cores."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     from oracle import oracle
+    from siminf_gb300 import workloads
     oracle.build()
-    for _ in range(args.warmup):
-        cpu_baseline(args.cpu_scale, args.days, threads)
+    nodes = max(1, int(1_000_000 * args.scale))
+    transfers = max(1, int(500_000 * args.scale))
+    m = workloads.seir_events(nodes=nodes, days=args.days, transfers=transfers)
+    for _ in range(min(args.warmup, 1)):
+        cpu_baseline(args.scale, args.days, threads, m=m)
     vals, trans, secs = [], [], []
     for _ in range(args.steps):
-        v, tr, dt, kind, res = cpu_baseline(args.cpu_scale, args.days, threads)
+        v, tr, dt, kind, res = cpu_baseline(args.scale, args.days, threads, m=m)
         vals.append(v)
         trans.append(tr)
         secs.append(dt)
-    value = float(np.mean(vals))
-    sample = ("SEIR with events at %.3g of the nodes and transfers (%d nodes, %d days, "
-              "%d transfers/day), cap_transfers on, %d threads" %
-              (args.cpu_scale, int(1e6 * args.cpu_scale), args.days,
-               int(5e5 * args.cpu_scale), threads))
+    ms = float(np.mean(secs)) * 1e3
+    value = res.node_days / (ms / 1e3)
+    sample = ("the whole workload (%d nodes, %d days, %d transfers/day), cap_transfers on, "
+              "%d threads, one run per step" % (nodes, args.days, transfers, threads))
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": float(np.mean(secs)) * 1e3, "higher_is_better": True,
+        "n_gpus": world, "steps": args.steps, "warmup": min(args.warmup, 1),
+        "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32 state, f64 rates",
         "data": "synthetic",
-        "config": {"workload": "seir_events_1e6x365 (bounded sample, see cpu_baseline)",
-                   "nodes": int(1e6 * args.cpu_scale), "days": args.days},
+        "config": workload_config(args, m, args.days),
         "transitions_per_s": float(np.mean(trans)),
+        "transitions_per_step": int(res.transitions),
+        "serial_e2_ms_per_step": res.seconds_e2 * 1e3,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "untruncated": dict(untruncated_cpu(threads),
+                            graph="destination weights power law 2.1 on [1, inf), no cutoff",
+                            nodes=int(1_000_000 * UNTRUNCATED_SCALE)),
     }
     print(json.dumps(out), flush=True)
 
@@ -472,8 +559,10 @@ def run_ours(args):
     event_sort = events_bench(m, peak) if rank == 0 and world == 1 else None
     individual = (individual_bench(peak, os.cpu_count() or 1, cpu=not args.no_cpu)
                   if rank == 0 and world == 1 else None)
+    # the aem leg's CPU sample stays at 5% of the workload: the oracle's
+    # aem is a secondary baseline and a whole run would add half a minute
     aem = (aem_bench(m, node_days, torch, C, stream, os.cpu_count() or 1,
-                     0.0 if args.no_cpu else args.cpu_scale)
+                     0.0 if args.no_cpu else min(args.cpu_scale, 0.05))
            if rank == 0 and world == 1 else None)
 
     # batched form: R replicates of the same workload in one device-resident
@@ -542,14 +631,20 @@ def run_ours(args):
         e2e["ms_solve"] = estats.ms_solve
         e2e["ms_download"] = estats.ms_download
 
+    untrunc = (untruncated_bench(torch, C, stream, os.cpu_count() or 1, cpu=not args.no_cpu)
+               if args.untruncated and rank == 0 and world == 1 else None)
+
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import oracle
         oracle.build()
-        v, tr, dt, kind, res = cpu_baseline(args.cpu_scale, args.days, os.cpu_count() or 1)
+        whole = args.cpu_scale >= 1.0
+        v, tr, dt, kind, res = cpu_baseline(args.cpu_scale, args.days, os.cpu_count() or 1,
+                                            m=m if whole else None)
         cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": kind,
-               "sample": "SEIR with events at %.3g scale (%d nodes, %d days), %.1f s" %
-                         (args.cpu_scale, int(1e6 * args.cpu_scale), args.days, dt),
+               "sample": ("one run of the whole workload, %.1f s" % dt if whole else
+                          "SEIR with events at %.3g scale (%d nodes, %d days), %.1f s" %
+                          (args.cpu_scale, int(1e6 * args.cpu_scale), args.days, dt)),
                "transitions_per_s": tr}
 
     if rank == 0:
@@ -563,11 +658,9 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32 state, f64 rates", "data": "synthetic",
-            "config": {"workload": "seir_events_1e6x365", "nodes": nodes, "days": st.days,
-                       "transfers_per_day": transfers, "events": int(len(m.events["event"])),
-                       "e2_waves": st.e2_waves, "cap_transfers": True,
-                       "l2": "state and U (5.8 GB) exceed the 129 MB L2; no flush",
-                       "parallelism": "replicas x%d" % world},
+            "config": dict(workload_config(args, m, st.days, st.e2_waves),
+                           l2="state and U (5.8 GB) exceed the 129 MB L2; no flush",
+                           parallelism="replicas x%d" % world),
             "transitions_per_s": transitions_per_s,
             "transitions_per_step": int(st.transitions),
             "gpu_launches": launches * args.steps,
@@ -597,6 +690,7 @@ def run_ours(args):
             "serve": serve,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "untruncated": untrunc,
             "t_generate_s": t_gen,
         }
         print(json.dumps(out), flush=True)

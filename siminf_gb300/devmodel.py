@@ -176,7 +176,10 @@ def device_source(c_code, Nc, Nt, Nd, Ngd, pts_local=None):
         out.append("")
     cases = "\n".join("        case %d: return ::%s(u, v, ldata, gdata, t);" % (k, n)
                       for k, n in enumerate(code.tr_names[:-1]))
-    out.append("""namespace siminf {
+    # The model struct has internal linkage: every model library then has
+    # its own kernel and launcher instantiations, which would otherwise be
+    # process-wide unique symbols shared by every model library loaded.
+    out.append("""namespace {
 struct ModelCompiled {
     static constexpr int NC = %(nc)d, NT = %(nt)d, ND = %(nd)d, NGD = %(ngd)d;
     static constexpr bool PTS_LOCAL = %(local)s;
@@ -197,7 +200,7 @@ struct ModelCompiled {
         return ::%(pts)s(v_new, u, v, ldata, gdata, node, t);
     }
 };
-}  // namespace siminf
+}  // namespace
 
 extern "C" __attribute__((visibility("default"))) int siminf_model_abi(void)
 {
@@ -207,7 +210,7 @@ extern "C" __attribute__((visibility("default"))) int siminf_model_abi(void)
 extern "C" __attribute__((visibility("default"))) const siminf::Launchers *
 siminf_model_launchers(void)
 {
-    return siminf::Launch<siminf::ModelCompiled>::table();
+    return siminf::Launch<ModelCompiled>::table();
 }
 """ % {"nc": Nc, "nt": Nt, "nd": Nd, "ngd": Ngd, "local": "true" if pts_local else "false",
        "tinv": "true" if time_invariant else "false", "cases": cases,
@@ -239,8 +242,8 @@ def compile(c_code, Nc, Nt, Nd, Ngd, pts_local=None, verbose=False):
         with open(cu, "w") as f:
             f.write(src)
         tmp = lib + ".%d.tmp" % os.getpid()
-        cmd = ([build.nvcc()] + flags + ["-shared", "-I", build.CSRC, cu, "-o", tmp,
-                                         "-lcudart"])
+        cmd = ([build.nvcc()] + flags + ["-Xcompiler", "-fvisibility=hidden", "-shared",
+                                         "-I", build.CSRC, cu, "-o", tmp, "-lcudart"])
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)

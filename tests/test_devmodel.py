@@ -194,6 +194,22 @@ def test_generated_model_compiles_for_the_device():
     assert devmodel.compile(gen.C_code, gen.Nc, gen.Nt, gen.Nd, 2) == path   # cached
 
 
+def test_model_libraries_keep_their_own_tables():
+    """Several model libraries in one process each hand out their own
+    launcher table (their instantiations must not be shared through
+    process-wide symbols); no GPU is needed to load them."""
+    import ctypes as C
+    from siminf_gb300 import native
+    native.lib()
+    dims = []
+    for gen, ngd in ((sir_generated()[0], 2), (sise_pf_generated()[0], 2),
+                     (seirs_custom(nodes=4, days=3, events=False), 3)):
+        lib = C.CDLL(devmodel.compile(gen.C_code, gen.Nc, gen.Nt, gen.Nd, ngd))
+        lib.siminf_model_launchers.restype = C.POINTER(C.c_int * 4)
+        dims.append(list(lib.siminf_model_launchers().contents))
+    assert dims == [[3, 2, 0, 2], [2, 2, 1, 2], [4, 4, 1, 3]]
+
+
 @pytest.mark.parametrize("factory", [sir_generated, sise_pf_generated])
 def test_oracle_generated_equals_hand_written(oracle_lib, factory):
     """The host build of the generated code gives the hand-written host
