@@ -217,16 +217,161 @@ __device__ __forceinline__ bool ssa_begin(SsaLane<M> &ln, const si_rng &key, uin
     philox_block(key, (c + 1) >> 2, ln.q0, ln.q1, ln.q2, ln.q3);
     ln.L = si_neglog_u32(word_of(p0, p1, p2, p3, (uint32_t) c & 3u));
     ln.U = si_u32_to_uniform_pos(word_of(ln.q0, ln.q1, ln.q2, ln.q3, (uint32_t) (c + 1) & 3u));
-    ln.tau = si_div(ln.L, ln.sum);
+    if (!M::RATES_TIME_INVARIANT)
+        ln.tau = si_div(ln.L, ln.sum);  /* ssa_step_ahead divides at each step */
     return false;
 }
 
-/* One step of the direct method: the waiting time ends the day, or one
- * transition fires.  Returns true when the node's day is over. */
+/* One step of the direct method for models whose rates do not read t:
+ * the same operations as ssa_step_in_order, arranged so that the waiting
+ * time's division (~550 cycles) does not hold up the next transition.
+ * The transition the step would fire is selected and applied to copies of
+ * the state while the division runs -- its rates need no time -- and the
+ * copies replace the state only once the waiting time shows that it fires
+ * before the day ends.  The loop-carried chain is then the selection, the
+ * state update and the rate refresh; the division and the day-end check
+ * run beside it.  Returns true when the node's day is over. */
 template <class M>
-__device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, double next,
-                                         const double *v, const double *ld, const double *gd,
-                                         const int *sS, const uint32_t *sG, unsigned max_fired)
+__device__ __forceinline__ bool ssa_step_ahead(SsaLane<M> &ln, const si_rng &key, double next,
+                                               const double *v, const double *ld,
+                                               const double *gd, const int *sS,
+                                               const uint32_t *sG, unsigned max_fired)
+{
+    constexpr int NC = M::NC, NT = M::NT;
+    const double tau = si_div(ln.L, ln.sum);
+    const double rnd = ln.U * ln.sum;
+
+    /* Inversion: the first k with !(rnd > cum[k]), else NT - 1. */
+    int tr = NT - 1;
+#pragma unroll
+    for (int k = NT - 2; k >= 0; k--)
+        if (!(rnd > ln.cum[k]))
+            tr = k;
+    double rtr = ln.rate[0];
+#pragma unroll
+    for (int k = 1; k < NT; k++)
+        if (tr == k)
+            rtr = ln.rate[k];
+    bool nil = false;
+    if (si_is_zero(rtr)) {
+        /* Back-scan to the first non-zero rate (ssm.c:171-189). */
+#pragma unroll
+        for (int k = NT - 1; k >= 1; k--)
+            if (tr == k && si_is_zero(ln.rate[k]))
+                tr = k - 1;
+        double r2 = ln.rate[0];
+#pragma unroll
+        for (int k = 1; k < NT; k++)
+            if (tr == k)
+                r2 = ln.rate[k];
+        nil = si_is_zero(r2);
+    }
+
+    /* The state after that transition, in copies. */
+    int u2[NC];
+    int neg = 0;
+#pragma unroll
+    for (int cc = 0; cc < NC; cc++) {
+        const int d = sS[tr * NC + cc];
+        u2[cc] = ln.u[cc] + d;
+        neg |= (d != 0) & (u2[cc] < 0);
+    }
+    double rate2[NT];
+    double delta = 0.0;
+    const uint32_t gm = sG[tr];
+    int bad = -1;
+    double bad_rate = 0.0;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        rate2[k] = ln.rate[k];
+        if (gm & (1u << k)) {
+            const double nr = M::rate(k, u2, v, ld, gd, ln.t, ln.dc);
+            rate2[k] = nr;
+            delta += nr - ln.rate[k];
+            if (si_bad_rate(nr)) {
+                bad = k;
+                bad_rate = nr;
+            }
+        }
+    }
+    const double sum2 = ln.sum + delta;
+
+    /* Draws of the transition after it. */
+    const uint64_t c2 = ln.c + 2;
+    uint32_t n0, n1, n2, n3;
+    philox_block(key, (c2 + 1) >> 2, n0, n1, n2, n3);
+    const uint32_t ci = (uint32_t) c2 & 3u;
+    const uint32_t wl = (ci == 3u) ? ln.q3 : word_of(n0, n1, n2, n3, ci);
+    const uint32_t wu = word_of(n0, n1, n2, n3, (ci + 1u) & 3u);
+
+    /* The waiting time decides: the day ends first, or the transition fires. */
+    const double tn = tau + ln.t;
+    if (tn >= next) {
+        ln.t = next;
+        ln.c += 1;                            /* the waiting time's draw was used */
+        return true;
+    }
+    ln.t = tn;
+    ln.c = c2;
+    if (nil) {
+        ln.sum = 0.0;
+        return true;
+    }
+    if (++ln.fired > max_fired) {
+        ln.err = ERR_TIMEOUT;
+        ln.err_tr = tr;
+        ln.err_t = ln.t;
+        ln.t = next;
+        return true;
+    }
+#pragma unroll
+    for (int cc = 0; cc < NC; cc++)
+        ln.u[cc] = u2[cc];
+#pragma unroll
+    for (int k = 0; k < NT; k++)
+        ln.rate[k] = rate2[k];
+    ln.sum = sum2;
+    ln.q0 = n0;
+    ln.q1 = n1;
+    ln.q2 = n2;
+    ln.q3 = n3;
+    ln.L = si_neglog_u32(wl);
+    ln.U = si_u32_to_uniform_pos(wu);
+    if (neg) {
+        ln.err = ERR_NEGATIVE_STATE;
+        ln.err_tr = tr;
+        ln.err_t = ln.t;
+        ln.err_rate = 0.0;
+    }
+    if (bad >= 0) {
+        ln.err = ERR_INVALID_RATE;
+        ln.err_tr = bad;
+        ln.err_t = ln.t;
+        ln.err_rate = bad_rate;
+    }
+    prefix_sums<M>(ln.rate, ln.cum);
+    if (!si_finite_pos(ln.sum)) {
+        if (!le_zero(si_double_bits(ln.sum)) && !ln.err) {
+            ln.err = ERR_INVALID_RATE;
+            ln.err_tr = -1;
+            ln.err_t = ln.t;
+            ln.err_rate = ln.sum;
+        }
+        ln.t = next;
+        return true;
+    }
+    return false;
+}
+
+/* One step of the direct method in the reference's order: the waiting
+ * time ends the day, or one transition fires.  Returns true when the
+ * node's day is over. */
+template <class M>
+__device__ __forceinline__ bool ssa_step_in_order(SsaLane<M> &ln, const si_rng &key,
+                                                  double next, const double *v,
+                                                  const double *ld, const double *gd,
+                                                  const int *sS, const uint32_t *sG,
+                                                  unsigned max_fired)
 {
     constexpr int NC = M::NC, NT = M::NT;
     const double tn = ln.tau + ln.t;
@@ -347,6 +492,19 @@ __device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, doub
     }
     ln.tau = si_div(ln.L, ln.sum);
     return false;
+}
+
+/* One step of the direct method (src/solvers/SimInf_solver_ssm.c:
+ * 144-235): ahead of the waiting time where the rates do not read t. */
+template <class M>
+__device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, double next,
+                                         const double *v, const double *ld, const double *gd,
+                                         const int *sS, const uint32_t *sG, unsigned max_fired)
+{
+    if constexpr (M::RATES_TIME_INVARIANT)
+        return ssa_step_ahead<M>(ln, key, next, v, ld, gd, sS, sG, max_fired);
+    else
+        return ssa_step_in_order<M>(ln, key, next, v, ld, gd, sS, sG, max_fired);
 }
 
 /* A node's whole SSA day in one call (used where one thread keeps one

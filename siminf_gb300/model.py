@@ -93,9 +93,12 @@ class SimInfModel:
         """The same model with n replicates of u0/v0 (R's replicates slot)."""
         u0 = np.tile(self.u0[:, :self.Nn], (1, n))
         v0 = np.tile(self.v0[:, :self.Nn], (1, n)) if self.Nd else None
-        return SimInfModel(self.name, self.G, self.S, u0, self.tspan, v0=v0,
-                           ldata=self.ldata, gdata=self.gdata, E=self.E, N=self.N,
-                           events=self.events, replicates=n)
+        m = SimInfModel(self.name, self.G, self.S, u0, self.tspan, v0=v0,
+                        ldata=self.ldata, gdata=self.gdata, E=self.E, N=self.N,
+                        events=self.events, replicates=n)
+        if hasattr(self, "C_code"):
+            m.C_code = self.C_code
+        return m
 
 
 def _rep_ldata(n, *params):
