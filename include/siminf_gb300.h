@@ -344,6 +344,46 @@ typedef struct siminf_gpu_pfilter_args {
 int siminf_gpu_pfilter(const siminf_gpu_solver_args *args, const siminf_gpu_model *model,
                        siminf_gpu_pfilter_args *pf);
 
+/*
+ * Particle-marginal Metropolis-Hastings with the particle filter above:
+ * the chain of pmcmc() and continue_pmcmc() (R/pmcmc.R:470-600).  The
+ * chain is resident: siminf_gpu_pmcmc_create keeps the filter's plan,
+ * observations and buffers on the device, and every siminf_gpu_pmcmc_run
+ * call continues the chain where the last one stopped, so that n calls of
+ * k iterations give the rows of one call of n k iterations.  Row 1 is the
+ * initial theta; each later row proposes theta + z Q (z standard normal,
+ * Q = chol, the upper Cholesky factor of the proposal covariance, as
+ * R/pmcmc.R:423-437 with the adaptive part off), runs one filter pass when
+ * the prior density is positive, and accepts with probability
+ * exp(logLik' + logPrior' - logLik - logPrior).  Parameters are gdata
+ * entries with uniform priors; args->gdata holds the other entries.
+ * Draws come from counter-based streams keyed by (seed, iteration), so a
+ * continued chain equals an uninterrupted one.  The pfilter arguments'
+ * outputs (loglik, ess, ancestors) are not used.
+ */
+typedef struct siminf_gpu_pmcmc_args {
+    int n_pars;
+    const int *gdata_index;     /* zero-based gdata entry of each parameter */
+    const double *theta;        /* initial values */
+    const double *prior_lo;     /* uniform priors U(lo, hi) */
+    const double *prior_hi;
+    const double *chol;         /* n_pars x n_pars, row-major, upper triangular */
+    unsigned long seed;
+    int reserved[4];
+} siminf_gpu_pmcmc_args;
+
+typedef struct siminf_gpu_pmcmc siminf_gpu_pmcmc;
+
+int siminf_gpu_pmcmc_create(const siminf_gpu_solver_args *args, const siminf_gpu_model *model,
+                            const siminf_gpu_pfilter_args *pf, const siminf_gpu_pmcmc_args *pm,
+                            siminf_gpu_pmcmc **out);
+/* n_iterations more rows; rows (or NULL) receives n_iterations x
+ * (4 + n_pars) doubles, row-major: logPost, logLik, logPrior, accept,
+ * theta -- the columns of the reference's chain. */
+int siminf_gpu_pmcmc_run(siminf_gpu_pmcmc *chain, int n_iterations, double *rows);
+long long siminf_gpu_pmcmc_length(const siminf_gpu_pmcmc *chain);
+void siminf_gpu_pmcmc_free(siminf_gpu_pmcmc *chain);
+
 /* Diagnostics of the last failing call on the calling thread: the fields
  * SimInf_print_status (src/solvers/SimInf_solver.c:1191-1249) and
  * SimInf_print_event (src/solvers/SimInf_solver.c:550-645) print. */
@@ -449,7 +489,10 @@ void siminf_gpu_plan_free(siminf_gpu_plan *plan);
 enum {
     SIMINF_GPU_REQUEST_RUN = 0,         /* args + model + options: U/V written */
     SIMINF_GPU_REQUEST_PFILTER = 1,     /* args + model + pfilter */
-    SIMINF_GPU_REQUEST_PLAN = 2         /* plan: run again, results stay on the device */
+    SIMINF_GPU_REQUEST_PLAN = 2,        /* plan: run again, results stay on the device */
+    SIMINF_GPU_REQUEST_PMCMC = 3        /* pmcmc: continue a resident chain by
+                                         * pmcmc_iterations rows into pmcmc_rows
+                                         * (continue_pmcmc, R/pmcmc.R:474-600) */
 };
 
 typedef struct siminf_gpu_request {
@@ -468,6 +511,10 @@ typedef struct siminf_gpu_request {
     long long submit_ns;
     siminf_gpu_stats stats;             /* runs and plans */
     char message[200];                  /* the error's diagnostics */
+    /* SIMINF_GPU_REQUEST_PMCMC */
+    siminf_gpu_pmcmc *pmcmc;
+    int pmcmc_iterations;
+    double *pmcmc_rows;
 } siminf_gpu_request;
 
 typedef struct siminf_gpu_server_options {

@@ -235,6 +235,71 @@ def pfilter(model, n_particles, obs_time, obs, obs_compartment, detect_p, seed=4
     return code, float(ll[0]), ess, anc
 
 
+PMCMC_SID = 5 << 60
+
+
+def pmcmc(model, n_particles, obs_time, obs, obs_compartment, detect_p, pars, theta,
+          prior_lo, prior_hi, chol, seed, n_iterations, threads=1):
+    """The PMCMC chain (R/pmcmc.R:470-600 with the adaptive part off) on the
+    oracle's particle filter, iteration for iteration as the library's
+    siminf_gpu_pmcmc_run: rows of logPost, logLik, logPrior, accept and
+    theta.  chol is the upper Cholesky factor of the proposal covariance."""
+    import math
+    n = len(pars)
+    gdata = np.array(model.gdata, dtype=np.float64)
+    m = type(model).__new__(type(model))
+    m.__dict__.update(model.__dict__)
+
+    def loglik(th, it):
+        g = gdata.copy()
+        for k in range(n):
+            g[pars[k]] = th[k]
+        m.gdata = g
+        s = (seed ^ ((it * 0xD1B54A32D192ED03) & 0xFFFFFFFFFFFFFFFF)) & 0xFFFFFFFFFFFFFFFF
+        code, ll, _, _ = pfilter(m, n_particles, obs_time, obs, obs_compartment, detect_p,
+                                 seed=s, threads=threads)
+        assert code == 0, code
+        return ll
+
+    def log_prior(th):
+        lp = 0.0
+        for k in range(n):
+            if not (prior_lo[k] <= th[k] <= prior_hi[k]):
+                return -math.inf
+            lp -= math.log(prior_hi[k] - prior_lo[k])
+        return lp
+
+    rows = []
+    th = [float(x) for x in theta]
+    ll = lp = 0.0
+    for it in range(1, n_iterations + 1):
+        accept = 0.0
+        if it == 1:
+            ll = loglik(th, it)
+            lp = log_prior(th)
+        else:
+            u = uniform_pos(seed, PMCMC_SID + it, 0, 2 * n + 1)
+            z = [math.sqrt(-2.0 * math.log(u[2 * k])) * math.cos(6.283185307179586 * u[2 * k + 1])
+                 for k in range(n)]
+            prop = []
+            for j in range(n):
+                acc = th[j]
+                for k in range(j + 1):
+                    acc = acc + z[k] * chol[k][j]
+                prop.append(acc)
+            lp_p = log_prior(prop)
+            if math.isfinite(lp_p):
+                ll_p = loglik(prop, it)
+                try:
+                    alpha = math.exp(ll_p + lp_p - ll - lp)
+                except OverflowError:
+                    alpha = math.inf
+                if math.isfinite(alpha) and u[2 * n] < alpha:
+                    ll, lp, th, accept = ll_p, lp_p, prop, 1.0
+        rows.append([ll + lp, ll, lp, accept] + list(th))
+    return np.array(rows)
+
+
 def _cols(id, event, time, node, dest):
     return [np.ascontiguousarray(x, dtype=np.int32) for x in (id, event, time, node, dest)]
 

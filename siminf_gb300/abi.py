@@ -228,10 +228,27 @@ class Request(C.Structure):
         ("submit_ns", C.c_longlong),
         ("stats", Stats),
         ("message", C.c_char * 200),
+        ("pmcmc", C.c_void_p),
+        ("pmcmc_iterations", C.c_int),
+        ("pmcmc_rows", C.c_void_p),
     ]
 
 
-REQUEST_RUN, REQUEST_PFILTER, REQUEST_PLAN = 0, 1, 2
+REQUEST_RUN, REQUEST_PFILTER, REQUEST_PLAN, REQUEST_PMCMC = 0, 1, 2, 3
+
+
+class PmcmcArgs(C.Structure):
+    """siminf_gpu_pmcmc_args."""
+    _fields_ = [
+        ("n_pars", C.c_int),
+        ("gdata_index", C.POINTER(C.c_int)),
+        ("theta", C.POINTER(C.c_double)),
+        ("prior_lo", C.POINTER(C.c_double)),
+        ("prior_hi", C.POINTER(C.c_double)),
+        ("chol", C.POINTER(C.c_double)),
+        ("seed", C.c_ulong),
+        ("reserved", C.c_int * 4),
+    ]
 
 
 def csc(dense):

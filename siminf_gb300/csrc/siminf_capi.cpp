@@ -1792,51 +1792,219 @@ static int plan_set_tspan(siminf_gpu_plan *p, const double *tspan, int tlen)
     return e == cudaSuccess ? 0 : cuda_fail(e, "days upload");
 }
 
-/* Intervals g0 .. n_obs - 1 of the particle filter as replays of one CUDA
- * graph: the interval's seed, day schedule and observation row are read
- * from the device, and the finalize kernel moves the interval counter on.
- * One replay: reset the state from the gathered ancestors, k_init,
- * k_horizon, weights, finalize (normalise, ESS, resample), gather for the
- * next interval.  Errors are read once, after the last replay. */
-static int pfilter_graph(siminf_gpu_plan *p, const siminf_gpu_pfilter_args *pf, int g0,
-                         const std::vector<std::array<double, 2>> &tsps,
-                         const std::vector<int> &tlens, int nd, int prev_tlen,
-                         const double *d_lfact, int tablen, double logp, double logq,
-                         double log_np, double *d_w, double *d_loglik, double *d_ess, int *d_anc,
-                         int *d_anc_out, const int *d_obs, size_t nu, size_t nv)
-{
-    const int n_obs = pf->n_obs, Np = p->s.Nrep, tl = tlens[g0];
-    const cudaStream_t pst = p->stream;
-    std::vector<DayInfo> alldays((size_t) n_obs * nd);
-    std::vector<uint64_t> seeds(n_obs);
-    for (int i = 0; i < n_obs; i++) {
-        seeds[i] = (uint64_t) pf->seed + ((uint64_t) i + 1) * 0x9E3779B97F4A7C15ULL;
-        if (i < g0)
-            continue;
-        std::vector<DayInfo> dd;
-        plan_days(tsps[i].data(), tlens[i], dd);
-        std::copy(dd.begin(), dd.end(), alldays.begin() + (size_t) i * nd);
-    }
-    DayInfo *d_days = nullptr;
+/* A particle filter's plan, buffers and interval graph, resident across
+ * filter passes over the same model, observations and particle count.
+ * siminf_gpu_pfilter is one pass of a session made for it; a PMCMC chain
+ * keeps one session for all its iterations. */
+struct PfSession {
+    siminf_gpu_plan *p = nullptr;
+    int Np = 0, Nn = 0, Nc = 0, Nd = 0, n_obs = 0, obs_c = 0, per_particle = 0, Ngd = 0;
+    size_t nu = 0, nv = 0;
+    int tablen = 1;
+    double logp = 0, logq = 0, log_np = 0;
+    double *d_lfact = nullptr, *d_w = nullptr, *d_loglik = nullptr, *d_ess = nullptr;
+    int *d_anc = nullptr, *d_anc_out = nullptr, *d_obs = nullptr;
+    int *d_u0_start = nullptr;          /* the particles' initial state (p->d_u0 takes the */
+    double *d_v0_start = nullptr;       /* gathered ancestors interval by interval) */
+    std::vector<std::array<double, 2>> tsps;
+    std::vector<int> tlens, ndays_i;
+    int g0 = 0;                         /* intervals g0 .. replay one graph */
+    /* the replayed intervals: day schedules, seeds, interval counter, graph */
+    int nd = 0;
+    DayInfo *d_alldays = nullptr;
     uint64_t *d_seeds = nullptr;
     int *d_interval = nullptr;
-    int rc = upload(&d_days, alldays.data(), alldays.size(), p->owned, pst);
-    if (!rc) rc = upload(&d_seeds, seeds.data(), seeds.size(), p->owned, pst);
-    if (!rc) rc = upload(&d_interval, &g0, 1, p->owned, pst);
-    if (!rc) rc = plan_set_tspan(p, tsps[g0].data(), tl);
+    cudaStream_t gs = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+static void pf_session_free(PfSession *ss)
+{
+    if (!ss)
+        return;
+    if (ss->exec)
+        cudaGraphExecDestroy(ss->exec);
+    if (ss->gs)
+        cudaStreamDestroy(ss->gs);
+    siminf_gpu_plan_free(ss->p);
+    delete ss;
+}
+
+/* Seed of particle-filter interval i. */
+static inline uint64_t pf_interval_seed(uint64_t seed, int i)
+{
+    return seed + ((uint64_t) i + 1) * 0x9E3779B97F4A7C15ULL;
+}
+
+static int pf_session_create(const siminf_gpu_solver_args *a1, const siminf_gpu_model *model,
+                             const siminf_gpu_pfilter_args *pf, PfSession **out)
+{
+    memset(&g_status, 0, sizeof(g_status));
+    *out = nullptr;
+    if (!a1 || !model || !pf || pf->n_particles < 1 || pf->n_obs < 1 || !pf->obs ||
+        !pf->obs_time || a1->len > 0 || a1->solver != 0 || pf->obs_compartment < 0 ||
+        pf->obs_compartment >= a1->Nc || !(pf->detect_p > 0.0 && pf->detect_p < 1.0)) {
+        set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
+                   "invalid particle filter arguments (events and the aem solver are not supported)");
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    }
+    for (int i = 0; i < pf->n_obs; i++) {
+        if ((i == 0 && pf->obs_time[0] < a1->tspan[0]) ||
+            (i > 0 && pf->obs_time[i] <= pf->obs_time[i - 1])) {
+            set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
+                       "observation times must increase from tspan[0]");
+            return SIMINF_GPU_ERR_INVALID_MODEL;
+        }
+    }
+    PfSession *ss = new PfSession();
+    const int Np = pf->n_particles, Nn = a1->Nn, Nc = a1->Nc, Nd = a1->Nd;
+    ss->Np = Np;
+    ss->Nn = Nn;
+    ss->Nc = Nc;
+    ss->Nd = Nd;
+    ss->n_obs = pf->n_obs;
+    ss->obs_c = pf->obs_compartment;
+    ss->per_particle = pf->gdata_per_particle;
+    ss->Ngd = model->L->Ngd;
+    const size_t nu = (size_t) Nn * Nc, nv = (size_t) Nn * Nd;
+    ss->nu = nu;
+    ss->nv = nv;
+    /* particles = replicates of one plan */
+    std::vector<int> u0((size_t) Np * nu);
+    std::vector<double> v0((size_t) Np * nv + 1);
+    for (int q = 0; q < Np; q++) {
+        memcpy(&u0[q * nu], a1->u0, nu * sizeof(int));
+        if (nv)
+            memcpy(&v0[q * nv], a1->v0, nv * sizeof(double));
+    }
+    for (int node = 0; node < Nn; node++) {
+        long long tot = 0;
+        for (int c = 0; c < Nc; c++)
+            tot += a1->u0[(size_t) node * Nc + c];
+        ss->tablen = (int) std::max<long long>(ss->tablen, tot + 1);
+    }
+    std::vector<double> lfact(ss->tablen);
+    si_lfact_fill(lfact.data(), ss->tablen);
+    double tsp0[2] = {a1->tspan[0], a1->tspan[0] + 1.0};
+    int dummyU = 0;
+    double dummyV = 0;
+    siminf_gpu_solver_args a = *a1;
+    a.u0 = u0.data();
+    a.v0 = v0.data();
+    a.Nrep = Np;
+    a.tspan = tsp0;
+    a.tlen = 2;
+    a.U = &dummyU;
+    a.V = Nd > 0 ? &dummyV : nullptr;
+    a.len = 0;
+    siminf_gpu_options opt{};
+    opt.gdata_per_replicate = pf->gdata_per_particle;
+    int rc = siminf_gpu_plan_create_ex(&a, model, &opt, &ss->p);
+    if (rc) {
+        delete ss;
+        return rc;
+    }
+    siminf_gpu_plan *p = ss->p;
+    p->days_cap = p->ndays;
+    const cudaStream_t pst = p->stream;
+    rc = upload(&ss->d_lfact, lfact.data(), lfact.size(), p->owned, pst);
+    if (!rc) rc = dalloc(&ss->d_w, (size_t) Np, p->owned);
+    if (!rc) rc = dalloc(&ss->d_anc, (size_t) Np, p->owned);
+    if (!rc) rc = dalloc(&ss->d_anc_out, (size_t) Np * pf->n_obs, p->owned);
+    if (!rc) rc = upload(&ss->d_obs, pf->obs, (size_t) pf->n_obs * Nn, p->owned, pst);
+    if (!rc) rc = dalloc(&ss->d_loglik, 1, p->owned);
+    if (!rc) rc = dalloc(&ss->d_ess, (size_t) pf->n_obs, p->owned);
+    if (!rc) rc = upload(&ss->d_u0_start, u0.data(), u0.size(), p->owned, pst);
+    if (!rc && nv) rc = upload(&ss->d_v0_start, v0.data(), (size_t) Np * nv, p->owned, pst);
+    ss->logp = si_log(pf->detect_p);
+    ss->logq = si_log(1.0 - pf->detect_p);
+    ss->log_np = si_log((double) Np);
+    /* interval i runs tspan tsps[i] (R/pfilter.R:177-193) */
+    ss->tsps.resize(pf->n_obs);
+    ss->tlens.resize(pf->n_obs);
+    ss->ndays_i.resize(pf->n_obs);
+    for (int i = 0; i < pf->n_obs; i++) {
+        const double prev = (i == 0) ? a1->tspan[0] : (double) pf->obs_time[i - 1];
+        if ((i == 0 && prev < pf->obs_time[0]) ||
+            (i > 0 && pf->obs_time[i] - pf->obs_time[i - 1] > 1)) {
+            ss->tsps[i] = {prev, (double) pf->obs_time[i]};
+            ss->tlens[i] = 2;
+        } else {
+            ss->tsps[i] = {(double) pf->obs_time[i], 0.0};
+            ss->tlens[i] = 1;
+        }
+        std::vector<DayInfo> dd;
+        plan_days(ss->tsps[i].data(), ss->tlens[i], dd);
+        ss->ndays_i[i] = (int) dd.size();
+    }
+    /* Intervals 1.. with one shape (tspan length and day count) replay one
+     * CUDA graph; the rest run launch by launch. */
+    ss->g0 = pf->n_obs;
+    if (p->horizon && pf->n_obs > 2) {
+        ss->g0 = 1;
+        for (int i = 2; i < pf->n_obs; i++)
+            if (ss->tlens[i] != ss->tlens[1] || ss->ndays_i[i] != ss->ndays_i[1])
+                ss->g0 = pf->n_obs;
+    }
+    if (!rc && ss->g0 < ss->n_obs) {
+        ss->nd = ss->ndays_i[ss->g0];
+        std::vector<DayInfo> alldays((size_t) ss->n_obs * ss->nd);
+        for (int i = ss->g0; i < ss->n_obs; i++) {
+            std::vector<DayInfo> dd;
+            plan_days(ss->tsps[i].data(), ss->tlens[i], dd);
+            std::copy(dd.begin(), dd.end(), alldays.begin() + (size_t) i * ss->nd);
+        }
+        rc = upload(&ss->d_alldays, alldays.data(), alldays.size(), p->owned, pst);
+        if (!rc) rc = dalloc(&ss->d_seeds, (size_t) ss->n_obs + 1, p->owned);
+        if (!rc) rc = dalloc(&ss->d_interval, 1, p->owned);
+    }
+    if (rc) {
+        pf_session_free(ss);
+        return rc;
+    }
+    *out = ss;
+    return 0;
+}
+
+/* Intervals g0 .. n_obs - 1 as replays of one CUDA graph, captured on the
+ * session's first pass: the interval's seed, day schedule and observation
+ * row are read from the device, and the finalize kernel moves the
+ * interval counter on.  One replay: reset the state from the gathered
+ * ancestors, k_init, k_horizon, weights, finalize (normalise, ESS,
+ * resample), gather for the next interval.  Errors are read once, after
+ * the last replay. */
+static int pf_session_graph(PfSession *ss, uint64_t seed, int prev_tlen)
+{
+    siminf_gpu_plan *p = ss->p;
+    const int g0 = ss->g0, n_obs = ss->n_obs, Np = ss->Np, tl = ss->tlens[g0];
+    const cudaStream_t pst = p->stream;
+    /* the intervals' seeds, then the pass's own (resampling) seed */
+    std::vector<uint64_t> seeds(n_obs + 1);
+    for (int i = 0; i < n_obs; i++)
+        seeds[i] = pf_interval_seed(seed, i);
+    seeds[n_obs] = seed;
+    cudaError_t e = cudaMemcpyAsync(ss->d_seeds, seeds.data(), (n_obs + 1) * sizeof(uint64_t),
+                                    cudaMemcpyHostToDevice, pst);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ss->d_interval, &g0, sizeof(int), cudaMemcpyHostToDevice, pst);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(pst);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "pfilter graph set-up");
+    int rc = plan_set_tspan(p, ss->tsps[g0].data(), tl);
     if (rc)
         return rc;
     DevState s = p->s;
-    s.pf_interval = d_interval;
-    s.pf_seeds = d_seeds;
-    s.pf_days = d_days;
-    s.pf_days_stride = nd;
+    s.pf_interval = ss->d_interval;
+    s.pf_seeds = ss->d_seeds;
+    s.pf_days = ss->d_alldays;
+    s.pf_days_stride = ss->nd;
     const Launchers *L = p->L;
     const int Nn = s.Nn, Nc = s.Nc;
 
     /* the state of interval g0 from its ancestors, then the error flags */
-    cudaError_t e = pf_gather(s.U, s.V, prev_tlen, (long long) nu, (long long) nv, d_anc, Np,
-                              p->d_u0, p->d_v0, pst);
+    e = pf_gather(s.U, s.V, prev_tlen, (long long) ss->nu, (long long) ss->nv, ss->d_anc, Np,
+                  p->d_u0, p->d_v0, pst);
     const int init_flags[3] = {0, INT_MAX, INT_MAX};
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s.err_count, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice,
@@ -1846,50 +2014,50 @@ static int pfilter_graph(siminf_gpu_plan *p, const siminf_gpu_pfilter_args *pf, 
     if (e != cudaSuccess)
         return cuda_fail(e, "pfilter graph set-up");
 
-    cudaStream_t gs = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    e = cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking);
-    if (e == cudaSuccess)
-        e = cudaStreamBeginCapture(gs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-        cudaError_t c = cudaMemcpyAsync(s.u, p->d_u0, (size_t) s.Ntot * Nc * sizeof(int),
-                                        cudaMemcpyDeviceToDevice, gs);
-        if (c == cudaSuccess && s.Nd > 0)
-            c = cudaMemcpyAsync(s.vA, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
-                                cudaMemcpyDeviceToDevice, gs);
-        if (c == cudaSuccess && s.Nd > 0)
-            c = cudaMemcpyAsync(s.vB, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
-                                cudaMemcpyDeviceToDevice, gs);
-        if (c == cudaSuccess)
-            c = L->init(s, 0.0, gs);
-        if (c == cudaSuccess)
-            c = L->horizon(s, d_days, nd, gs);
-        if (c == cudaSuccess)
-            c = pf_weights(s.U, tl, Nn, Nc, Np, d_obs, pf->obs_compartment, d_lfact, tablen, logp,
-                           logq, d_w, gs, d_interval);
-        if (c == cudaSuccess)
-            c = pf_finalize(d_w, Np, log_np, d_loglik, d_ess, 0, (uint64_t) pf->seed,
-                            ((uint64_t) 1) << 62, d_anc, d_anc_out, gs, d_interval);
-        if (c == cudaSuccess)
-            c = pf_gather(s.U, s.V, tl, (long long) nu, (long long) nv, d_anc, Np, p->d_u0,
-                          p->d_v0, gs);
-        e = cudaStreamEndCapture(gs, &graph);
+    if (!ss->exec) {
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamCreateWithFlags(&ss->gs, cudaStreamNonBlocking);
         if (e == cudaSuccess)
-            e = c;
+            e = cudaStreamBeginCapture(ss->gs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaStream_t gs = ss->gs;
+            cudaError_t c = cudaMemcpyAsync(s.u, p->d_u0, (size_t) s.Ntot * Nc * sizeof(int),
+                                            cudaMemcpyDeviceToDevice, gs);
+            if (c == cudaSuccess && s.Nd > 0)
+                c = cudaMemcpyAsync(s.vA, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, gs);
+            if (c == cudaSuccess && s.Nd > 0)
+                c = cudaMemcpyAsync(s.vB, p->d_v0, (size_t) s.Ntot * s.Nd * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, gs);
+            if (c == cudaSuccess)
+                c = L->init(s, 0.0, gs);
+            if (c == cudaSuccess)
+                c = L->horizon(s, ss->d_alldays, ss->nd, gs);
+            if (c == cudaSuccess)
+                c = pf_weights(s.U, tl, Nn, Nc, Np, ss->d_obs, ss->obs_c, ss->d_lfact,
+                               ss->tablen, ss->logp, ss->logq, ss->d_w, gs, ss->d_interval);
+            if (c == cudaSuccess)
+                c = pf_finalize(ss->d_w, Np, ss->log_np, ss->d_loglik, ss->d_ess, 0, seed,
+                                ((uint64_t) 1) << 62, ss->d_anc, ss->d_anc_out, gs,
+                                ss->d_interval, ss->d_seeds + n_obs);
+            if (c == cudaSuccess)
+                c = pf_gather(s.U, s.V, tl, (long long) ss->nu, (long long) ss->nv, ss->d_anc,
+                              Np, p->d_u0, p->d_v0, gs);
+            e = cudaStreamEndCapture(gs, &graph);
+            if (e == cudaSuccess)
+                e = c;
+        }
+        if (e == cudaSuccess)
+            e = cudaGraphInstantiate(&ss->exec, graph, 0);
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "pfilter graph");
     }
-    if (e == cudaSuccess)
-        e = cudaGraphInstantiate(&exec, graph, 0);
     for (int i = g0; i < n_obs && e == cudaSuccess; i++)
-        e = cudaGraphLaunch(exec, gs);
+        e = cudaGraphLaunch(ss->exec, ss->gs);
     if (e == cudaSuccess)
-        e = cudaStreamSynchronize(gs);
-    if (exec)
-        cudaGraphExecDestroy(exec);
-    if (graph)
-        cudaGraphDestroy(graph);
-    if (gs)
-        cudaStreamDestroy(gs);
+        e = cudaStreamSynchronize(ss->gs);
     if (e != cudaSuccess)
         return cuda_fail(e, "pfilter graph");
 
@@ -1908,112 +2076,39 @@ static int pfilter_graph(siminf_gpu_plan *p, const siminf_gpu_pfilter_args *pf, 
     return resolve_errors(p, cands);
 }
 
-int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model *model,
-                       siminf_gpu_pfilter_args *pf)
+/* One filter pass from the particles' initial state.  gdata, if not
+ * NULL, replaces the plan's gdata first (Ngd values, or Np rows of them
+ * for a session with one row per particle).  Outputs as in
+ * siminf_gpu_pfilter_args (ess, ancestors may be NULL). */
+static int pf_session_run(PfSession *ss, const double *gdata, uint64_t seed, double *loglik,
+                          double *ess, int *ancestors)
 {
-    auto t0 = std::chrono::steady_clock::now();
-    memset(&g_status, 0, sizeof(g_status));
-    if (!a1 || !model || !pf || pf->n_particles < 1 || pf->n_obs < 1 || !pf->obs ||
-        !pf->obs_time || !pf->loglik || !pf->ess || a1->len > 0 || a1->solver != 0 ||
-        pf->obs_compartment < 0 || pf->obs_compartment >= a1->Nc ||
-        !(pf->detect_p > 0.0 && pf->detect_p < 1.0)) {
-        set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
-                   "invalid particle filter arguments (events and the aem solver are not supported)");
-        return SIMINF_GPU_ERR_INVALID_MODEL;
-    }
-    for (int i = 0; i < pf->n_obs; i++) {
-        if ((i == 0 && pf->obs_time[0] < a1->tspan[0]) ||
-            (i > 0 && pf->obs_time[i] <= pf->obs_time[i - 1])) {
-            set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
-                       "observation times must increase from tspan[0]");
-            return SIMINF_GPU_ERR_INVALID_MODEL;
-        }
-    }
-    const int Np = pf->n_particles, Nn = a1->Nn, Nc = a1->Nc, Nd = a1->Nd;
-    const size_t nu = (size_t) Nn * Nc, nv = (size_t) Nn * Nd;
-    /* particles = replicates of one plan */
-    std::vector<int> u0((size_t) Np * nu);
-    std::vector<double> v0((size_t) Np * nv + 1);
-    for (int q = 0; q < Np; q++) {
-        memcpy(&u0[q * nu], a1->u0, nu * sizeof(int));
-        if (nv)
-            memcpy(&v0[q * nv], a1->v0, nv * sizeof(double));
-    }
-    int tablen = 1;
-    for (int node = 0; node < Nn; node++) {
-        long long tot = 0;
-        for (int c = 0; c < Nc; c++)
-            tot += a1->u0[(size_t) node * Nc + c];
-        tablen = (int) std::max<long long>(tablen, tot + 1);
-    }
-    std::vector<double> lfact(tablen);
-    si_lfact_fill(lfact.data(), tablen);
-    double tsp0[2] = {a1->tspan[0], a1->tspan[0] + 1.0};
-    int dummyU = 0;
-    double dummyV = 0;
-    siminf_gpu_solver_args a = *a1;
-    a.u0 = u0.data();
-    a.v0 = v0.data();
-    a.Nrep = Np;
-    a.tspan = tsp0;
-    a.tlen = 2;
-    a.U = &dummyU;
-    a.V = Nd > 0 ? &dummyV : nullptr;
-    a.len = 0;
-    siminf_gpu_options opt{};
-    opt.gdata_per_replicate = pf->gdata_per_particle;
-    siminf_gpu_plan *p = nullptr;
-    int rc = siminf_gpu_plan_create_ex(&a, model, &opt, &p);
-    if (rc)
-        return rc;
-    p->days_cap = p->ndays;
-    double *d_lfact = nullptr, *d_w = nullptr, *d_loglik = nullptr, *d_ess = nullptr;
-    int *d_anc = nullptr, *d_anc_out = nullptr, *d_obs = nullptr;
+    siminf_gpu_plan *p = ss->p;
     const cudaStream_t pst = p->stream;
-    rc = upload(&d_lfact, lfact.data(), lfact.size(), p->owned, pst);
-    if (!rc) rc = dalloc(&d_w, (size_t) Np, p->owned);
-    if (!rc) rc = dalloc(&d_anc, (size_t) Np, p->owned);
-    if (!rc && pf->ancestors) rc = dalloc(&d_anc_out, (size_t) Np * pf->n_obs, p->owned);
-    if (!rc) rc = upload(&d_obs, pf->obs, (size_t) pf->n_obs * Nn, p->owned, pst);
-    if (!rc) rc = dalloc(&d_loglik, 1, p->owned);
-    if (!rc) rc = dalloc(&d_ess, (size_t) pf->n_obs, p->owned);
-    if (!rc && cudaMemsetAsync(d_loglik, 0, sizeof(double), pst) != cudaSuccess)
-        rc = cuda_fail(cudaGetLastError(), "memset");
-    const double logp = si_log(pf->detect_p), logq = si_log(1.0 - pf->detect_p);
-    const double log_np = si_log((double) Np);
-    /* interval i runs tspan tsps[i] (R/pfilter.R:177-193) */
-    std::vector<std::array<double, 2>> tsps(pf->n_obs);
-    std::vector<int> tlens(pf->n_obs), ndays_i(pf->n_obs);
-    for (int i = 0; i < pf->n_obs; i++) {
-        const double prev = (i == 0) ? a1->tspan[0] : (double) pf->obs_time[i - 1];
-        if ((i == 0 && prev < pf->obs_time[0]) ||
-            (i > 0 && pf->obs_time[i] - pf->obs_time[i - 1] > 1)) {
-            tsps[i] = {prev, (double) pf->obs_time[i]};
-            tlens[i] = 2;
-        } else {
-            tsps[i] = {(double) pf->obs_time[i], 0.0};
-            tlens[i] = 1;
-        }
-        std::vector<DayInfo> dd;
-        plan_days(tsps[i].data(), tlens[i], dd);
-        ndays_i[i] = (int) dd.size();
-    }
-    /* Intervals 1.. with one shape (tspan length and day count) replay one
-     * CUDA graph; the rest run launch by launch. */
-    int g0 = pf->n_obs;
-    if (p->horizon && pf->n_obs > 2) {
-        g0 = 1;
-        for (int i = 2; i < pf->n_obs; i++)
-            if (tlens[i] != tlens[1] || ndays_i[i] != ndays_i[1])
-                g0 = pf->n_obs;
-    }
-    int prev_tlen = 2;
-    for (int i = 0; i < g0 && !rc; i++) {
-        const double *tsp = tsps[i].data();
-        const int tlen = tlens[i];
+    const int Np = ss->Np, Nn = ss->Nn, Nc = ss->Nc, n_obs = ss->n_obs;
+    cudaError_t e = cudaMemsetAsync(ss->d_loglik, 0, sizeof(double), pst);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_u0, ss->d_u0_start, (size_t) Np * ss->nu * sizeof(int),
+                            cudaMemcpyDeviceToDevice, pst);
+    if (e == cudaSuccess && ss->nv)
+        e = cudaMemcpyAsync(p->d_v0, ss->d_v0_start, (size_t) Np * ss->nv * sizeof(double),
+                            cudaMemcpyDeviceToDevice, pst);
+    if (e == cudaSuccess && gdata && ss->Ngd > 0)
+        e = cudaMemcpyAsync((void *) p->s.gdata, gdata,
+                            (size_t) ss->Ngd * (ss->per_particle ? Np : 1) * sizeof(double),
+                            cudaMemcpyHostToDevice, pst);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(pst);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "pfilter reset");
+    plan_changed(p);
+    int rc = 0, prev_tlen = 2;
+    for (int i = 0; i < ss->g0 && !rc; i++) {
+        const double *tsp = ss->tsps[i].data();
+        const int tlen = ss->tlens[i];
         if (i > 0) {
-            cudaError_t e = pf_gather(p->s.U, p->s.V, prev_tlen, (long long) nu, (long long) nv,
-                                      d_anc, Np, p->d_u0, p->d_v0, pst);
+            e = pf_gather(p->s.U, p->s.V, prev_tlen, (long long) ss->nu, (long long) ss->nv,
+                          ss->d_anc, Np, p->d_u0, p->d_v0, pst);
             if (e != cudaSuccess) {
                 rc = cuda_fail(e, "pf_gather");
                 break;
@@ -2021,41 +2116,214 @@ int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model 
         }
         if ((rc = plan_set_tspan(p, tsp, tlen)))
             break;
-        p->s.seed = (uint64_t) pf->seed + ((uint64_t) i + 1) * 0x9E3779B97F4A7C15ULL;
+        p->s.seed = pf_interval_seed(seed, i);
         if ((rc = plan_run_impl(p, pst, nullptr)))
             break;
-        cudaError_t e = pf_weights(p->s.U, tlen, Nn, Nc, Np, d_obs + (size_t) i * Nn,
-                                   pf->obs_compartment, d_lfact, tablen, logp, logq, d_w, pst);
+        e = pf_weights(p->s.U, tlen, Nn, Nc, Np, ss->d_obs + (size_t) i * Nn, ss->obs_c,
+                       ss->d_lfact, ss->tablen, ss->logp, ss->logq, ss->d_w, pst);
         if (e == cudaSuccess)
-            e = pf_finalize(d_w, Np, log_np, d_loglik, d_ess, i, (uint64_t) pf->seed,
-                            (((uint64_t) 1) << 62) + (uint64_t) i, d_anc,
-                            d_anc_out ? d_anc_out + (size_t) i * Np : nullptr, pst);
+            e = pf_finalize(ss->d_w, Np, ss->log_np, ss->d_loglik, ss->d_ess, i, seed,
+                            (((uint64_t) 1) << 62) + (uint64_t) i, ss->d_anc,
+                            ss->d_anc_out + (size_t) i * Np, pst);
         if (e != cudaSuccess) {
             rc = cuda_fail(e, "pf kernels");
             break;
         }
         prev_tlen = tlen;
     }
-    if (!rc && g0 < pf->n_obs)
-        rc = pfilter_graph(p, pf, g0, tsps, tlens, ndays_i[g0], prev_tlen, d_lfact, tablen, logp,
-                           logq, log_np, d_w, d_loglik, d_ess, d_anc, d_anc_out, d_obs, nu, nv);
+    if (!rc && ss->g0 < n_obs)
+        rc = pf_session_graph(ss, seed, prev_tlen);
     if (!rc) {
-        cudaError_t e = cudaMemcpyAsync(pf->loglik, d_loglik, sizeof(double),
-                                        cudaMemcpyDeviceToHost, pst);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(pf->ess, d_ess, (size_t) pf->n_obs * sizeof(double),
+        e = cudaMemcpyAsync(loglik, ss->d_loglik, sizeof(double), cudaMemcpyDeviceToHost, pst);
+        if (e == cudaSuccess && ess)
+            e = cudaMemcpyAsync(ess, ss->d_ess, (size_t) n_obs * sizeof(double),
                                 cudaMemcpyDeviceToHost, pst);
-        if (e == cudaSuccess && pf->ancestors)
-            e = cudaMemcpyAsync(pf->ancestors, d_anc_out, (size_t) pf->n_obs * Np * sizeof(int),
+        if (e == cudaSuccess && ancestors)
+            e = cudaMemcpyAsync(ancestors, ss->d_anc_out, (size_t) n_obs * Np * sizeof(int),
                                 cudaMemcpyDeviceToHost, pst);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(pst);
         if (e != cudaSuccess)
             rc = cuda_fail(e, "pf results");
     }
-    pf->ms_total = ms_since(t0);
-    siminf_gpu_plan_free(p);
     return rc;
+}
+
+int siminf_gpu_pfilter(const siminf_gpu_solver_args *a1, const siminf_gpu_model *model,
+                       siminf_gpu_pfilter_args *pf)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    if (!pf || !pf->loglik || !pf->ess) {
+        set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
+                   "invalid particle filter arguments");
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    }
+    PfSession *ss = nullptr;
+    int rc = pf_session_create(a1, model, pf, &ss);
+    if (!rc)
+        rc = pf_session_run(ss, nullptr, (uint64_t) pf->seed, pf->loglik, pf->ess,
+                            pf->ancestors);
+    pf_session_free(ss);
+    pf->ms_total = ms_since(t0);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* Particle-marginal Metropolis-Hastings (R/pmcmc.R:470-600): a chain    */
+/* resident across calls, whose particle filter session stays on the     */
+/* device from iteration to iteration and from call to call.             */
+/* ------------------------------------------------------------------ */
+#define PMCMC_SID (5ULL << 60)
+
+struct siminf_gpu_pmcmc {
+    std::mutex mu;                      /* one call at a time on a chain */
+    PfSession *ss = nullptr;
+    int n_pars = 0;
+    std::vector<int> idx;
+    std::vector<double> lo, hi, chol, gdata, theta;
+    uint64_t seed = 0;
+    long long length = 0;               /* iterations so far */
+    double logLik = 0, logPrior = 0, logPost = 0;
+};
+
+/* log of the uniform priors' density at th (R/pmcmc.R dpriors for
+ * U(lo, hi)): -sum log(hi - lo) inside the box, -Inf outside. */
+static double pmcmc_log_prior(const siminf_gpu_pmcmc *c, const std::vector<double> &th)
+{
+    double lp = 0.0;
+    for (int k = 0; k < c->n_pars; k++) {
+        if (!(th[k] >= c->lo[k] && th[k] <= c->hi[k]))
+            return -INFINITY;
+        lp -= std::log(c->hi[k] - c->lo[k]);
+    }
+    return lp;
+}
+
+/* One filter pass at th: the chain's gdata with th at its parameters. */
+static int pmcmc_loglik(siminf_gpu_pmcmc *c, const std::vector<double> &th, long long it,
+                        double *ll)
+{
+    for (int k = 0; k < c->n_pars; k++)
+        c->gdata[c->idx[k]] = th[k];
+    const uint64_t seed = c->seed ^ ((uint64_t) it * 0xD1B54A32D192ED03ULL);
+    return pf_session_run(c->ss, c->gdata.data(), seed, ll, nullptr, nullptr);
+}
+
+int siminf_gpu_pmcmc_create(const siminf_gpu_solver_args *args, const siminf_gpu_model *model,
+                            const siminf_gpu_pfilter_args *pf, const siminf_gpu_pmcmc_args *pm,
+                            siminf_gpu_pmcmc **out)
+{
+    memset(&g_status, 0, sizeof(g_status));
+    if (!out || !pm || !args || !model || pm->n_pars < 1 || !pm->gdata_index || !pm->theta ||
+        !pm->prior_lo || !pm->prior_hi || !pm->chol || !args->gdata ||
+        (pf && pf->gdata_per_particle)) {
+        set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0, "invalid pmcmc arguments");
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    }
+    *out = nullptr;
+    const int Ngd = model->L->Ngd;
+    for (int k = 0; k < pm->n_pars; k++) {
+        if (pm->gdata_index[k] < 0 || pm->gdata_index[k] >= Ngd ||
+            !(pm->prior_lo[k] < pm->prior_hi[k])) {
+            set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0,
+                       "pmcmc parameter outside gdata or with an empty prior");
+            return SIMINF_GPU_ERR_INVALID_MODEL;
+        }
+    }
+    siminf_gpu_pmcmc *c = new siminf_gpu_pmcmc();
+    int rc = pf_session_create(args, model, pf, &c->ss);
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    c->n_pars = pm->n_pars;
+    c->idx.assign(pm->gdata_index, pm->gdata_index + pm->n_pars);
+    c->lo.assign(pm->prior_lo, pm->prior_lo + pm->n_pars);
+    c->hi.assign(pm->prior_hi, pm->prior_hi + pm->n_pars);
+    c->chol.assign(pm->chol, pm->chol + (size_t) pm->n_pars * pm->n_pars);
+    c->gdata.assign(args->gdata, args->gdata + Ngd);
+    c->theta.assign(pm->theta, pm->theta + pm->n_pars);
+    c->seed = (uint64_t) pm->seed;
+    *out = c;
+    return 0;
+}
+
+int siminf_gpu_pmcmc_run(siminf_gpu_pmcmc *c, int n_iterations, double *rows)
+{
+    if (!c || n_iterations < 0)
+        return SIMINF_GPU_ERR_INVALID_MODEL;
+    std::lock_guard<std::mutex> lock(c->mu);
+    memset(&g_status, 0, sizeof(g_status));
+    const int np = c->n_pars, width = 4 + np;
+    for (int r = 0; r < n_iterations; r++) {
+        const long long it = ++c->length;         /* one-based, as the chain's rows */
+        double accept = 0.0;
+        int rc = 0;
+        if (it == 1) {
+            /* the first row: the initial theta (R/pmcmc.R:519-545) */
+            rc = pmcmc_loglik(c, c->theta, it, &c->logLik);
+            c->logPrior = pmcmc_log_prior(c, c->theta);
+            c->logPost = c->logLik + c->logPrior;
+        } else {
+            /* random-walk proposal theta + z Q, Q the upper Cholesky
+             * factor (R/pmcmc.R:423-437); z by Box-Muller (Box & Muller,
+             * 1958) from the chain's stream, then one uniform to accept */
+            si_rng rng;
+            si_rng_init(&rng, c->seed, PMCMC_SID + (uint64_t) it, 0);
+            std::vector<double> z(np), prop(np);
+            for (int k = 0; k < np; k++) {
+                const double u1 = si_uniform_pos(&rng), u2 = si_uniform_pos(&rng);
+                z[k] = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+            }
+            for (int j = 0; j < np; j++) {
+                double acc = c->theta[j];
+                for (int k = 0; k <= j; k++)
+                    acc += z[k] * c->chol[(size_t) k * np + j];
+                prop[j] = acc;
+            }
+            const double u = si_uniform_pos(&rng);
+            const double lp_prop = pmcmc_log_prior(c, prop);
+            if (std::isfinite(lp_prop)) {
+                double ll_prop = 0.0;
+                rc = pmcmc_loglik(c, prop, it, &ll_prop);
+                const double alpha = std::exp(ll_prop + lp_prop - c->logLik - c->logPrior);
+                if (!rc && std::isfinite(alpha) && u < alpha) {
+                    c->logLik = ll_prop;
+                    c->logPrior = lp_prop;
+                    c->logPost = c->logLik + c->logPrior;
+                    c->theta = prop;
+                    accept = 1.0;
+                }
+            }
+        }
+        if (rc) {
+            c->length--;
+            return rc;
+        }
+        if (rows) {
+            double *row = rows + (size_t) r * width;
+            row[0] = c->logPost;
+            row[1] = c->logLik;
+            row[2] = c->logPrior;
+            row[3] = accept;
+            for (int k = 0; k < np; k++)
+                row[4 + k] = c->theta[k];
+        }
+    }
+    return 0;
+}
+
+long long siminf_gpu_pmcmc_length(const siminf_gpu_pmcmc *c)
+{
+    return c ? c->length : 0;
+}
+
+void siminf_gpu_pmcmc_free(siminf_gpu_pmcmc *c)
+{
+    if (!c)
+        return;
+    pf_session_free(c->ss);
+    delete c;
 }
 
 static int run_solver(siminf_gpu_solver_args *args, const siminf_gpu_model *model,

@@ -45,8 +45,10 @@ __global__ void k_pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, con
  * sums, log-likelihood, ESS and resampling on thread 0. */
 __global__ void k_pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess,
                               int i, uint64_t seed, uint64_t sid, int *anc, int *anc_out,
-                              int *interval)
+                              int *interval, const uint64_t *seed_dev)
 {
+    if (seed_dev)
+        seed = *seed_dev;               /* graph replay: the pass's seed */
     if (interval) {
         /* graph replay: the interval, its resampling stream and its row of
          * ancestors come from the device counter, which moves on at the end */
@@ -136,10 +138,10 @@ cudaError_t pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, const int
 
 cudaError_t pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess, int i,
                         uint64_t seed, uint64_t sid, int *anc, int *anc_out, cudaStream_t st,
-                        int *interval)
+                        int *interval, const uint64_t *seed_dev)
 {
     k_pf_finalize<<<1, 1024, 0, st>>>(w, Np, log_np, loglik, ess, i, seed, sid, anc, anc_out,
-                                      interval);
+                                      interval, seed_dev);
     return cudaGetLastError();
 }
 

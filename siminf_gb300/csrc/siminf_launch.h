@@ -39,7 +39,7 @@ cudaError_t pf_weights(const int *U, int tlen, int Nn, int Nc, int Np, const int
                        double *w, cudaStream_t st, const int *interval = nullptr);
 cudaError_t pf_finalize(double *w, int Np, double log_np, double *loglik, double *ess, int i,
                         uint64_t seed, uint64_t sid, int *anc, int *anc_out, cudaStream_t st,
-                        int *interval = nullptr);
+                        int *interval = nullptr, const uint64_t *seed_dev = nullptr);
 cudaError_t pf_gather(const int *U, const double *V, int tlen, long long nu, long long nv,
                       const int *anc, int Np, int *u0, double *v0, cudaStream_t st);
 

@@ -123,6 +123,9 @@ int execute(siminf_gpu_request *r, cudaStream_t stream)
         siminf_gpu_plan_stats(r->plan, &r->stats);
         return rc;
     }
+    case SIMINF_GPU_REQUEST_PMCMC:
+        /* the chain's filter session is resident: only its iterations run */
+        return siminf_gpu_pmcmc_run(r->pmcmc, r->pmcmc_iterations, r->pmcmc_rows);
     default:
         capi_set_status(SIMINF_GPU_ERR_INVALID_MODEL, -1, -1, -1, 0, 0, "unknown request kind");
         return SIMINF_GPU_ERR_INVALID_MODEL;

@@ -61,6 +61,15 @@ def lib():
                                       C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                       C.POINTER(C.c_int)]
     L.siminf_gpu_schedule.restype = C.c_int
+    L.siminf_gpu_pmcmc_create.argtypes = [vp, vp, C.POINTER(abi.PfilterArgs),
+                                          C.POINTER(abi.PmcmcArgs), C.POINTER(vp)]
+    L.siminf_gpu_pmcmc_create.restype = C.c_int
+    L.siminf_gpu_pmcmc_run.argtypes = [vp, C.c_int, vp]
+    L.siminf_gpu_pmcmc_run.restype = C.c_int
+    L.siminf_gpu_pmcmc_length.argtypes = [vp]
+    L.siminf_gpu_pmcmc_length.restype = C.c_longlong
+    L.siminf_gpu_pmcmc_free.argtypes = [vp]
+    L.siminf_gpu_pmcmc_free.restype = None
     L.siminf_gpu_pfilter.argtypes = [vp, vp, C.POINTER(abi.PfilterArgs)]
     L.siminf_gpu_pfilter.restype = C.c_int
     L.siminf_gpu_individual_events_ex.argtypes = ([C.c_longlong] + [vp] * 6 +
@@ -122,6 +131,8 @@ EXPORTS = (
     "siminf_gpu_prevalence", "siminf_gpu_plan_outputs", "siminf_gpu_sort_events",
     "siminf_gpu_plan_day_max", "siminf_gpu_individual_events",
     "siminf_gpu_individual_events_ex", "siminf_gpu_model_load",
+    "siminf_gpu_pmcmc_create", "siminf_gpu_pmcmc_run", "siminf_gpu_pmcmc_length",
+    "siminf_gpu_pmcmc_free",
 )
 
 

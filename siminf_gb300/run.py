@@ -107,6 +107,66 @@ def pfilter(model, n_particles, obs_time, obs, obs_compartment, detect_p, seed=4
     return PfilterResult(float(ll[0]), ess, anc, pa.ms_total)
 
 
+class Pmcmc:
+    """A particle-marginal Metropolis-Hastings chain resident on the GPU
+    (siminf_gpu_pmcmc_*), the counterpart of R's pmcmc() and
+    continue_pmcmc() (R/pmcmc.R:470-600) for gdata parameters with uniform
+    priors and a fixed Gaussian random-walk proposal.  run(n) continues the
+    chain by n iterations and returns their rows (logPost, logLik,
+    logPrior, accept, theta...); chain holds every row so far."""
+
+    COLUMNS = ("logPost", "logLik", "logPrior", "accept")
+
+    def __init__(self, model, n_particles, obs_time, obs, obs_compartment, detect_p, pars,
+                 theta, prior_lo, prior_hi, covmat, seed=42):
+        self.model = model
+        self.pars = [int(k) for k in pars]
+        self._holder = abi.build_args(model, seed)
+        self._obs = np.ascontiguousarray(obs, dtype=np.int32)
+        self._obs_time = np.ascontiguousarray(obs_time, dtype=np.int32)
+        self._pf = abi.PfilterArgs(
+            n_particles=n_particles, gdata_per_particle=0, n_obs=len(self._obs_time),
+            obs_time=self._obs_time.ctypes.data_as(C.POINTER(C.c_int)),
+            obs=self._obs.ctypes.data_as(C.POINTER(C.c_int)), obs_compartment=obs_compartment,
+            detect_p=detect_p, seed=seed)
+        n = len(self.pars)
+        chol = np.linalg.cholesky(np.asarray(covmat, dtype=np.float64)).T   # upper: covmat = Q'Q
+        self._keep = [np.ascontiguousarray(x, dtype=dt) for x, dt in (
+            (self.pars, np.int32), (theta, np.float64), (prior_lo, np.float64),
+            (prior_hi, np.float64), (chol, np.float64))]
+        k = self._keep
+        self._args = abi.PmcmcArgs(
+            n_pars=n, gdata_index=k[0].ctypes.data_as(C.POINTER(C.c_int)),
+            theta=k[1].ctypes.data_as(C.POINTER(C.c_double)),
+            prior_lo=k[2].ctypes.data_as(C.POINTER(C.c_double)),
+            prior_hi=k[3].ctypes.data_as(C.POINTER(C.c_double)),
+            chol=k[4].ctypes.data_as(C.POINTER(C.c_double)), seed=seed)
+        h = C.c_void_p()
+        native.check(native.lib().siminf_gpu_pmcmc_create(
+            C.cast(self._holder.ref(), C.c_void_p), native.device_model(model.name).handle,
+            C.byref(self._pf), C.byref(self._args), C.byref(h)))
+        self.handle = h
+        self.chain = np.zeros((0, 4 + n))
+
+    def run(self, n_iterations):
+        rows = np.zeros((n_iterations, 4 + len(self.pars)))
+        native.check(native.lib().siminf_gpu_pmcmc_run(self.handle, int(n_iterations),
+                                                       rows.ctypes.data_as(C.c_void_p)))
+        self.chain = np.vstack([self.chain, rows])
+        return rows
+
+    def close(self):
+        if getattr(self, "handle", None):
+            native.lib().siminf_gpu_pmcmc_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def compartment_mask(model, names_or_indices):
     """Bit mask of compartments given by index or by u0 row position."""
     mask = 0

@@ -108,12 +108,28 @@ class Server:
         t.req.plan = plan.handle
         return self._submit(t)
 
+    def pmcmc(self, chain, n_iterations):
+        """A continuation of a resident run.Pmcmc chain by n_iterations
+        (continue_pmcmc, R/pmcmc.R:474-600): its filter session stays on
+        the device between requests; the rows arrive in ticket.rows and are
+        appended to chain.chain once the ticket is waited for."""
+        t = Ticket(abi.REQUEST_PMCMC)
+        t.rows = np.zeros((n_iterations, 4 + len(chain.pars)))
+        t.chain = chain
+        t.req.pmcmc = chain.handle
+        t.req.pmcmc_iterations = int(n_iterations)
+        t.req.pmcmc_rows = t.rows.ctypes.data_as(C.c_void_p)
+        return self._submit(t)
+
     def wait(self, ticket, timeout_ms=-1.0):
         """True when the request has finished; raises on its error."""
         done = native.lib().siminf_gpu_server_wait(self.handle, C.byref(ticket.req),
                                                    float(timeout_ms))
         if done and ticket.req.status:
             raise abi.SimInfError(ticket.req.status, ticket.req.message.decode(errors="replace"))
+        if done and getattr(ticket, "chain", None) is not None:
+            ticket.chain.chain = np.vstack([ticket.chain.chain, ticket.rows])
+            ticket.chain = None
         return bool(done)
 
     def load(self):

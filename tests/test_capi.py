@@ -15,7 +15,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     with open(os.path.join(ROOT, "include", "siminf_gb300.h")) as f:
         text = f.read()
-    return sorted(set(re.findall(r"^(?:int|void)\s+(siminf_gpu_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:int|void|long long)\s+(siminf_gpu_\w+)\s*\(", text,
+                                 re.M)))
 
 
 def test_header_declares_entry_points():

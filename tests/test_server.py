@@ -19,7 +19,7 @@ STRUCTS = [("siminf_gpu_request", abi.Request), ("siminf_gpu_server_options", ab
            ("siminf_gpu_pfilter_args", abi.PfilterArgs), ("siminf_gpu_options", abi.Options),
            ("siminf_gpu_stats", abi.Stats), ("siminf_gpu_solver_args", abi.SolverArgs),
            ("siminf_gpu_tune_result", abi.TuneResult),
-           ("siminf_gpu_reduce_stats", abi.ReduceStats),
+           ("siminf_gpu_reduce_stats", abi.ReduceStats), ("siminf_gpu_pmcmc_args", abi.PmcmcArgs),
            ("siminf_gpu_prevalence_spec", abi.PrevalenceSpec)]
 
 
