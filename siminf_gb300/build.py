@@ -1,7 +1,9 @@
 """Build libsiminf_gb300.so in-tree with nvcc for sm_103a.
 
 The library is the C ABI of include/siminf_gb300.h: siminf_kernels.cu (the
-kernels, one instantiation per shipped model), siminf_capi.cpp (planning
+particle filter's kernels and the model lookup), siminf_models_a/b/c.cu
+(the SSA and event kernels, one instantiation per shipped model),
+siminf_capi.cpp (planning
 and the exported entry points), siminf_noalloc.cu (the allocation-free
 solver entry point and its static scratch), siminf_batch.cu (batches of
 uneven models), siminf_server.cpp (the request loop), siminf_reduce.cu (trajectory and
@@ -25,8 +27,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # reference's C (bit-identical trajectories).
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off"]
-SOURCES = ["siminf_kernels.cu", "siminf_capi.cpp", "siminf_noalloc.cu", "siminf_batch.cu",
-           "siminf_server.cpp", "siminf_reduce.cu", "siminf_events.cu", "siminf_individual.cu"]
+SOURCES = ["siminf_kernels.cu", "siminf_models_a.cu", "siminf_models_b.cu", "siminf_models_c.cu",
+           "siminf_capi.cpp", "siminf_noalloc.cu", "siminf_batch.cu", "siminf_server.cpp",
+           "siminf_reduce.cu", "siminf_events.cu", "siminf_individual.cu"]
 
 
 def nvcc():

@@ -1,7 +1,8 @@
 /*
- * siminf_kernels.cu -- the kernel templates of siminf_kernels.cuh
- * instantiated for the models the library ships (siminf_models.cuh), and
- * the particle filter's kernels, which do not depend on the model.
+ * siminf_kernels.cu -- the lookup of the models the library ships
+ * (siminf_models.cuh; their kernels are instantiated in siminf_models_a.cu,
+ * _b.cu and _c.cu), and the particle filter's kernels, which do not depend
+ * on the model.
  */
 #include "siminf_kernels.cuh"
 
@@ -153,33 +154,18 @@ cudaError_t pf_gather(const int *U, const double *V, int tlen, long long nu, lon
     return cudaGetLastError();
 }
 
+/* The shipped models' launcher tables, instantiated in three translation
+ * units (siminf_models_a.cu, _b.cu, _c.cu) that compile in parallel. */
+const Launchers *launchers_shipped_a(const char *name);
+const Launchers *launchers_shipped_b(const char *name);
+const Launchers *launchers_shipped_c(const char *name);
+
 const Launchers *launchers_for(const char *name)
 {
-    struct Entry {
-        const char *name;
-        const Launchers *(*table)();
-    };
-    static const Entry entries[] = {
-        {"SIR", Launch<ModelSIR>::table},
-        {"SEIR", Launch<ModelSEIR>::table},
-        {"SIS", Launch<ModelSIS>::table},
-        {"SISe", Launch<ModelSISe>::table},
-        {"SISe3", Launch<ModelSISe3>::table},
-        {"SIR_mparse", Launch<ModelSIRmparse>::table},
-        {"SISe_pf", Launch<ModelSISePF>::table},
-        {"SISe_sp", Launch<ModelSISe_sp>::table},
-        {"SISe3_sp", Launch<ModelSISe3_sp>::table},
-    };
-    for (const Entry &e : entries) {
-        const char *a = e.name, *b = name;
-        while (*a && *a == *b) {
-            a++;
-            b++;
-        }
-        if (*a == 0 && *b == 0)
-            return e.table();
-    }
-    return nullptr;
+    const Launchers *t = launchers_shipped_a(name);
+    if (!t)
+        t = launchers_shipped_b(name);
+    return t ? t : launchers_shipped_c(name);
 }
 
 }  // namespace siminf

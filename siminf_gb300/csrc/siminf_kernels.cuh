@@ -54,9 +54,9 @@ enum { ERR_NEGATIVE_STATE = -1, ERR_UNDEFINED_EVENT = -3, ERR_SAMPLE_SELECT = -8
 enum { EV_EXIT = 0, EV_ENTER = 1, EV_INTERNAL = 2, EV_EXTERNAL = 3 };
 
 /* Out of line: errors are rare, and every kernel calls this. */
-__device__ __noinline__ void record_error(const DevState &s, int code, int phase, int day,
-                                             long long g, int tr, int evi, double time,
-                                             double rate)
+static __device__ __noinline__ void record_error(const DevState &s, int code, int phase,
+                                                int day, long long g, int tr, int evi,
+                                                double time, double rate)
 {
     const int slot = atomicAdd(s.err_count, 1);
     atomicMin(s.err_day, day);
@@ -151,6 +151,24 @@ __device__ __forceinline__ void prefix_sums(const double (&rate)[M::NT], double 
         cum[k] = cum[k - 1] + rate[k];
 }
 
+/* The transition the inversion picks (ssm.c:165-169): the first k with
+ * !(rnd > rate[0] + ... + rate[k]), else NT - 1.  The prefix sums are
+ * formed from the rates at each selection -- they depend on the rates
+ * alone, so they run beside the rate sum's update -- instead of being
+ * carried from step to step in registers. */
+template <class M>
+__device__ __forceinline__ int select_transition(const double (&rate)[M::NT], double rnd)
+{
+    double cum[M::NT];
+    prefix_sums<M>(rate, cum);
+    int tr = M::NT - 1;
+#pragma unroll
+    for (int k = M::NT - 2; k >= 0; k--)
+        if (!(rnd > cum[k]))
+            tr = k;
+    return tr;
+}
+
 __device__ __forceinline__ uint32_t word_of(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3,
                                             uint32_t i)
 {
@@ -179,7 +197,7 @@ __device__ __forceinline__ void philox_block(const si_rng &r, uint64_t blk, uint
 template <class M>
 struct SsaLane {
     int u[M::NC];
-    double rate[M::NT], cum[M::NT];
+    double rate[M::NT];
     double sum, t, L, U, tau;
     uint64_t c;                       /* draw index of the next waiting time */
     uint32_t q0, q1, q2, q3;          /* Philox block (c + 1) >> 2 */
@@ -210,7 +228,6 @@ __device__ __forceinline__ bool ssa_begin(SsaLane<M> &ln, const si_rng &key, uin
         ln.t = next;
         return true;
     }
-    prefix_sums<M>(ln.rate, ln.cum);
     /* the pair of the first transition */
     uint32_t p0, p1, p2, p3;
     philox_block(key, c >> 2, p0, p1, p2, p3);
@@ -241,12 +258,7 @@ __device__ __forceinline__ bool ssa_step_ahead(SsaLane<M> &ln, const si_rng &key
     const double tau = si_div(ln.L, ln.sum);
     const double rnd = ln.U * ln.sum;
 
-    /* Inversion: the first k with !(rnd > cum[k]), else NT - 1. */
-    int tr = NT - 1;
-#pragma unroll
-    for (int k = NT - 2; k >= 0; k--)
-        if (!(rnd > ln.cum[k]))
-            tr = k;
+    int tr = select_transition<M>(ln.rate, rnd);
     double rtr = ln.rate[0];
 #pragma unroll
     for (int k = 1; k < NT; k++)
@@ -349,7 +361,6 @@ __device__ __forceinline__ bool ssa_step_ahead(SsaLane<M> &ln, const si_rng &key
         ln.err_t = ln.t;
         ln.err_rate = bad_rate;
     }
-    prefix_sums<M>(ln.rate, ln.cum);
     if (!si_finite_pos(ln.sum)) {
         if (!le_zero(si_double_bits(ln.sum)) && !ln.err) {
             ln.err = ERR_INVALID_RATE;
@@ -361,6 +372,109 @@ __device__ __forceinline__ bool ssa_step_ahead(SsaLane<M> &ln, const si_rng &key
         return true;
     }
     return false;
+}
+
+/* The step of ssa_step_ahead as one block of straight-line code, for
+ * the common case: no zero rate selected, no negative state, no invalid
+ * or non-positive rate sum, no division off the integer path, a prepared
+ * divisor that every rate's division finds in the cache, a next waiting
+ * time on the table path of -log(u), and the transition count within
+ * max_fired.  Every rate is evaluated (and kept where its G bit is set),
+ * so that no branch splits the block and the compiler can interleave the
+ * waiting time's division, the next draws and the rate refresh, which do
+ * not depend on one another.  Returns SSA_FIRED or SSA_DAY_OVER with the
+ * state updated exactly as ssa_step_ahead updates it, or SSA_REDO with
+ * the state untouched when any of those conditions fails; the caller then
+ * runs ssa_step_ahead on the same state. */
+enum { SSA_FIRED = 0, SSA_DAY_OVER = 1, SSA_REDO = 2 };
+
+template <class M>
+__device__ __forceinline__ int ssa_step_spec(SsaLane<M> &ln, const si_rng &key, double next,
+                                             const double *v, const double *ld,
+                                             const double *gd, const int *sS,
+                                             const uint32_t *sG, unsigned max_fired)
+{
+    constexpr int NC = M::NC, NT = M::NT;
+    int tau_special = 0;
+    const double tau = si_div_spec(ln.L, ln.sum, &tau_special);
+    const double rnd = ln.U * ln.sum;
+
+    int tr = select_transition<M>(ln.rate, rnd);
+    double rtr = ln.rate[0];
+#pragma unroll
+    for (int k = 1; k < NT; k++)
+        if (tr == k)
+            rtr = ln.rate[k];
+    int redo = si_is_zero(rtr);             /* the back-scan of ssm.c:171-189 */
+
+    /* The state after that transition. */
+    int u2[NC];
+#pragma unroll
+    for (int cc = 0; cc < NC; cc++) {
+        const int d = sS[tr * NC + cc];
+        u2[cc] = ln.u[cc] + d;
+        redo |= (d != 0) & (u2[cc] < 0);
+    }
+    /* Every rate at that state; those flagged in column tr of G replace
+     * the old ones and enter the delta in row order. */
+    const uint32_t gm = sG[tr];
+    si_recip_spec dcs;
+    dcs.c = &ln.dc;
+    dcs.flag = 0;
+    double rate2[NT];
+    double delta = 0.0;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        const int f0 = dcs.flag;            /* a rate that is not kept flags nothing */
+        const double nr = M::rate(k, u2, v, ld, gd, ln.t, dcs);
+        const bool g = (gm >> k) & 1u;
+        dcs.flag = g ? dcs.flag : f0;
+        rate2[k] = g ? nr : ln.rate[k];
+        const double dk = delta + (nr - ln.rate[k]);
+        delta = g ? dk : delta;
+        redo |= g & si_bad_rate(nr);
+    }
+    const double sum2 = ln.sum + delta;
+    redo |= dcs.flag | !si_finite_pos(sum2);
+    redo |= ln.fired + 1u > max_fired;
+
+    /* Draws of the transition after it. */
+    const uint64_t c2 = ln.c + 2;
+    uint32_t n0, n1, n2, n3;
+    philox_block(key, (c2 + 1) >> 2, n0, n1, n2, n3);
+    const uint32_t ci = (uint32_t) c2 & 3u;
+    const uint32_t wl = (ci == 3u) ? ln.q3 : word_of(n0, n1, n2, n3, ci);
+    const uint32_t wu = word_of(n0, n1, n2, n3, (ci + 1u) & 3u);
+    const double L2 = si_neglog_u32_spec(wl, &redo);
+    const double U2 = si_u32_to_uniform_pos(wu);
+
+    if (tau_special)
+        return SSA_REDO;
+    const double tn = tau + ln.t;
+    if (tn >= next) {
+        ln.t = next;
+        ln.c += 1;                            /* the waiting time's draw was used */
+        return SSA_DAY_OVER;
+    }
+    if (redo)
+        return SSA_REDO;
+    ln.t = tn;
+    ln.c = c2;
+    ln.fired++;
+#pragma unroll
+    for (int cc = 0; cc < NC; cc++)
+        ln.u[cc] = u2[cc];
+#pragma unroll
+    for (int k = 0; k < NT; k++)
+        ln.rate[k] = rate2[k];
+    ln.sum = sum2;
+    ln.q0 = n0;
+    ln.q1 = n1;
+    ln.q2 = n2;
+    ln.q3 = n3;
+    ln.L = L2;
+    ln.U = U2;
+    return SSA_FIRED;
 }
 
 /* One step of the direct method in the reference's order: the waiting
@@ -401,12 +515,7 @@ __device__ __forceinline__ bool ssa_step_in_order(SsaLane<M> &ln, const si_rng &
         ln.U = si_u32_to_uniform_pos(wu);
     }
 
-    /* Inversion: the first k with !(rnd > cum[k]), else NT - 1. */
-    int tr = NT - 1;
-#pragma unroll
-    for (int k = NT - 2; k >= 0; k--)
-        if (!(rnd > ln.cum[k]))
-            tr = k;
+    int tr = select_transition<M>(ln.rate, rnd);
     double rtr = ln.rate[0];
 #pragma unroll
     for (int k = 1; k < NT; k++)
@@ -478,7 +587,6 @@ __device__ __forceinline__ bool ssa_step_in_order(SsaLane<M> &ln, const si_rng &
         ln.err_rate = bad_rate;
     }
     ln.sum += delta;
-    prefix_sums<M>(ln.rate, ln.cum);
 
     if (!si_finite_pos(ln.sum)) {
         if (!le_zero(si_double_bits(ln.sum)) && !ln.err) {
@@ -495,16 +603,22 @@ __device__ __forceinline__ bool ssa_step_in_order(SsaLane<M> &ln, const si_rng &
 }
 
 /* One step of the direct method (src/solvers/SimInf_solver_ssm.c:
- * 144-235): ahead of the waiting time where the rates do not read t. */
+ * 144-235): where the rates do not read t, the straight-line speculative
+ * step, redone ahead of the waiting time on the exact path when it meets
+ * a rare case. */
 template <class M>
 __device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, double next,
                                          const double *v, const double *ld, const double *gd,
                                          const int *sS, const uint32_t *sG, unsigned max_fired)
 {
-    if constexpr (M::RATES_TIME_INVARIANT)
+    if constexpr (M::RATES_TIME_INVARIANT) {
+        const int st = ssa_step_spec<M>(ln, key, next, v, ld, gd, sS, sG, max_fired);
+        if (st != SSA_REDO)
+            return st == SSA_DAY_OVER;
         return ssa_step_ahead<M>(ln, key, next, v, ld, gd, sS, sG, max_fired);
-    else
+    } else {
         return ssa_step_in_order<M>(ln, key, next, v, ld, gd, sS, sG, max_fired);
+    }
 }
 
 /* A node's whole SSA day in one call (used where one thread keeps one
@@ -734,11 +848,11 @@ __device__ int apply_e1(const DevState &s, int *uu, const E1Rec &e, si_rng *r)
     }
 }
 
-/* The E1 events of one node-day, applied out of line: about one node-day
- * in 250 has any, and inlined, the samplers they use would sit in the
- * code of the SSA loop that every warp of k_ssa_e1 runs.  State and
- * stream counter go in and out by value, so the caller's copies stay in
- * registers. */
+/* The E1 events of one node-day.  Inlined: a call would make the SSA
+ * kernels save the registers live across it to local memory (spills),
+ * while the samplers' code, after the SSA loop, runs only on the one
+ * node-day in about 250 that has events.  State and stream counter go in
+ * and out by value, so the caller's copies stay in registers. */
 template <int NC>
 struct E1Out {
     int u[NC];
@@ -748,7 +862,7 @@ struct E1Out {
 };
 
 template <int NC>
-__device__ __noinline__ E1Out<NC> node_e1_apply(const DevState &s, E1Out<NC> o, si_rng r, int lo,
+__device__ __forceinline__ E1Out<NC> node_e1_apply(const DevState &s, E1Out<NC> o, si_rng r, int lo,
                                                 int end, int day)
 {
     for (int k = lo; k < end; k++) {

@@ -20,6 +20,9 @@
  * IEEE round-to-nearest division on the integer pipes.  rate() takes a
  * one-entry cache of the prepared divisor (si_div_cached): a population
  * count, which the transitions keep constant, is prepared once per change.
+ * The cache is an si_recip, or in the SSA's speculative step an
+ * si_recip_spec, which reads the prepared divisor and flags a stale one
+ * instead of preparing it (the step is then redone on the exact path).
  */
 #ifndef SIMINF_MODELS_CUH
 #define SIMINF_MODELS_CUH
@@ -32,9 +35,10 @@ struct ModelSIR {
     static constexpr int NGD = 0;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         if (k == 0) {
             const double S_n = si_i2d(u[0]);
@@ -59,9 +63,10 @@ struct ModelSEIR {
     static constexpr int NGD = 0;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         if (k == 0) {
             const double S_n = si_i2d(u[0]);
@@ -88,9 +93,10 @@ struct ModelSIS {
     static constexpr int NGD = 0;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         if (k == 0) {
             const double S_n = si_i2d(u[0]);
@@ -143,9 +149,10 @@ struct ModelSISe {
     static constexpr int NGD = 8;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         if (k == 0)
             return gdata[0] * v[0] * si_i2d(u[0]);
@@ -182,9 +189,10 @@ struct ModelSISe3 {
     static constexpr int NGD = 12;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         switch (k) {
         case 0: return gdata[0] * v[0] * si_i2d(u[0]);
@@ -254,9 +262,10 @@ struct ModelSISe_sp {
     static constexpr int NGD = 8;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = false;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         if (k == 0)
             return gdata[0] * v[0] * si_i2d(u[0]);
@@ -292,9 +301,10 @@ struct ModelSISe3_sp {
     static constexpr int NGD = 12;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = false;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         return ModelSISe3::rate(k, u, v, ldata, gdata, t, dc);
     }
@@ -327,9 +337,10 @@ struct ModelSIRmparse {
     static constexpr int NGD = 2;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         if (k == 0) {
             const double N = si_i2d(u[0] + u[1] + u[2]);             /* int sum, as in C */
@@ -352,9 +363,10 @@ struct ModelSISePF {
     static constexpr int NGD = 2;  /* gdata entries read */
     static constexpr bool PTS_LOCAL = true;
     static constexpr bool RATES_TIME_INVARIANT = true;  /* rate() ignores t */
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &dc)
+                                                  double t, DC &dc)
     {
         if (k == 0)
             return gdata[0] * v[0] * si_i2d(u[0]);

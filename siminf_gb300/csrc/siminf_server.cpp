@@ -225,8 +225,12 @@ int siminf_gpu_server_submit(siminf_gpu_server *sv, siminf_gpu_request *r)
 {
     if (!sv || !r)
         return SIMINF_GPU_ERR_INVALID_MODEL;
+    /* a plan or a pmcmc chain is resident and carries its own model */
+    const bool resident = r->kind == SIMINF_GPU_REQUEST_PLAN ||
+                          r->kind == SIMINF_GPU_REQUEST_PMCMC;
     if ((r->kind == SIMINF_GPU_REQUEST_PLAN && !r->plan) ||
-        (r->kind != SIMINF_GPU_REQUEST_PLAN && (!r->args || !r->model)) ||
+        (r->kind == SIMINF_GPU_REQUEST_PMCMC && (!r->pmcmc || r->pmcmc_iterations < 0)) ||
+        (!resident && (!r->args || !r->model)) ||
         (r->kind == SIMINF_GPU_REQUEST_PFILTER && !r->pfilter))
         return SIMINF_GPU_ERR_INVALID_MODEL;
     r->status = 0;

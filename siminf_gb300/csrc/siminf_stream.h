@@ -517,14 +517,31 @@ SI_HD double si_neglog_u32_tab(uint32_t w)
     const uint64_t l2h = (uint64_t) (l2 >> 63);              /* sign extension */
     hi -= l2h + (lo < l2u);
     lo -= l2u;
-    /* to double: the value is >= 1/16, so its top bit is at 64 + (0..4)
-     * or at 60..63 of lo */
-    int p;
-    if (hi)
-        p = 64 + 31 - si_clz32((uint32_t) hi);
-    else
-        p = 63 - si_clz32((uint32_t) (lo >> 32));
-    return si_u128_to_double_at(hi, lo, p, 64);
+    /* to double: the value lies in [2^-8, 23), so its top bit p is at
+     * 64 + (0..4) or at 56..63 of lo, and the rounding of
+     * si_u128_to_double_at(hi, lo, p, 64) takes the shift sh = p - 52 in
+     * 4..16 -- written out here as straight-line code */
+    const int p = hi ? 64 + 31 - si_clz32((uint32_t) hi)
+                     : 63 - si_clz32((uint32_t) (lo >> 32));
+    const int sh = p - 52;
+    uint64_t m = (lo >> sh) | (hi << (64 - sh));
+    const uint64_t rnd = (lo >> (sh - 1)) & 1;
+    const uint64_t sticky = lo & ((1ULL << (sh - 1)) - 1);
+    m += rnd & ((sticky != 0) | (m & 1));
+    const int ov = (int) (m >> 53);
+    m >>= ov;
+    const uint64_t expo = (uint64_t) (p + ov - 64 + 1023);
+    return si_bits_double((expo << 52) | (m & 0x000FFFFFFFFFFFFFULL));
+}
+
+/* si_neglog_u32 for a speculative step: the table value in straight-line
+ * code, with *slow set when w is one of the words (probability 2^-8) that
+ * si_neglog_u32 hands to si_log instead. */
+SI_HD double si_neglog_u32_spec(uint32_t w, int *slow)
+{
+    const uint64_t x = 2 * (uint64_t) w + 1;
+    *slow |= x >= ((uint64_t) 1 << 33) - ((uint64_t) 1 << 25);
+    return si_neglog_u32_tab(w);
 }
 
 #ifdef __CUDACC__
@@ -674,10 +691,9 @@ SI_HD si_recip si_recip_prep(double b)
     si_recip r;
     r.B = si_double_bits(b);
     const int eb = (int) ((r.B >> 52) & 0x7FF);
-    r.mb = 0;
-    r.y = 0;
-    if (eb == 0 || eb == 0x7FF)
-        return r;
+    /* straight-line: the steps run on any bits, and a divisor without
+     * a normal mantissa keeps mb = y = 0 */
+    const int normal = (eb != 0) & (eb != 0x7FF);
     const uint64_t mb = (r.B & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
     uint64_t y = si_recip_seed((uint32_t) (mb >> 29));
     for (int it = 0; it < 2; it++) {
@@ -691,8 +707,8 @@ SI_HD si_recip si_recip_prep(double b)
         const int64_t hi = si_mulhi64((int64_t) (y >> 1), d32);
         y = (uint64_t) ((int64_t) y + (hi >> 18));
     }
-    r.mb = mb;
-    r.y = y;
+    r.mb = normal ? mb : 0;
+    r.y = normal ? y : 0;
     return r;
 }
 
@@ -703,8 +719,10 @@ SI_HD si_recip si_recip_prep(double b)
  * ma 2^52 / mb (y is a lower bound good to ~2^-60), and the exact
  * remainder fixes it; the fix-ups are selects, so the path is straight
  * code.  Every other case (zero, subnormal, infinite, NaN operands or an
- * overflowing or underflowing quotient) uses the hardware division. */
-SI_HD double si_div_r(double a, const si_recip *r, double b)
+ * overflowing or underflowing quotient) sets *special, and the value
+ * returned is then meaningless: si_div_r takes the hardware division for
+ * it, a speculative step redoes its work on the exact path. */
+SI_HD double si_div_r_spec(double a, const si_recip *r, int *special)
 {
     const uint64_t A = si_double_bits(a);
     const int ea = (int) ((A >> 52) & 0x7FF), eb = (int) ((r->B >> 52) & 0x7FF);
@@ -713,8 +731,7 @@ SI_HD double si_div_r(double a, const si_recip *r, double b)
     const int lt = ma < mb;                  /* quotient of the mantissas in [1, 2) */
     ma <<= lt;
     const int e = ea - eb - lt;
-    if ((mb == 0) | (ea == 0) | (ea == 0x7FF) | (e > 1022) | (e < -1022))
-        return a / b;
+    *special |= (mb == 0) | (ea == 0) | (ea == 0x7FF) | (e > 1022) | (e < -1022);
     const uint64_t sign = (A ^ r->B) & 0x8000000000000000ULL;
     uint64_t Q = si_umulhi64(ma << 1, r->y);
     int64_t R = (int64_t) ((ma << 52) - Q * mb);
@@ -740,10 +757,25 @@ SI_HD double si_div_r(double a, const si_recip *r, double b)
     return si_bits_double(sign | (expo << 52) | (Q & 0x000FFFFFFFFFFFFFULL));
 }
 
+SI_HD double si_div_r(double a, const si_recip *r, double b)
+{
+    int special = 0;
+    const double q = si_div_r_spec(a, r, &special);
+    return special ? a / b : q;
+}
+
 SI_HD double si_div(double a, double b)
 {
     const si_recip r = si_recip_prep(b);
     return si_div_r(a, &r, b);
+}
+
+/* a / b on the integer path alone, *special set where si_div would take
+ * the hardware division. */
+SI_HD double si_div_spec(double a, double b, int *special)
+{
+    const si_recip r = si_recip_prep(b);
+    return si_div_r_spec(a, &r, special);
 }
 
 /* a / b through a one-entry cache of prepared divisors: a rate that
@@ -755,6 +787,23 @@ SI_HD double si_div_cached(double a, double b, si_recip *c)
         *c = si_recip_prep(b);
     return si_div_r(a, c, b);
 }
+
+#ifdef __cplusplus
+/* The divisor cache as a speculative step reads it: the prepared divisor
+ * is used as it is, and a division by another divisor, or one that
+ * leaves the integer path, sets flag instead of branching (the step is
+ * then redone with the si_recip itself). */
+struct si_recip_spec {
+    const si_recip *c;
+    int flag;
+};
+
+SI_HD double si_div_cached(double a, double b, si_recip_spec *s)
+{
+    s->flag |= si_double_bits(b) != s->c->B;
+    return si_div_r_spec(a, s->c, &s->flag);
+}
+#endif
 
 /* An empty cache (no divisor has these bits and a zero mantissa). */
 SI_HD si_recip si_recip_none(void)

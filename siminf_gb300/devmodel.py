@@ -184,9 +184,10 @@ struct ModelCompiled {
     static constexpr int NC = %(nc)d, NT = %(nt)d, ND = %(nd)d, NGD = %(ngd)d;
     static constexpr bool PTS_LOCAL = %(local)s;
     static constexpr bool RATES_TIME_INVARIANT = %(tinv)s;
+    template <class DC>
     __device__ __forceinline__ static double rate(int k, const int *u, const double *v,
                                                   const double *ldata, const double *gdata,
-                                                  double t, si_recip &)
+                                                  double t, DC &)
     {
         switch (k) {
 %(cases)s
