@@ -377,27 +377,28 @@ __device__ __forceinline__ bool ssa_step_ahead(SsaLane<M> &ln, const si_rng &key
 /* The step of ssa_step_ahead as one block of straight-line code, for
  * the common case: no zero rate selected, no negative state, no invalid
  * or non-positive rate sum, no division off the integer path, a prepared
- * divisor that every rate's division finds in the cache, a next waiting
- * time on the table path of -log(u), and the transition count within
+ * divisor that every rate's division finds in the cache, a waiting time
+ * on the table path of -log(u), and the transition count within
  * max_fired.  Every rate is evaluated (and kept where its G bit is set),
- * so that no branch splits the block and the compiler can interleave the
- * waiting time's division, the next draws and the rate refresh, which do
- * not depend on one another.  Returns SSA_FIRED or SSA_DAY_OVER with the
- * state updated exactly as ssa_step_ahead updates it, or SSA_REDO with
- * the state untouched when any of those conditions fails; the caller then
- * runs ssa_step_ahead on the same state. */
+ * so that no branch splits the block.  L and U are the step's -log(u) and
+ * selection uniform; with NEXT, the step also computes the next step's
+ * pair into ln.L and ln.U (the way ssa_step_ahead does), without it the
+ * caller supplies every step's pair.  Returns SSA_FIRED or SSA_DAY_OVER
+ * with the state updated exactly as ssa_step_ahead updates it, or
+ * SSA_REDO with the state untouched when any of those conditions fails;
+ * the caller then runs ssa_step_ahead on the same state and draws. */
 enum { SSA_FIRED = 0, SSA_DAY_OVER = 1, SSA_REDO = 2 };
 
-template <class M>
-__device__ __forceinline__ int ssa_step_spec(SsaLane<M> &ln, const si_rng &key, double next,
-                                             const double *v, const double *ld,
-                                             const double *gd, const int *sS,
+template <class M, bool NEXT>
+__device__ __forceinline__ int ssa_step_spec(SsaLane<M> &ln, const si_rng &key, double L,
+                                             double U, double next, const double *v,
+                                             const double *ld, const double *gd, const int *sS,
                                              const uint32_t *sG, unsigned max_fired)
 {
     constexpr int NC = M::NC, NT = M::NT;
     int tau_special = 0;
-    const double tau = si_div_spec(ln.L, ln.sum, &tau_special);
-    const double rnd = ln.U * ln.sum;
+    const double tau = si_div_spec(L, ln.sum, &tau_special);
+    const double rnd = U * ln.sum;
 
     int tr = select_transition<M>(ln.rate, rnd);
     double rtr = ln.rate[0];
@@ -440,13 +441,16 @@ __device__ __forceinline__ int ssa_step_spec(SsaLane<M> &ln, const si_rng &key, 
 
     /* Draws of the transition after it. */
     const uint64_t c2 = ln.c + 2;
-    uint32_t n0, n1, n2, n3;
-    philox_block(key, (c2 + 1) >> 2, n0, n1, n2, n3);
-    const uint32_t ci = (uint32_t) c2 & 3u;
-    const uint32_t wl = (ci == 3u) ? ln.q3 : word_of(n0, n1, n2, n3, ci);
-    const uint32_t wu = word_of(n0, n1, n2, n3, (ci + 1u) & 3u);
-    const double L2 = si_neglog_u32_spec(wl, &redo);
-    const double U2 = si_u32_to_uniform_pos(wu);
+    uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+    double L2 = 0.0, U2 = 0.0;
+    if constexpr (NEXT) {
+        philox_block(key, (c2 + 1) >> 2, n0, n1, n2, n3);
+        const uint32_t ci = (uint32_t) c2 & 3u;
+        const uint32_t wl = (ci == 3u) ? ln.q3 : word_of(n0, n1, n2, n3, ci);
+        const uint32_t wu = word_of(n0, n1, n2, n3, (ci + 1u) & 3u);
+        L2 = si_neglog_u32_spec(wl, &redo);
+        U2 = si_u32_to_uniform_pos(wu);
+    }
 
     if (tau_special)
         return SSA_REDO;
@@ -468,13 +472,82 @@ __device__ __forceinline__ int ssa_step_spec(SsaLane<M> &ln, const si_rng &key, 
     for (int k = 0; k < NT; k++)
         ln.rate[k] = rate2[k];
     ln.sum = sum2;
-    ln.q0 = n0;
-    ln.q1 = n1;
-    ln.q2 = n2;
-    ln.q3 = n3;
-    ln.L = L2;
-    ln.U = U2;
+    if constexpr (NEXT) {
+        ln.q0 = n0;
+        ln.q1 = n1;
+        ln.q2 = n2;
+        ln.q3 = n3;
+        ln.L = L2;
+        ln.U = U2;
+    }
     return SSA_FIRED;
+}
+
+/* Draws of four transitions of a node whose next waiting-time draw is c:
+ * words c .. c + 7 of its stream (waiting time, selection, four times),
+ * from the three Philox blocks that can hold them, as -log(u) and
+ * uniform values.  The four -log(u) are independent chains of integer
+ * operations that the compiler interleaves. */
+__device__ __forceinline__ void draw_four(const si_rng &key, uint64_t c, double (&L)[4],
+                                          double (&U)[4])
+{
+    uint32_t w[12];
+    const uint64_t b = c >> 2;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        philox_block(key, b + k, w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+    const uint32_t o = (uint32_t) c & 3u;
+    uint32_t x[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+        x[i] = o == 0 ? w[i] : o == 1 ? w[i + 1] : o == 2 ? w[i + 2] : w[i + 3];
+    int slow = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        L[j] = si_neglog_u32_spec(x[2 * j], &slow);
+        U[j] = si_u32_to_uniform_pos(x[2 * j + 1]);
+    }
+    if (slow) {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            L[j] = si_neglog_u32(x[2 * j]);
+    }
+}
+
+/* The rest of a node's day after ssa_begin, for models whose rates do not
+ * read t: straight-line steps in batches of four, their draws computed
+ * together ahead of them (draw_four); a step that meets a rare case is
+ * redone by ssa_step_ahead with the same draws, and the next batch starts
+ * at the draw index it leaves.  The draws, and so the trajectory, are
+ * those of ssa_step. */
+template <class M>
+__device__ __forceinline__ void ssa_run_day(SsaLane<M> &ln, const si_rng &key, double next,
+                                            const double *v, const double *ld, const double *gd,
+                                            const int *sS, const uint32_t *sG,
+                                            unsigned max_fired)
+{
+    for (;;) {
+        double L[4], U[4];
+        draw_four(key, ln.c, L, U);
+        int j = 0, st;
+        double Lj, Uj;
+        do {
+            Lj = j == 0 ? L[0] : j == 1 ? L[1] : j == 2 ? L[2] : L[3];
+            Uj = j == 0 ? U[0] : j == 1 ? U[1] : j == 2 ? U[2] : U[3];
+            st = ssa_step_spec<M, false>(ln, key, Lj, Uj, next, v, ld, gd, sS, sG, max_fired);
+        } while (st == SSA_FIRED && ++j < 4);
+        if (st == SSA_DAY_OVER)
+            return;
+        if (st == SSA_REDO) {
+            /* the exact step, with this step's draws and the Philox block
+             * of its selection draw, as ssa_step_ahead expects them */
+            ln.L = Lj;
+            ln.U = Uj;
+            philox_block(key, (ln.c + 1) >> 2, ln.q0, ln.q1, ln.q2, ln.q3);
+            if (ssa_step_ahead<M>(ln, key, next, v, ld, gd, sS, sG, max_fired))
+                return;
+        }
+    }
 }
 
 /* One step of the direct method in the reference's order: the waiting
@@ -612,7 +685,8 @@ __device__ __forceinline__ bool ssa_step(SsaLane<M> &ln, const si_rng &key, doub
                                          const int *sS, const uint32_t *sG, unsigned max_fired)
 {
     if constexpr (M::RATES_TIME_INVARIANT) {
-        const int st = ssa_step_spec<M>(ln, key, next, v, ld, gd, sS, sG, max_fired);
+        const int st = ssa_step_spec<M, true>(ln, key, ln.L, ln.U, next, v, ld, gd, sS, sG,
+                                              max_fired);
         if (st != SSA_REDO)
             return st == SSA_DAY_OVER;
         return ssa_step_ahead<M>(ln, key, next, v, ld, gd, sS, sG, max_fired);
@@ -628,9 +702,19 @@ __device__ __forceinline__ unsigned ssa_day(SsaLane<M> &ln, si_rng &r, double ne
                                             const double *v, const double *ld, const double *gd,
                                             const int *sS, const uint32_t *sG, unsigned max_fired)
 {
-    if (!ssa_begin<M>(ln, r, r.ctr, next))
-        while (!ssa_step<M>(ln, r, next, v, ld, gd, sS, sG, max_fired)) {
+    if (!ssa_begin<M>(ln, r, r.ctr, next)) {
+        /* two steps one at a time, then, for a node that is still going,
+         * batches of four (a node with one transition or none in the day
+         * computes no draws it does not use) */
+        for (int n = 0;; n++) {
+            if (M::RATES_TIME_INVARIANT && n == 2) {
+                ssa_run_day<M>(ln, r, next, v, ld, gd, sS, sG, max_fired);
+                break;
+            }
+            if (ssa_step<M>(ln, r, next, v, ld, gd, sS, sG, max_fired))
+                break;
         }
+    }
     r.ctr = ln.c;
     r.have = 0;
     return ln.fired;
@@ -1375,11 +1459,20 @@ __global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, do
                 heavy = false;
             } else {
                 /* one step; a heavy warp has nothing else to do and runs
-                 * its whole day in this loop (one call site of the step
-                 * keeps the loop's code small) */
-                do
-                    done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG, s.max_fired);
-                while (heavy && !done);
+                 * its whole day, in batches of four steps where the rates
+                 * do not read t */
+                if constexpr (M::RATES_TIME_INVARIANT) {
+                    if (heavy) {
+                        ssa_run_day<M>(ln, r, next, v, ld, gd, sS, sG, s.max_fired);
+                        done = true;
+                    } else {
+                        done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG, s.max_fired);
+                    }
+                } else {
+                    do
+                        done = ssa_step<M>(ln, r, next, v, ld, gd, sS, sG, s.max_fired);
+                    while (heavy && !done);
+                }
             }
         }
     }
