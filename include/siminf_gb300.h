@@ -313,6 +313,16 @@ int siminf_gpu_schedule(const siminf_gpu_solver_args *args, int *days, int *wave
                         long long *e1_events, long long *e2_events, int *wave);
 
 /*
+ * The same schedule planned on the GPU (siminf_schedule.cu), with the same
+ * outputs as siminf_gpu_schedule: the events are classified, ordered and
+ * levelled a chunk of days at a time by rounds of relaxation over per-node
+ * event lists, the planner the streamed runs use.  Days whose wavefronts
+ * run deeper than the rounds allow are levelled by the host planner.
+ */
+int siminf_gpu_schedule_device(const siminf_gpu_solver_args *args, int *days, int *waves,
+                               long long *e1_events, long long *e2_events, int *wave);
+
+/*
  * Bootstrap particle filter on the GPU: the loop of pfilter_internal
  * (R/pfilter.R:315-499) with SimInf_systematic_resampling
  * (src/misc/SimInf_particle_filter.c:33-67).  args describes one particle's

@@ -29,7 +29,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC
            "-Xcompiler", "-ffp-contract=off"]
 SOURCES = ["siminf_kernels.cu", "siminf_models_a.cu", "siminf_models_b.cu", "siminf_models_c.cu",
            "siminf_capi.cpp", "siminf_noalloc.cu", "siminf_batch.cu", "siminf_server.cpp",
-           "siminf_reduce.cu", "siminf_events.cu", "siminf_individual.cu"]
+           "siminf_reduce.cu", "siminf_events.cu", "siminf_individual.cu", "siminf_schedule.cu"]
 
 
 def nvcc():

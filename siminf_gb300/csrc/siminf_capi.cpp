@@ -46,6 +46,7 @@
 #include "siminf_capi_internal.h"
 #include "siminf_launch.h"
 #include "siminf_plan.h"
+#include "siminf_schedule.h"
 #include "siminf_stream.h"
 
 using namespace siminf;
@@ -642,6 +643,37 @@ static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, 
                                     a->shift[i] - 1, (int) i, a->proportion[i]};
     }
     p->day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
+}
+
+/* Levels of one day's transfers (input range [lo, hi)) by the host
+ * planner, for the days the device planner leaves to it. */
+long long siminf::host_day_waves(const int *event, const int *node, const int *dest, const int *n,
+                                 const double *proportion, const int *select, const int *shift,
+                                 long long lo, long long hi, int Nn, int nsel, E2Rec *out,
+                                 std::vector<long long> &waves)
+{
+    siminf_gpu_plan p;
+    p.nsel = nsel;
+    p.e2_lo.assign(1, lo);
+    p.e2_hi.assign(1, hi);
+    p.e2_day_off.assign(2, 0);
+    p.day_waves.assign(1, std::vector<long long>());
+    siminf_gpu_solver_args a{};
+    a.Nn = Nn;
+    a.event = event;
+    a.node = node;
+    a.dest = dest;
+    a.n = n;
+    a.proportion = proportion;
+    a.select = select;
+    a.shift = shift;
+    WaveTracker w(Nn);
+    plan_day_waves(&p, &a, 0, w, out, 0);
+    waves = p.day_waves[0];
+    long long c = 0;
+    for (long long x : waves)
+        c += x;
+    return c;
 }
 
 /* Wave offsets of every day, from day_waves. */

@@ -61,6 +61,10 @@ def lib():
                                       C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                       C.POINTER(C.c_int)]
     L.siminf_gpu_schedule.restype = C.c_int
+    L.siminf_gpu_schedule_device.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                             C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                             C.POINTER(C.c_int)]
+    L.siminf_gpu_schedule_device.restype = C.c_int
     L.siminf_gpu_pmcmc_create.argtypes = [vp, vp, C.POINTER(abi.PfilterArgs),
                                           C.POINTER(abi.PmcmcArgs), C.POINTER(vp)]
     L.siminf_gpu_pmcmc_create.restype = C.c_int
@@ -123,7 +127,8 @@ EXPORTS = (
     "siminf_gpu_plan_create_ex", "siminf_gpu_last_status",
     "siminf_gpu_last_stats", "siminf_gpu_plan_create", "siminf_gpu_plan_run",
     "siminf_gpu_plan_download", "siminf_gpu_plan_stats", "siminf_gpu_plan_free",
-    "siminf_gpu_plan_profile", "siminf_gpu_schedule", "siminf_gpu_pfilter",
+    "siminf_gpu_plan_profile", "siminf_gpu_schedule", "siminf_gpu_schedule_device",
+    "siminf_gpu_pfilter",
     "siminf_gpu_run_solver_ssm_noalloc", "siminf_gpu_run_batch",
     "siminf_gpu_server_create", "siminf_gpu_server_submit", "siminf_gpu_server_wait",
     "siminf_gpu_server_load", "siminf_gpu_server_free", "siminf_gpu_plan_tune",
@@ -154,17 +159,18 @@ def check(code):
         raise abi.SimInfError(code, st.message.decode(errors="replace"))
 
 
-def schedule(holder):
-    """Host-only wave planning of an args holder: (days, waves, e1, e2,
+def schedule(holder, device=False):
+    """Wave planning of an args holder, on the host (siminf_gpu_schedule)
+    or on the GPU (siminf_gpu_schedule_device): (days, waves, e1, e2,
     per-event wave array)."""
     import numpy as np
     n = max(1, holder.args.len)
     wave = np.zeros(n, dtype=np.int32)
     days, waves = C.c_int(), C.c_int()
     e1, e2 = C.c_longlong(), C.c_longlong()
-    check(lib().siminf_gpu_schedule(C.cast(holder.ref(), C.c_void_p), C.byref(days),
-                                    C.byref(waves), C.byref(e1), C.byref(e2),
-                                    wave.ctypes.data_as(C.POINTER(C.c_int))))
+    fn = lib().siminf_gpu_schedule_device if device else lib().siminf_gpu_schedule
+    check(fn(C.cast(holder.ref(), C.c_void_p), C.byref(days), C.byref(waves), C.byref(e1),
+             C.byref(e2), wave.ctypes.data_as(C.POINTER(C.c_int))))
     return days.value, waves.value, e1.value, e2.value, wave[:holder.args.len]
 
 

@@ -121,3 +121,116 @@ def test_schedule_self_transfers_and_deep_days():
     assert e2 == days * 300
     assert np.array_equal(wave, ref)
     assert waves > days * 50            # deep days: many wavefronts each
+
+
+def relaxation_levels(src, dst):
+    """The device planner's levelling of one day's transfers, written with
+    numpy: the serial rule as a fixed point.  Links per transfer k: p1, the
+    previous transfer with the same source; p3, the last earlier transfer
+    whose source is k's destination; q, the position (in the destination-
+    sorted order) of the last earlier transfer into k's source.  Each round
+    takes the segmented prefix maximum of the levels over the destination-
+    sorted order and sets L[k] = 1 + max(L[p1], prefix max at q, L[p3]),
+    until nothing changes.  Returns (levels, rounds)."""
+    n = len(src)
+    k = np.arange(n)
+    by_src = np.lexsort((k, src))
+    by_dst = np.lexsort((k, dst))
+    p1 = np.full(n, -1)
+    same = src[by_src[1:]] == src[by_src[:-1]]
+    p1[by_src[1:][same]] = by_src[:-1][same]
+    # last j < k with src[j] == dst[k]: in (src, index) order, the element
+    # before the insertion point of (dst[k], k)
+    key_src = src[by_src].astype(np.int64) * (n + 1) + by_src
+    pos = np.searchsorted(key_src, dst.astype(np.int64) * (n + 1) + k) - 1
+    p3 = np.where((pos >= 0) & (src[by_src[np.maximum(pos, 0)]] == dst), by_src[np.maximum(pos, 0)], -1)
+    key_dst = dst[by_dst].astype(np.int64) * (n + 1) + by_dst
+    qpos = np.searchsorted(key_dst, src.astype(np.int64) * (n + 1) + k) - 1
+    q = np.where((qpos >= 0) & (dst[by_dst[np.maximum(qpos, 0)]] == src), qpos, -1)
+    head = np.ones(n, bool)
+    head[1:] = dst[by_dst[1:]] != dst[by_dst[:-1]]
+    L = np.ones(n, np.int64)
+    rounds = 0
+    while True:
+        rounds += 1
+        v = L[by_dst]
+        pm = np.empty(n, np.int64)
+        run = 0
+        for j in range(n):                  # segmented prefix max
+            run = v[j] if head[j] else max(run, v[j])
+            pm[j] = run
+        get = lambda a, i: np.where(i >= 0, a[np.maximum(i, 0)], 0)
+        new = 1 + np.maximum(np.maximum(get(L, p1), get(pm, q)), get(L, p3))
+        if np.array_equal(new, L):
+            return L, rounds
+        L = new
+
+
+def test_relaxation_levels_equal_serial_rule():
+    """The fixed point of the device planner's rounds is the serial rule's
+    level on random days: hubs, self-transfers, deep chains and wide
+    days."""
+    rng = np.random.default_rng(5)
+    for trial in range(40):
+        Nn = int(rng.integers(2, 60))
+        n = int(rng.integers(1, 400))
+        src = rng.integers(0, Nn, n)
+        if trial % 3 == 0:                  # a hub that most transfers enter
+            dst = np.where(rng.random(n) < 0.7, 0, rng.integers(0, Nn, n))
+        else:
+            dst = rng.integers(0, Nn, n)
+        if trial % 4 == 1:                  # self-transfers
+            dst = np.where(rng.random(n) < 0.3, src, dst)
+        # the serial rule (siminf_gpu_schedule's, as reference_levels)
+        excl, add = {}, {}
+        ref = np.empty(n, np.int64)
+        for i in range(n):
+            s, t = int(src[i]), int(dst[i])
+            Lv = 1 + max(excl.get(s, 0), add.get(s, 0), excl.get(t, 0))
+            excl[s] = Lv
+            add[t] = max(add.get(t, 0), Lv)
+            ref[i] = Lv
+        got, rounds = relaxation_levels(src, dst)
+        assert np.array_equal(got, ref), trial
+        assert rounds <= ref.max() + 1
+
+
+@pytest.mark.gpu
+def test_device_schedule_equals_host(gpu):
+    """The device planner's waves, counts and E1/E2 split equal the host
+    planner's on every parity case with events, a wide workload, deep days
+    with self-transfers, and 2% of the headline schedule."""
+    cases = [(label, m) for label, m in parity_cases() if len(m.events["event"])]
+    cases.append(("small", workloads.seir_events(nodes=300, days=20, transfers=400)))
+    cases.append(("headline_2pct", workloads.seir_events(nodes=20_000, days=365,
+                                                         transfers=10_000)))
+    from siminf_gb300 import model as M
+    rng = np.random.default_rng(23)
+    Nn, days = 12, 6
+    ev = {k: [] for k in M.EVENT_FIELDS}
+    for t in range(1, days + 1):
+        for _ in range(3000):               # deeper than the rounds allow on some days
+            s_ = int(rng.integers(1, Nn + 1))
+            d_ = s_ if rng.random() < 0.2 else int(rng.integers(1, Nn + 1))
+            for key, val in zip(M.EVENT_FIELDS, (3, t, s_, d_, 1, 0.0, 2, 0)):
+                ev[key].append(val)
+    u0 = {"S": np.full(Nn, 500), "E": 0, "I": 0, "R": 0}
+    cases.append(("deep", M.SEIR(u0, np.arange(1, days + 1), 0.0, 0.0, 0.0,
+                                 events=M.make_events(**{k: np.array(v) for k, v in ev.items()}))))
+    for label, m in cases:
+        h = abi.build_args(m, 1)
+        host = native.schedule(h)
+        dev = native.schedule(h, device=True)
+        assert host[:4] == dev[:4], label
+        assert np.array_equal(host[4], dev[4]), label
+
+
+@pytest.mark.gpu
+def test_device_schedule_rejects_unsorted(gpu):
+    from siminf_gb300 import model as M
+    m = M.SIR({"S": [5, 5], "I": [0, 0], "R": [0, 0]}, [1, 2, 3], 0.0, 0.0,
+              events=M.make_events([3, 0], [1, 1], [1, 2], [2, 0], 1, 0.0, 1, 0, sort=False))
+    h = abi.build_args(m, 1)
+    with pytest.raises(abi.SimInfError) as e:
+        native.schedule(h, device=True)
+    assert e.value.code == -31
