@@ -223,7 +223,10 @@ typedef struct siminf_gpu_options {
     int gdata_per_replicate;
     int two_pass;       /* > 0 on, < 0 off, 0 = on from 500,000 nodes (all replicates) */
     int max_node_day_transitions;   /* > 0: the bound; 0: 2^28 */
-    int reserved[3];
+    int streamed;       /* siminf_gpu_plan_create_ex: plan the events during the first run,
+                         * beside the GPU (on the device for large tables), as the run entry
+                         * points do; 0: before the plan returns */
+    int reserved[2];
 } siminf_gpu_options;
 
 /* The default of siminf_gpu_options.max_node_day_transitions. */

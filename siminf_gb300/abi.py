@@ -117,7 +117,8 @@ class Status(C.Structure):
 class Options(C.Structure):
     _fields_ = [("cap_transfers", C.c_int), ("heavy_rate", C.c_int),
                 ("gdata_per_replicate", C.c_int), ("two_pass", C.c_int),
-                ("max_node_day_transitions", C.c_int), ("reserved", C.c_int * 3)]
+                ("max_node_day_transitions", C.c_int), ("streamed", C.c_int),
+                ("reserved", C.c_int * 2)]
 
 
 class PfilterArgs(C.Structure):

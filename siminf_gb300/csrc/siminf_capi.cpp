@@ -362,6 +362,16 @@ static inline long long event_day(int time, double tt0)
     return (long long) time - (long long) std::floor(tt0);
 }
 
+/* Whether a streamed plan of len events plans them on the device
+ * (SIMINF_DEVICE_PLANNER=0 / 1 forces host / device; by default tables of
+ * at least 2^20 events). */
+static bool device_planner_for(long long len)
+{
+    if (const char *ev = getenv("SIMINF_DEVICE_PLANNER"))
+        return ev[0] == '1';
+    return len >= (1LL << 20);
+}
+
 /* Threads used by the host planner (SIMINF_PLANNER_THREADS overrides the
  * hardware's count). */
 static int planner_threads()
@@ -844,7 +854,7 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
 int siminf_gpu_plan_create_ex(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
                               const siminf_gpu_options *opt, siminf_gpu_plan **out)
 {
-    return plan_create_impl(a, model, opt, out, false);
+    return plan_create_impl(a, model, opt, out, opt && opt->streamed != 0);
 }
 
 int siminf_gpu_plan_create(const siminf_gpu_solver_args *a, const siminf_gpu_model *model,
@@ -919,20 +929,36 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     std::vector<E1Rec> e1;
     std::vector<int> e1_ptr;
     std::unique_ptr<E2Rec[]> e2;
-    rc = stream ? plan_scan(p, a, nsel, e1, e1_ptr) : plan_events(p, a, nsel, e1, e1_ptr, e2);
-    if (rc) {
-        delete p;
-        return rc;
-    }
-    if (stream && p->e2_count == 0)
-        plan_wave_index(p);
-    if (stream && p->e2_count > 0) {
-        /* the waves are planned during the first run, beside the GPU */
+    if (stream && a->len > 0 && device_planner_for(a->len) &&
+        event_day_ranges(a, p->days, p->e2_lo, p->e2_hi)) {
+        /* the device plans the events during the first run: only the day
+         * ranges now (E and N grow to the largest select and shift the
+         * planner finds; E1 lists and waves come chunk by chunk) */
+        p->dev_plan = true;
+        p->nsel = nsel;
+        p->max_select = p->max_shift = 0;
+        p->e2_count = (uint64_t) a->len;        /* room for every event */
+        p->e2_day_off.assign(p->ndays + 1, 0);
+        p->day_waves.assign(p->ndays, std::vector<long long>());
+        e1_ptr.assign((size_t) Nn + 1, 0);
         p->e2_pending = true;
         p->args = *a;
+    } else {
+        rc = stream ? plan_scan(p, a, nsel, e1, e1_ptr) : plan_events(p, a, nsel, e1, e1_ptr, e2);
+        if (rc) {
+            delete p;
+            return rc;
+        }
+        if (stream && p->e2_count == 0)
+            plan_wave_index(p);
+        if (stream && p->e2_count > 0) {
+            /* the waves are planned during the first run, beside the GPU */
+            p->e2_pending = true;
+            p->args = *a;
+        }
     }
     p->stats.ms_plan = ms_since(t0);
-    p->horizon = (p->e2_count == 0) && L->pts_local && a->solver == 0;
+    p->horizon = !p->dev_plan && (p->e2_count == 0) && L->pts_local && a->solver == 0;
 
     cudaStream_t st = g_plan_stream;
     p->stream = st;
@@ -1477,6 +1503,310 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
     return e;
 }
 
+/* The first run of a streamed plan whose events the device plans
+ * (siminf_schedule.cu).  A planner thread copies each chunk of days'
+ * event columns to the device and plans them on its own stream -- the
+ * chunk's external transfers in wave order go to d_e2 after the previous
+ * chunks', its E1 records by node to e1_all after the previous chunks',
+ * its per-node offsets to one of E1_RING buffers -- while this thread
+ * queues each planned chunk's kernels, so planning overlaps the GPU's work
+ * on earlier days.  After the run, the planner's status gives the order
+ * check and the planned failures, and the E1 records of all chunks merge
+ * into the per-node CSR later runs read. */
+static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStream_t st)
+{
+    const Launchers *L = p->L;
+    const siminf_gpu_solver_args *a = &p->args;
+    const int ndays = p->ndays, Nn = a->Nn;
+    enum { CHUNK_DAYS = 8, E1_RING = 3 };
+    const int nchunks = (ndays + CHUNK_DAYS - 1) / CHUNK_DAYS;
+    const long long len = a->len, tail_lo = p->e2_hi[ndays - 1];
+    long long cap = 1;
+    for (int c = 0; c < nchunks; c++) {
+        const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
+        cap = std::max(cap, p->e2_hi[d1 - 1] - p->e2_lo[d0]);
+    }
+    cudaError_t e = s.aem ? L->aem_init(s, p->tt0, st) : L->init(s, p->tt0, st);
+    if (e != cudaSuccess)
+        return e;
+
+    cudaStream_t ps = nullptr, ds = nullptr;
+    e = cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking);
+    if (e == cudaSuccess && p->out_args)
+        e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    DevScheduler sch;
+    if (e == cudaSuccess)
+        e = sch.init(std::min(cap, std::max(len - tail_lo, cap)), Nn, p->nsel, ps);
+    /* E1 records of every chunk, their nodes, and a ring of offsets */
+    long long e1_cap = std::max(1LL, len / 64);
+    E1Rec *e1_all = nullptr;
+    uint32_t *e1_nodes = nullptr;
+    std::vector<void *> old_e1;
+    int *ring[E1_RING] = {};
+    if (e == cudaSuccess) e = cudaMalloc((void **) &e1_all, (size_t) e1_cap * sizeof(E1Rec));
+    if (e == cudaSuccess) e = cudaMalloc((void **) &e1_nodes, (size_t) e1_cap * sizeof(uint32_t));
+    for (int r = 0; r < E1_RING && e == cudaSuccess; r++)
+        e = cudaMalloc((void **) &ring[r], ((size_t) Nn + 1) * sizeof(int));
+    if (e != cudaSuccess) {
+        for (int r = 0; r < E1_RING; r++)
+            cudaFree(ring[r]);
+        cudaFree(e1_all);
+        cudaFree(e1_nodes);
+        for (cudaStream_t x : {ps, ds})
+            if (x)
+                cudaStreamDestroy(x);
+        return e;
+    }
+
+    struct Planned {
+        SchedChunk ch;
+        long long base2 = 0;
+        E1Rec *e1 = nullptr;
+        cudaError_t err = cudaSuccess;
+    };
+    std::vector<Planned> plans(nchunks);
+    std::unique_ptr<std::atomic<int>[]> ready(new std::atomic<int>[nchunks]);
+    std::unique_ptr<std::atomic<int>[]> queued(new std::atomic<int>[nchunks]);
+    std::vector<cudaEvent_t> done(nchunks, nullptr);
+    for (int c = 0; c < nchunks; c++) {
+        ready[c].store(0);
+        queued[c].store(0);
+    }
+    std::atomic<int> abort(0);
+    long long e1_total = 0, e2_total = 0;
+    unsigned long long bad = ~0ULL;
+
+    std::thread planner([&]() {
+        cudaSetDevice(dev);
+        long long base1 = 0, base2 = 0;
+        for (int c = 0; c < nchunks && !abort.load(); c++) {
+            Planned &pl = plans[c];
+            const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS),
+                      nd = d1 - d0;
+            const long long l0 = p->e2_lo[d0], m = p->e2_hi[d1 - 1] - l0;
+            cudaError_t pe = cudaSuccess;
+            if (c >= E1_RING) {
+                /* the offsets buffer is free once that chunk's days ran */
+                while (!queued[c - E1_RING].load(std::memory_order_acquire) && !abort.load())
+                    std::this_thread::sleep_for(std::chrono::microseconds(20));
+                if (abort.load())
+                    break;
+                pe = cudaStreamWaitEvent(ps, done[c - E1_RING], 0);
+            }
+            /* room for the chunk's E1 records (earlier buffers stay until
+             * the run ends: their chunks' kernels may still read them) */
+            if (pe == cudaSuccess && base1 + m > e1_cap) {
+                const long long ncap = std::max(2 * e1_cap, base1 + m);
+                E1Rec *n_all = nullptr;
+                uint32_t *n_nodes = nullptr;
+                pe = cudaMalloc((void **) &n_all, (size_t) ncap * sizeof(E1Rec));
+                if (pe == cudaSuccess)
+                    pe = cudaMalloc((void **) &n_nodes, (size_t) ncap * sizeof(uint32_t));
+                if (pe == cudaSuccess && base1 > 0)
+                    pe = cudaMemcpyAsync(n_all, e1_all, base1 * sizeof(E1Rec),
+                                         cudaMemcpyDeviceToDevice, ps);
+                if (pe == cudaSuccess && base1 > 0)
+                    pe = cudaMemcpyAsync(n_nodes, e1_nodes, base1 * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToDevice, ps);
+                old_e1.push_back(e1_all);
+                old_e1.push_back(e1_nodes);
+                e1_all = n_all;
+                e1_nodes = n_nodes;
+                e1_cap = ncap;
+            }
+            long long bounds[DevScheduler::MAX_CHUNK_DAYS + 1];
+            for (int j = 0; j < nd; j++)
+                bounds[j] = p->e2_lo[d0 + j] - l0;
+            bounds[nd] = m;
+            const int *cols_i[7] = {a->time, a->event, a->node, a->dest, a->n, a->select, a->shift};
+            int *dst_i[7] = {sch.time, sch.event, sch.node, sch.dest, sch.n, sch.select, sch.shift};
+            for (int k = 0; k < 7 && pe == cudaSuccess && m > 0; k++)
+                pe = cudaMemcpyAsync(dst_i[k], cols_i[k] + l0, (size_t) m * sizeof(int),
+                                     cudaMemcpyHostToDevice, ps);
+            if (pe == cudaSuccess && m > 0)
+                pe = cudaMemcpyAsync(sch.proportion, a->proportion + l0, (size_t) m * sizeof(double),
+                                     cudaMemcpyHostToDevice, ps);
+            if (pe == cudaSuccess)
+                pe = sch.plan_chunk(l0, m, d0, nd, bounds, l0 > 0 ? a->time[l0 - 1] : 0,
+                                    l0 > 0 ? a->event[l0 - 1] : 0, l0 > 0, p->d_e2 + base2,
+                                    e1_all + base1, ring[c % E1_RING], nullptr, pl.ch,
+                                    e1_nodes + base1);
+            /* days too deep for the rounds: the host planner's waves */
+            for (size_t k = 0; pe == cudaSuccess && k < pl.ch.deep.size(); k++) {
+                const int j = pl.ch.deep[k];
+                std::vector<E2Rec> recs((size_t) (p->e2_hi[d0 + j] - p->e2_lo[d0 + j]) + 1);
+                host_day_waves(a->event, a->node, a->dest, a->n, a->proportion, a->select,
+                               a->shift, p->e2_lo[d0 + j], p->e2_hi[d0 + j], Nn, p->nsel,
+                               recs.data(), pl.ch.waves[j]);
+                const long long cnt = pl.ch.off[j + 1] - pl.ch.off[j];
+                if (cnt > 0)
+                    pe = cudaMemcpyAsync(p->d_e2 + base2 + pl.ch.off[j], recs.data(),
+                                         (size_t) cnt * sizeof(E2Rec), cudaMemcpyHostToDevice, ps);
+                if (pe == cudaSuccess)
+                    pe = cudaStreamSynchronize(ps);
+            }
+            pl.base2 = base2;
+            pl.e1 = e1_all + base1;
+            pl.err = pe;
+            base1 += pl.ch.n1;
+            base2 += pl.ch.n2;
+            e1_total = base1;
+            e2_total = base2;
+            ready[c].store(1, std::memory_order_release);
+            if (pe != cudaSuccess || pl.ch.bad != ~0ULL)
+                break;
+        }
+    });
+
+    for (int c = 0; c < nchunks && e == cudaSuccess; c++) {
+        while (!ready[c].load(std::memory_order_acquire))
+            std::this_thread::yield();
+        const Planned &pl = plans[c];
+        if (pl.err != cudaSuccess) {
+            e = pl.err;
+            break;
+        }
+        if (pl.ch.bad != ~0ULL) {
+            bad = pl.ch.bad;            /* out of order: the run stops here */
+            break;
+        }
+        /* E and N up to the largest select and shift seen so far */
+        if (pl.ch.max_select > p->max_select && a->jcE) {
+            int *djcE, *dirE;
+            double *dprE;
+            const int nnz = a->jcE[pl.ch.max_select];
+            int rc = upload(&djcE, a->jcE, (size_t) pl.ch.max_select + 1, p->owned, st);
+            if (!rc) rc = upload(&dirE, a->irE, (size_t) nnz, p->owned, st);
+            if (!rc) rc = upload(&dprE, (const double *) a->prE, (size_t) nnz, p->owned, st);
+            if (rc) {
+                e = cudaErrorMemoryAllocation;
+                break;
+            }
+            s.jcE = p->s.jcE = djcE;
+            s.irE = p->s.irE = dirE;
+            s.prE = p->s.prE = dprE;
+            p->max_select = pl.ch.max_select;
+        }
+        if (pl.ch.max_shift > p->max_shift && a->N) {
+            int *dN;
+            if (upload(&dN, a->N, (size_t) pl.ch.max_shift * a->Nc, p->owned, st)) {
+                e = cudaErrorMemoryAllocation;
+                break;
+            }
+            s.Nshift = p->s.Nshift = dN;
+            p->max_shift = pl.ch.max_shift;
+        }
+        s.e1 = pl.e1;
+        s.e1_ptr = ring[c % E1_RING];
+        const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
+        for (int d = d0; d < d1 && e == cudaSuccess; d++) {
+            const int j = d - d0;
+            const DayInfo &di = p->days[d];
+            p->e2_day_off[d] = pl.base2 + pl.ch.off[j];
+            p->e2_day_off[d + 1] = pl.base2 + pl.ch.off[j + 1];
+            p->day_waves[d] = pl.ch.waves[j];
+            if (s.two_pass && !s.aem)
+                e = L->quick(s, d, di.tt, di.next, st);
+            if (e == cudaSuccess)
+                e = s.aem ? L->aem_day(s, d, di.tt, di.next, st)
+                          : L->ssa_e1(s, d, di.tt, di.next, st);
+            if (e == cudaSuccess) {
+                const std::vector<long long> &cnt = p->day_waves[d];
+                std::vector<long long> off(cnt.size());
+                long long o = p->e2_day_off[d];
+                for (size_t w = 0; w < cnt.size(); w++) {
+                    off[w] = o;
+                    o += cnt[w];
+                }
+                e = launch_day_waves(p, s, off.data(), cnt.data(), (int) cnt.size(), d, di.tt,
+                                     st, nullptr);
+            }
+            if (e == cudaSuccess)
+                e = s.aem ? L->aem_pts(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st)
+                          : L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
+            std::swap(s.vA, s.vB);
+        }
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&done[c], cudaEventDisableTiming);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(done[c], st);
+        queued[c].store(1, std::memory_order_release);
+        /* the columns this chunk finished go back while later days run */
+        const int c_hi = p->days[d1 - 1].c1;
+        if (ds && e == cudaSuccess && c_hi > p->cols_sent) {
+            e = cudaStreamWaitEvent(ds, done[c], 0);
+            if (e == cudaSuccess)
+                e = download_columns(p, p->out_args, p->cols_sent, c_hi, ds);
+            if (e == cudaSuccess)
+                p->cols_sent = c_hi;
+        }
+    }
+    abort.store(1);
+    planner.join();
+
+    /* events past the last day: the order check and the maxima */
+    for (long long l0 = tail_lo; e == cudaSuccess && bad == ~0ULL && l0 < len; ) {
+        const long long m = std::min(len - l0, cap);
+        const int *cols_i[4] = {a->time, a->event, a->select, a->shift};
+        int *dst_i[4] = {sch.time, sch.event, sch.select, sch.shift};
+        for (int k = 0; k < 4 && e == cudaSuccess; k++)
+            e = cudaMemcpyAsync(dst_i[k], cols_i[k] + l0, (size_t) m * sizeof(int),
+                                cudaMemcpyHostToDevice, ps);
+        if (e == cudaSuccess)
+            e = sch.check_tail(l0, m, l0 > 0 ? a->time[l0 - 1] : 0, l0 > 0 ? a->event[l0 - 1] : 0,
+                               l0 > 0);
+        l0 += m;
+    }
+    std::vector<SchedPlanned> planned;
+    int msel = 0, mshift = 0;
+    if (e == cudaSuccess) {
+        unsigned long long b2 = ~0ULL;
+        e = sch.status(b2, msel, mshift, planned);
+        bad = std::min(bad, b2);
+    }
+    p->dev_bad = (long long) (bad == ~0ULL ? -1 : (long long) bad);
+    if (e == cudaSuccess && bad == ~0ULL) {
+        for (const SchedPlanned &x : planned)
+            p->planned.push_back({x.day, x.code, x.index, x.node, x.phase});
+        p->e1_count = (uint64_t) e1_total;
+        p->e2_count = (uint64_t) e2_total;
+        /* the E1 records of all chunks as one per-node CSR for later runs
+         * (after every chunk's kernels: they read the chunk buffers) */
+        E1Rec *de1 = nullptr;
+        int *de1p = nullptr;
+        e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess && !dalloc(&de1, (size_t) std::max(1LL, e1_total), p->owned) &&
+            !dalloc(&de1p, (size_t) Nn + 1, p->owned))
+            e = sch.merge_e1(e1_all, e1_nodes, e1_total, de1, de1p);
+        else if (e == cudaSuccess)
+            e = cudaErrorMemoryAllocation;
+        if (e == cudaSuccess) {
+            p->s.e1 = de1;
+            p->s.e1_ptr = de1p;
+        }
+    }
+    if (ds) {
+        const cudaError_t e2 = cudaStreamSynchronize(ds);
+        if (e == cudaSuccess)
+            e = e2;
+        cudaStreamDestroy(ds);
+    }
+    cudaStreamSynchronize(ps);
+    for (cudaEvent_t ev : done)
+        if (ev)
+            cudaEventDestroy(ev);
+    for (int r = 0; r < E1_RING; r++)
+        cudaFree(ring[r]);
+    cudaFree(e1_all);
+    cudaFree(e1_nodes);
+    for (void *q : old_e1)
+        cudaFree(q);
+    cudaStreamDestroy(ps);
+    return e;
+}
+
 /* The reset at the start of every run: error counters, transition counter,
  * work queues, the state from u0/v0. */
 static cudaError_t reset_run(siminf_gpu_plan *p, const DevState &s, cudaStream_t st,
@@ -1594,11 +1924,23 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
     if (replay) {
         /* the graph holds the whole run */
     } else if (p->e2_pending) {
-        e = launch_streamed(p, s, st);
+        e = p->dev_plan ? launch_streamed_dev(p, s, st) : launch_streamed(p, s, st);
         p->e2_pending = false;
         p->h_e2.reset();
         plan_wave_index(p);
         p->stats.e2_waves = (int) p->wave_ptr.size() - 1;
+        p->stats.e1_events = p->e1_count * (uint64_t) s.Nrep;
+        p->stats.e2_events = p->e2_count * (uint64_t) s.Nrep;
+        if (e == cudaSuccess && p->dev_bad >= 0) {
+            /* the device planner found the table out of order */
+            const long long bad = p->dev_bad;
+            char msg[200];
+            snprintf(msg, sizeof(msg), "event %lld (time %d) breaks the (time, E1 before E2) order",
+                     bad + 1, p->args.time[bad]);
+            cudaStreamSynchronize(st);
+            set_status(SIMINF_GPU_ERR_EVENTS_UNSORTED, -1, -1, (int) bad, p->args.time[bad], 0, msg);
+            return SIMINF_GPU_ERR_EVENTS_UNSORTED;
+        }
     } else {
         e = launch_all(p, s, st, kp);
     }

@@ -78,6 +78,11 @@ struct siminf_gpu_plan {
     /* Streamed runs: the waves are planned on host threads while the GPU
      * runs earlier days; the caller's arrays stay valid until the run. */
     bool e2_pending = false;
+    /* Streamed runs whose events the device plans (siminf_schedule.cu):
+     * e2_lo / e2_hi are the days' input ranges; dev_bad is the first event
+     * out of order the planner found, or -1. */
+    bool dev_plan = false;
+    long long dev_bad = -1;
     siminf_gpu_solver_args args{};
     std::unique_ptr<E2Rec[]> h_e2;
     /* Streamed runs with pinned output arrays: each chunk's finished

@@ -450,6 +450,21 @@ __global__ void __launch_bounds__(SCHED_BLOCK) k_e1_ptr(long long n1, const uint
         ptr[x] = (int) lower_bound_u32(ke, 0, n1, (uint32_t) x);
 }
 
+__global__ void __launch_bounds__(SCHED_BLOCK) k_iota(uint32_t *p, long long n)
+{
+    const long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (i < n)
+        p[i] = (uint32_t) i;
+}
+
+__global__ void __launch_bounds__(SCHED_BLOCK) k_gather_e1(const E1Rec *in, const uint32_t *pos,
+                                                           long long n, E1Rec *out)
+{
+    const long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = in[pos[i]];
+}
+
 }  // namespace
 
 DevScheduler::~DevScheduler()
@@ -458,6 +473,8 @@ DevScheduler::~DevScheduler()
         cudaFreeHost(h_info_);
     if (h_wout_)
         cudaFreeHost(h_wout_);
+    if (h_status_)
+        cudaFreeHost(h_status_);
     for (void *p : bufs_)
         cudaFree(p);
 }
@@ -538,6 +555,8 @@ cudaError_t DevScheduler::init(long long max_events, int Nn, int nsel, cudaStrea
         e = cudaMallocHost((void **) &h_info_, (MAX_CHUNK_DAYS + 3) * sizeof(long long));
     if (e == cudaSuccess)
         e = cudaMallocHost((void **) &h_wout_, WOUT_CAP * sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **) &h_status_, sizeof(SchedStatus));
     if (e == cudaSuccess) {
         SchedStatus s0{};
         s0.bad = ~0ULL;
@@ -566,7 +585,7 @@ cudaError_t DevScheduler::check_tail(long long lo, long long m, int prev_time, i
 cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
                                      const long long *bounds, int prev_time, int prev_event,
                                      bool has_prev, E2Rec *e2_out, E1Rec *e1_out, int *e1_ptr,
-                                     int *wave_out, SchedChunk &out)
+                                     int *wave_out, SchedChunk &out, uint32_t *e1_node_out)
 {
     if (m > cap_ || m < 0 || nd < 1 || nd > MAX_CHUNK_DAYS)
         return cudaErrorInvalidValue;
@@ -670,13 +689,23 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
                 n1, ke, Nn_, e1_ptr);
             e = cudaGetLastError();
         }
+        if (e == cudaSuccess && e1_node_out)
+            e = cudaMemcpyAsync(e1_node_out, ke, n1 * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                                st_);
     } else if (e == cudaSuccess) {
         e = cudaMemsetAsync(e1_ptr, 0, ((size_t) Nn_ + 1) * sizeof(int), st_);
     }
     if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h_status_, status_, sizeof(SchedStatus), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess)
         e = cudaStreamSynchronize(st_);
-    if (e != cudaSuccess || n2 == 0)
+    if (e != cudaSuccess)
         return e;
+    out.bad = h_status_->bad;
+    out.max_select = h_status_->max_select;
+    out.max_shift = h_status_->max_shift;
+    if (n2 == 0)
+        return cudaSuccess;
 
     /* the per-day wave sizes */
     std::vector<int> sizes;
@@ -702,6 +731,45 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
         base += dm;
     }
     return cudaSuccess;
+}
+
+cudaError_t DevScheduler::merge_e1(const E1Rec *in, const uint32_t *nodes, long long n,
+                                   E1Rec *out, int *ptr)
+{
+    if (n <= 0)
+        return cudaMemsetAsync(ptr, 0, ((size_t) Nn_ + 1) * sizeof(int), st_);
+    uint32_t *k = nullptr, *p = nullptr, *k2 = nullptr, *p2 = nullptr, *hist = nullptr;
+    unsigned long long *tot = nullptr;
+    cudaError_t e = cudaMallocAsync((void **) &k, n * sizeof(uint32_t), st_);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **) &p, n * sizeof(uint32_t), st_);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **) &k2, n * sizeof(uint32_t), st_);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **) &p2, n * sizeof(uint32_t), st_);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync((void **) &hist, radix_hist_len(n) * sizeof(uint32_t), st_);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync((void **) &tot, (radix_tot_len(n) + 1) * sizeof(unsigned long long),
+                            st_);
+    uint32_t *kk = k, *pp = p, *kk2 = k2, *pp2 = p2;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(k, nodes, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st_);
+    if (e == cudaSuccess) {
+        k_iota<<<blocks_of(n, SCHED_BLOCK), SCHED_BLOCK, 0, st_>>>(p, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && n > 1)
+        e = radix_sort<uint32_t>(kk, pp, kk2, pp2, n, nb_, hist, tot, st_);
+    if (e == cudaSuccess) {
+        k_gather_e1<<<blocks_of(n, SCHED_BLOCK), SCHED_BLOCK, 0, st_>>>(in, pp, n, out);
+        k_e1_ptr<<<blocks_of((long long) Nn_ + 1, SCHED_BLOCK), SCHED_BLOCK, 0, st_>>>(n, kk, Nn_,
+                                                                                    ptr);
+        e = cudaGetLastError();
+    }
+    for (void *q : {(void *) k, (void *) p, (void *) k2, (void *) p2, (void *) hist, (void *) tot})
+        if (q)
+            cudaFreeAsync(q, st_);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st_);
+    return e;
 }
 
 cudaError_t DevScheduler::status(unsigned long long &bad, int &max_select, int &max_shift,

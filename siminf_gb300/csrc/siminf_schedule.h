@@ -39,6 +39,8 @@ struct SchedStatus {
 /* One planned chunk, as the host needs it to launch the chunk's days. */
 struct SchedChunk {
     long long n1 = 0, n2 = 0;               /* E1 events, external transfers */
+    unsigned long long bad = ~0ULL;         /* the status after this chunk: first */
+    int max_select = 0, max_shift = 0;      /* event out of order, select / shift maxima */
     std::vector<long long> off;             /* nd + 1: first transfer of each day */
     std::vector<std::vector<long long>> waves;  /* per day: wave sizes */
     std::vector<int> deep;                  /* days left to the host planner */
@@ -70,7 +72,14 @@ public:
      * is written (its kernels ran on the scheduler's stream). */
     cudaError_t plan_chunk(long long lo, long long m, int d0, int nd, const long long *bounds,
                            int prev_time, int prev_event, bool has_prev, E2Rec *e2_out,
-                           E1Rec *e1_out, int *e1_ptr, int *wave_out, SchedChunk &out);
+                           E1Rec *e1_out, int *e1_ptr, int *wave_out, SchedChunk &out,
+                           uint32_t *e1_node_out = nullptr);
+
+    /* The E1 records of several chunks (in chunk order, each chunk's by
+     * node, with their nodes) as one per-node CSR: stable by node, so each
+     * node keeps day and array order.  out holds n records, ptr Nn + 1. */
+    cudaError_t merge_e1(const E1Rec *in, const uint32_t *nodes, long long n, E1Rec *out,
+                         int *ptr);
 
     /* Order check and select / shift maxima of events past the last day. */
     cudaError_t check_tail(long long lo, long long m, int prev_time, int prev_event,
@@ -100,6 +109,7 @@ private:
     unsigned long long *tot_ = nullptr;
     int *dmax_ = nullptr, *deep_ = nullptr;
     long long *info_ = nullptr, *h_info_ = nullptr;    /* device / pinned host */
+    SchedStatus *h_status_ = nullptr;                   /* pinned: the status header */
     int *wout_ = nullptr, *h_wout_ = nullptr;          /* compact wave sizes */
     SchedStatus *status_ = nullptr;
 
