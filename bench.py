@@ -864,11 +864,14 @@ def aem_bench(m, node_days, torch, C, stream, threads, cpu_scale, seed=42):
 
 def tune_summary(tune):
     """The autotuner's candidates, probe times and choice."""
-    return {"probe_days": tune.probe_days,
-            "candidates": [{"heavy_rate": tune.heavy_rate[k], "two_pass": tune.two_pass[k],
-                            "ms": tune.ms[k]} for k in range(len(tune.ms))],
-            "chosen_heavy_rate": tune.heavy_rate[tune.chosen],
-            "chosen_two_pass": tune.two_pass[tune.chosen]}
+    k = tune.chosen
+    return {"probe_days": tune.probe_days, "cached": bool(tune.cached),
+            "candidates": [{"heavy_rate": tune.heavy_rate[i], "two_pass": tune.two_pass[i],
+                            "ssa_variant": tune.ssa_variant[i],
+                            "wave_block": tune.wave_block[i], "ms": tune.ms[i]}
+                           for i in range(tune.n_candidates)],
+            "chosen_heavy_rate": tune.heavy_rate[k], "chosen_two_pass": tune.two_pass[k],
+            "chosen_ssa_variant": tune.ssa_variant[k], "chosen_wave_block": tune.wave_block[k]}
 
 
 def plan_kernel_profile(plan, C, stream):

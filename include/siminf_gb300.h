@@ -226,7 +226,9 @@ typedef struct siminf_gpu_options {
     int streamed;       /* siminf_gpu_plan_create_ex: plan the events during the first run,
                          * beside the GPU (on the device for large tables), as the run entry
                          * points do; 0: before the plan returns */
-    int reserved[2];
+    int ssa_variant;    /* SSA kernel register budget: 0 the model's default, 1 more
+                         * registers a thread and fewer resident warps (see the autotuner) */
+    int wave_block;     /* threads per block of the wavefront kernel: 128, 256 or 512 (0: 256) */
 } siminf_gpu_options;
 
 /* The default of siminf_gpu_options.max_node_day_transitions. */
@@ -466,20 +468,31 @@ int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
 
 /*
  * Autotuner (no counterpart in the reference): times the plan's first
- * probe_days days (0: 16) for each candidate layout of the SSA work queue
- * -- the threshold of its heavy part (rate sum from which a node is queued
- * first and run 32 to a warp; 0 turns the part off: 0, 2, 8, 32) with
- * one-pass and with two-pass days (siminf_gpu_options.two_pass) -- keeps
- * the fastest in the plan, and reports the times.  Results never depend on
- * the layout; only the order in which nodes are simulated does.
+ * probe_days days (0: 16) for candidate launch layouts and keeps the
+ * fastest in the plan, reporting every candidate's time.  Stage 1: the
+ * SSA work queue's heavy-part threshold (rate sum from which a node is
+ * queued first and run 32 to a warp; 0 turns the part off: 0, 2, 8, 32),
+ * with one-pass and with two-pass days (siminf_gpu_options.two_pass).
+ * Stage 2, from the best of stage 1: the SSA kernel's other register
+ * budget (ssa_variant 1: more registers a thread, fewer resident warps).
+ * Stage 3, for plans with external transfers: the wavefront kernel's block
+ * of 128 and 512 threads (256 otherwise).  The choice is kept per device
+ * model and size class (node count and day count to a power of two,
+ * transfers or not): a later plan of the same class takes it without
+ * probing (cached = 1; probe_days < 0 forces a new search).  Results never
+ * depend on the layout; only the order in which nodes are simulated does.
  */
-#define SIMINF_GPU_TUNE_CANDIDATES 8
+#define SIMINF_GPU_TUNE_CANDIDATES 16
 typedef struct siminf_gpu_tune_result {
     double heavy_rate[SIMINF_GPU_TUNE_CANDIDATES];
     int two_pass[SIMINF_GPU_TUNE_CANDIDATES];   /* 1: two-pass days */
+    int ssa_variant[SIMINF_GPU_TUNE_CANDIDATES];    /* SSA kernel register budget */
+    int wave_block[SIMINF_GPU_TUNE_CANDIDATES];     /* threads per wavefront block */
     double ms[SIMINF_GPU_TUNE_CANDIDATES];     /* device time of the probe days */
+    int n_candidates;                           /* candidates timed */
     int chosen;                                 /* index of the kept candidate */
     int probe_days;
+    int cached;                                 /* 1: taken from an earlier plan's search */
 } siminf_gpu_tune_result;
 
 int siminf_gpu_plan_tune(siminf_gpu_plan *plan, void *cuda_stream, int probe_days,

@@ -118,7 +118,7 @@ class Options(C.Structure):
     _fields_ = [("cap_transfers", C.c_int), ("heavy_rate", C.c_int),
                 ("gdata_per_replicate", C.c_int), ("two_pass", C.c_int),
                 ("max_node_day_transitions", C.c_int), ("streamed", C.c_int),
-                ("reserved", C.c_int * 2)]
+                ("ssa_variant", C.c_int), ("wave_block", C.c_int)]
 
 
 class PfilterArgs(C.Structure):
@@ -174,14 +174,21 @@ class Stats(C.Structure):
     ]
 
 
+TUNE_CANDIDATES = 16
+
+
 class TuneResult(C.Structure):
     """siminf_gpu_tune_result."""
     _fields_ = [
-        ("heavy_rate", C.c_double * 8),
-        ("two_pass", C.c_int * 8),
-        ("ms", C.c_double * 8),
+        ("heavy_rate", C.c_double * TUNE_CANDIDATES),
+        ("two_pass", C.c_int * TUNE_CANDIDATES),
+        ("ssa_variant", C.c_int * TUNE_CANDIDATES),
+        ("wave_block", C.c_int * TUNE_CANDIDATES),
+        ("ms", C.c_double * TUNE_CANDIDATES),
+        ("n_candidates", C.c_int),
         ("chosen", C.c_int),
         ("probe_days", C.c_int),
+        ("cached", C.c_int),
     ]
 
 

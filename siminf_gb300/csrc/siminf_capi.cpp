@@ -34,9 +34,11 @@
 #include <cstring>
 #include <atomic>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -362,14 +364,15 @@ static inline long long event_day(int time, double tt0)
     return (long long) time - (long long) std::floor(tt0);
 }
 
-/* Whether a streamed plan of len events plans them on the device
- * (SIMINF_DEVICE_PLANNER=0 / 1 forces host / device; by default tables of
- * at least 2^20 events). */
+/* Whether a streamed plan plans its events on the device
+ * (SIMINF_DEVICE_PLANNER=1) instead of on host threads (the default).
+ * The device planner equals the host one, but during a run it competes
+ * with the SSA kernel, whose persistent grid holds every SM, so its work
+ * adds to the run's device time; the host threads are otherwise idle. */
 static bool device_planner_for(long long len)
 {
-    if (const char *ev = getenv("SIMINF_DEVICE_PLANNER"))
-        return ev[0] == '1';
-    return len >= (1LL << 20);
+    const char *ev = getenv("SIMINF_DEVICE_PLANNER");
+    return len > 0 && ev && ev[0] == '1';
 }
 
 /* Threads used by the host planner (SIMINF_PLANNER_THREADS overrides the
@@ -908,6 +911,10 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     s.max_fired = (opt && opt->max_node_day_transitions > 0)
                       ? (unsigned) opt->max_node_day_transitions
                       : SIMINF_GPU_MAX_NODE_DAY_TRANSITIONS;
+    s.ssa_variant = (opt && opt->ssa_variant == 1) ? 1 : 0;
+    if (const char *ev = getenv("SIMINF_SSA_VARIANT"))
+        s.ssa_variant = ev[0] == '1';
+    s.wave_block = opt ? opt->wave_block : 0;
     p->tt0 = a->tspan[0];
 
     if ((rc = make_days(p, a))) {
@@ -1418,11 +1425,15 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
     e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e == cudaSuccess && p->out_args)
         e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking);
+    static const bool prof = getenv("SIMINF_SCHED_PROFILE") && getenv("SIMINF_SCHED_PROFILE")[0] == '1';
+    double waited = 0;
     for (int c = 0; c < nchunks && e == cudaSuccess; c++) {
         const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
+        auto w0 = std::chrono::steady_clock::now();
         for (int d = d0; d < d1 && !failed.load(); d++)
             while (!done[d].load(std::memory_order_acquire) && !failed.load())
                 std::this_thread::yield();
+        waited += ms_since(w0);
         if (failed.load()) {
             e = cudaErrorMemoryAllocation;
             break;
@@ -1482,6 +1493,8 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
     abort.store(1);
     for (auto &t : workers)
         t.join();
+    if (prof)
+        fprintf(stderr, "streamed run (host waves): %.2f ms waiting for plans\n", waited);
     if (cs) {
         const cudaError_t e2 = cudaStreamSynchronize(cs);
         if (e == cudaSuccess)
@@ -1526,12 +1539,28 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
         const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
         cap = std::max(cap, p->e2_hi[d1 - 1] - p->e2_lo[d0]);
     }
-    cudaError_t e = s.aem ? L->aem_init(s, p->tt0, st) : L->init(s, p->tt0, st);
+    /* the day kernels go to a stream of the highest priority, so that the
+     * planner's kernels fill the SMs they leave idle instead of delaying
+     * them; it starts after and ends before the caller's stream */
+    cudaStream_t caller = st;
+    int lo_pri = 0, hi_pri = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri);
+    cudaStream_t hs = nullptr;
+    cudaEvent_t hs_start = nullptr, hs_end = nullptr;
+    cudaError_t e = cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, hi_pri);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&hs_start, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&hs_end, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(hs_start, caller);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(hs, hs_start, 0);
+    if (e != cudaSuccess)
+        return e;
+    st = hs;
+    e = s.aem ? L->aem_init(s, p->tt0, st) : L->init(s, p->tt0, st);
     if (e != cudaSuccess)
         return e;
 
     cudaStream_t ps = nullptr, ds = nullptr;
-    e = cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, lo_pri);
     if (e == cudaSuccess && p->out_args)
         e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking);
     int dev = 0;
@@ -1660,9 +1689,13 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
         }
     });
 
+    static const bool prof = getenv("SIMINF_SCHED_PROFILE") && getenv("SIMINF_SCHED_PROFILE")[0] == '1';
+    double waited = 0;
     for (int c = 0; c < nchunks && e == cudaSuccess; c++) {
+        auto w0 = std::chrono::steady_clock::now();
         while (!ready[c].load(std::memory_order_acquire))
             std::this_thread::yield();
+        waited += ms_since(w0);
         const Planned &pl = plans[c];
         if (pl.err != cudaSuccess) {
             e = pl.err;
@@ -1745,6 +1778,8 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
     }
     abort.store(1);
     planner.join();
+    if (prof)
+        fprintf(stderr, "streamed run: %.2f ms waiting for plans\n", waited);
 
     /* events past the last day: the order check and the maxima */
     for (long long l0 = tail_lo; e == cudaSuccess && bad == ~0ULL && l0 < len; ) {
@@ -1794,9 +1829,16 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
         cudaStreamDestroy(ds);
     }
     cudaStreamSynchronize(ps);
+    /* the caller's stream continues after the day kernels */
+    if (cudaEventRecord(hs_end, hs) == cudaSuccess)
+        cudaStreamWaitEvent(caller, hs_end, 0);
+    cudaStreamSynchronize(hs);
     for (cudaEvent_t ev : done)
         if (ev)
             cudaEventDestroy(ev);
+    cudaEventDestroy(hs_start);
+    cudaEventDestroy(hs_end);
+    cudaStreamDestroy(hs);
     for (int r = 0; r < E1_RING; r++)
         cudaFree(ring[r]);
     cudaFree(e1_all);
@@ -1988,36 +2030,107 @@ int siminf_gpu_plan_run(siminf_gpu_plan *p, void *cuda_stream)
     return plan_run_impl(p, (cudaStream_t) cuda_stream, nullptr);
 }
 
+/* The autotuner's choices, kept per device model and size class. */
+struct TuneKey {
+    const Launchers *L;
+    int nodes_class, days_class, transfers, aem, probe_days;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(L, nodes_class, days_class, transfers, aem, probe_days) <
+               std::tie(o.L, o.nodes_class, o.days_class, o.transfers, o.aem, o.probe_days);
+    }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, siminf_gpu_tune_result> g_tune_cache;
+
+static int log2_class(long long n)
+{
+    int c = 0;
+    while (n > 1) {
+        n >>= 1;
+        c++;
+    }
+    return c;
+}
+
 int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
                          siminf_gpu_tune_result *out)
 {
     if (!p || p->e2_pending)
         return SIMINF_GPU_ERR_INVALID_MODEL;
+    const bool force = probe_days < 0;
+    const int pdays = std::min(probe_days > 0 ? probe_days : 16, p->ndays);
+    const TuneKey key{p->L, log2_class(p->s.Ntot), log2_class(p->ndays), p->e2_count > 0,
+                      p->s.aem, pdays};
+    auto apply = [&](const siminf_gpu_tune_result &r, int k) {
+        p->s.heavy_rate = r.heavy_rate[k];
+        p->s.two_pass = r.two_pass[k];
+        p->s.ssa_variant = r.ssa_variant[k];
+        p->s.wave_block = r.wave_block[k];
+        plan_changed(p);
+    };
+    if (!force) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end() && it->second.chosen >= 0) {
+            siminf_gpu_tune_result r = it->second;
+            r.cached = 1;
+            apply(r, r.chosen);
+            if (out)
+                *out = r;
+            return 0;
+        }
+    }
     static const double cand[4] = {0.0, 2.0, 8.0, 32.0};
     const cudaStream_t st = (cudaStream_t) cuda_stream;
     const double saved = p->s.heavy_rate;
-    const int saved_tp = p->s.two_pass;
-    p->max_days = probe_days > 0 ? probe_days : 16;
+    const int saved_tp = p->s.two_pass, saved_v = p->s.ssa_variant, saved_w = p->s.wave_block;
+    p->max_days = pdays;
     plan_changed(p);
     siminf_gpu_tune_result r{};
     int best = -1, rc = plan_run_impl(p, st, nullptr);     /* warm-up */
-    for (int k = 0; k < SIMINF_GPU_TUNE_CANDIDATES && !rc; k++) {
-        p->s.heavy_rate = cand[k % 4];
-        p->s.two_pass = p->s.aem ? 0 : k / 4;       /* two-pass days are the direct method's */
-        plan_changed(p);
+    auto probe = [&](double hr, int tp, int var, int wb) {
+        const int k = r.n_candidates++;
+        r.heavy_rate[k] = hr;
+        r.two_pass[k] = p->s.aem ? 0 : tp;      /* two-pass days are the direct method's */
+        r.ssa_variant[k] = var;
+        r.wave_block[k] = wb;
+        apply(r, k);
         rc = plan_run_impl(p, st, nullptr);
-        r.heavy_rate[k] = cand[k % 4];
-        r.two_pass[k] = p->s.two_pass;
         r.ms[k] = p->stats.ms_solve;
         if (!rc && (best < 0 || r.ms[k] < r.ms[best]))
             best = k;
+    };
+    /* stage 1: the work queue's layout */
+    for (int k = 0; k < 8 && !rc; k++)
+        probe(cand[k % 4], k / 4, 0, 256);
+    /* stage 2: the SSA kernel's other register budget */
+    if (!rc && best >= 0 && !p->s.aem)
+        probe(r.heavy_rate[best], r.two_pass[best], 1, 256);
+    /* stage 3: the wavefront block */
+    if (!rc && best >= 0 && p->e2_count > 0) {
+        const siminf_gpu_tune_result b = r;
+        const int kb = best;
+        for (int wb : {128, 512})
+            if (!rc)
+                probe(b.heavy_rate[kb], b.two_pass[kb], b.ssa_variant[kb], wb);
     }
     p->max_days = 0;
-    p->s.heavy_rate = (best >= 0) ? cand[best % 4] : saved;
-    p->s.two_pass = (best >= 0 && !p->s.aem) ? best / 4 : saved_tp;
-    plan_changed(p);
+    if (best >= 0) {
+        apply(r, best);
+    } else {
+        p->s.heavy_rate = saved;
+        p->s.two_pass = saved_tp;
+        p->s.ssa_variant = saved_v;
+        p->s.wave_block = saved_w;
+        plan_changed(p);
+    }
     r.chosen = best;
-    r.probe_days = std::min(probe_days > 0 ? probe_days : 16, p->ndays);
+    r.probe_days = pdays;
+    if (!rc && best >= 0) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = r;
+    }
     if (out)
         *out = r;
     return rc;

@@ -1342,8 +1342,8 @@ __global__ void __launch_bounds__(256) k_quick(DevState s, int day, double tt, d
  * thread whose node's day is over takes the next entry at once, so the
  * lanes of a warp keep stepping transitions instead of waiting for the
  * warp's busiest node.  One atomic per warp hands out the entries. */
-template <class M>
-__global__ void __launch_bounds__(SSA_BLOCK, 4) k_ssa_e1(DevState s, int day, double tt,
+template <class M, int MINB>
+__global__ void __launch_bounds__(SSA_BLOCK, MINB) k_ssa_e1(DevState s, int day, double tt,
                                                          double next)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
@@ -1541,7 +1541,7 @@ __device__ __forceinline__ void e2_apply(const DevState &s, const E2Rec &e, int 
 }
 
 template <class M>
-__global__ void __launch_bounds__(256) k_e2_wave(DevState s, const E2Rec *ev, int count, int day,
+__global__ void __launch_bounds__(512) k_e2_wave(DevState s, const E2Rec *ev, int count, int day,
                                                  double tt)
 {
     const long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x;
@@ -1932,8 +1932,8 @@ __device__ __forceinline__ void aem_finish(const DevState &s, AemNode<M> &a, lon
  * order, lane by lane, a lane whose node's day is over taking the next
  * node at once.  One atomic per warp hands out the entries. */
 template <class M>
-__global__ void __launch_bounds__(SSA_BLOCK, 4) k_aem_day(DevState s, int day, double tt,
-                                                          double next)
+__global__ void __launch_bounds__(SSA_BLOCK, M::NT <= 4 ? 4 : 3) k_aem_day(DevState s, int day,
+                                                                          double tt, double next)
 {
     constexpr int NC = M::NC, NT = M::NT, ND = M::ND;
     __shared__ int sS[NT * NC];
@@ -2264,6 +2264,13 @@ struct Launch {
     }
     /* k_ssa_e1 is persistent: as many blocks as can be resident at once
      * (looked up once per model), fewer for small models. */
+    /* The SSA kernel's two register budgets: blocks of SSA_BLOCK threads
+     * resident per SM that __launch_bounds__ asks for (the default keeps
+     * larger models within their registers; the other trades warps for
+     * registers). */
+    static constexpr int SSA_MINB0 = M::NT <= 4 ? 4 : 3;
+    static constexpr int SSA_MINB1 = M::NT <= 4 ? 3 : 2;
+    template <int MINB>
     static int ssa_resident_blocks()
     {
         static int blocks = 0;
@@ -2271,10 +2278,20 @@ struct Launch {
             int dev = 0, nsm = 1, per = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ssa_e1<M>, SSA_BLOCK, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ssa_e1<M, MINB>, SSA_BLOCK, 0);
             blocks = nsm * (per > 0 ? per : 1);
         }
         return blocks;
+    }
+    template <int MINB>
+    static cudaError_t ssa_e1_with(const DevState &s, int day, double tt, double next,
+                                   cudaStream_t st)
+    {
+        const long long need = (long long) blocks_for(s.Ntot, SSA_BLOCK);
+        const int resident = ssa_resident_blocks<MINB>();
+        const int grid = (int) (need < resident ? need : resident);
+        k_ssa_e1<M, MINB><<<grid, SSA_BLOCK, 0, st>>>(s, day, tt, next);
+        return cudaGetLastError();
     }
     static cudaError_t quick(const DevState &s, int day, double tt, double next, cudaStream_t st)
     {
@@ -2283,10 +2300,8 @@ struct Launch {
     }
     static cudaError_t ssa_e1(const DevState &s, int day, double tt, double next, cudaStream_t st)
     {
-        const long long need = (long long) blocks_for(s.Ntot, SSA_BLOCK);
-        const int grid = (int) (need < ssa_resident_blocks() ? need : ssa_resident_blocks());
-        k_ssa_e1<M><<<grid, SSA_BLOCK, 0, st>>>(s, day, tt, next);
-        return cudaGetLastError();
+        return s.ssa_variant == 1 ? ssa_e1_with<SSA_MINB1>(s, day, tt, next, st)
+                                  : ssa_e1_with<SSA_MINB0>(s, day, tt, next, st);
     }
     static cudaError_t e2_tail(const DevState &s, const E2Rec *ev, const E2Tail &tail, int day,
                                double tt, cudaStream_t st)
@@ -2300,7 +2315,8 @@ struct Launch {
         const long long n = (long long) count * s.Nrep;
         if (n == 0)
             return cudaSuccess;
-        k_e2_wave<M><<<blocks_for(n, 256), 256, 0, st>>>(s, ev, count, day, tt);
+        const int b = (s.wave_block == 128 || s.wave_block == 512) ? s.wave_block : 256;
+        k_e2_wave<M><<<blocks_for(n, b), b, 0, st>>>(s, ev, count, day, tt);
         return cudaGetLastError();
     }
     static cudaError_t pts_store(const DevState &s, int day, double tt, int c0, int c1,

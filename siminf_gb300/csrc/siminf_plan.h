@@ -150,6 +150,13 @@ struct DevState {
     int two_pass;
     int *active;
 
+    /* Launch layout the autotuner picks: the SSA kernel's register budget
+     * (0: the model's default, 1: more registers a thread and fewer
+     * resident warps) and the external-transfer wave kernel's block size
+     * (128, 256 or 512; 0: 256). */
+    int ssa_variant;
+    int wave_block;
+
     /* Profiling: per day, the most transitions any node fired that day
      * (nullptr: not recorded). */
     unsigned *day_max;

