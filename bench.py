@@ -79,6 +79,10 @@ def parse():
                     help="ABC proposals (uneven models) run as one batch and one by one (0: skip)")
     ap.add_argument("--pfilter", type=int, default=4096,
                     help="particles of the particle-filter workload (0: skip)")
+    ap.add_argument("--serve-full", action="store_true",
+                    help="serve the request mix at its stated sizes (plain path: first 10 s)")
+    ap.add_argument("--abc-smc", type=int, default=0,
+                    help="generations of the ABC-SMC run over uneven models (0: off)")
     ap.add_argument("--serve-seconds", type=float, default=5.0,
                     help="length of the open-loop serving trace (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="arrivals per second")
@@ -256,13 +260,16 @@ def pfilter_bench(particles):
             "data": "synthetic SISe particle filter (phi pts), end to end through the C ABI"}
 
 
-def serve_bench(seconds, rate, seed=5):
+def serve_bench(seconds, rate, seed=5, full=False, plain_seconds=None):
     """Open-loop Poisson arrivals of a request mix (60% SIR runs, 100-20,000
     nodes log-uniform, 30-365 days; 30% particle filters on the SISe model,
     256-4,096 particles; 10% SEIR-with-events runs, 10,000-200,000 nodes)
     served by the request loop, and the same trace served one request at a
-    time (the plain path).  Particle filters use 40 nodes and 6 weekly
-    observations and SEIR runs 30 days so the trace stays inside a minute."""
+    time (the plain path).  By default particle filters use 40 nodes and 6
+    weekly observations and SEIR runs 30 days so the trace stays inside a
+    minute; full=True takes the stated sizes (500 nodes x 52 weeks, SEIR
+    over 365 days), and the plain path then serves only the first
+    plain_seconds of the trace."""
     from siminf_gb300 import model as M
     from siminf_gb300 import workloads
     from siminf_gb300.run import pfilter, run
@@ -276,10 +283,11 @@ def serve_bench(seconds, rate, seed=5):
         pool_sir.append(M.SIR_mparse(u0, np.arange(1, days + 1), 0.16, 0.077))
     pool_pf = []
     for k in range(4):
-        pm, gdata, t_obs, obs = workloads.sise_pfilter(nodes=40, particles=4096, weeks=6,
-                                                       seed=7 + k)
+        pm, gdata, t_obs, obs = workloads.sise_pfilter(nodes=500 if full else 40, particles=4096,
+                                                       weeks=52 if full else 6, seed=7 + k)
         pool_pf.append((pm, gdata, t_obs, obs))
-    pool_seir = [workloads.seir_events_fast(n, 30, n // 2, rng) for n in (10000, 60000, 200000)]
+    pool_seir = [workloads.seir_events_fast(n, 365 if full else 30, n // 2, rng)
+                 for n in (10000, 60000, 200000)]
     trace, t = [], 0.0
     while True:
         t += rng.exponential(1.0 / rate)
@@ -326,9 +334,11 @@ def serve_bench(seconds, rate, seed=5):
     srv.close()
 
     # plain path: the same trace, one request at a time on the caller's thread
+    plain_trace = trace if plain_seconds is None else [x for x in trace if x[0] <= plain_seconds]
+    plain_nd = sum(node_days(kind, n_p, k) for _, kind, _, n_p, k in plain_trace)
     t0 = time.perf_counter()
     plain_lat = []
-    for at, kind, sd, n_p, k in trace:
+    for at, kind, sd, n_p, k in plain_trace:
         now = time.perf_counter() - t0
         if at > now:
             time.sleep(at - now)
@@ -347,10 +357,69 @@ def serve_bench(seconds, rate, seed=5):
             "value": total_nd / served_s, "unit": UNIT, "seconds": served_s,
             "plain_p50_ms": float(np.percentile(plain_lat, 50)),
             "plain_p99_ms": float(np.percentile(plain_lat, 99)),
-            "plain_value": total_nd / plain_s, "plain_seconds": plain_s,
-            "slots": 8, "hbm_budget_bytes": 150 * 10 ** 9,
+            "plain_value": plain_nd / plain_s, "plain_seconds": plain_s,
+            "plain_requests": len(plain_trace),
+            "slots": 8, "hbm_budget_bytes": 150 * 10 ** 9, "stated_sizes": bool(full),
+            "node_days": int(total_nd),
             "data": "synthetic request mix, open-loop Poisson arrivals; latency from "
                     "submission to completion; plain = one request at a time"}
+
+
+def abc_smc_bench(generations, n_particles=2048, seed=3):
+    """ABC-SMC over uneven models (config 4): particles' node counts from
+    {100, 1e3, 1e4, 5e4} w.p. {.4, .3, .2, .1}, tspans U{60, 365}, events as
+    the headline's scaled to size (a pool of 64 such structures, each
+    proposal taking one with its own parameters and seed); priors beta ~
+    U(0.05, 0.5), epsilon ~ U(0.1, 0.5), gamma ~ U(0.02, 0.2); distance: the
+    L2 norm of daily prevalence I/N against one seeded target run (10,000
+    nodes, 365 days, beta 0.16, epsilon 0.25, gamma 0.077, seed 7).  First
+    tolerance from 2 n_particles prior draws, then the median rule
+    (siminf_gb300/abc.py); proposals in batches of n_particles."""
+    import copy
+    from siminf_gb300 import abc, workloads
+    from siminf_gb300 import model as M
+    from siminf_gb300.run import run, run_batch
+    rng = np.random.default_rng(seed)
+    pool = []
+    for _ in range(64):
+        Nn = int(rng.choice((100, 1000, 10000, 50000), p=(0.4, 0.3, 0.2, 0.1)))
+        T = int(rng.integers(60, 366))
+        pool.append(workloads.seir_events_fast(Nn, T, max(1, Nn // 2), rng))
+    truth = workloads.seir_events_fast(10000, 365, 5000, np.random.default_rng(7))
+    r = run(truth, seed=7, cap_transfers=True)
+    I = r.U[2::4].sum(axis=0).astype(float)         # rows: node * 4 + compartment
+    N = r.U.sum(axis=0).astype(float)
+    target = np.where(N > 0, I / np.maximum(N, 1.0), 0.0)
+
+    def simulate(theta, g):
+        models, seeds, targets = [], [], []
+        for b, e, gm in theta:
+            s = copy.copy(pool[int(g.integers(0, len(pool)))])
+            s.ldata = M._rep_ldata(s.Nn, b, e, gm)
+            models.append(s)
+            seeds.append(int(g.integers(1, 2 ** 62)))
+            targets.append(target[:len(s.tspan)])
+        return models, seeds, targets
+
+    priors = [abc.Prior("beta", "uniform", 0.05, 0.5), abc.Prior("epsilon", "uniform", 0.1, 0.5),
+              abc.Prior("gamma", "uniform", 0.02, 0.2)]
+    pm0, ps0, pt0 = simulate(abc.proposals(priors, 8, rng)[0], rng)
+    run_batch(pm0, ps0, pt0, cap_transfers=True)             # warm-up
+    t0 = time.perf_counter()
+    gens = abc.abc_smc(simulate, priors, n_particles, generations, batch=n_particles,
+                       n_init=2 * n_particles, seed=seed)
+    dt = time.perf_counter() - t0
+    nd = sum(g.node_days for g in gens)
+    return {"generations": generations, "particles": n_particles, "seconds": dt,
+            "node_days": int(nd), "value": nd / dt, "unit": UNIT,
+            "per_generation": [{"tolerance": g.tolerance, "proposals": g.nprop,
+                                "ess": g.ess, "seconds": g.seconds,
+                                "posterior_mean": [float(v) for v in
+                                                   np.average(g.x, axis=0, weights=g.w)]}
+                               for g in gens],
+            "data": "config-4 ABC-SMC: synthetic uneven SEIR models with events, prior "
+                    "proposals and SMC perturbations, distances on the device; end to end "
+                    "through the C ABI (host buffers)"}
 
 
 UNTRUNCATED_SCALE = 0.1
@@ -599,8 +668,11 @@ def run_ours(args):
     abc = abc_bench(args.abc) if args.abc > 0 and rank == 0 and world == 1 else None
     pf = (pfilter_bench(args.pfilter)
           if args.pfilter > 0 and rank == 0 and world == 1 else None)
-    serve = (serve_bench(args.serve_seconds, args.serve_rate)
+    serve = (serve_bench(args.serve_seconds, args.serve_rate, full=args.serve_full,
+                         plain_seconds=10.0 if args.serve_full else None)
              if args.serve_seconds > 0 and rank == 0 and world == 1 else None)
+    abc_smc = (abc_smc_bench(args.abc_smc)
+               if args.abc_smc > 0 and rank == 0 and world == 1 else None)
 
     e2e = None
     if not args.no_e2e:
@@ -685,6 +757,7 @@ def run_ours(args):
             "aem": aem,
             "batched": batched,
             "sir_plain": sir,
+            "abc_smc": abc_smc,
             "abc": abc,
             "pfilter": pf,
             "serve": serve,

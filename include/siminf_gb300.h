@@ -476,7 +476,10 @@ int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
  * Stage 2, from the best of stage 1: the SSA kernel's other register
  * budget (ssa_variant 1: more registers a thread, fewer resident warps).
  * Stage 3, for plans with external transfers: the wavefront kernel's block
- * of 128 and 512 threads (256 otherwise).  The choice is kept per device
+ * of 128 and 512 threads (256 otherwise).  The three fastest are then
+ * timed again as repeated runs execute them (the third run of each, which
+ * replays the run's CUDA graph), and their times replace the probes'; the
+ * fastest of those is kept.  The choice is kept per device
  * model and size class (node count and day count to a power of two,
  * transfers or not): a later plan of the same class takes it without
  * probing (cached = 1; probe_days < 0 forces a new search).  Results never

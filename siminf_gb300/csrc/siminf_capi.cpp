@@ -2059,7 +2059,8 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
     if (!p || p->e2_pending)
         return SIMINF_GPU_ERR_INVALID_MODEL;
     const bool force = probe_days < 0;
-    const int pdays = std::min(probe_days > 0 ? probe_days : 16, p->ndays);
+    const int want_days = probe_days < 0 ? -probe_days : probe_days;
+    const int pdays = std::min(want_days > 0 ? want_days : 16, p->ndays);
     const TuneKey key{p->L, log2_class(p->s.Ntot), log2_class(p->ndays), p->e2_count > 0,
                       p->s.aem, pdays};
     auto apply = [&](const siminf_gpu_tune_result &r, int k) {
@@ -2114,6 +2115,27 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
         for (int wb : {128, 512})
             if (!rc)
                 probe(b.heavy_rate[kb], b.two_pass[kb], b.ssa_variant[kb], wb);
+    }
+    /* final: the three fastest again, as repeated runs execute them (a
+     * run after an unchanged one replays the run's graph, which takes the
+     * launch overhead off the layouts with more launches): the third run
+     * of each is timed and replaces its probe time */
+    if (!rc && r.n_candidates > 1) {
+        int order[SIMINF_GPU_TUNE_CANDIDATES];
+        for (int k = 0; k < r.n_candidates; k++)
+            order[k] = k;
+        std::sort(order, order + r.n_candidates,
+                  [&](int x, int y) { return r.ms[x] < r.ms[y]; });
+        best = -1;
+        for (int i = 0; i < std::min(3, r.n_candidates) && !rc; i++) {
+            const int k = order[i];
+            apply(r, k);
+            for (int rep = 0; rep < 3 && !rc; rep++)
+                rc = plan_run_impl(p, st, nullptr);
+            r.ms[k] = p->stats.ms_solve;
+            if (!rc && (best < 0 || r.ms[k] < r.ms[best]))
+                best = k;
+        }
     }
     p->max_days = 0;
     if (best >= 0) {

@@ -95,3 +95,47 @@ def test_generation_loop_on_a_stand_in_batch(monkeypatch):
         assert g.x.shape == (200, 1) and (g.distance <= g.tolerance).all()
         assert abs(g.w.sum() - 1.0) < 1e-12
     assert abs(np.average(gens[-1].x[:, 0], weights=gens[-1].w) - truth) < 0.02
+
+
+@pytest.mark.gpu
+def test_abc_smc_on_device_batches(gpu):
+    """Three generations over real batches of small uneven SEIR models:
+    every accepted particle's distance, which the device computed, is within
+    its generation's tolerance, and equals the distance of the same model
+    run alone."""
+    import copy
+    from siminf_gb300 import model as M
+    from siminf_gb300 import workloads
+    from siminf_gb300.run import run, run_batch
+    rng = np.random.default_rng(2)
+    pool = [workloads.seir_events_fast(int(n), int(T), int(n) // 2, rng)
+            for n, T in zip(rng.choice((50, 200), 6), rng.integers(20, 41, 6))]
+    target = np.linspace(0.0, 0.02, 41)
+    made = []
+
+    def simulate(theta, g):
+        models, seeds, targets = [], [], []
+        for b, e, gm in theta:
+            s = copy.copy(pool[int(g.integers(0, len(pool)))])
+            s.ldata = M._rep_ldata(s.Nn, b, e, gm)
+            models.append(s)
+            seeds.append(int(g.integers(1, 2 ** 62)))
+            targets.append(target[:len(s.tspan)])
+        made.append((models, seeds, targets))
+        return models, seeds, targets
+
+    priors = [abc.Prior("beta", "uniform", 0.05, 0.5), abc.Prior("epsilon", "uniform", 0.1, 0.5),
+              abc.Prior("gamma", "uniform", 0.02, 0.2)]
+    gens = abc.abc_smc(simulate, priors, n_particles=32, generations=3, batch=64, n_init=64,
+                       seed=4)
+    for g in gens:
+        assert len(g.x) == 32 and (g.distance <= g.tolerance).all()
+    # one proposal of the first batch, run alone, gives the batch's distance
+    models, seeds, targets = made[0]
+    _, d_batch = run_batch(models[:3], seeds[:3], targets[:3], cap_transfers=True)
+    for m, sd, tg, db in zip(models[:3], seeds[:3], targets[:3], d_batch):
+        r = run(m, seed=sd, cap_transfers=True)
+        I = r.U[2::4].sum(axis=0).astype(float)
+        N = r.U.sum(axis=0).astype(float)
+        prev = np.where(N > 0, I / np.maximum(N, 1.0), 0.0)
+        assert abs(np.sqrt(np.sum((prev - tg) ** 2)) - db) < 1e-12
