@@ -56,10 +56,10 @@ UNIT = "node-days/s"
 # (4 compartments x 4 B) + events read (0.504 events per node-day x 36 B).
 ALGO_BYTES_PER_NODE_DAY = 16 + 0.504 * 36
 # DRAM traffic of one k_ssa_e1 launch (dram__bytes_read.sum +
-# dram__bytes_write.sum) from an ncu capture of the 250,000-node, 60-day
-# case of this workload (day 30: 20.4 MB read, 0 written), per node; the
-# traffic grows with the node count, so a launch of N nodes moves N times it.
-SSA_TRAFFIC_BYTES_PER_NODE = 20.408320e6 / 250_000
+# dram__bytes_write.sum) measured by ncu on this workload at its full node
+# count (10^6 nodes, day 110 of a 120-day run: 93.3 MB read, 10.6 MB
+# written), per node; another node count moves that much per node.
+SSA_TRAFFIC_BYTES_PER_NODE = (93.299968e6 + 10.620928e6) / 1_000_000
 
 
 def parse():
@@ -365,7 +365,7 @@ def serve_bench(seconds, rate, seed=5, full=False, plain_seconds=None):
                     "submission to completion; plain = one request at a time"}
 
 
-def abc_smc_bench(generations, n_particles=2048, seed=3):
+def abc_smc_bench(generations, n_particles=2048, seed=3, batch=512):
     """ABC-SMC over uneven models (config 4): particles' node counts from
     {100, 1e3, 1e4, 5e4} w.p. {.4, .3, .2, .1}, tspans U{60, 365}, events as
     the headline's scaled to size (a pool of 64 such structures, each
@@ -374,7 +374,8 @@ def abc_smc_bench(generations, n_particles=2048, seed=3):
     L2 norm of daily prevalence I/N against one seeded target run (10,000
     nodes, 365 days, beta 0.16, epsilon 0.25, gamma 0.077, seed 7).  First
     tolerance from 2 n_particles prior draws, then the median rule
-    (siminf_gb300/abc.py); proposals in batches of n_particles."""
+    (siminf_gb300/abc.py); proposals in batches of `batch` models (each
+    model averages ~0.8M events, so a batch of 512 holds ~4e8)."""
     import copy
     from siminf_gb300 import abc, workloads
     from siminf_gb300 import model as M
@@ -406,11 +407,11 @@ def abc_smc_bench(generations, n_particles=2048, seed=3):
     pm0, ps0, pt0 = simulate(abc.proposals(priors, 8, rng)[0], rng)
     run_batch(pm0, ps0, pt0, cap_transfers=True)             # warm-up
     t0 = time.perf_counter()
-    gens = abc.abc_smc(simulate, priors, n_particles, generations, batch=n_particles,
+    gens = abc.abc_smc(simulate, priors, n_particles, generations, batch=batch,
                        n_init=2 * n_particles, seed=seed)
     dt = time.perf_counter() - t0
     nd = sum(g.node_days for g in gens)
-    return {"generations": generations, "particles": n_particles, "seconds": dt,
+    return {"generations": generations, "particles": n_particles, "batch": batch, "seconds": dt,
             "node_days": int(nd), "value": nd / dt, "unit": UNIT,
             "per_generation": [{"tolerance": g.tolerance, "proposals": g.nprop,
                                 "ess": g.ess, "seconds": g.seconds,
@@ -746,7 +747,8 @@ def run_ours(args):
                          "algorithmic_bytes_per_launch": (ALGO_BYTES_PER_NODE_DAY * nodes),
                          "peak_source": peak_kind,
                          "note": "algorithmic bytes = %.1f B/node-day x node-days per launch; "
-                                 "the SSA kernel is bound by FP64 latency, not HBM"
+                                 "traffic measured by ncu at 10^6 nodes (day 110 of 120); "
+                                 "the SSA kernel is bound by its serial chain, not HBM"
                                  % ALGO_BYTES_PER_NODE_DAY},
             "kernels": prof["kernels"],
             "autotune": autotune,
