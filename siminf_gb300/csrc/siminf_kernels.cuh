@@ -245,11 +245,13 @@ __device__ __forceinline__ bool ssa_begin(SsaLane<M> &ln, const si_rng &key, uin
  * The transition the step would fire is selected and applied to copies of
  * the state while the division runs -- its rates need no time -- and the
  * copies replace the state only once the waiting time shows that it fires
- * before the day ends.  The loop-carried chain is then the selection, the
- * state update and the rate refresh; the division and the day-end check
- * run beside it.  Returns true when the node's day is over. */
+ * before the day ends.  Returns true when the node's day is over.  It is
+ * the exact path behind ssa_step_spec, taken only for that step's rare
+ * cases, so it stays out of line: inlined, it doubled the code of the SSA
+ * loop that every warp keeps in its instruction cache (3% of the headline
+ * run's time). */
 template <class M>
-__device__ __forceinline__ bool ssa_step_ahead(SsaLane<M> &ln, const si_rng &key, double next,
+__device__ __noinline__ bool ssa_step_ahead(SsaLane<M> &ln, const si_rng &key, double next,
                                                const double *v, const double *ld,
                                                const double *gd, const int *sS,
                                                const uint32_t *sG, unsigned max_fired)
