@@ -320,22 +320,77 @@ def serve_bench(seconds, rate, seed=5, full=False, plain_seconds=None):
     srv = Server(slots=8, hbm_budget_bytes=150 * 10 ** 9)
     for kind, k in (("sir", 0), ("pf", 0), ("seir", 0)):
         srv.wait(submit(srv, kind, 1, 256, k))                     # warm-up
+    # Finished requests are collected while the trace runs and their
+    # outputs dropped (a SEIR request of 200,000 nodes x 365 days returns
+    # 1.2 GB of U).  At the stated sizes the offered load is several times
+    # what one GPU serves, so the backlog's result buffers are bounded: a
+    # request whose arrival would take the outstanding U bytes above
+    # max_backlog_bytes is submitted when enough earlier ones finish.
+    # Latency is counted from the request's arrival time in the trace, so
+    # that wait is part of it.
+    def out_bytes(kind, k):
+        if kind == "sir":
+            return pool_sir[k].Nn * pool_sir[k].Nc * len(pool_sir[k].tspan) * 4
+        if kind == "seir":
+            return pool_seir[k].Nn * pool_seir[k].Nc * len(pool_seir[k].tspan) * 4
+        return 0
+
+    max_backlog_bytes = 16 * 10 ** 9
     t0 = time.perf_counter()
-    tickets = []
+    live, lat = [], []
+    backlog = [0]
+    held_s = 0.0
+
+    def reap():
+        still = []
+        for tk, at, t_sub, nb in live:
+            if tk.finished:
+                srv.wait(tk)                # raises on the request's error
+                lat.append((t_sub - at) * 1e3 + tk.latency_ms)
+                backlog[0] -= nb
+                tk.holder = tk.model = None
+                tk.keep = []
+            else:
+                still.append((tk, at, t_sub, nb))
+        live[:] = still
+
+    t_log = 0.0
     for at, kind, sd, n_p, k in trace:
-        now = time.perf_counter() - t0
-        if at > now:
-            time.sleep(at - now)
-        tickets.append(submit(srv, kind, sd, n_p, k))
-    for tk in tickets:
-        srv.wait(tk)
+        nb = out_bytes(kind, k)
+        if full and at >= t_log:
+            print("serve: t %.0f s of the trace, %d served, %d in flight, %.1f GB of results "
+                  "held, %.0f s elapsed" % (at, len(lat), len(live), backlog[0] / 1e9,
+                                            time.perf_counter() - t0),
+                  file=sys.stderr, flush=True)
+            t_log += 10.0
+        while True:
+            reap()
+            now = time.perf_counter() - t0
+            if at <= now and (backlog[0] + nb <= max_backlog_bytes or not live):
+                break
+            time.sleep(min(max(at - now, 0.0), 0.002) or 0.002)
+        t_sub = time.perf_counter() - t0
+        held_s = max(held_s, t_sub - at)
+        backlog[0] += nb
+        live.append((submit(srv, kind, sd, n_p, k), at, t_sub, nb))
+    n_log = 0
+    while live:
+        reap()
+        if full and len(lat) >= n_log:
+            print("serve: trace submitted, %d served, %d in flight, %.0f s elapsed"
+                  % (len(lat), len(live), time.perf_counter() - t0), file=sys.stderr, flush=True)
+            n_log = len(lat) + 1000
+        time.sleep(0.001)
     served_s = time.perf_counter() - t0
-    lat = np.array([tk.latency_ms for tk in tickets])
+    lat = np.array(lat)
     srv.close()
 
     # plain path: the same trace, one request at a time on the caller's thread
     plain_trace = trace if plain_seconds is None else [x for x in trace if x[0] <= plain_seconds]
     plain_nd = sum(node_days(kind, n_p, k) for _, kind, _, n_p, k in plain_trace)
+    if full:
+        print("serve: served in %.0f s; plain path over %d requests" % (served_s, len(plain_trace)),
+              file=sys.stderr, flush=True)
     t0 = time.perf_counter()
     plain_lat = []
     for at, kind, sd, n_p, k in plain_trace:
@@ -360,6 +415,7 @@ def serve_bench(seconds, rate, seed=5, full=False, plain_seconds=None):
             "plain_value": plain_nd / plain_s, "plain_seconds": plain_s,
             "plain_requests": len(plain_trace),
             "slots": 8, "hbm_budget_bytes": 150 * 10 ** 9, "stated_sizes": bool(full),
+            "max_backlog_bytes": max_backlog_bytes, "max_submit_delay_s": held_s,
             "node_days": int(total_nd),
             "data": "synthetic request mix, open-loop Poisson arrivals; latency from "
                     "submission to completion; plain = one request at a time"}
@@ -408,7 +464,7 @@ def abc_smc_bench(generations, n_particles=2048, seed=3, batch=512):
     run_batch(pm0, ps0, pt0, cap_transfers=True)             # warm-up
     t0 = time.perf_counter()
     gens = abc.abc_smc(simulate, priors, n_particles, generations, batch=batch,
-                       n_init=2 * n_particles, seed=seed)
+                       n_init=2 * n_particles, seed=seed, verbose=True)
     dt = time.perf_counter() - t0
     nd = sum(g.node_days for g in gens)
     return {"generations": generations, "particles": n_particles, "batch": batch, "seconds": dt,
@@ -943,10 +999,12 @@ def tune_summary(tune):
     return {"probe_days": tune.probe_days, "cached": bool(tune.cached),
             "candidates": [{"heavy_rate": tune.heavy_rate[i], "two_pass": tune.two_pass[i],
                             "ssa_variant": tune.ssa_variant[i],
-                            "wave_block": tune.wave_block[i], "ms": tune.ms[i]}
+                            "wave_block": tune.wave_block[i],
+                            "heavy_lanes": tune.heavy_lanes[i] or 32, "ms": tune.ms[i]}
                            for i in range(tune.n_candidates)],
             "chosen_heavy_rate": tune.heavy_rate[k], "chosen_two_pass": tune.two_pass[k],
-            "chosen_ssa_variant": tune.ssa_variant[k], "chosen_wave_block": tune.wave_block[k]}
+            "chosen_ssa_variant": tune.ssa_variant[k], "chosen_wave_block": tune.wave_block[k],
+            "chosen_heavy_lanes": tune.heavy_lanes[k] or 32}
 
 
 def plan_kernel_profile(plan, C, stream):

@@ -229,6 +229,8 @@ typedef struct siminf_gpu_options {
     int ssa_variant;    /* SSA kernel register budget: 0 the model's default, 1 more
                          * registers a thread and fewer resident warps (see the autotuner) */
     int wave_block;     /* threads per block of the wavefront kernel: 128, 256 or 512 (0: 256) */
+    int heavy_lanes;    /* lanes of a warp that take nodes of the heaviest class (rate sum
+                         * >= 16 x heavy_rate), 1..32 (0: 32) */
 } siminf_gpu_options;
 
 /* The default of siminf_gpu_options.max_node_day_transitions. */
@@ -474,8 +476,9 @@ int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
  * queued first and run 32 to a warp; 0 turns the part off: 0, 2, 8, 32),
  * with one-pass and with two-pass days (siminf_gpu_options.two_pass).
  * Stage 2, from the best of stage 1: the SSA kernel's other register
- * budget (ssa_variant 1: more registers a thread, fewer resident warps).
- * Stage 3, for plans with external transfers: the wavefront kernel's block
+ * budget (ssa_variant 1: more registers a thread, fewer resident warps),
+ * then, where the heavy part is on, 8 lanes a warp for the heaviest class
+ * (heavy_lanes; 32 otherwise).  Stage 3, for plans with external transfers: the wavefront kernel's block
  * of 128 and 512 threads (256 otherwise).  The three fastest are then
  * timed again as repeated runs execute them (the third run of each, which
  * replays the run's CUDA graph), and their times replace the probes'; the
@@ -491,6 +494,7 @@ typedef struct siminf_gpu_tune_result {
     int two_pass[SIMINF_GPU_TUNE_CANDIDATES];   /* 1: two-pass days */
     int ssa_variant[SIMINF_GPU_TUNE_CANDIDATES];    /* SSA kernel register budget */
     int wave_block[SIMINF_GPU_TUNE_CANDIDATES];     /* threads per wavefront block */
+    int heavy_lanes[SIMINF_GPU_TUNE_CANDIDATES];    /* lanes a warp for the heaviest class */
     double ms[SIMINF_GPU_TUNE_CANDIDATES];     /* device time of the probe days */
     int n_candidates;                           /* candidates timed */
     int chosen;                                 /* index of the kept candidate */

@@ -26,6 +26,7 @@ previous generation's accepted distances.  The reference's adaptive rule
 rule stands in for it here.  Random numbers come from numpy's Generator
 seeded by `seed`, not R's: runs are reproducible but not R's draws.
 """
+import sys
 import time
 
 import numpy as np
@@ -183,7 +184,8 @@ def abc_smc(simulate, priors, n_particles, generations, batch=2048, tolerance=No
         out.append(Generation(xx, w_new, dd, eps, nprop, time.perf_counter() - t0, node_days))
         if verbose:
             print("generation %d: tolerance %.4g, %d proposals, ESS %.0f, %.1f s"
-                  % (g + 1, eps, nprop, out[-1].ess, out[-1].seconds))
+                  % (g + 1, eps, nprop, out[-1].ess, out[-1].seconds), file=sys.stderr,
+                  flush=True)
         x, w = xx, w_new
         if g + 1 < generations:
             eps = float(tolerance[g + 1]) if tolerance is not None else float(np.median(dd))

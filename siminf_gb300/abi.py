@@ -118,7 +118,7 @@ class Options(C.Structure):
     _fields_ = [("cap_transfers", C.c_int), ("heavy_rate", C.c_int),
                 ("gdata_per_replicate", C.c_int), ("two_pass", C.c_int),
                 ("max_node_day_transitions", C.c_int), ("streamed", C.c_int),
-                ("ssa_variant", C.c_int), ("wave_block", C.c_int)]
+                ("ssa_variant", C.c_int), ("wave_block", C.c_int), ("heavy_lanes", C.c_int)]
 
 
 class PfilterArgs(C.Structure):
@@ -184,6 +184,7 @@ class TuneResult(C.Structure):
         ("two_pass", C.c_int * TUNE_CANDIDATES),
         ("ssa_variant", C.c_int * TUNE_CANDIDATES),
         ("wave_block", C.c_int * TUNE_CANDIDATES),
+        ("heavy_lanes", C.c_int * TUNE_CANDIDATES),
         ("ms", C.c_double * TUNE_CANDIDATES),
         ("n_candidates", C.c_int),
         ("chosen", C.c_int),

@@ -364,15 +364,21 @@ static inline long long event_day(int time, double tt0)
     return (long long) time - (long long) std::floor(tt0);
 }
 
-/* Whether a streamed plan plans its events on the device
- * (SIMINF_DEVICE_PLANNER=1) instead of on host threads (the default).
- * The device planner equals the host one, but during a run it competes
- * with the SSA kernel, whose persistent grid holds every SM, so its work
- * adds to the run's device time; the host threads are otherwise idle. */
-static bool device_planner_for(long long len)
+/* How a streamed plan plans its events: 0 (the default) on host threads
+ * after a scan of the whole table; 1 on the device (siminf_schedule.cu),
+ * levels included; 2 the device's planner with the levels from host
+ * threads (SIMINF_DEVICE_PLANNER=1 or 2).  The device planner equals the
+ * host one and starts the first day without the host's scan, but during a
+ * run its kernels wait for the SSA kernel, whose persistent grid holds
+ * every SM, so its work adds to the run's device time; the host threads
+ * are otherwise idle. */
+static int device_planner_for(long long len)
 {
-    const char *ev = getenv("SIMINF_DEVICE_PLANNER");
-    return len > 0 && ev && ev[0] == '1';
+    if (len <= 0)
+        return 0;
+    if (const char *ev = getenv("SIMINF_DEVICE_PLANNER"))
+        return ev[0] == '1' ? 1 : ev[0] == '2' ? 2 : 0;
+    return 0;
 }
 
 /* Threads used by the host planner (SIMINF_PLANNER_THREADS overrides the
@@ -562,13 +568,14 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
  * the day being planned (the last event with the node as source, `excl`,
  * and the last add into it, `add`), packed into one word so that an event
  * touches one cache line per node: 16 bits each, so the table of a
- * million nodes (4 MB) stays in cache.  Zero outside the day; the nodes a
- * day touches are listed and cleared after it.  A day whose wavefronts run
+ * million nodes (4 MB) stays in cache.  Zero outside the day: after a day
+ * that touches few nodes they are cleared one by one (listed in
+ * `touched`), after a busy day the whole table at once.  A day whose wavefronts run
  * deeper than 2^16 - 1 is planned again with 32-bit levels. */
 struct WaveTracker {
     std::vector<uint32_t> lv;
     std::vector<int> touched, level;
-    std::vector<long long> idx;
+    std::vector<uint32_t> idx;          /* input positions, relative to the day's first */
     std::vector<long long> cnt, off;
     explicit WaveTracker(int Nn) : lv(Nn, 0) {}
 };
@@ -592,6 +599,10 @@ static bool day_levels(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a
     w.touched.clear();
     maxl = 0;
     bool ok = true;
+    /* a day that touches a fair part of the nodes clears the whole table
+     * afterwards (one sequential pass) instead of listing the nodes it
+     * touched and clearing them one by one (a random write each) */
+    const bool sparse = 2 * (hi - lo) < (long long) Nn / 8;
     for (long long i = lo; i < hi; i++) {
         if (i + PF < hi) {
             const unsigned ps = (unsigned) (src[i + PF] - 1), pd = (unsigned) (dst[i + PF] - 1);
@@ -604,9 +615,9 @@ static bool day_levels(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a
         if (s >= Nn || t >= Nn || (unsigned) (sel[i] - 1) >= nsel)
             continue;
         const P vs = lv[s], vt = lv[t];
-        if (!vs)
+        if (sparse && !vs)
             w.touched.push_back((int) s);
-        if (!vt)
+        if (sparse && !vt)
             w.touched.push_back((int) t);
         const long long es = (long long) (vs & LO), as = (long long) (vs >> SH),
                         et = (long long) (vt & LO);
@@ -620,11 +631,15 @@ static bool day_levels(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a
         if ((long long) (vt2 >> SH) < L)
             lv[t] = (vt2 & LO) | ((P) L << SH);
         w.level.push_back((int) L);
-        w.idx.push_back(i);
+        w.idx.push_back((uint32_t) (i - lo));
         maxl = std::max(maxl, (int) L);
     }
-    for (int n : w.touched)
-        lv[n] = 0;
+    if (sparse) {
+        for (int n : w.touched)
+            lv[n] = 0;
+    } else {
+        std::memset(lv, 0, (size_t) Nn * sizeof(P));
+    }
     return ok;
 }
 
@@ -642,8 +657,10 @@ static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, 
         day_levels<uint32_t>(p, a, d, w, lv.data(), maxl);
     }
     const int *src = a->node, *dst = a->dest, *sel = a->select;
+    const long long lo = p->e2_lo[d];
     std::vector<int> &level = w.level;
-    std::vector<long long> &idx = w.idx, &cnt = w.cnt, &off = w.off;
+    std::vector<uint32_t> &idx = w.idx;
+    std::vector<long long> &cnt = w.cnt, &off = w.off;
     cnt.assign(maxl + 2, 0);
     for (int L : level)
         cnt[L]++;
@@ -651,11 +668,56 @@ static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, 
     for (int L = 1; L <= maxl; L++)
         off[L + 1] = off[L] + cnt[L];
     for (size_t k = 0; k < level.size(); k++) {
-        const long long i = idx[k];
+        const long long i = lo + idx[k];
         e2[off[level[k]]++] = E2Rec{src[i] - 1, dst[i] - 1, a->n[i], sel[i] - 1,
                                     a->shift[i] - 1, (int) i, a->proportion[i]};
     }
     p->day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
+}
+
+/* plan_day_waves for a streamed run: the day's transfers in wave order as
+ * their positions relative to the input position rel (order[k], from
+ * p->e2_day_off[d] - base), for the device to gather the records from the
+ * event columns it receives by DMA (k_gather_e2). */
+static void plan_day_order(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
+                           WaveTracker &w, uint32_t *order, long long base, long long rel)
+{
+    int maxl = 0;
+    if (!day_levels<uint16_t>(p, a, d, w, w.lv.data(), maxl)) {
+        std::vector<uint64_t> lv(a->Nn, 0);
+        day_levels<uint32_t>(p, a, d, w, lv.data(), maxl);
+    }
+    std::vector<int> &level = w.level;
+    std::vector<uint32_t> &idx = w.idx;
+    std::vector<long long> &cnt = w.cnt, &off = w.off;
+    cnt.assign(maxl + 2, 0);
+    for (int L : level)
+        cnt[L]++;
+    off.assign(maxl + 2, p->e2_day_off[d] - base);
+    for (int L = 1; L <= maxl; L++)
+        off[L + 1] = off[L] + cnt[L];
+    const uint32_t shift = (uint32_t) (p->e2_lo[d] - rel);
+    for (size_t k = 0; k < level.size(); k++)
+        order[off[level[k]]++] = idx[k] + shift;
+    p->day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
+}
+
+/* The levels of day d's transfers for the device planner (mode 2): pos[k]
+ * for the day's input position e2_lo[d] + k is the transfer's 1-based
+ * level, 0 for an event that is no valid transfer.  Returns the day's
+ * deepest level. */
+static int plan_day_pos_levels(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
+                               WaveTracker &w, uint32_t *pos)
+{
+    int maxl = 0;
+    if (!day_levels<uint16_t>(p, a, d, w, w.lv.data(), maxl)) {
+        std::vector<uint64_t> lv(a->Nn, 0);
+        day_levels<uint32_t>(p, a, d, w, lv.data(), maxl);
+    }
+    std::memset(pos, 0, (size_t) (p->e2_hi[d] - p->e2_lo[d]) * sizeof(uint32_t));
+    for (size_t k = 0; k < w.level.size(); k++)
+        pos[w.idx[k]] = (uint32_t) w.level[k];
+    return maxl;
 }
 
 /* Levels of one day's transfers (input range [lo, hi)) by the host
@@ -915,6 +977,9 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     if (const char *ev = getenv("SIMINF_SSA_VARIANT"))
         s.ssa_variant = ev[0] == '1';
     s.wave_block = opt ? opt->wave_block : 0;
+    s.heavy_lanes = opt ? std::max(0, std::min(32, opt->heavy_lanes)) : 0;
+    if (const char *ev = getenv("SIMINF_HEAVY_LANES"))
+        s.heavy_lanes = std::max(0, std::min(32, atoi(ev)));
     p->tt0 = a->tspan[0];
 
     if ((rc = make_days(p, a))) {
@@ -936,12 +1001,13 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     std::vector<E1Rec> e1;
     std::vector<int> e1_ptr;
     std::unique_ptr<E2Rec[]> e2;
-    if (stream && a->len > 0 && device_planner_for(a->len) &&
-        event_day_ranges(a, p->days, p->e2_lo, p->e2_hi)) {
+    const int dev_mode = stream ? device_planner_for(a->len) : 0;
+    if (dev_mode && event_day_ranges(a, p->days, p->e2_lo, p->e2_hi)) {
         /* the device plans the events during the first run: only the day
          * ranges now (E and N grow to the largest select and shift the
          * planner finds; E1 lists and waves come chunk by chunk) */
         p->dev_plan = true;
+        p->dev_levels = dev_mode == 2;
         p->nsel = nsel;
         p->max_select = p->max_shift = 0;
         p->e2_count = (uint64_t) a->len;        /* room for every event */
@@ -1351,6 +1417,32 @@ static cudaError_t launch_all(siminf_gpu_plan *p, DevState s, cudaStream_t st, K
     return e;
 }
 
+/* Records of n external transfers in wave order, from the event columns
+ * of one chunk's input range (staged on the device, position 0 = input
+ * position rel) and the order the host planned (positions within it). */
+struct StagedCols {
+    int *node, *dest, *n, *select, *shift;
+    double *proportion;
+};
+
+__global__ void k_gather_e2(StagedCols c, const uint32_t *order, long long n, long long rel,
+                            E2Rec *out)
+{
+    const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    const uint32_t j = order[k];
+    E2Rec e;
+    e.src = c.node[j] - 1;
+    e.dst = c.dest[j] - 1;
+    e.n = c.n[j];
+    e.select = c.select[j] - 1;
+    e.shift = c.shift[j] - 1;
+    e.index = (int) (rel + j);
+    e.proportion = c.proportion[j];
+    out[k] = e;
+}
+
 /* The first run of a streamed plan: host threads plan the external
  * transfers' waves day by day while this thread copies each chunk of
  * finished days to the device on a copy stream and queues the chunk's
@@ -1372,16 +1464,48 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
         return e;
 
     const int nchunks = (ndays + CHUNK_DAYS - 1) / CHUNK_DAYS;
-    long long slot_len = 1;
+    long long slot_len = 1, in_len = 1;
     for (int c = 0; c < nchunks; c++) {
         const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
         slot_len = std::max(slot_len, p->e2_day_off[d1] - p->e2_day_off[d0]);
+        in_len = std::max(in_len, p->e2_hi[d1 - 1] - p->e2_lo[d0]);
     }
-    E2Rec *ring = nullptr;
+    /* With the transfer columns in pinned host memory, the planners write
+     * each day's order (4 B a transfer) and the device gathers the records
+     * from the columns it receives by DMA (28 B an event); otherwise they
+     * write the records (32 B a transfer) into the ring, as the copy then
+     * needs */
+    const bool gather = host_pinned(a->node) && host_pinned(a->dest) && host_pinned(a->n) &&
+                        host_pinned(a->select) && host_pinned(a->shift) &&
+                        host_pinned(a->proportion);
+    const size_t elem = gather ? sizeof(uint32_t) : sizeof(E2Rec);
+    char *ring = nullptr;
     size_t ring_bytes = 0;
-    e = pinned_acquire((size_t) RING * slot_len * sizeof(E2Rec), (void **) &ring, &ring_bytes);
+    e = pinned_acquire((size_t) RING * slot_len * elem, (void **) &ring, &ring_bytes);
     if (e != cudaSuccess)
         return e;
+    /* two sets of staged event columns and orders on the device */
+    StagedCols stg[2] = {};
+    uint32_t *dorder[2] = {};
+    std::vector<void *> dbufs;
+    for (int k = 0; k < 2 && gather && e == cudaSuccess; k++) {
+        int **cols[5] = {&stg[k].node, &stg[k].dest, &stg[k].n, &stg[k].select, &stg[k].shift};
+        for (int j = 0; j < 5 && e == cudaSuccess; j++) {
+            e = cudaMalloc((void **) cols[j], (size_t) in_len * sizeof(int));
+            if (e == cudaSuccess)
+                dbufs.push_back(*cols[j]);
+        }
+        if (e == cudaSuccess) e = cudaMalloc((void **) &stg[k].proportion, (size_t) in_len * sizeof(double));
+        if (e == cudaSuccess) dbufs.push_back(stg[k].proportion);
+        if (e == cudaSuccess) e = cudaMalloc((void **) &dorder[k], (size_t) slot_len * sizeof(uint32_t));
+        if (e == cudaSuccess) dbufs.push_back(dorder[k]);
+    }
+    if (e != cudaSuccess) {
+        for (void *q : dbufs)
+            cudaFree(q);
+        pinned_release(ring, ring_bytes);
+        return e;
+    }
 
     std::unique_ptr<std::atomic<int>[]> done(new std::atomic<int>[ndays]);
     std::unique_ptr<std::atomic<int>[]> issued(new std::atomic<int>[nchunks]);
@@ -1411,8 +1535,12 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
                             break;
                         cudaEventSynchronize(copied[c - RING]);
                     }
-                    E2Rec *slot = ring + (size_t) (c % RING) * slot_len;
-                    plan_day_waves(p, a, d, w, slot, p->e2_day_off[c * CHUNK_DAYS]);
+                    char *slot = ring + (size_t) (c % RING) * slot_len * elem;
+                    if (gather)
+                        plan_day_order(p, a, d, w, (uint32_t *) slot,
+                                       p->e2_day_off[c * CHUNK_DAYS], p->e2_lo[c * CHUNK_DAYS]);
+                    else
+                        plan_day_waves(p, a, d, w, (E2Rec *) slot, p->e2_day_off[c * CHUNK_DAYS]);
                     done[d].store(1, std::memory_order_release);
                 }
             } catch (...) {
@@ -1439,10 +1567,34 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             break;
         }
         const long long lo = p->e2_day_off[d0], hi = p->e2_day_off[d1];
+        /* the chunk's event columns and the planned order go up, and the
+         * records are gathered on the device (the copy stream runs chunks
+         * in order, so a staging set is free again two chunks later) */
+        const long long in_lo = p->e2_lo[d0], in_n = p->e2_hi[d1 - 1] - in_lo;
+        StagedCols &sc = stg[c % 2];
         e = cudaEventCreateWithFlags(&copied[c], cudaEventDisableTiming | cudaEventBlockingSync);
-        if (e == cudaSuccess && hi > lo)
-            e = cudaMemcpyAsync(p->d_e2 + lo, ring + (size_t) (c % RING) * slot_len,
+        if (e == cudaSuccess && hi > lo && !gather) {
+            e = cudaMemcpyAsync(p->d_e2 + lo, ring + (size_t) (c % RING) * slot_len * elem,
                                 (size_t) (hi - lo) * sizeof(E2Rec), cudaMemcpyHostToDevice, cs);
+        } else if (e == cudaSuccess && hi > lo) {
+            const int *src_i[5] = {a->node, a->dest, a->n, a->select, a->shift};
+            int *dst_i[5] = {sc.node, sc.dest, sc.n, sc.select, sc.shift};
+            for (int k = 0; k < 5 && e == cudaSuccess; k++)
+                e = cudaMemcpyAsync(dst_i[k], src_i[k] + in_lo, (size_t) in_n * sizeof(int),
+                                    cudaMemcpyHostToDevice, cs);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(sc.proportion, a->proportion + in_lo,
+                                    (size_t) in_n * sizeof(double), cudaMemcpyHostToDevice, cs);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(dorder[c % 2], ring + (size_t) (c % RING) * slot_len * elem,
+                                    (size_t) (hi - lo) * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                    cs);
+            if (e == cudaSuccess) {
+                k_gather_e2<<<(unsigned) ((hi - lo + 255) / 256), 256, 0, cs>>>(
+                    sc, dorder[c % 2], hi - lo, in_lo, p->d_e2 + lo);
+                e = cudaGetLastError();
+            }
+        }
         if (e == cudaSuccess)
             e = cudaEventRecord(copied[c], cs);
         if (e != cudaSuccess)
@@ -1512,6 +1664,8 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             cudaEventDestroy(ev);
     for (cudaEvent_t ev : stored)
         cudaEventDestroy(ev);
+    for (void *q : dbufs)
+        cudaFree(q);
     pinned_release(ring, ring_bytes);
     return e;
 }
@@ -1539,15 +1693,21 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
         const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
         cap = std::max(cap, p->e2_hi[d1 - 1] - p->e2_lo[d0]);
     }
-    /* the day kernels go to a stream of the highest priority, so that the
-     * planner's kernels fill the SMs they leave idle instead of delaying
-     * them; it starts after and ends before the caller's stream */
+    /* the day kernels go to their own stream, which starts after and ends
+     * before the caller's.  When the device plans the levels (its rounds
+     * are most of its work), that stream has the highest priority, so that
+     * the planner's kernels fill the SMs the day kernels leave idle instead
+     * of delaying them; when the host plans them, the planner's few kernels
+     * a chunk go first, each between two of the day kernels, instead of
+     * waiting for a gap in them */
     cudaStream_t caller = st;
     int lo_pri = 0, hi_pri = 0;
     cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri);
+    const int day_pri = p->dev_levels ? lo_pri : hi_pri;
+    const int plan_pri = p->dev_levels ? hi_pri : lo_pri;
     cudaStream_t hs = nullptr;
     cudaEvent_t hs_start = nullptr, hs_end = nullptr;
-    cudaError_t e = cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, hi_pri);
+    cudaError_t e = cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, day_pri);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&hs_start, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&hs_end, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(hs_start, caller);
@@ -1560,7 +1720,7 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
         return e;
 
     cudaStream_t ps = nullptr, ds = nullptr;
-    e = cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, lo_pri);
+    e = cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, plan_pri);
     if (e == cudaSuccess && p->out_args)
         e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking);
     int dev = 0;
@@ -1578,11 +1738,24 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
     if (e == cudaSuccess) e = cudaMalloc((void **) &e1_nodes, (size_t) e1_cap * sizeof(uint32_t));
     for (int r = 0; r < E1_RING && e == cudaSuccess; r++)
         e = cudaMalloc((void **) &ring[r], ((size_t) Nn + 1) * sizeof(int));
+    /* levels from host threads (p->dev_levels): each chunk's transfers'
+     * levels by input position in one of LRING pinned slots, copied up
+     * before the device plans the chunk */
+    enum { LRING = 4 };
+    const bool hl = p->dev_levels;
+    uint32_t *lslot = nullptr, *d_lslot = nullptr;
+    size_t lslot_bytes = 0;
+    if (hl && e == cudaSuccess)
+        e = pinned_acquire((size_t) LRING * cap * sizeof(uint32_t), (void **) &lslot, &lslot_bytes);
+    if (hl && e == cudaSuccess)
+        e = cudaMalloc((void **) &d_lslot, (size_t) cap * sizeof(uint32_t));
     if (e != cudaSuccess) {
         for (int r = 0; r < E1_RING; r++)
             cudaFree(ring[r]);
         cudaFree(e1_all);
         cudaFree(e1_nodes);
+        cudaFree(d_lslot);
+        pinned_release(lslot, lslot_bytes);
         for (cudaStream_t x : {ps, ds})
             if (x)
                 cudaStreamDestroy(x);
@@ -1606,6 +1779,47 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
     std::atomic<int> abort(0);
     long long e1_total = 0, e2_total = 0;
     unsigned long long bad = ~0ULL;
+
+    /* the host's level planners: days in order, each into its chunk's
+     * slot; a slot is reused once the device planner has copied it up */
+    std::unique_ptr<std::atomic<int>[]> lday(new std::atomic<int>[hl ? ndays : 1]);
+    std::unique_ptr<std::atomic<int>[]> lfree(new std::atomic<int>[hl ? nchunks : 1]);
+    std::unique_ptr<std::atomic<int>[]> ldeep(new std::atomic<int>[hl ? nchunks : 1]);
+    std::atomic<int> lnext(0), lfail(0);
+    std::vector<std::thread> lworkers;
+    if (hl) {
+        for (int d = 0; d < ndays; d++)
+            lday[d].store(0);
+        for (int c = 0; c < nchunks; c++) {
+            lfree[c].store(0);
+            ldeep[c].store(0);
+        }
+        const int nthreads = std::max(1, planner_threads() - 2);
+        for (int t = 0; t < nthreads; t++)
+            lworkers.emplace_back([&]() {
+                try {
+                    WaveTracker w(Nn);
+                    for (int d = lnext++; d < ndays && !abort.load(); d = lnext++) {
+                        const int c = d / CHUNK_DAYS;
+                        if (c >= LRING) {
+                            while (!lfree[c - LRING].load(std::memory_order_acquire) &&
+                                   !abort.load())
+                                std::this_thread::sleep_for(std::chrono::microseconds(50));
+                            if (abort.load())
+                                break;
+                        }
+                        const long long l0 = p->e2_lo[c * CHUNK_DAYS];
+                        uint32_t *slot = lslot + (size_t) (c % LRING) * cap;
+                        const int maxl = plan_day_pos_levels(p, a, d, w, slot + (p->e2_lo[d] - l0));
+                        if (maxl > DevScheduler::max_host_level())
+                            ldeep[c].store(1);
+                        lday[d].store(1, std::memory_order_release);
+                    }
+                } catch (...) {
+                    lfail.store(1);
+                }
+            });
+    }
 
     std::thread planner([&]() {
         cudaSetDevice(dev);
@@ -1657,11 +1871,31 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
             if (pe == cudaSuccess && m > 0)
                 pe = cudaMemcpyAsync(sch.proportion, a->proportion + l0, (size_t) m * sizeof(double),
                                      cudaMemcpyHostToDevice, ps);
+            /* the host's levels of the chunk, once its days are planned */
+            const uint32_t *pos_level = nullptr;
+            if (hl && pe == cudaSuccess) {
+                for (int d = d0; d < d1 && !abort.load() && !lfail.load(); d++)
+                    while (!lday[d].load(std::memory_order_acquire) && !abort.load() &&
+                           !lfail.load())
+                        std::this_thread::sleep_for(std::chrono::microseconds(20));
+                if (lfail.load())
+                    pe = cudaErrorMemoryAllocation;
+                else if (abort.load())
+                    break;
+                if (pe == cudaSuccess && m > 0 && !ldeep[c].load()) {
+                    pe = cudaMemcpyAsync(d_lslot, lslot + (size_t) (c % LRING) * cap,
+                                         (size_t) m * sizeof(uint32_t), cudaMemcpyHostToDevice, ps);
+                    pos_level = d_lslot;
+                }
+            }
             if (pe == cudaSuccess)
                 pe = sch.plan_chunk(l0, m, d0, nd, bounds, l0 > 0 ? a->time[l0 - 1] : 0,
                                     l0 > 0 ? a->event[l0 - 1] : 0, l0 > 0, p->d_e2 + base2,
                                     e1_all + base1, ring[c % E1_RING], nullptr, pl.ch,
-                                    e1_nodes + base1);
+                                    e1_nodes + base1, pos_level);
+            /* plan_chunk returns with its stream idle: the slot is free */
+            if (hl && pe == cudaSuccess)
+                lfree[c].store(1, std::memory_order_release);
             /* days too deep for the rounds: the host planner's waves */
             for (size_t k = 0; pe == cudaSuccess && k < pl.ch.deep.size(); k++) {
                 const int j = pl.ch.deep[k];
@@ -1778,8 +2012,11 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
     }
     abort.store(1);
     planner.join();
+    for (auto &t : lworkers)
+        t.join();
     if (prof)
-        fprintf(stderr, "streamed run: %.2f ms waiting for plans\n", waited);
+        fprintf(stderr, "streamed run (%s levels): %.2f ms waiting for plans\n",
+                hl ? "host" : "device", waited);
 
     /* events past the last day: the order check and the maxima */
     for (long long l0 = tail_lo; e == cudaSuccess && bad == ~0ULL && l0 < len; ) {
@@ -1845,6 +2082,8 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
     cudaFree(e1_nodes);
     for (void *q : old_e1)
         cudaFree(q);
+    cudaFree(d_lslot);
+    pinned_release(lslot, lslot_bytes);
     cudaStreamDestroy(ps);
     return e;
 }
@@ -2068,6 +2307,7 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
         p->s.two_pass = r.two_pass[k];
         p->s.ssa_variant = r.ssa_variant[k];
         p->s.wave_block = r.wave_block[k];
+        p->s.heavy_lanes = r.heavy_lanes[k];
         plan_changed(p);
     };
     if (!force) {
@@ -2085,17 +2325,19 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
     static const double cand[4] = {0.0, 2.0, 8.0, 32.0};
     const cudaStream_t st = (cudaStream_t) cuda_stream;
     const double saved = p->s.heavy_rate;
-    const int saved_tp = p->s.two_pass, saved_v = p->s.ssa_variant, saved_w = p->s.wave_block;
+    const int saved_tp = p->s.two_pass, saved_v = p->s.ssa_variant, saved_w = p->s.wave_block,
+              saved_hl = p->s.heavy_lanes;
     p->max_days = pdays;
     plan_changed(p);
     siminf_gpu_tune_result r{};
     int best = -1, rc = plan_run_impl(p, st, nullptr);     /* warm-up */
-    auto probe = [&](double hr, int tp, int var, int wb) {
+    auto probe = [&](double hr, int tp, int var, int wb, int hl) {
         const int k = r.n_candidates++;
         r.heavy_rate[k] = hr;
         r.two_pass[k] = p->s.aem ? 0 : tp;      /* two-pass days are the direct method's */
         r.ssa_variant[k] = var;
         r.wave_block[k] = wb;
+        r.heavy_lanes[k] = hl;
         apply(r, k);
         rc = plan_run_impl(p, st, nullptr);
         r.ms[k] = p->stats.ms_solve;
@@ -2104,17 +2346,21 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
     };
     /* stage 1: the work queue's layout */
     for (int k = 0; k < 8 && !rc; k++)
-        probe(cand[k % 4], k / 4, 0, 256);
-    /* stage 2: the SSA kernel's other register budget */
+        probe(cand[k % 4], k / 4, 0, 256, 0);
+    /* stage 2: the SSA kernel's other register budget, then fewer lanes a
+     * warp for the heaviest nodes (a warp holding the day's longest chains
+     * shares its issue slots and FP64 pipe with fewer lanes) */
     if (!rc && best >= 0 && !p->s.aem)
-        probe(r.heavy_rate[best], r.two_pass[best], 1, 256);
+        probe(r.heavy_rate[best], r.two_pass[best], 1, 256, 0);
+    if (!rc && best >= 0 && !p->s.aem && r.heavy_rate[best] > 0.0 && p->L->time_invariant)
+        probe(r.heavy_rate[best], r.two_pass[best], r.ssa_variant[best], 256, 8);
     /* stage 3: the wavefront block */
     if (!rc && best >= 0 && p->e2_count > 0) {
         const siminf_gpu_tune_result b = r;
         const int kb = best;
         for (int wb : {128, 512})
             if (!rc)
-                probe(b.heavy_rate[kb], b.two_pass[kb], b.ssa_variant[kb], wb);
+                probe(b.heavy_rate[kb], b.two_pass[kb], b.ssa_variant[kb], wb, b.heavy_lanes[kb]);
     }
     /* final: the three fastest again, as repeated runs execute them (a
      * run after an unchanged one replays the run's graph, which takes the
@@ -2145,6 +2391,7 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
         p->s.two_pass = saved_tp;
         p->s.ssa_variant = saved_v;
         p->s.wave_block = saved_w;
+        p->s.heavy_lanes = saved_hl;
         plan_changed(p);
     }
     r.chosen = best;

@@ -80,8 +80,12 @@ struct siminf_gpu_plan {
     bool e2_pending = false;
     /* Streamed runs whose events the device plans (siminf_schedule.cu):
      * e2_lo / e2_hi are the days' input ranges; dev_bad is the first event
-     * out of order the planner found, or -1. */
+     * out of order the planner found, or -1.  dev_levels: host threads
+     * plan the transfers' levels and the device the rest (classification,
+     * order check, E1 lists, wave order); otherwise the device plans the
+     * levels too. */
     bool dev_plan = false;
+    bool dev_levels = false;
     long long dev_bad = -1;
     siminf_gpu_solver_args args{};
     std::unique_ptr<E2Rec[]> h_e2;

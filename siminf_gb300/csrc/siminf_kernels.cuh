@@ -1385,10 +1385,19 @@ __global__ void __launch_bounds__(SSA_BLOCK, MINB) k_ssa_e1(DevState s, int day,
     bool heavy_left = H > 0;         /* warp-uniform: the heavy part may have entries */
     const double *v = nullptr, *ld = nullptr, *gd = nullptr;
     for (;;) {
-        /* hand queue entries to the lanes without a node */
-        const unsigned want = __ballot_sync(FULL, alive && need);
+        /* hand queue entries to the lanes without a node; while the
+         * heaviest class lasts, only the first heavy_lanes lanes take them */
+        unsigned want = __ballot_sync(FULL, alive && need);
         const bool holds_heavy = __any_sync(FULL, alive && !need && heavy);
         const bool from_heavy = heavy_left;
+        if (from_heavy && s.heavy_lanes > 0 && s.heavy_lanes < 32 && want && !holds_heavy) {
+            unsigned long long at = 0;
+            if (lane == 0)
+                at = *(volatile const unsigned long long *) &s.queue_next[par * 2];
+            at = __shfl_sync(FULL, at, 0);
+            if (at < (unsigned long long) n[0])
+                want &= (1u << s.heavy_lanes) - 1u;
+        }
         if (want && !holds_heavy) {
             const int leader = __ffs(want) - 1;
             unsigned long long base = 0;
@@ -1398,7 +1407,7 @@ __global__ void __launch_bounds__(SSA_BLOCK, MINB) k_ssa_e1(DevState s, int day,
             base = __shfl_sync(FULL, base, leader);
             long long cand = -1;
             bool empty = false;
-            if (alive && need) {
+            if ((want >> lane) & 1u) {
                 const unsigned long long pos = base + __popc(want & ((1u << lane) - 1u));
                 if (from_heavy) {
                     if (pos < H) {
@@ -2360,6 +2369,7 @@ struct Launch {
     static const Launchers *table()
     {
         static const Launchers t = {M::NC, M::NT, M::ND, M::NGD, M::PTS_LOCAL,
+                                    M::RATES_TIME_INVARIANT,
                                     init, horizon, quick, ssa_e1, e2_wave, pts_store,
                                     aem_init, aem_day, aem_pts, e2_tail};
         return &t;

@@ -14,6 +14,7 @@ struct Launchers {
     int Nc, Nt, Nd;
     int Ngd;            /* gdata entries the model reads */
     bool pts_local;     /* post-time-step reads only its own node */
+    bool time_invariant;    /* rates ignore t (the heavy part of the work queue applies) */
     cudaError_t (*init)(const DevState &s, double tt0, cudaStream_t st);
     cudaError_t (*horizon)(const DevState &s, const DayInfo *days, int ndays, cudaStream_t st);
     /* the first pass of a two-pass day (k_quick); ssa_e1 is the second */

@@ -156,6 +156,10 @@ struct DevState {
      * (128, 256 or 512; 0: 256). */
     int ssa_variant;
     int wave_block;
+    /* Lanes of a warp that take nodes of the heaviest class (1..32; 0:
+     * 32): a warp that holds the day's longest chains shares its issue
+     * slots and FP64 pipe with fewer lanes. */
+    int heavy_lanes;
 
     /* Profiling: per day, the most transitions any node fired that day
      * (nullptr: not recorded). */

@@ -305,18 +305,46 @@ __global__ void __launch_bounds__(SCHED_BLOCK) k_round(int r, int *flags, long l
     }
 }
 
-/* Each day's wave sizes (cnt[off[day] + level]) and wave count. */
+/* 3'. The levels the host planned, by the transfers' chunk positions
+ * (1-based there, zero-based here); flag[0] is set when a transfer has no
+ * host level or one deeper than the wave keys hold. */
+__global__ void __launch_bounds__(SCHED_BLOCK) k_host_levels(long long n, const uint32_t *idx2,
+                                                             const uint32_t *pos_level, int *Lz,
+                                                             int *flag)
+{
+    const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    const uint32_t v = pos_level[idx2[k]];
+    if (v == 0u || v > (1u << LEVEL_BITS)) {
+        flag[0] = 1;
+        Lz[k] = 0;
+    } else {
+        Lz[k] = (int) v - 1;
+    }
+}
+
+/* Each day's wave sizes (cnt[off[day] + level]) and wave count.  Most
+ * transfers share a few low levels, so the lanes of a warp that count
+ * into one wave add their number with one atomic, and those of one day
+ * their deepest level with one. */
 __global__ void __launch_bounds__(SCHED_BLOCK) k_level_counts(long long n, int nb,
                                                               const uint32_t *ks0, const int *Lz,
                                                               const long long *off, int *cnt,
                                                               int *dmax)
 {
     const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (k >= n)
-        return;
-    const int day = (int) (ks0[k] >> nb), l = Lz[k];     /* 0 <= l < the day's transfers */
-    atomicAdd(&cnt[off[day] + l], 1);
-    atomicMax(&dmax[day], l + 1);
+    const bool act = k < n;
+    const int day = act ? (int) (ks0[k] >> nb) : -1, l = act ? Lz[k] : 0;
+    const long long slot = act ? off[day] + l : -1;    /* 0 <= l < the day's transfers */
+    const int lane = threadIdx.x & 31;
+    const unsigned same_slot = __match_any_sync(0xFFFFFFFFu, (unsigned long long) slot);
+    if (act && lane == __ffs(same_slot) - 1)
+        atomicAdd(&cnt[slot], __popc(same_slot));
+    const unsigned same_day = __match_any_sync(0xFFFFFFFFu, day);
+    const int deepest = (int) __reduce_max_sync(same_day, (unsigned) (l + 1));
+    if (act && lane == __ffs(same_day) - 1)
+        atomicMax(&dmax[day], deepest);
 }
 
 /* Days whose levels still changed in the last round allowed: 1 (left to
@@ -555,10 +583,16 @@ cudaError_t DevScheduler::check_tail(long long lo, long long m, int prev_time, i
     return cudaGetLastError();
 }
 
+int DevScheduler::max_host_level()
+{
+    return 1 << LEVEL_BITS;
+}
+
 cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
                                      const long long *bounds, int prev_time, int prev_event,
                                      bool has_prev, E2Rec *e2_out, E1Rec *e1_out, int *e1_ptr,
-                                     int *wave_out, SchedChunk &out, uint32_t *e1_node_out)
+                                     int *wave_out, SchedChunk &out, uint32_t *e1_node_out,
+                                     const uint32_t *pos_level)
 {
     if (m > cap_ || m < 0 || nd < 1 || nd > MAX_CHUNK_DAYS)
         return cudaErrorInvalidValue;
@@ -617,55 +651,87 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
     const int jb = bits_for(nd);
 
     mark();
-    if (n2 > 0) {
-        uint32_t *ks = ka_, *ps = pa_, *ks2 = kb_, *ps2 = pb_;
-        if (n2 > 1)
-            e = radix_sort<uint32_t>(ks, ps, ks2, ps2, n2, jb + nb_, hist_, tot_, st_);
+    /* the host's levels, if it planned them: no links, no rounds */
+    bool host = pos_level != nullptr && n2 > 0;
+    if (host) {
         const unsigned g2 = blocks_of(n2, SCHED_BLOCK);
-        mark();
+        e = cudaMemsetAsync(flags_, 0, sizeof(int), st_);
         if (e == cudaSuccess) {
-            k_inverse<<<g2, SCHED_BLOCK, 0, st_>>>(ps, n2, inv_);
-            k_links<<<g2, SCHED_BLOCK, 0, st_>>>(n2, ks0_, kd0_, ks, ps, inv_, p1_, p3_, attach_);
+            k_host_levels<<<g2, SCHED_BLOCK, 0, st_>>>(n2, idx2_, pos_level, L_, flags_);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess)
-            e = cudaMemsetAsync(cnt_, 0, n2 * sizeof(int), st_);
+            e = cudaMemcpyAsync(h_flag_, flags_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st_);
+        if (e != cudaSuccess)
+            return e;
+        host = *h_flag_ == 0;
+    }
+    if (n2 > 0 && host) {
+        /* every day within the rounds' depth: none left to the host */
+        const unsigned g2 = blocks_of(n2, SCHED_BLOCK);
+        e = cudaMemsetAsync(cnt_, 0, n2 * sizeof(int), st_);
         if (e == cudaSuccess)
             e = cudaMemsetAsync(dmax_, 0, MAX_CHUNK_DAYS * sizeof(int), st_);
         if (e == cudaSuccess)
-            e = cudaMemsetAsync(deep_, 0xFF, MAX_CHUNK_DAYS * sizeof(int), st_);  /* lastchg = -1 */
-        if (e == cudaSuccess)
-            e = cudaMemsetAsync(L_, 0, n2 * sizeof(int), st_);
-        if (e == cudaSuccess)
-            e = cudaMemsetAsync(A_, 0xFF, n2 * sizeof(int), st_);                 /* A = -1 */
-        if (e == cudaSuccess)
-            e = cudaMemsetAsync(flags_, 0, MAX_ROUNDS * sizeof(int), st_);
+            e = cudaMemsetAsync(deep_, 0, MAX_CHUNK_DAYS * sizeof(int), st_);
         if (e == cudaSuccess) {
-            k_attach_init<<<g2, SCHED_BLOCK, 0, st_>>>(n2, attach_, A_);
+            k_level_counts<<<g2, SCHED_BLOCK, 0, st_>>>(n2, nb_, ks0_, L_, info_ + 2, cnt_, dmax_);
             e = cudaGetLastError();
         }
+    }
+    if (n2 > 0) {
+        uint32_t *ks = ka_, *ps = pa_, *ks2 = kb_, *ps2 = pb_;
+        if (n2 > 1 && !host)
+            e = radix_sort<uint32_t>(ks, ps, ks2, ps2, n2, jb + nb_, hist_, tot_, st_);
+        const unsigned g2 = blocks_of(n2, SCHED_BLOCK);
         mark();
-        /* rounds in batches; the host looks at the last round's flag after
-         * each batch */
-        int r = 0;
-        while (e == cudaSuccess && r < MAX_ROUNDS) {
-            for (int b = 0; b < ROUND_BATCH && r < MAX_ROUNDS && e == cudaSuccess; b++, r++) {
-                k_round<<<g2, SCHED_BLOCK, 0, st_>>>(r, flags_, n2, nb_, ks0_, p1_, p3_, attach_, L_,
-                                                     A_, deep_);
+        if (!host) {
+            if (e == cudaSuccess) {
+                k_inverse<<<g2, SCHED_BLOCK, 0, st_>>>(ps, n2, inv_);
+                k_links<<<g2, SCHED_BLOCK, 0, st_>>>(n2, ks0_, kd0_, ks, ps, inv_, p1_, p3_, attach_);
                 e = cudaGetLastError();
             }
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(h_flag_, flags_ + r - 1, sizeof(int), cudaMemcpyDeviceToHost,
-                                    st_);
+                e = cudaMemsetAsync(cnt_, 0, n2 * sizeof(int), st_);
             if (e == cudaSuccess)
-                e = cudaStreamSynchronize(st_);
-            if (e != cudaSuccess || !*h_flag_)
-                break;
-        }
-        if (e == cudaSuccess) {
-            k_level_counts<<<g2, SCHED_BLOCK, 0, st_>>>(n2, nb_, ks0_, L_, info_ + 2, cnt_, dmax_);
-            k_deep_days<<<1, 32, 0, st_>>>(nd, deep_, MAX_ROUNDS - 1);
-            e = cudaGetLastError();
+                e = cudaMemsetAsync(dmax_, 0, MAX_CHUNK_DAYS * sizeof(int), st_);
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(deep_, 0xFF, MAX_CHUNK_DAYS * sizeof(int), st_);  /* lastchg = -1 */
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(L_, 0, n2 * sizeof(int), st_);
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(A_, 0xFF, n2 * sizeof(int), st_);                 /* A = -1 */
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(flags_, 0, MAX_ROUNDS * sizeof(int), st_);
+            if (e == cudaSuccess) {
+                k_attach_init<<<g2, SCHED_BLOCK, 0, st_>>>(n2, attach_, A_);
+                e = cudaGetLastError();
+            }
+            mark();
+            /* rounds in batches; the host looks at the last round's flag after
+             * each batch */
+            int r = 0;
+            while (e == cudaSuccess && r < MAX_ROUNDS) {
+                for (int b = 0; b < ROUND_BATCH && r < MAX_ROUNDS && e == cudaSuccess; b++, r++) {
+                    k_round<<<g2, SCHED_BLOCK, 0, st_>>>(r, flags_, n2, nb_, ks0_, p1_, p3_, attach_, L_,
+                                                         A_, deep_);
+                    e = cudaGetLastError();
+                }
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(h_flag_, flags_ + r - 1, sizeof(int), cudaMemcpyDeviceToHost,
+                                        st_);
+                if (e == cudaSuccess)
+                    e = cudaStreamSynchronize(st_);
+                if (e != cudaSuccess || !*h_flag_)
+                    break;
+            }
+            if (e == cudaSuccess) {
+                k_level_counts<<<g2, SCHED_BLOCK, 0, st_>>>(n2, nb_, ks0_, L_, info_ + 2, cnt_, dmax_);
+                k_deep_days<<<1, 32, 0, st_>>>(nd, deep_, MAX_ROUNDS - 1);
+                e = cudaGetLastError();
+            }
         }
         mark();
         /* the wave order: the (day, source) sort's buffers are free now */

@@ -69,11 +69,19 @@ public:
      * per-node offsets e1_ptr (Nn + 1 entries), and, if wave_out is not
      * null, each transfer's zero-based wave to wave_out[event index].  The
      * host reads the chunk's counts back; the call returns when the plan
-     * is written (its kernels ran on the scheduler's stream). */
+     * is written (its kernels ran on the scheduler's stream).
+     * pos_level (device, m entries, or null): the transfers' levels from
+     * the host planner, by position in the chunk (1-based; 0 where the
+     * event is no valid transfer); the rounds are then skipped.  A level
+     * the host left at 0 for a transfer the device finds valid, or a day
+     * deeper than the wave keys hold, sends the chunk to the rounds. */
     cudaError_t plan_chunk(long long lo, long long m, int d0, int nd, const long long *bounds,
                            int prev_time, int prev_event, bool has_prev, E2Rec *e2_out,
                            E1Rec *e1_out, int *e1_ptr, int *wave_out, SchedChunk &out,
-                           uint32_t *e1_node_out = nullptr);
+                           uint32_t *e1_node_out = nullptr, const uint32_t *pos_level = nullptr);
+
+    /* Deepest level the wave keys hold (pos_level above it: the rounds). */
+    static int max_host_level();
 
     /* The E1 records of several chunks (in chunk order, each chunk's by
      * node, with their nodes) as one per-node CSR: stable by node, so each

@@ -234,7 +234,7 @@ class Plan:
     def __init__(self, holder, model_name, cap_transfers=False, **options):
         """options: further siminf_gpu_options fields (heavy_rate,
         two_pass, gdata_per_replicate, max_node_day_transitions, streamed,
-        ssa_variant, wave_block)."""
+        ssa_variant, wave_block, heavy_lanes)."""
         self.holder = holder
         self.model = device_model(model_name)
         h = C.c_void_p()
@@ -251,7 +251,8 @@ class Plan:
 
     def tune(self, probe_days=16, stream=None):
         """Autotune the launch layout (heavy threshold, one- or two-pass
-        days, SSA register budget, wavefront block) on the first probe_days
+        days, SSA register budget, lanes a warp for the heaviest nodes,
+        wavefront block) on the first probe_days
         days (siminf_gpu_plan_tune; negative: a new search even if the size
         class has a cached choice); returns the TuneResult."""
         r = abi.TuneResult()

@@ -1,6 +1,7 @@
 """Streamed runs whose scheduled events are planned on the device
 (siminf_schedule.cu, chosen for large event tables; forced here with
-SIMINF_DEVICE_PLANNER=1): the trajectories, counts and error codes equal
+SIMINF_DEVICE_PLANNER=1, the device planning the levels too, and =2, the
+levels from host threads): the trajectories, counts and error codes equal
 those of the oracle and of host planning, for every parity case, with
 pinned outputs streamed back, with E and N growing chunk by chunk, and for
 a plan re-run after its device-planned first run."""
@@ -15,9 +16,9 @@ from test_oracle import error_cases
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture
-def device_planner(monkeypatch):
-    monkeypatch.setenv("SIMINF_DEVICE_PLANNER", "1")
+@pytest.fixture(params=["1", "2"], ids=["device_levels", "host_levels"])
+def device_planner(monkeypatch, request):
+    monkeypatch.setenv("SIMINF_DEVICE_PLANNER", request.param)
 
 
 CASES = [c for c in parity_cases() if len(c[1].events["event"])]
