@@ -83,6 +83,8 @@ def parse():
                     help="serve the request mix at its stated sizes (plain path: first 10 s)")
     ap.add_argument("--abc-smc", type=int, default=0,
                     help="generations of the ABC-SMC run over uneven models (0: off)")
+    ap.add_argument("--abc-smc-quantile", type=float, default=0.5,
+                    help="quantile of the accepted distances that sets the next tolerance")
     ap.add_argument("--serve-seconds", type=float, default=5.0,
                     help="length of the open-loop serving trace (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="arrivals per second")
@@ -421,7 +423,7 @@ def serve_bench(seconds, rate, seed=5, full=False, plain_seconds=None):
                     "submission to completion; plain = one request at a time"}
 
 
-def abc_smc_bench(generations, n_particles=2048, seed=3, batch=512):
+def abc_smc_bench(generations, n_particles=2048, seed=3, batch=512, quantile=0.5):
     """ABC-SMC over uneven models (config 4): particles' node counts from
     {100, 1e3, 1e4, 5e4} w.p. {.4, .3, .2, .1}, tspans U{60, 365}, events as
     the headline's scaled to size (a pool of 64 such structures, each
@@ -429,7 +431,7 @@ def abc_smc_bench(generations, n_particles=2048, seed=3, batch=512):
     U(0.05, 0.5), epsilon ~ U(0.1, 0.5), gamma ~ U(0.02, 0.2); distance: the
     L2 norm of daily prevalence I/N against one seeded target run (10,000
     nodes, 365 days, beta 0.16, epsilon 0.25, gamma 0.077, seed 7).  First
-    tolerance from 2 n_particles prior draws, then the median rule
+    tolerance from 2 n_particles prior draws, then the `quantile` rule (the median by default)
     (siminf_gb300/abc.py); proposals in batches of `batch` models (each
     model averages ~0.8M events, so a batch of 512 holds ~4e8)."""
     import copy
@@ -464,10 +466,11 @@ def abc_smc_bench(generations, n_particles=2048, seed=3, batch=512):
     run_batch(pm0, ps0, pt0, cap_transfers=True)             # warm-up
     t0 = time.perf_counter()
     gens = abc.abc_smc(simulate, priors, n_particles, generations, batch=batch,
-                       n_init=2 * n_particles, seed=seed, verbose=True)
+                       n_init=2 * n_particles, seed=seed, verbose=True, quantile=quantile)
     dt = time.perf_counter() - t0
     nd = sum(g.node_days for g in gens)
     return {"generations": generations, "particles": n_particles, "batch": batch, "seconds": dt,
+            "tolerance_quantile": quantile,
             "node_days": int(nd), "value": nd / dt, "unit": UNIT,
             "per_generation": [{"tolerance": g.tolerance, "proposals": g.nprop,
                                 "ess": g.ess, "seconds": g.seconds,
@@ -728,7 +731,7 @@ def run_ours(args):
     serve = (serve_bench(args.serve_seconds, args.serve_rate, full=args.serve_full,
                          plain_seconds=10.0 if args.serve_full else None)
              if args.serve_seconds > 0 and rank == 0 and world == 1 else None)
-    abc_smc = (abc_smc_bench(args.abc_smc)
+    abc_smc = (abc_smc_bench(args.abc_smc, quantile=args.abc_smc_quantile)
                if args.abc_smc > 0 and rank == 0 and world == 1 else None)
 
     e2e = None

@@ -224,8 +224,9 @@ typedef struct siminf_gpu_options {
     int two_pass;       /* > 0 on, < 0 off, 0 = on from 500,000 nodes (all replicates) */
     int max_node_day_transitions;   /* > 0: the bound; 0: 2^28 */
     int streamed;       /* siminf_gpu_plan_create_ex: plan the events during the first run,
-                         * beside the GPU (on the device for large tables), as the run entry
-                         * points do; 0: before the plan returns */
+                         * beside the GPU, as the run entry points do (on host threads;
+                         * SIMINF_DEVICE_PLANNER=1 or 2 selects the device planner); 0:
+                         * before the plan returns */
     int ssa_variant;    /* SSA kernel register budget: 0 the model's default, 1 more
                          * registers a thread and fewer resident warps (see the autotuner) */
     int wave_block;     /* threads per block of the wavefront kernel: 128, 256 or 512 (0: 256) */

@@ -20,10 +20,10 @@ Per generation:
 
 The tolerances are given (the reference's `tolerance` matrix, one
 statistic), or chosen as the reference's first epsilon from n_init prior
-draws (R/abc.R:429-432) and then, per later generation, the median of the
-previous generation's accepted distances.  The reference's adaptive rule
-(Simola et al. 2021, abc_adaptive_tolerance) is not restated: the median
-rule stands in for it here.  Random numbers come from numpy's Generator
+draws (R/abc.R:429-432) and then, per later generation, a quantile of the
+previous generation's accepted distances (the median by default).  The
+reference's adaptive rule (Simola et al. 2021, abc_adaptive_tolerance) is
+not restated: the quantile rule stands in for it here.  Random numbers come from numpy's Generator
 seeded by `seed`, not R's: runs are reproducible but not R's draws.
 """
 import sys
@@ -141,12 +141,14 @@ class Generation:
 
 
 def abc_smc(simulate, priors, n_particles, generations, batch=2048, tolerance=None,
-            n_init=None, seed=1, verbose=False):
+            n_init=None, seed=1, verbose=False, quantile=0.5):
     """ABC-SMC.  simulate(theta_batch, rng) -> (models, seeds, targets) for
     the proposals' parameter rows; their distances come from run_batch.
     tolerance: one value per generation, or None for the first epsilon
-    from n_init prior draws and the median rule after it.  Returns the list
-    of Generation."""
+    from n_init prior draws and after it the `quantile` of the previous
+    generation's accepted distances.  Returns the list of Generation."""
+    if not 0.0 < quantile <= 1.0:
+        raise ValueError("'quantile' must be in (0, 1].")
     rng = np.random.default_rng(seed)
     if tolerance is None and n_init is None:
         raise ValueError("Both 'n_init' and 'tolerance' can not be NULL.")
@@ -188,5 +190,6 @@ def abc_smc(simulate, priors, n_particles, generations, batch=2048, tolerance=No
                   flush=True)
         x, w = xx, w_new
         if g + 1 < generations:
-            eps = float(tolerance[g + 1]) if tolerance is not None else float(np.median(dd))
+            eps = (float(tolerance[g + 1]) if tolerance is not None
+                   else float(np.quantile(dd, quantile)))
     return out

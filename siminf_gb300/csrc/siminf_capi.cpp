@@ -381,6 +381,20 @@ static int device_planner_for(long long len)
     return 0;
 }
 
+/* Whether a streamed plan on host threads skips the scan of the whole
+ * table before its first day: from 2^22 events (SIMINF_SCAN_FREE=0/1
+ * overrides).  Each planner thread then checks its own day (order, E1
+ * events, planned failures, maxima), the launching thread buckets each
+ * chunk's E1 events and grows E and N as the days reveal them, and the
+ * run starts as soon as the first chunk is planned. */
+enum { SCAN_FREE_FROM = 1 << 22 };
+static bool scan_free_for(long long len)
+{
+    if (const char *ev = getenv("SIMINF_SCAN_FREE"))
+        return len > 0 && ev[0] == '1';
+    return len >= SCAN_FREE_FROM;
+}
+
 /* Threads used by the host planner (SIMINF_PLANNER_THREADS overrides the
  * hardware's count). */
 static int planner_threads()
@@ -564,6 +578,122 @@ static int plan_scan(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int ns
     return 0;
 }
 
+/* What a streamed run without the scan (p->scan_free) learns from one
+ * day's input range on its planner thread, as plan_scan learns it for the
+ * whole table: the first event out of order, the select and shift maxima,
+ * the valid E1 events, the planned failures; and the day's valid external
+ * transfers (their count, from the wave planner). */
+struct DayScan {
+    long long bad = -1;
+    int max_select = 0, max_shift = 0;
+    long long n2 = 0;
+    std::vector<long long> e1;
+    std::vector<PlannedErr> planned;
+};
+
+static void scan_day(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d, DayScan &r)
+{
+    const int Nn = a->Nn, nsel = p->nsel, E2 = SIMINF_GPU_EXTERNAL_TRANSFER_EVENT;
+    const long long lo = p->e2_lo[d], hi = p->e2_hi[d];
+    const int *time = a->time, *event = a->event, *node_ = a->node, *dest_ = a->dest,
+              *select = a->select, *shift = a->shift;
+    r.bad = -1;
+    r.e1.clear();
+    r.planned.clear();
+    int msel = 0, mshift = 0;
+    int pt = lo > 0 ? time[lo - 1] : INT_MIN, pk = lo > 0 ? event[lo - 1] : 0;
+    for (long long i = lo; i < hi; i++) {
+        const int tm = time[i], kind = event[i];
+        if ((tm < pt || (tm == pt && pk == E2 && kind != E2)) && r.bad < 0)
+            r.bad = i;
+        pt = tm;
+        pk = kind;
+        msel = std::max(msel, select[i]);
+        mshift = std::max(mshift, shift[i]);
+        const unsigned node = (unsigned) (node_[i] - 1), dest = (unsigned) (dest_[i] - 1),
+                       sel = (unsigned) (select[i] - 1);
+        const bool ok = node < (unsigned) Nn && (unsigned) kind <= 3u && sel < (unsigned) nsel;
+        if (ok && kind == E2 && dest < (unsigned) Nn)
+            continue;
+        const int phase = kind == E2 ? PHASE_E2 : PHASE_E1;
+        if (node >= (unsigned) Nn)
+            r.planned.push_back({d, SIMINF_GPU_ERR_NODE_OUT_OF_BOUNDS, (int) i, (int) node, phase});
+        else if ((unsigned) kind > 3u)
+            r.planned.push_back({d, SIMINF_GPU_UNDEFINED_EVENT, (int) i, (int) node, phase});
+        else if (sel >= (unsigned) nsel)
+            r.planned.push_back({d, SIMINF_GPU_ERR_SAMPLE_SELECT, (int) i, (int) node, phase});
+        else if (kind == E2)
+            r.planned.push_back({d, SIMINF_GPU_ERR_DEST_OUT_OF_BOUNDS, (int) i, (int) node, phase});
+        else
+            r.e1.push_back(i);
+    }
+    r.max_select = msel;
+    r.max_shift = mshift;
+}
+
+/* The E1 records of the events at positions pos (lists in day order,
+ * each in position order), bucketed by node: stable, so a node keeps day
+ * and array order (plan_scan's E1 part).  ptr gets Nn + 1 offsets. */
+static void bucket_e1(const siminf_gpu_solver_args *a,
+                      const std::vector<const std::vector<long long> *> &pos, E1Rec *rec, int *ptr)
+{
+    const int Nn = a->Nn;
+    const double tt0 = a->tspan[0];
+    std::memset(ptr, 0, ((size_t) Nn + 1) * sizeof(int));
+    for (const auto *v : pos)
+        for (long long i : *v)
+            ptr[a->node[i]]++;                  /* node i - 1, counted at i */
+    for (int k = 0; k < Nn; k++)
+        ptr[k + 1] += ptr[k];
+    for (const auto *v : pos)
+        for (long long i : *v) {
+            const int node = a->node[i] - 1;
+            rec[ptr[node]++] = E1Rec{(int) event_day(a->time[i], tt0), a->event[i], a->n[i],
+                                     a->select[i] - 1, a->shift[i] - 1, (int) i, a->proportion[i]};
+        }
+    /* ptr[k] now ends node k's records: shift back to starts */
+    for (int k = Nn; k > 0; k--)
+        ptr[k] = ptr[k - 1];
+    ptr[0] = 0;
+}
+
+/* Orders one day's E1 positions by node, then position (scan_day leaves
+ * them in position order). */
+static void sort_e1_by_node(const siminf_gpu_solver_args *a, std::vector<long long> &e1)
+{
+    const int *node = a->node;
+    std::sort(e1.begin(), e1.end(), [node](long long x, long long y) {
+        return node[x] != node[y] ? node[x] < node[y] : x < y;
+    });
+}
+
+/* The E1 records of several days (each day's positions sorted by node,
+ * then position; days in order) merged by node, then position -- stable by
+ * node, so a node keeps day and array order (plan_scan's E1 part) -- into
+ * rec, with each record's zero-based node in keys. */
+static void merge_e1_days(const siminf_gpu_solver_args *a,
+                          const std::vector<const std::vector<long long> *> &days, E1Rec *rec,
+                          uint32_t *keys, std::vector<long long> &tmp, std::vector<long long> &out)
+{
+    const int *node = a->node;
+    auto less = [node](long long x, long long y) {
+        return node[x] != node[y] ? node[x] < node[y] : x < y;
+    };
+    out.clear();
+    for (const auto *v : days) {
+        tmp.swap(out);
+        out.resize(tmp.size() + v->size());
+        std::merge(tmp.begin(), tmp.end(), v->begin(), v->end(), out.begin(), less);
+    }
+    const double tt0 = a->tspan[0];
+    for (size_t k = 0; k < out.size(); k++) {
+        const long long i = out[k];
+        rec[k] = E1Rec{(int) event_day(a->time[i], tt0), a->event[i], a->n[i], a->select[i] - 1,
+                       a->shift[i] - 1, (int) i, a->proportion[i]};
+        keys[k] = (uint32_t) (node[i] - 1);
+    }
+}
+
 /* Per-thread scratch of the wave planner: per node, its two levels on
  * the day being planned (the last event with the node as source, `excl`,
  * and the last add into it, `add`), packed into one word so that an event
@@ -646,10 +776,10 @@ static bool day_levels(const siminf_gpu_plan *p, const siminf_gpu_solver_args *a
 /* Wave levels of day d: level = 1 + max(level of the last event with the
  * same source, of any add into the source, of the last event whose source
  * is our destination).  Then a stable counting sort of the day's events by
- * level into e2 (positions e2_day_off[d] - base ..), and the wave sizes
- * into p->day_waves[d]. */
-static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
-                           WaveTracker &w, E2Rec *e2, long long base = 0)
+ * level into e2 (positions at ..), and the wave sizes into
+ * p->day_waves[d].  Returns the day's transfer count. */
+static long long plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
+                                WaveTracker &w, E2Rec *e2, long long at)
 {
     int maxl = 0;
     if (!day_levels<uint16_t>(p, a, d, w, w.lv.data(), maxl)) {
@@ -664,7 +794,7 @@ static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, 
     cnt.assign(maxl + 2, 0);
     for (int L : level)
         cnt[L]++;
-    off.assign(maxl + 2, p->e2_day_off[d] - base);
+    off.assign(maxl + 2, at);
     for (int L = 1; L <= maxl; L++)
         off[L + 1] = off[L] + cnt[L];
     for (size_t k = 0; k < level.size(); k++) {
@@ -673,14 +803,15 @@ static void plan_day_waves(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, 
                                     a->shift[i] - 1, (int) i, a->proportion[i]};
     }
     p->day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
+    return (long long) level.size();
 }
 
 /* plan_day_waves for a streamed run: the day's transfers in wave order as
  * their positions relative to the input position rel (order[k], from
- * p->e2_day_off[d] - base), for the device to gather the records from the
- * event columns it receives by DMA (k_gather_e2). */
-static void plan_day_order(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
-                           WaveTracker &w, uint32_t *order, long long base, long long rel)
+ * k = at), for the device to gather the records from the event columns it
+ * receives by DMA (k_gather_e2).  Returns the day's transfer count. */
+static long long plan_day_order(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int d,
+                                WaveTracker &w, uint32_t *order, long long at, long long rel)
 {
     int maxl = 0;
     if (!day_levels<uint16_t>(p, a, d, w, w.lv.data(), maxl)) {
@@ -693,13 +824,14 @@ static void plan_day_order(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, 
     cnt.assign(maxl + 2, 0);
     for (int L : level)
         cnt[L]++;
-    off.assign(maxl + 2, p->e2_day_off[d] - base);
+    off.assign(maxl + 2, at);
     for (int L = 1; L <= maxl; L++)
         off[L + 1] = off[L] + cnt[L];
     const uint32_t shift = (uint32_t) (p->e2_lo[d] - rel);
     for (size_t k = 0; k < level.size(); k++)
         order[off[level[k]]++] = idx[k] + shift;
     p->day_waves[d].assign(cnt.begin() + 1, cnt.begin() + 1 + maxl);
+    return (long long) level.size();
 }
 
 /* The levels of day d's transfers for the device planner (mode 2): pos[k]
@@ -779,7 +911,7 @@ static int plan_events(siminf_gpu_plan *p, const siminf_gpu_solver_args *a, int 
     parallel([&](int, int) {
         WaveTracker w(a->Nn);
         for (int d = next_day++; d < p->ndays; d = next_day++)
-            plan_day_waves(p, a, d, w, dst);
+            plan_day_waves(p, a, d, w, dst, p->e2_day_off[d]);
     });
     plan_wave_index(p);
     return 0;
@@ -1002,12 +1134,14 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
     std::vector<int> e1_ptr;
     std::unique_ptr<E2Rec[]> e2;
     const int dev_mode = stream ? device_planner_for(a->len) : 0;
-    if (dev_mode && event_day_ranges(a, p->days, p->e2_lo, p->e2_hi)) {
+    const bool scan_free = stream && !dev_mode && scan_free_for(a->len);
+    if ((dev_mode || scan_free) && event_day_ranges(a, p->days, p->e2_lo, p->e2_hi)) {
         /* the device plans the events during the first run: only the day
          * ranges now (E and N grow to the largest select and shift the
          * planner finds; E1 lists and waves come chunk by chunk) */
-        p->dev_plan = true;
+        p->dev_plan = dev_mode != 0;
         p->dev_levels = dev_mode == 2;
+        p->scan_free = scan_free;
         p->nsel = nsel;
         p->max_select = p->max_shift = 0;
         p->e2_count = (uint64_t) a->len;        /* room for every event */
@@ -1031,7 +1165,8 @@ static int plan_create_impl(const siminf_gpu_solver_args *a, const siminf_gpu_mo
         }
     }
     p->stats.ms_plan = ms_since(t0);
-    p->horizon = !p->dev_plan && (p->e2_count == 0) && L->pts_local && a->solver == 0;
+    p->horizon = !p->dev_plan && !p->scan_free && (p->e2_count == 0) && L->pts_local &&
+                 a->solver == 0;
 
     cudaStream_t st = g_plan_stream;
     p->stream = st;
@@ -1464,12 +1599,20 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
         return e;
 
     const int nchunks = (ndays + CHUNK_DAYS - 1) / CHUNK_DAYS;
+    /* without the scan (p->scan_free) a day's transfers go to its chunk's
+     * slot at the day's input offset in the chunk, and the day offsets in
+     * d_e2 come from the planners' counts chunk by chunk */
+    const bool sf = p->scan_free;
     long long slot_len = 1, in_len = 1;
     for (int c = 0; c < nchunks; c++) {
         const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
-        slot_len = std::max(slot_len, p->e2_day_off[d1] - p->e2_day_off[d0]);
+        if (!sf)
+            slot_len = std::max(slot_len, p->e2_day_off[d1] - p->e2_day_off[d0]);
         in_len = std::max(in_len, p->e2_hi[d1 - 1] - p->e2_lo[d0]);
     }
+    if (sf)
+        slot_len = in_len;
+    std::vector<DayScan> scans(sf ? ndays : 0);
     /* With the transfer columns in pinned host memory, the planners write
      * each day's order (4 B a transfer) and the device gathers the records
      * from the columns it receives by DMA (28 B an event); otherwise they
@@ -1499,6 +1642,25 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
         if (e == cudaSuccess) dbufs.push_back(stg[k].proportion);
         if (e == cudaSuccess) e = cudaMalloc((void **) &dorder[k], (size_t) slot_len * sizeof(uint32_t));
         if (e == cudaSuccess) dbufs.push_back(dorder[k]);
+    }
+    /* without the scan: each chunk's E1 lists by node go up through one of
+     * E1_RING pinned slots into one of E1_RING device buffers, which the
+     * chunk's kernels read (a buffer is rewritten once the kernels of the
+     * chunk E1_RING earlier are done) */
+    enum { E1_RING = 4 };
+    const int Nn = a->Nn;
+    int *d_e1p[E1_RING] = {};
+    E1Rec *d_e1r[E1_RING] = {};
+    uint32_t *d_e1k[E1_RING] = {};
+    long long d_e1r_cap[E1_RING] = {};
+    std::vector<long long> e1_tmp, e1_merged;
+    char *h_e1[E1_RING] = {};
+    size_t h_e1_bytes[E1_RING] = {};
+    std::vector<cudaEvent_t> e1_used(sf ? nchunks : 0, nullptr);
+    for (int r = 0; r < E1_RING && sf && e == cudaSuccess; r++) {
+        e = cudaMalloc((void **) &d_e1p[r], ((size_t) Nn + 1) * sizeof(int));
+        if (e == cudaSuccess)
+            dbufs.push_back(d_e1p[r]);
     }
     if (e != cudaSuccess) {
         for (void *q : dbufs)
@@ -1536,11 +1698,18 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
                         cudaEventSynchronize(copied[c - RING]);
                     }
                     char *slot = ring + (size_t) (c % RING) * slot_len * elem;
-                    if (gather)
-                        plan_day_order(p, a, d, w, (uint32_t *) slot,
-                                       p->e2_day_off[c * CHUNK_DAYS], p->e2_lo[c * CHUNK_DAYS]);
-                    else
-                        plan_day_waves(p, a, d, w, (E2Rec *) slot, p->e2_day_off[c * CHUNK_DAYS]);
+                    const int d0 = c * CHUNK_DAYS;
+                    if (sf) {
+                        scan_day(p, a, d, scans[d]);
+                        sort_e1_by_node(a, scans[d].e1);
+                    }
+                    const long long at = sf ? p->e2_lo[d] - p->e2_lo[d0]
+                                            : p->e2_day_off[d] - p->e2_day_off[d0];
+                    const long long n2 =
+                        gather ? plan_day_order(p, a, d, w, (uint32_t *) slot, at, p->e2_lo[d0])
+                               : plan_day_waves(p, a, d, w, (E2Rec *) slot, at);
+                    if (sf)
+                        scans[d].n2 = n2;
                     done[d].store(1, std::memory_order_release);
                 }
             } catch (...) {
@@ -1555,6 +1724,8 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
         e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking);
     static const bool prof = getenv("SIMINF_SCHED_PROFILE") && getenv("SIMINF_SCHED_PROFILE")[0] == '1';
     double waited = 0;
+    long long e1_total = 0;
+    int issued_chunks = 0;
     for (int c = 0; c < nchunks && e == cudaSuccess; c++) {
         const int d0 = c * CHUNK_DAYS, d1 = std::min(ndays, d0 + (int) CHUNK_DAYS);
         auto w0 = std::chrono::steady_clock::now();
@@ -1566,6 +1737,103 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             e = cudaErrorMemoryAllocation;
             break;
         }
+        if (sf) {
+            /* what plan_scan would have found in these days */
+            long long bad = -1;
+            for (int d = d0; d < d1 && bad < 0; d++)
+                bad = scans[d].bad;
+            if (bad >= 0) {
+                p->dev_bad = bad;       /* out of order: the run stops here */
+                break;
+            }
+            int msel = p->max_select, mshift = p->max_shift;
+            long long n1 = 0;
+            std::vector<const std::vector<long long> *> pos;
+            for (int d = d0; d < d1; d++) {
+                p->e2_day_off[d + 1] = p->e2_day_off[d] + scans[d].n2;
+                p->planned.insert(p->planned.end(), scans[d].planned.begin(),
+                                  scans[d].planned.end());
+                msel = std::max(msel, scans[d].max_select);
+                mshift = std::max(mshift, scans[d].max_shift);
+                n1 += (long long) scans[d].e1.size();
+                pos.push_back(&scans[d].e1);
+            }
+            /* E and N up to the largest select and shift seen so far */
+            if (msel > p->max_select && a->jcE) {
+                int *djcE, *dirE;
+                double *dprE;
+                const int nnz = a->jcE[msel];
+                int rc = upload(&djcE, a->jcE, (size_t) msel + 1, p->owned, st);
+                if (!rc) rc = upload(&dirE, a->irE, (size_t) nnz, p->owned, st);
+                if (!rc) rc = upload(&dprE, (const double *) a->prE, (size_t) nnz, p->owned, st);
+                if (rc) {
+                    e = cudaErrorMemoryAllocation;
+                    break;
+                }
+                s.jcE = p->s.jcE = djcE;
+                s.irE = p->s.irE = dirE;
+                s.prE = p->s.prE = dprE;
+                p->max_select = msel;
+            }
+            if (mshift > p->max_shift && a->N) {
+                int *dN;
+                if (upload(&dN, a->N, (size_t) mshift * a->Nc, p->owned, st)) {
+                    e = cudaErrorMemoryAllocation;
+                    break;
+                }
+                s.Nshift = p->s.Nshift = dN;
+                p->max_shift = mshift;
+            }
+            /* the chunk's E1 lists by node: records and their nodes go up,
+             * the per-node offsets are found on the device */
+            const int r = c % E1_RING;
+            if (c >= E1_RING) {
+                e = cudaEventSynchronize(copied[c - E1_RING]);     /* the slot's last copy */
+                if (e == cudaSuccess)
+                    e = cudaStreamWaitEvent(cs, e1_used[c - E1_RING], 0);
+            }
+            const size_t need = (size_t) std::max(1LL, n1) * (sizeof(E1Rec) + sizeof(uint32_t));
+            if (e == cudaSuccess && need > h_e1_bytes[r]) {
+                pinned_release(h_e1[r], h_e1_bytes[r]);
+                h_e1[r] = nullptr;
+                h_e1_bytes[r] = 0;
+                e = pinned_acquire(need, (void **) &h_e1[r], &h_e1_bytes[r]);
+            }
+            if (e == cudaSuccess && std::max(1LL, n1) > d_e1r_cap[r]) {
+                const long long cap1 = std::max(1LL, n1);
+                E1Rec *nb = nullptr;
+                uint32_t *nk = nullptr;
+                e = cudaMalloc((void **) &nb, (size_t) cap1 * sizeof(E1Rec));
+                if (e == cudaSuccess)
+                    dbufs.push_back(nb);        /* the old ones are freed at the end */
+                if (e == cudaSuccess)
+                    e = cudaMalloc((void **) &nk, (size_t) cap1 * sizeof(uint32_t));
+                if (e == cudaSuccess) {
+                    dbufs.push_back(nk);
+                    d_e1r[r] = nb;
+                    d_e1k[r] = nk;
+                    d_e1r_cap[r] = cap1;
+                }
+            }
+            if (e != cudaSuccess)
+                break;
+            E1Rec *hr = (E1Rec *) h_e1[r];
+            uint32_t *hk = (uint32_t *) (h_e1[r] + (size_t) std::max(1LL, n1) * sizeof(E1Rec));
+            merge_e1_days(a, pos, hr, hk, e1_tmp, e1_merged);
+            if (n1 > 0)
+                e = cudaMemcpyAsync(d_e1r[r], hr, (size_t) n1 * sizeof(E1Rec),
+                                    cudaMemcpyHostToDevice, cs);
+            if (e == cudaSuccess && n1 > 0)
+                e = cudaMemcpyAsync(d_e1k[r], hk, (size_t) n1 * sizeof(uint32_t),
+                                    cudaMemcpyHostToDevice, cs);
+            if (e == cudaSuccess)
+                e = e1_ptr_from_keys(d_e1k[r], n1, Nn, d_e1p[r], cs);
+            if (e != cudaSuccess)
+                break;
+            s.e1 = d_e1r[r];
+            s.e1_ptr = d_e1p[r];
+            e1_total += n1;
+        }
         const long long lo = p->e2_day_off[d0], hi = p->e2_day_off[d1];
         /* the chunk's event columns and the planned order go up, and the
          * records are gathered on the device (the copy stream runs chunks
@@ -1573,7 +1841,16 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
         const long long in_lo = p->e2_lo[d0], in_n = p->e2_hi[d1 - 1] - in_lo;
         StagedCols &sc = stg[c % 2];
         e = cudaEventCreateWithFlags(&copied[c], cudaEventDisableTiming | cudaEventBlockingSync);
-        if (e == cudaSuccess && hi > lo && !gather) {
+        if (e == cudaSuccess && hi > lo && !gather && sf) {
+            /* each day's records from its place in the slot */
+            for (int d = d0; d < d1 && e == cudaSuccess; d++)
+                if (scans[d].n2 > 0)
+                    e = cudaMemcpyAsync(p->d_e2 + p->e2_day_off[d],
+                                        ring + ((size_t) (c % RING) * slot_len +
+                                                (size_t) (p->e2_lo[d] - in_lo)) * elem,
+                                        (size_t) scans[d].n2 * sizeof(E2Rec),
+                                        cudaMemcpyHostToDevice, cs);
+        } else if (e == cudaSuccess && hi > lo && !gather) {
             e = cudaMemcpyAsync(p->d_e2 + lo, ring + (size_t) (c % RING) * slot_len * elem,
                                 (size_t) (hi - lo) * sizeof(E2Rec), cudaMemcpyHostToDevice, cs);
         } else if (e == cudaSuccess && hi > lo) {
@@ -1585,13 +1862,24 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(sc.proportion, a->proportion + in_lo,
                                     (size_t) in_n * sizeof(double), cudaMemcpyHostToDevice, cs);
+            /* the order: one run of hi - lo entries, or with the days at
+             * their input offsets (gaps where other events sit) */
+            const long long ord_n = sf ? in_n : hi - lo;
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(dorder[c % 2], ring + (size_t) (c % RING) * slot_len * elem,
-                                    (size_t) (hi - lo) * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                                    cs);
-            if (e == cudaSuccess) {
+                                    (size_t) ord_n * sizeof(uint32_t), cudaMemcpyHostToDevice, cs);
+            if (e == cudaSuccess && !sf) {
                 k_gather_e2<<<(unsigned) ((hi - lo + 255) / 256), 256, 0, cs>>>(
                     sc, dorder[c % 2], hi - lo, in_lo, p->d_e2 + lo);
+                e = cudaGetLastError();
+            }
+            for (int d = d0; sf && d < d1 && e == cudaSuccess; d++) {
+                const long long n2 = scans[d].n2;
+                if (n2 <= 0)
+                    continue;
+                k_gather_e2<<<(unsigned) ((n2 + 255) / 256), 256, 0, cs>>>(
+                    sc, dorder[c % 2] + (p->e2_lo[d] - in_lo), n2, in_lo,
+                    p->d_e2 + p->e2_day_off[d]);
                 e = cudaGetLastError();
             }
         }
@@ -1624,6 +1912,14 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
                           : L->pts_store(s, d, di.tt, di.c0, di.c1, s.vA, s.vB, st);
             std::swap(s.vA, s.vB);
         }
+        if (sf && e == cudaSuccess) {
+            /* the chunk's E1 buffers are free once its days have run */
+            e = cudaEventCreateWithFlags(&e1_used[c], cudaEventDisableTiming);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(e1_used[c], st);
+        }
+        if (e == cudaSuccess)
+            issued_chunks = c + 1;
         /* the columns this chunk finished go back while later days run */
         const int c_hi = p->days[d1 - 1].c1;
         if (ds && e == cudaSuccess && c_hi > p->cols_sent) {
@@ -1645,6 +1941,38 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
     abort.store(1);
     for (auto &t : workers)
         t.join();
+    if (sf && e == cudaSuccess && p->dev_bad < 0 && issued_chunks == nchunks) {
+        /* events past the last day: the order check */
+        const long long len = a->len, tail_lo = p->e2_hi[ndays - 1];
+        for (long long i = std::max(1LL, tail_lo); i < len; i++) {
+            const int tm = a->time[i], pt = a->time[i - 1];
+            const int kind = a->event[i], pk = a->event[i - 1];
+            if (tm < pt || (tm == pt && pk == SIMINF_GPU_EXTERNAL_TRANSFER_EVENT &&
+                            kind != SIMINF_GPU_EXTERNAL_TRANSFER_EVENT)) {
+                p->dev_bad = i;
+                break;
+            }
+        }
+        /* the E1 lists of the whole run by node, for later runs */
+        std::vector<const std::vector<long long> *> pos;
+        for (int d = 0; d < ndays; d++)
+            pos.push_back(&scans[d].e1);
+        std::vector<int> ptr((size_t) Nn + 1);
+        std::vector<E1Rec> rec((size_t) std::max(1LL, e1_total));
+        bucket_e1(a, pos, rec.data(), ptr.data());
+        int *dptr = nullptr;
+        E1Rec *drec = nullptr;
+        if (upload(&dptr, ptr.data(), ptr.size(), p->owned, cs) ||
+            upload(&drec, rec.data(), rec.size(), p->owned, cs)) {
+            e = cudaErrorMemoryAllocation;
+        } else {
+            e = cudaStreamSynchronize(cs);
+            p->s.e1 = drec;
+            p->s.e1_ptr = dptr;
+            p->e1_count = (uint64_t) e1_total;
+            p->e2_count = (uint64_t) p->e2_day_off[ndays];
+        }
+    }
     if (prof)
         fprintf(stderr, "streamed run (host waves): %.2f ms waiting for plans\n", waited);
     if (cs) {
@@ -1664,8 +1992,15 @@ static cudaError_t launch_streamed(siminf_gpu_plan *p, DevState s, cudaStream_t 
             cudaEventDestroy(ev);
     for (cudaEvent_t ev : stored)
         cudaEventDestroy(ev);
+    for (cudaEvent_t ev : e1_used)
+        if (ev)
+            cudaEventDestroy(ev);
+    if (!dbufs.empty())
+        cudaStreamSynchronize(st);      /* the chunk buffers' last readers */
     for (void *q : dbufs)
         cudaFree(q);
+    for (int r = 0; r < E1_RING; r++)
+        pinned_release(h_e1[r], h_e1_bytes[r]);
     pinned_release(ring, ring_bytes);
     return e;
 }
@@ -2206,6 +2541,7 @@ static int plan_run_impl(siminf_gpu_plan *p, cudaStream_t st, KernelProfile *kp)
         /* the graph holds the whole run */
     } else if (p->e2_pending) {
         e = p->dev_plan ? launch_streamed_dev(p, s, st) : launch_streamed(p, s, st);
+        p->scan_free = false;
         p->e2_pending = false;
         p->h_e2.reset();
         plan_wave_index(p);

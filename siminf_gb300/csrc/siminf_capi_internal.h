@@ -86,6 +86,11 @@ struct siminf_gpu_plan {
      * levels too. */
     bool dev_plan = false;
     bool dev_levels = false;
+    /* Streamed runs planned on host threads without a scan of the whole
+     * table first (siminf_capi.cpp, scan_free_for): e2_lo / e2_hi are the
+     * days' input ranges; the first run fills e2_day_off, the E1 lists,
+     * the planned failures and dev_bad. */
+    bool scan_free = false;
     long long dev_bad = -1;
     siminf_gpu_solver_args args{};
     std::unique_ptr<E2Rec[]> h_e2;

@@ -820,6 +820,13 @@ cudaError_t DevScheduler::plan_chunk(long long lo, long long m, int d0, int nd,
     return cudaSuccess;
 }
 
+cudaError_t e1_ptr_from_keys(const uint32_t *keys, long long n, int Nn, int *ptr,
+                             cudaStream_t st)
+{
+    k_e1_ptr<<<blocks_of((long long) Nn + 1, SCHED_BLOCK), SCHED_BLOCK, 0, st>>>(n, keys, Nn, ptr);
+    return cudaGetLastError();
+}
+
 cudaError_t DevScheduler::merge_e1(const E1Rec *in, const uint32_t *nodes, long long n,
                                    E1Rec *out, int *ptr)
 {

@@ -126,6 +126,11 @@ private:
     cudaError_t alloc(T **p, size_t n);
 };
 
+/* Per-node offsets ptr[0 .. Nn] of n E1 records whose nodes, keys[0 ..
+ * n), are sorted (on stream st). */
+cudaError_t e1_ptr_from_keys(const uint32_t *keys, long long n, int Nn, int *ptr,
+                             cudaStream_t st);
+
 /* Input range [lo[d], hi[d]) of each day's events (binary search on time).
  * Returns false when the ranges do not tile the table in order, which
  * only an unsorted table can make happen. */

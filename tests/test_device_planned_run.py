@@ -1,10 +1,11 @@
-"""Streamed runs whose scheduled events are planned on the device
-(siminf_schedule.cu, chosen for large event tables; forced here with
-SIMINF_DEVICE_PLANNER=1, the device planning the levels too, and =2, the
-levels from host threads): the trajectories, counts and error codes equal
+"""Streamed runs whose scheduled events are planned while the run goes:
+on the device (siminf_schedule.cu; SIMINF_DEVICE_PLANNER=1, the device
+planning the levels too, and =2, the levels from host threads), and on host
+threads without a scan of the whole table first (SIMINF_SCAN_FREE=1, the
+default for large tables): the trajectories, counts and error codes equal
 those of the oracle and of host planning, for every parity case, with
 pinned outputs streamed back, with E and N growing chunk by chunk, and for
-a plan re-run after its device-planned first run."""
+a plan re-run after its first run."""
 import ctypes as C
 
 import numpy as np
@@ -16,9 +17,14 @@ from test_oracle import error_cases
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=["1", "2"], ids=["device_levels", "host_levels"])
+@pytest.fixture(params=["1", "2", "scan_free"], ids=["device_levels", "host_levels", "scan_free"])
 def device_planner(monkeypatch, request):
-    monkeypatch.setenv("SIMINF_DEVICE_PLANNER", request.param)
+    if request.param == "scan_free":
+        monkeypatch.setenv("SIMINF_DEVICE_PLANNER", "0")
+        monkeypatch.setenv("SIMINF_SCAN_FREE", "1")
+    else:
+        monkeypatch.setenv("SIMINF_DEVICE_PLANNER", request.param)
+        monkeypatch.setenv("SIMINF_SCAN_FREE", "0")
 
 
 CASES = [c for c in parity_cases() if len(c[1].events["event"])]
@@ -106,3 +112,21 @@ def test_device_planned_plan_reruns(gpu, oracle_lib, device_planner):
             assert np.array_equal(h.U, ho.U)
     finally:
         lib.siminf_gpu_plan_free(plan)
+
+
+@pytest.mark.parametrize("name", ["seir_events_300x120", "sise3_events"])
+def test_device_planned_pinned_inputs(gpu, oracle_lib, device_planner, name):
+    """Inputs and outputs in pinned host memory: the transfer records are
+    gathered on the device from the columns copied by DMA."""
+    from helpers import pin_inputs_outputs
+    from siminf_gb300 import abi, native
+    torch = pytest.importorskip("torch")
+    m = dict(parity_cases())[name]
+    _, _, ho = run_oracle(m, threads=4)
+    h = abi.build_args(m, 42)
+    pin_inputs_outputs(h, m, torch)
+    h.U[:] = -1
+    code = native.lib().siminf_gpu_run_solver_ex(C.cast(h.ref(), C.c_void_p),
+                                                 native.device_model(m.name).handle, None)
+    assert code == 0
+    assert np.array_equal(h.U, ho.U), name
