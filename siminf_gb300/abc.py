@@ -1,5 +1,6 @@
 """ABC-SMC over the device batch: the generation loop of the reference's
-abc (R/abc.R:742-843, abc_internal) with its proposal and weight kernels
+abc (R/abc.R:742-843, abc_internal) and continue_abc (R/abc.R:996-1027),
+with its proposal and weight kernels
 (src/misc/SimInf_abc.c, SimInf_abc_proposals and SimInf_abc_weights)
 restated in numpy, and every generation's simulations run as batches of
 uneven models on the GPU with their prevalence distances reduced there
@@ -140,22 +141,59 @@ class Generation:
         self.ess = 1.0 / float(np.sum(w * w))
 
 
+class ABCResult(list):
+    """The generations of an ABC-SMC run (a list of Generation), with what
+    continue_abc needs to add generations as if the run had not stopped:
+    the random generator's state and the next generation's tolerance."""
+
+    def __init__(self, gens, priors, n_particles, batch, quantile, rng, next_eps):
+        super().__init__(gens)
+        self.priors, self.n_particles, self.batch = priors, n_particles, batch
+        self.quantile, self.rng, self.next_eps = quantile, rng, next_eps
+
+
 def abc_smc(simulate, priors, n_particles, generations, batch=2048, tolerance=None,
             n_init=None, seed=1, verbose=False, quantile=0.5):
     """ABC-SMC.  simulate(theta_batch, rng) -> (models, seeds, targets) for
     the proposals' parameter rows; their distances come from run_batch.
     tolerance: one value per generation, or None for the first epsilon
     from n_init prior draws and after it the `quantile` of the previous
-    generation's accepted distances.  Returns the list of Generation."""
+    generation's accepted distances.  Returns an ABCResult (the list of
+    Generation)."""
     if not 0.0 < quantile <= 1.0:
         raise ValueError("'quantile' must be in (0, 1].")
-    rng = np.random.default_rng(seed)
     if tolerance is None and n_init is None:
         raise ValueError("Both 'n_init' and 'tolerance' can not be NULL.")
-    out = []
-    x = w = None
     eps = None if tolerance is None else float(tolerance[0])
-    for g in range(generations):
+    return _generations(simulate, priors, n_particles, generations, batch, tolerance, n_init,
+                        np.random.default_rng(seed), verbose, quantile, [], None, None, eps)
+
+
+def continue_abc(result, simulate, generations, tolerance=None, verbose=False):
+    """More generations of an ABC-SMC run (R/abc.R:996-1027, continue_abc):
+    from its last generation's particles and weights, with the next
+    tolerances given (one per generation) or by the run's quantile rule, and
+    the run's random generator where it stopped -- so that a run continued
+    for k generations equals the same run made k generations longer.
+    Returns a new ABCResult holding every generation."""
+    if not len(result):
+        raise ValueError("The ABC run has no generation to continue from.")
+    last = result[-1]
+    eps = float(tolerance[0]) if tolerance is not None else result.next_eps
+    rng = np.random.default_rng()
+    rng.bit_generator.state = result.rng.bit_generator.state
+    return _generations(simulate, result.priors, result.n_particles, generations, result.batch,
+                        tolerance, None, rng, verbose, result.quantile, list(result),
+                        last.x, last.w, eps)
+
+
+def _generations(simulate, priors, n_particles, generations, batch, tolerance, n_init, rng,
+                 verbose, quantile, out, x, w, eps):
+    """The generation loop shared by abc_smc and continue_abc."""
+    if tolerance is not None and len(tolerance) < generations:
+        raise ValueError("'tolerance' needs one value per generation.")
+    g0 = len(out)
+    for g in range(g0, g0 + generations):
         t0 = time.perf_counter()
         sigma = None if x is None else 2.0 * np.atleast_2d(np.cov(x, rowvar=False))
         want = n_particles if (g > 0 or eps is not None) else int(n_init)
@@ -189,7 +227,9 @@ def abc_smc(simulate, priors, n_particles, generations, batch=2048, tolerance=No
                   % (g + 1, eps, nprop, out[-1].ess, out[-1].seconds), file=sys.stderr,
                   flush=True)
         x, w = xx, w_new
-        if g + 1 < generations:
-            eps = (float(tolerance[g + 1]) if tolerance is not None
-                   else float(np.quantile(dd, quantile)))
-    return out
+        k = g - g0 + 1                  # generations of this call done
+        if tolerance is not None:
+            eps = float(tolerance[k]) if k < len(tolerance) else None
+        else:
+            eps = float(np.quantile(dd, quantile))
+    return ABCResult(out, priors, n_particles, batch, quantile, rng, eps)

@@ -2120,7 +2120,15 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
     std::unique_ptr<std::atomic<int>[]> lday(new std::atomic<int>[hl ? ndays : 1]);
     std::unique_ptr<std::atomic<int>[]> lfree(new std::atomic<int>[hl ? nchunks : 1]);
     std::unique_ptr<std::atomic<int>[]> ldeep(new std::atomic<int>[hl ? nchunks : 1]);
-    std::atomic<int> lnext(0), lfail(0);
+    /* the first dev_first chunks the device plans whole (levels too):
+     * early in a run the day kernels leave the GPU idle more than the host
+     * threads can plan for it, and those threads start further ahead */
+    int dev_first = 0;
+    if (const char *ev = getenv("SIMINF_DEVICE_FIRST_CHUNKS"))
+        dev_first = std::max(0, std::min(nchunks, atoi(ev)));
+    if (!hl)
+        dev_first = 0;
+    std::atomic<int> lnext(std::min(ndays, dev_first * (int) CHUNK_DAYS)), lfail(0);
     std::vector<std::thread> lworkers;
     if (hl) {
         for (int d = 0; d < ndays; d++)
@@ -2208,7 +2216,7 @@ static cudaError_t launch_streamed_dev(siminf_gpu_plan *p, DevState s, cudaStrea
                                      cudaMemcpyHostToDevice, ps);
             /* the host's levels of the chunk, once its days are planned */
             const uint32_t *pos_level = nullptr;
-            if (hl && pe == cudaSuccess) {
+            if (hl && pe == cudaSuccess && c >= dev_first) {
                 for (int d = d0; d < d1 && !abort.load() && !lfail.load(); d++)
                     while (!lday[d].load(std::memory_order_acquire) && !abort.load() &&
                            !lfail.load())

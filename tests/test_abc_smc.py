@@ -139,3 +139,42 @@ def test_abc_smc_on_device_batches(gpu):
         N = r.U.sum(axis=0).astype(float)
         prev = np.where(N > 0, I / np.maximum(N, 1.0), 0.0)
         assert abs(np.sqrt(np.sum((prev - tg) ** 2)) - db) < 1e-12
+
+
+def test_continue_abc_equals_the_longer_run(monkeypatch):
+    """continue_abc (R/abc.R:996-1027) from a 3-generation run, for 2 more,
+    gives the 5-generation run's particles, weights and tolerances: the
+    quantile rule's next tolerance and the random generator carry over."""
+    truth = 0.4
+
+    class Stub:
+        def __init__(self, th):
+            self.th = th
+            self.Nn, self.tspan = 10, np.arange(5)
+
+    def fake_batch(models, seeds, targets, cap_transfers=False):
+        th = np.array([m.th for m in models])
+        noise = np.random.default_rng(int(seeds[0])).normal(0, 0.01, len(th))
+        return None, np.abs(th - truth) + np.abs(noise)
+
+    monkeypatch.setattr(abc, "run_batch", fake_batch)
+
+    def simulate(theta, rng):
+        seeds = [int(rng.integers(1, 2 ** 31))] * len(theta)
+        return [Stub(t[0]) for t in theta], seeds, [None] * len(theta)
+
+    priors = [abc.Prior("th", "uniform", 0.0, 1.0)]
+    whole = abc.abc_smc(simulate, priors, n_particles=100, generations=5, batch=128, n_init=400,
+                        seed=11, quantile=0.6)
+    part = abc.abc_smc(simulate, priors, n_particles=100, generations=3, batch=128, n_init=400,
+                       seed=11, quantile=0.6)
+    more = abc.continue_abc(part, simulate, 2)
+    assert len(more) == 5 and len(part) == 3
+    for a, b in zip(whole, more):
+        assert a.tolerance == b.tolerance and a.nprop == b.nprop
+        assert np.array_equal(a.x, b.x) and np.array_equal(a.w, b.w)
+    # given tolerances: one per new generation
+    given = abc.continue_abc(part, simulate, 2, tolerance=[0.05, 0.03])
+    assert [g.tolerance for g in given[3:]] == [0.05, 0.03]
+    with pytest.raises(ValueError):
+        abc.continue_abc(part, simulate, 3, tolerance=[0.05])
