@@ -478,8 +478,8 @@ int siminf_gpu_plan_stats(const siminf_gpu_plan *plan, siminf_gpu_stats *out);
  * with one-pass and with two-pass days (siminf_gpu_options.two_pass).
  * Stage 2, from the best of stage 1: the SSA kernel's other register
  * budget (ssa_variant 1: more registers a thread, fewer resident warps),
- * then, where the heavy part is on, 8 lanes a warp for the heaviest class
- * (heavy_lanes; 32 otherwise).  Stage 3, for plans with external transfers: the wavefront kernel's block
+ * then, for a plan of one model and one replicate with the heavy part on,
+ * 8 lanes a warp for the heaviest class (heavy_lanes; 32 otherwise).  Stage 3, for plans with external transfers: the wavefront kernel's block
  * of 128 and 512 threads (256 otherwise).  The three fastest are then
  * timed again as repeated runs execute them (the third run of each, which
  * replays the run's CUDA graph), and their times replace the probes'; the

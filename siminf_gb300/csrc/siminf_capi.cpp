@@ -2691,12 +2691,17 @@ int siminf_gpu_plan_tune(siminf_gpu_plan *p, void *cuda_stream, int probe_days,
     /* stage 1: the work queue's layout */
     for (int k = 0; k < 8 && !rc; k++)
         probe(cand[k % 4], k / 4, 0, 256, 0);
-    /* stage 2: the SSA kernel's other register budget, then fewer lanes a
-     * warp for the heaviest nodes (a warp holding the day's longest chains
-     * shares its issue slots and FP64 pipe with fewer lanes) */
+    /* stage 2: the SSA kernel's other register budget, then, for one
+     * model run once, fewer lanes a warp for the heaviest nodes (a warp
+     * holding the day's longest chains shares its issue slots and FP64 pipe
+     * with fewer lanes; with replicates or a batch of models the heavy
+     * class is large, the run is bound by throughput, and idle lanes only
+     * cost: 16 replicates of the headline took 3.13 s a year with 8 lanes
+     * against 2.76 s with 32) */
     if (!rc && best >= 0 && !p->s.aem)
         probe(r.heavy_rate[best], r.two_pass[best], 1, 256, 0);
-    if (!rc && best >= 0 && !p->s.aem && r.heavy_rate[best] > 0.0 && p->L->time_invariant)
+    if (!rc && best >= 0 && !p->s.aem && r.heavy_rate[best] > 0.0 && p->L->time_invariant &&
+        p->s.Nrep == 1 && !p->s.job_of)
         probe(r.heavy_rate[best], r.two_pass[best], r.ssa_variant[best], 256, 8);
     /* stage 3: the wavefront block */
     if (!rc && best >= 0 && p->e2_count > 0) {
