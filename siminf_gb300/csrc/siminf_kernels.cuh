@@ -1010,6 +1010,18 @@ __device__ __forceinline__ bool node_e1(const DevState &s, int (&u)[NC], int nod
     return o.any;
 }
 
+/* node_e1 as a call, for k_horizon with models of at most two
+ * compartments: inlined, its samplers take the registers the one-node-a-
+ * thread loop keeps live and 12 bytes spill; called, they do not (and the
+ * call is made only for a node that has E1 events at all). */
+template <int NC>
+__device__ __noinline__ bool node_e1_call(const DevState &s, int (&u)[NC], int node, int day,
+                                          si_rng &r, long long g, double tt, int &err_code,
+                                          int &err_event)
+{
+    return node_e1<NC>(s, u, node, day, r, g, tt, err_code, err_event);
+}
+
 /* The NC compartments of one node, loaded or stored with 16-byte (NC a
  * multiple of 4) or 8-byte (NC even) accesses: a node's block of u or of a
  * U column starts at a multiple of NC ints from a 256-byte aligned base. */
@@ -2196,7 +2208,13 @@ __global__ void __launch_bounds__(256, M::NT <= 4 ? 2 : 1) k_horizon(DevState s,
                 r.s1 ^= SI_CRN_S1;
                 r.have = 0;
             }
-            bool upd = node_e1<NC>(s, ln.u, node, d, r, g, di.tt, e_code, e_idx);
+            bool upd = false;
+            if constexpr (NC <= 2) {
+                if (s.e1_ptr[node] != s.e1_ptr[node + 1])
+                    upd = node_e1_call<NC>(s, ln.u, node, d, r, g, di.tt, e_code, e_idx);
+            } else {
+                upd = node_e1<NC>(s, ln.u, node, d, r, g, di.tt, e_code, e_idx);
+            }
             if (s.crn_ctr) {
                 const uint64_t t = r.ctr;   /* back to the SSA's */
                 r.ctr = c_other;
