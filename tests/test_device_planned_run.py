@@ -55,6 +55,17 @@ def test_device_planned_unsorted_rejected(gpu, device_planner):
     assert got == -31
 
 
+def test_device_planned_e2_before_e1_rejected(gpu, device_planner):
+    """Times in order but an external transfer before an E1 event of the
+    same time: the order (time, E1 before E2) is broken inside a day, which
+    only the day's own check sees."""
+    from siminf_gb300 import model as M
+    m = M.SIR({"S": [5, 5], "I": [0, 0], "R": [0, 0]}, [1, 2, 3], 0.0, 0.0,
+              events=M.make_events([3, 0], [2, 2], [1, 2], [2, 0], 1, 0.0, 1, 0, sort=False))
+    got, _, _ = run_gpu(m)
+    assert got == -31
+
+
 def test_device_planned_capped_workload(gpu, oracle_lib, device_planner):
     """The headline generator at 0.2% scale over 365 days (46 chunks of
     days, cap_transfers on): bit-exact with the oracle."""
